@@ -1,0 +1,170 @@
+/*
+ * paraprobe_gb300.h -- C ABI of the GB300 spatial-statistics path.
+ *
+ * Replaces, as a drop-in boundary, the in-process call the reference makes at
+ *   solver::characterize_spatstat -> horderdist::compute_generic_spatstat3
+ *   (src/PARAPROBE_SolverHdl.cpp:745-776, :3685-4297)
+ * together with the inputs that call reads: the ion positions and labels
+ * (threadmemory::ionpp3_kdtree, src/PARAPROBE_SolverHdl.h:133), the squared
+ * ion-to-hull distances (ion2surf_kdtree, :134; computed by
+ * solver::surface_distancing2, src/PARAPROBE_SolverHdl.cpp:312-479), the task
+ * list (horderdist::spatstat_tasks, src/PARAPROBE_SolverHdl.h:322, parsed by
+ * parse_tasks, src/PARAPROBE_PeriodicTable.cpp:653-690) and the Settings
+ * statics SpatStatRadiusMin/Incr/Max and SpatStatMKNNCode
+ * (src/PARAPROBE_Settings.cpp:473-503).
+ *
+ * Conventions
+ *   - Every function returns PP_OK (0) or a negative PP_ERR_* code and never
+ *     aborts the process.  pp_last_error() describes the last failure.
+ *   - The caller owns every host array; the library copies inputs and never
+ *     keeps a host pointer.  The library owns all device memory.
+ *   - One context per host thread; calls on one context are not re-entrant.
+ *   - pp_run* enqueue work on the caller's CUDA stream (NULL = the legacy
+ *     default stream) and return; pp_fetch* synchronise that stream.
+ *   - Results are exact uint64 counts.  The reference holds the same counts
+ *     as integral doubles; the CSV writer converts them when printing.
+ *   - Histogram layout: one histogram is H = nbins + 2 counts
+ *       [lowest, bin 0, ..., bin nbins-1, highest]
+ *     with nbins = (size_t)((rmax - rmin) / rincr) evaluated in double from
+ *     the float settings (src/PARAPROBE_Histogram.h:53-93).  pp_fetch writes
+ *     the groups RDF[ntasks], 1NN[ntasks], RIPK[ntasks], MKNN[ntasks][nk], in
+ *     that order, each present only when its flag was given to pp_run.
+ *   - Type masks: 8 uint32 words per task, bit t of word t/32 set when ion
+ *     type id t (0 = Unknown, ids as assigned by ranging) is in the set.
+ */
+#ifndef PARAPROBE_GB300_H
+#define PARAPROBE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* error codes */
+#define PP_OK 0
+#define PP_ERR_INVALID (-1)     /* bad argument or inconsistent sizes */
+#define PP_ERR_CUDA (-2)        /* a CUDA call failed */
+#define PP_ERR_NOMEM (-3)       /* device or host allocation refused */
+#define PP_ERR_UNSUPPORTED (-4) /* a feature outside this build's limits */
+#define PP_ERR_STATE (-5)       /* call order violated (e.g. run before tasks) */
+#define PP_ERR_OVERFLOW (-6)    /* a device capacity was exceeded */
+#define PP_ERR_DEVICE (-7)      /* a kernel reported a failure in its status word */
+#define PP_ERR_IO (-8)          /* a file could not be read or written */
+
+/* analysis flags: the digits of AnalysisSpatDistrType
+ * (src/PARAPROBE_Settings.cpp:348-392) as bits */
+#define PP_RDF 1u
+#define PP_1NN 2u
+#define PP_RIPK 4u
+#define PP_MKNN 8u
+#define PP_NPCORR 16u /* not provided: rejected with PP_ERR_UNSUPPORTED */
+#define PP_CNTNB 32u
+
+#define PP_TYPE_WORDS 8 /* 256 ion types */
+
+typedef struct pp_ctx pp_ctx;
+
+/* Context on CUDA device `device`.  Replaces the OpenMP team the reference
+ * opens inside compute_generic_spatstat3 (src/PARAPROBE_SolverHdl.cpp:3770). */
+int pp_create(pp_ctx** out, int device);
+void pp_destroy(pp_ctx* ctx);
+const char* pp_strerror(int code);
+const char* pp_last_error(pp_ctx* ctx);
+
+/* Upload one labelled ion cloud (host arrays): xyz is n x 3 float32,
+ * label is n type ids, ion_id (nullable) are the caller's ids reported by
+ * pp_neighbors (default: the input index).  Replaces the per-thread copies
+ * threadmemory::read_localions builds (src/PARAPROBE_SolverHdl.cpp:1330-1468)
+ * and the per-thread KD-trees of build_local_kdtree (:1593-1663): the cloud
+ * is binned on the device into a uniform cell grid instead. */
+int pp_cloud_upload(pp_ctx* ctx, const float* xyz, const uint8_t* label,
+                    const uint32_t* ion_id, uint64_t n, int* cloud);
+/* Same, from device-resident arrays (no host copy); runs on `stream`. */
+int pp_cloud_upload_device(pp_ctx* ctx, const float* d_xyz, const uint8_t* d_label,
+                           uint64_t n, int* cloud, void* stream);
+/* Ingest a raw POS byte image (n records of big-endian float32 x, y, z, m/q,
+ * src/PARAPROBE_EPOSEndianness.h:40-79) and range it on the device: the first
+ * range [lo, hi] (inclusive) containing m/q gives the type, else 0
+ * (PeriodicTable::mq2ionname, src/PARAPROBE_PeriodicTable.cpp:65-91).
+ * Ranges must be listed in the order mq2ionname visits them. */
+int pp_cloud_upload_pos(pp_ctx* ctx, const void* pos_bytes, uint64_t n,
+                        const float* range_lo, const float* range_hi,
+                        const uint8_t* range_type, int nranges, int* cloud);
+int pp_cloud_free(pp_ctx* ctx, int cloud);
+/* Type ids of a cloud in input order (n bytes), e.g. after pp_cloud_upload_pos. */
+int pp_cloud_labels(pp_ctx* ctx, int cloud, uint8_t* label_out, uint64_t n);
+
+/* Attach a closed triangle hull (ntri x 9 float32: v1, v2, v3) to a cloud.
+ * pp_run then computes ion2surf with R' = max(rmax, carve_radius) exactly as
+ * solver::surface_distancing2 does (src/PARAPROBE_SolverHdl.cpp:312-479). */
+int pp_hull_upload(pp_ctx* ctx, int cloud, const float* tri, uint64_t ntri,
+                   float carve_radius);
+/* Or give precomputed squared distances (n floats, input order). */
+int pp_surfdist_upload(pp_ctx* ctx, int cloud, const float* d2);
+/* The ion2surf values pp_run used last for this cloud (n floats, input order). */
+int pp_surfdist_fetch(pp_ctx* ctx, int cloud, float* d2_out, uint64_t n);
+
+/* Task list: ntasks x PP_TYPE_WORDS words each for the centre (trg) and the
+ * environment (env) sets of TypeSpecDescrStat
+ * (src/PARAPROBE_PeriodicTable.h:100-128). */
+int pp_tasks_set(pp_ctx* ctx, const uint32_t* trg_mask, const uint32_t* env_mask,
+                 int ntasks);
+/* SpatStatRadiusMin / Incr / Max as the reference stores them (float). */
+int pp_hist_params(pp_ctx* ctx, float rmin, float rincr, float rmax);
+
+/* One pass of compute_generic_spatstat3 over a cloud.  flags: PP_RDF |
+ * PP_1NN | PP_RIPK | PP_MKNN | PP_CNTNB.  k_list: the MKNN orders (1-based),
+ * in output order (the reference sorts them descending,
+ * src/PARAPROBE_SolverHdl.cpp:3739-3763).  label_perm (nullable, n entries):
+ * ion i takes the label of ion label_perm[i] for this run (the label-shuffle
+ * null model of rndlabeler, src/PARAPROBE_SolverHdl.cpp:2809-3003). */
+int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk,
+           const uint32_t* label_perm, void* stream);
+/* Results of the last pp_run (synchronises). cap = capacity in uint64. */
+int pp_fetch(pp_ctx* ctx, uint64_t* bins, size_t cap);
+/* Neighbour-count histograms (PP_CNTNB): ntasks x len counts; *len returns
+ * the common length (largest count + 1).  Pass bins = NULL to query *len. */
+int pp_fetch_cntnb(pp_ctx* ctx, uint64_t* bins, size_t cap, uint64_t* len);
+/* Number of uint64 pp_fetch writes and the bin count per histogram. */
+int pp_result_size(pp_ctx* ctx, uint64_t* total, uint64_t* nbins);
+/* Centres considered, ions discarded, and in-ball (centre, neighbour) pairs
+ * of the last run (the considered/discarded counts printed at
+ * src/PARAPROBE_SolverHdl.cpp:4112-4116). */
+int pp_run_stats(pp_ctx* ctx, uint64_t* centres, uint64_t* discarded, uint64_t* pairs);
+
+/* Batched realisations in one persistent launch: the plain labels
+ * (include_original != 0), then n_label_sets label arrays (n_label_sets x n
+ * type ids, input order, host or device memory), then n_rois spherical
+ * regions of interest (n_rois x 4 float: cx, cy, cz, radius; a centre must
+ * satisfy radius - |p - c| >= rmax in addition to the plain filter, the
+ * environment stays the whole cloud).  Same flags and k_list as pp_run. */
+int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk,
+                   int include_original, const uint8_t* label_sets, int n_label_sets,
+                   const float* rois, int n_rois, void* stream);
+/* Number of realisations of the last batched run. */
+int pp_batched_count(pp_ctx* ctx, int* n_realisations);
+/* Results of realisation r of the last batched run, pp_fetch layout. */
+int pp_fetch_batched(pp_ctx* ctx, int r, uint64_t* bins, size_t cap);
+int pp_batched_stats(pp_ctx* ctx, int r, uint64_t* centres, uint64_t* pairs);
+
+/* Neighbour set of one ion (input index): every other ion with float
+ * d^2 <= r^2, d^2 = (xi-xj)^2 + (yi-yj)^2 + (zi-zj)^2 evaluated left to right
+ * without contraction (src/PARAPROBE_KDTree.h:55-58), sorted by (d^2, id). */
+int pp_neighbors(pp_ctx* ctx, int cloud, uint64_t ion, float r, uint64_t* ids,
+                 float* d2, uint64_t cap, uint64_t* count);
+
+/* Deterministic label shuffle for the null model: a Fisher-Yates pass driven
+ * by splitmix64(seed).  The reference's std::shuffle over mt19937 is
+ * implementation-defined and depends on its thread count, so both sides of a
+ * comparison take the permuted labels this produces. */
+int pp_shuffle_labels(const uint8_t* label, uint64_t n, uint64_t seed, uint8_t* out);
+
+/* Device the context runs on and its SM count. */
+int pp_device_info(pp_ctx* ctx, int* device, int* sm_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PARAPROBE_GB300_H */

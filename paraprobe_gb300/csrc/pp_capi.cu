@@ -1,0 +1,1225 @@
+// pp_capi.cu -- host side of the C ABI in include/paraprobe_gb300.h.
+//
+// A context owns every device buffer.  A cloud keeps its input-order copy
+// (xyz, labels) plus the cell-sorted layout the kernels read; the cell grid is
+// (re)built lazily when a query's radius needs a different cell edge.  Each
+// run prepares small host tables (bin thresholds, type slots, environment
+// sets), launches the kernels on the caller's stream, and the fetch calls fold
+// the per-type "core" histograms into the per-task histograms of
+// compute_generic_spatstat3 (src/PARAPROBE_SolverHdl.cpp:3685-4177).
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/paraprobe_gb300.h"
+#include "pp_internal.h"
+#include "pp_host.h"
+
+using pp::Grid;
+
+namespace {
+
+constexpr double kEpsilon = 1.0e-6;  // src/PARAPROBE_Numerics.h:44
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t b) {
+    if (b <= bytes && p) return cudaSuccess;
+    release();
+    if (b == 0) b = 16;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    else p = nullptr;
+    return e;
+  }
+  template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+struct Hull {
+  std::vector<float> tri;  // ntri * 9
+  float carve = 2.0f;
+  bool present = false;
+};
+
+struct Cloud {
+  uint64_t n = 0;
+  DevBuf xyz, label;            // input order
+  std::vector<uint32_t> ids;    // caller ids (empty = input index)
+  // grid
+  bool grid_ok = false;
+  Grid g{};
+  uint64_t grid_version = 0;
+  DevBuf ions, cell_start, slot_of_id, id_of_slot, label_sorted;
+  // hull / ion2surf
+  Hull hull;
+  DevBuf user_surf;             // input order, when given
+  bool has_user_surf = false;
+  DevBuf surf;                  // sorted order, valid for (surf_rp, surf_version)
+  float surf_rp = -1.f;
+  uint64_t surf_version = ~0ull;
+  DevBuf tri_dev, tri_box, tcell_start, tcell_list;
+};
+
+struct Tables {
+  // histogram
+  float rmin = 0.f, rincr = 0.1f, rmax = 2.f;  // reference defaults, src/PARAPROBE_Settings.cpp:106-108
+  uint32_t nbins = 0;
+  double hstart = 0, hend = 0, hscale = 0;
+};
+
+struct RunPlan {
+  uint32_t flags = 0;
+  int H = 0;
+  std::vector<uint32_t> kvals;     // internal sorted unique ks
+  std::vector<uint32_t> k_out;     // MKNN k list as given
+  int nC = 0, nE = 0, nS = 0;
+  std::vector<int> ctype, etype;   // slot -> type
+  std::vector<int8_t> cslot_of, eslot_of;
+  std::vector<std::vector<uint32_t>> sets;  // global env sets as type lists (mask words)
+  std::vector<int> task_set;       // task -> global set id
+  std::vector<uint32_t> envbits;   // [nC][256]
+  std::vector<int> set_list;       // [nC][32]
+  std::vector<int> nsets;          // [nC]
+  int emax = 0, kr = 0, kmax = 0;
+  int cmax = 0;
+  int cat_miss = 0;
+  std::vector<float> catT;
+};
+
+struct Result {
+  bool valid = false;
+  bool batched = false;
+  int nreal = 1;
+  RunPlan plan;
+  uint32_t nbins = 0;
+  int ntasks = 0;
+  std::vector<uint32_t> trg, env;  // task masks
+  DevBuf rdf, knn, cnt, counters, status;
+  uint64_t ncentres_total = 0, n_ions = 0;
+  std::vector<unsigned long long> counters_h;  // per realisation [pairs, centres]
+  std::vector<uint64_t> centres_sel;           // per realisation (selected count, plain runs)
+  cudaStream_t stream = nullptr;
+  bool fetched = false;
+  std::vector<unsigned long long> rdf_h, knn_h, cnt_h;
+};
+
+}  // namespace
+
+struct pp_ctx {
+  int device = 0;
+  int sm_count = 0;
+  std::string err;
+  std::vector<std::unique_ptr<Cloud>> clouds;
+  bool tasks_ok = false;
+  int ntasks = 0;
+  std::vector<uint32_t> trg, env;
+  bool hist_ok = false;
+  Tables tab;
+  Result res;
+  // scratch
+  DevBuf tmp_cell_of, tmp_rank, scan_tmp, bbox, centres, centre_count, work, tables_dev;
+  DevBuf labels_run, perm_dev, gather_src;
+  // batched geometry cache
+  DevBuf pair_count, pair_off, pair_slot, pair_cat, geo_centres, centre_ok, real_labels, rois_dev;
+  uint64_t geo_key_version = ~0ull;
+  int geo_cloud = -1;
+  float geo_R = -1.f;
+  uint32_t geo_ncentres = 0;
+  uint64_t geo_pairs = 0;
+  int geo_H = 0;
+  float geo_rmin = 0, geo_rincr = 0;
+  uint64_t grid_counter = 1;
+};
+
+namespace {
+
+int fail(pp_ctx* c, int code, const char* fmt, ...) {
+  if (c) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    c->err = buf;
+  }
+  return code;
+}
+
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? PP_ERR_NOMEM : PP_ERR_CUDA, "%s: %s", \
+                  #call, cudaGetErrorString(e_));                                             \
+  } while (0)
+
+// ---------------------------------------------------------------- histogram
+// Category of one float distance under histogram::add
+// (src/PARAPROBE_Histogram.h:97-117): 0 lowest, 1 + b bin b, nbins + 1 highest.
+int category_of_distance(const Tables& t, float x) {
+  const double xx = x;
+  if (xx >= t.hstart && xx <= t.hend) {
+    const float rb = (float)((xx - t.hstart) * t.hscale);
+    const uint32_t b = (uint32_t)std::floor(rb);
+    return b < t.nbins ? (int)(1 + b) : (int)(t.nbins + 1);
+  }
+  if (xx < t.hstart) return 0;
+  return (int)(t.nbins + 1);
+}
+
+int category_of_d2(const Tables& t, float d2) { return category_of_distance(t, std::sqrt(d2)); }
+
+void set_tables(Tables& t, float rmin, float rincr, float rmax) {
+  t.rmin = rmin; t.rincr = rincr; t.rmax = rmax;
+  t.hstart = rmin; t.hend = rmax;
+  size_t nb = 0;
+  if ((double)rincr > kEpsilon) nb = (size_t)(((double)rmax - (double)rmin) / (double)rincr);
+  t.nbins = (uint32_t)nb;
+  t.hscale = nb ? 1.0 / (t.hend - t.hstart) * (double)nb : 0.0;
+}
+
+// T[k] = smallest non-negative float d^2 whose category is >= k (k = 1..H-1),
+// +inf when no finite d^2 reaches k.  The category is monotone in d^2, so a
+// binary search over the ordered bit patterns of non-negative floats finds it.
+std::vector<float> threshold_table(const Tables& t) {
+  const int H = (int)t.nbins + 2;
+  std::vector<float> T(H, 0.f);
+  for (int k = 1; k < H; ++k) {
+    uint32_t lo = 0, hi = 0x7f800000u;  // +inf
+    auto cat = [&](uint32_t u) {
+      float f;
+      std::memcpy(&f, &u, 4);
+      return category_of_d2(t, f);
+    };
+    if (cat(0x7f7fffffu) < k) { T[k] = INFINITY; continue; }
+    hi = 0x7f7fffffu;
+    while (lo < hi) {
+      const uint32_t mid = lo + (hi - lo) / 2;
+      if (cat(mid) >= k) hi = mid; else lo = mid + 1;
+    }
+    std::memcpy(&T[k], &lo, 4);
+  }
+  return T;
+}
+
+inline bool has_type(const uint32_t* m, int t) { return (m[t >> 5] >> (t & 31)) & 1u; }
+
+// --------------------------------------------------------------------- grid
+int build_grid(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
+  const uint64_t n = cl.n;
+  CK(ctx->bbox.ensure(8 * sizeof(uint32_t)));
+  uint32_t init[8] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0, 0, 0, 0, 0};
+  CK(cudaMemcpyAsync(ctx->bbox.p, init, sizeof init, cudaMemcpyHostToDevice, s));
+  pp::launch_bbox(cl.xyz.as<float>(), n, ctx->bbox.as<float>(), s);
+  uint32_t bb[8];
+  CK(cudaMemcpyAsync(bb, ctx->bbox.p, sizeof bb, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (bb[6]) return fail(ctx, PP_ERR_INVALID, "cloud has %u non-finite coordinates", bb[6]);
+  auto o2f = [](uint32_t o) {
+    const uint32_t u = (o & 0x80000000u) ? (o & 0x7fffffffu) : ~o;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+  };
+  float lo[3], hi[3];
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = n ? o2f(bb[k]) : 0.f;
+    hi[k] = n ? o2f(bb[3 + k]) : 0.f;
+  }
+  // cell edge R/2 (stencil rows of about five cells), coarsened if the grid
+  // would hold more than max(4 n, 2^20) cells
+  double h = std::max((double)R * 0.5, 1e-3);
+  const double ext[3] = {(double)hi[0] - lo[0], (double)hi[1] - lo[1], (double)hi[2] - lo[2]};
+  const double maxcells = std::max(4.0 * (double)n, (double)(1 << 20));
+  for (;;) {
+    double c = 1.0;
+    for (int k = 0; k < 3; ++k) c *= std::floor(ext[k] / h) + 1.0;
+    if (c <= maxcells && c < 4.0e9) break;
+    h *= 1.25;
+  }
+  Grid g{};
+  g.h = (float)h;
+  g.inv_h = (float)(1.0 / h);
+  g.lox = lo[0]; g.loy = lo[1]; g.loz = lo[2];
+  g.nx = (int)std::floor(ext[0] / h) + 1;
+  g.ny = (int)std::floor(ext[1] / h) + 1;
+  g.nz = (int)std::floor(ext[2] / h) + 1;
+  g.ncells = (uint64_t)g.nx * g.ny * g.nz;
+  const double amax = std::max({std::fabs((double)lo[0]), std::fabs((double)hi[0]), std::fabs((double)lo[1]),
+                                std::fabs((double)hi[1]), std::fabs((double)lo[2]), std::fabs((double)hi[2])});
+  g.margin = (float)std::max(1e-3 * h, 1e-5 * amax + 1e-6);
+
+  CK(ctx->tmp_cell_of.ensure(n * 4));
+  CK(ctx->tmp_rank.ensure(n * 4));
+  CK(cl.cell_start.ensure((g.ncells + 1) * 4));
+  CK(cudaMemsetAsync(cl.cell_start.p, 0, (g.ncells + 1) * 4, s));
+  pp::launch_cell_count(cl.xyz.as<float>(), n, g, ctx->tmp_cell_of.as<uint32_t>(), ctx->tmp_rank.as<uint32_t>(),
+                        cl.cell_start.as<uint32_t>(), s);
+  const uint64_t tmp_elems = (g.ncells + 1) / 2048 + 64;
+  CK(ctx->scan_tmp.ensure(tmp_elems * 8 * 2));
+  pp::launch_exclusive_scan_u32(cl.cell_start.as<uint32_t>(), g.ncells + 1, ctx->scan_tmp.as<uint32_t>(),
+                                tmp_elems * 4, s);
+  CK(cl.ions.ensure(std::max<uint64_t>(n, 1) * 16));
+  CK(cl.slot_of_id.ensure(std::max<uint64_t>(n, 1) * 4));
+  CK(cl.id_of_slot.ensure(std::max<uint64_t>(n, 1) * 4));
+  CK(cl.label_sorted.ensure(std::max<uint64_t>(n, 1)));
+  pp::launch_scatter(cl.xyz.as<float>(), cl.label.as<uint8_t>(), n, ctx->tmp_cell_of.as<uint32_t>(),
+                     ctx->tmp_rank.as<uint32_t>(), cl.cell_start.as<uint32_t>(), cl.ions.as<float4>(),
+                     cl.slot_of_id.as<uint32_t>(), cl.id_of_slot.as<uint32_t>(), cl.label_sorted.as<uint8_t>(), s);
+  CK(cudaGetLastError());
+  cl.g = g;
+  cl.grid_ok = true;
+  cl.grid_version = ctx->grid_counter++;
+  return PP_OK;
+}
+
+int ensure_grid(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
+  if (cl.grid_ok && cl.g.h <= R * 1.0001f && cl.g.h >= R / 6.f) return PP_OK;
+  if (cl.grid_ok && cl.g.h <= R * 1.0001f && cl.g.h < R / 6.f) {
+    // very fine grid relative to R: acceptable only if coarsening was forced
+  }
+  return build_grid(ctx, cl, R, s);
+}
+
+// ------------------------------------------------------------- ion2surf
+int ensure_surface(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
+  const uint64_t n = cl.n;
+  if (cl.has_user_surf) {
+    if (cl.surf_version == cl.grid_version && cl.surf_rp < 0.f) return PP_OK;
+    CK(cl.surf.ensure(std::max<uint64_t>(n, 1) * 4));
+    // sorted[slot] = user[id_of_slot[slot]] : reuse the label gather on 4-byte words
+    std::vector<uint32_t> dummy;
+    (void)dummy;
+    pp_host::gather_f32_sorted(cl.user_surf.as<float>(), cl.id_of_slot.as<uint32_t>(), n, cl.surf.as<float>(), s);
+    cl.surf_rp = -1.f;
+    cl.surf_version = cl.grid_version;
+    return PP_OK;
+  }
+  const float rp = std::max(R, cl.hull.carve);  // max(SpatStatRadiusMax, SurfaceCellsCarvingRadius)
+  if (cl.surf_version == cl.grid_version && cl.surf_rp == rp) return PP_OK;
+  CK(cl.surf.ensure(std::max<uint64_t>(n, 1) * 4));
+  if (!cl.hull.present) {
+    // no hull: every ion keeps the initial R'^2 (src/PARAPROBE_SolverHdl.cpp:335-348)
+    const float rp2 = rp * rp;
+    pp_host::fill_f32(cl.surf.as<float>(), n, rp2, s);
+    cl.surf_rp = rp;
+    cl.surf_version = cl.grid_version;
+    return PP_OK;
+  }
+  const std::vector<float>& tri = cl.hull.tri;
+  const uint64_t nt = tri.size() / 9;
+  std::vector<float> box(6 * nt);
+  float glo[3] = {INFINITY, INFINITY, INFINITY}, ghi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (uint64_t t = 0; t < nt; ++t) {
+    const float* v = &tri[9 * t];
+    for (int k = 0; k < 3; ++k) {
+      // src/PARAPROBE_SolverHdl.cpp:2712-2717: fmin/fmax of the three vertices
+      const float l = std::fmin(std::fmin(v[k], v[3 + k]), v[6 + k]);
+      const float h = std::fmax(std::fmax(v[k], v[3 + k]), v[6 + k]);
+      box[6 * t + k] = l; box[6 * t + 3 + k] = h;
+      glo[k] = std::min(glo[k], l); ghi[k] = std::max(ghi[k], h);
+    }
+  }
+  // triangle grid: cell edge about R', every triangle listed in each cell its
+  // box grown by R' (+ slack) reaches
+  Grid tg{};
+  const float slack = 1e-3f + 1e-5f * std::max({std::fabs(glo[0]), std::fabs(ghi[0]), std::fabs(glo[1]),
+                                                 std::fabs(ghi[1]), std::fabs(glo[2]), std::fabs(ghi[2])});
+  double h = std::max((double)rp, 0.25);
+  for (int k = 0; k < 3; ++k) { glo[k] -= rp + 2 * slack; ghi[k] += rp + 2 * slack; }
+  for (;;) {
+    double c = 1;
+    for (int k = 0; k < 3; ++k) c *= std::floor((ghi[k] - glo[k]) / h) + 1;
+    if (c < 6.0e7) break;
+    h *= 1.25;
+  }
+  tg.h = (float)h; tg.inv_h = (float)(1.0 / h);
+  tg.lox = glo[0]; tg.loy = glo[1]; tg.loz = glo[2];
+  tg.nx = (int)std::floor((ghi[0] - glo[0]) / h) + 1;
+  tg.ny = (int)std::floor((ghi[1] - glo[1]) / h) + 1;
+  tg.nz = (int)std::floor((ghi[2] - glo[2]) / h) + 1;
+  tg.ncells = (uint64_t)tg.nx * tg.ny * tg.nz;
+  std::vector<uint32_t> cnt(tg.ncells + 1, 0);
+  auto range = [&](uint64_t t, int k, int& c0, int& c1, int nmax, float org) {
+    const float l = box[6 * t + k] - rp - slack, u = box[6 * t + 3 + k] + rp + slack;
+    c0 = std::max(0, (int)std::floor((l - org) / h) - 1);
+    c1 = std::min(nmax - 1, (int)std::floor((u - org) / h) + 1);
+  };
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<uint32_t> list;
+    if (pass == 1) {
+      uint64_t acc = 0;
+      for (uint64_t c = 0; c < tg.ncells; ++c) { const uint32_t v = cnt[c]; cnt[c] = (uint32_t)acc; acc += v; }
+      cnt[tg.ncells] = (uint32_t)acc;
+      list.assign(acc, 0);
+    }
+    std::vector<uint32_t> fillp;
+    if (pass == 1) fillp.assign(cnt.begin(), cnt.end() - 1);
+    for (uint64_t t = 0; t < nt; ++t) {
+      int x0, x1, y0, y1, z0, z1;
+      range(t, 0, x0, x1, tg.nx, tg.lox);
+      range(t, 1, y0, y1, tg.ny, tg.loy);
+      range(t, 2, z0, z1, tg.nz, tg.loz);
+      for (int z = z0; z <= z1; ++z)
+        for (int y = y0; y <= y1; ++y)
+          for (int x = x0; x <= x1; ++x) {
+            const uint64_t c = ((uint64_t)z * tg.ny + y) * tg.nx + x;
+            if (pass == 0) cnt[c]++;
+            else list[fillp[c]++] = (uint32_t)t;
+          }
+    }
+    if (pass == 1) {
+      CK(cl.tcell_list.ensure(std::max<size_t>(list.size(), 1) * 4));
+      CK(cudaMemcpyAsync(cl.tcell_list.p, list.data(), list.size() * 4, cudaMemcpyHostToDevice, s));
+      CK(cl.tcell_start.ensure(cnt.size() * 4));
+      CK(cudaMemcpyAsync(cl.tcell_start.p, cnt.data(), cnt.size() * 4, cudaMemcpyHostToDevice, s));
+      CK(cl.tri_dev.ensure(std::max<size_t>(tri.size(), 1) * 4));
+      CK(cudaMemcpyAsync(cl.tri_dev.p, tri.data(), tri.size() * 4, cudaMemcpyHostToDevice, s));
+      CK(cl.tri_box.ensure(std::max<size_t>(box.size(), 1) * 4));
+      CK(cudaMemcpyAsync(cl.tri_box.p, box.data(), box.size() * 4, cudaMemcpyHostToDevice, s));
+      CK(cudaStreamSynchronize(s));  // host vectors die at scope end
+    }
+  }
+  pp::launch_surface(cl.ions.as<float4>(), n, cl.tri_box.as<float>(), cl.tri_dev.as<float>(),
+                     cl.tcell_start.as<uint32_t>(), cl.tcell_list.as<uint32_t>(), tg, rp, cl.surf.as<float>(), s);
+  CK(cudaGetLastError());
+  cl.surf_rp = rp;
+  cl.surf_version = cl.grid_version;
+  return PP_OK;
+}
+
+// ------------------------------------------------------------------- plan
+int make_plan(pp_ctx* ctx, uint32_t flags, const uint32_t* k_list, int nk, RunPlan& P) {
+  if (!ctx->tasks_ok) return fail(ctx, PP_ERR_STATE, "pp_tasks_set was not called");
+  if (!ctx->hist_ok) return fail(ctx, PP_ERR_STATE, "pp_hist_params was not called");
+  if (flags & PP_NPCORR) return fail(ctx, PP_ERR_UNSUPPORTED, "n-point correlations are not provided by this library");
+  if (flags & ~(PP_RDF | PP_1NN | PP_RIPK | PP_MKNN | PP_CNTNB)) return fail(ctx, PP_ERR_INVALID, "unknown flags");
+  const Tables& t = ctx->tab;
+  if (t.nbins == 0) return fail(ctx, PP_ERR_INVALID, "histogram has no bins (rincr <= 1e-6 or rmax <= rmin)");
+  if (t.nbins + 2 > 16384) return fail(ctx, PP_ERR_UNSUPPORTED, "more than 16382 bins");
+  P = RunPlan();
+  P.flags = flags;
+  P.H = (int)t.nbins + 2;
+  if ((flags & PP_MKNN) && nk > 0) {
+    if (!k_list) return fail(ctx, PP_ERR_INVALID, "k_list is NULL");
+    for (int i = 0; i < nk; ++i) {
+      if (k_list[i] < 1) return fail(ctx, PP_ERR_INVALID, "k order smaller than 1");
+      P.k_out.push_back(k_list[i]);
+    }
+  }
+  std::vector<uint32_t> ks = P.k_out;
+  if (flags & PP_1NN) ks.push_back(1);
+  std::sort(ks.begin(), ks.end());
+  ks.erase(std::unique(ks.begin(), ks.end()), ks.end());
+  P.kvals = ks;
+  P.kmax = ks.empty() ? 0 : (int)ks.back();
+  if (P.kmax > 128) return fail(ctx, PP_ERR_UNSUPPORTED, "k = %d exceeds the register-resident limit of 128", P.kmax);
+  P.kr = P.kmax == 0 ? 0 : (P.kmax <= 32 ? 1 : 4);
+  // type slots
+  const int nt = ctx->ntasks;
+  P.cslot_of.assign(256, -1);
+  P.eslot_of.assign(256, -1);
+  for (int ty = 0; ty < 256; ++ty) {
+    bool c = false, e = false;
+    for (int k = 0; k < nt; ++k) {
+      c |= has_type(&ctx->trg[8 * k], ty);
+      e |= has_type(&ctx->env[8 * k], ty);
+    }
+    if (c) { P.cslot_of[ty] = (int8_t)P.ctype.size(); P.ctype.push_back(ty); }
+    if (e) { P.eslot_of[ty] = (int8_t)P.etype.size(); P.etype.push_back(ty); }
+  }
+  if (P.ctype.size() > 127 || P.etype.size() > 127) return fail(ctx, PP_ERR_UNSUPPORTED, "more than 127 distinct types in tasks");
+  P.nC = (int)P.ctype.size();
+  P.nE = (int)P.etype.size();
+  // distinct environment sets
+  std::map<std::vector<uint32_t>, int> setid;
+  P.task_set.assign(nt, -1);
+  for (int k = 0; k < nt; ++k) {
+    std::vector<uint32_t> m(&ctx->env[8 * k], &ctx->env[8 * k] + 8);
+    auto it = setid.find(m);
+    if (it == setid.end()) { it = setid.emplace(m, (int)P.sets.size()).first; P.sets.push_back(m); }
+    P.task_set[k] = it->second;
+  }
+  P.nS = (int)P.sets.size();
+  P.envbits.assign((size_t)std::max(P.nC, 1) * 256, 0u);
+  P.set_list.assign((size_t)std::max(P.nC, 1) * 32, -1);
+  P.nsets.assign(std::max(P.nC, 1), 0);
+  for (int c = 0; c < P.nC; ++c) {
+    std::vector<int> local;
+    for (int k = 0; k < nt; ++k) {
+      if (!has_type(&ctx->trg[8 * k], P.ctype[c])) continue;
+      if (std::find(local.begin(), local.end(), P.task_set[k]) == local.end()) local.push_back(P.task_set[k]);
+    }
+    if (P.kr > 0 && local.size() > 32) return fail(ctx, PP_ERR_UNSUPPORTED, "more than 32 environment sets for one centre type");
+    P.nsets[c] = (int)local.size();
+    for (size_t p = 0; p < local.size() && p < 32; ++p) {
+      P.set_list[c * 32 + p] = local[p];
+      for (int ty = 0; ty < 256; ++ty)
+        if (has_type(P.sets[local[p]].data(), ty)) P.envbits[c * 256 + ty] |= (1u << p);
+    }
+    P.emax = std::max(P.emax, (int)local.size());
+  }
+  if (P.kr == 4 && P.emax > 8) return fail(ctx, PP_ERR_UNSUPPORTED, "k > 32 with more than 8 environment sets per centre type");
+  P.catT = threshold_table(t);
+  P.cat_miss = category_of_distance(t, (float)((double)t.rmax + kEpsilon));
+  return PP_OK;
+}
+
+// Upload the plan's tables into one device block; returns device pointers.
+struct DevTables {
+  float* catT; int8_t* cslot; int8_t* eslot; uint32_t* envbits; int* set_list; int* nsets; int* kvals;
+};
+
+int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
+  std::vector<unsigned char> blob;
+  auto put = [&](const void* src, size_t bytes) {
+    size_t off = (blob.size() + 15) & ~size_t(15);
+    blob.resize(off + bytes);
+    if (bytes) std::memcpy(blob.data() + off, src, bytes);
+    return off;
+  };
+  const size_t o1 = put(P.catT.data(), P.catT.size() * 4);
+  const size_t o2 = put(P.cslot_of.data(), 256);
+  const size_t o3 = put(P.eslot_of.data(), 256);
+  const size_t o4 = put(P.envbits.data(), P.envbits.size() * 4);
+  const size_t o5 = put(P.set_list.data(), P.set_list.size() * 4);
+  const size_t o6 = put(P.nsets.data(), P.nsets.size() * 4);
+  std::vector<int> kv(P.kvals.begin(), P.kvals.end());
+  if (kv.empty()) kv.push_back(1);
+  const size_t o7 = put(kv.data(), kv.size() * 4);
+  CK(ctx->tables_dev.ensure(blob.size()));
+  CK(cudaMemcpyAsync(ctx->tables_dev.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));  // blob is a host temporary
+  unsigned char* b = ctx->tables_dev.as<unsigned char>();
+  D.catT = (float*)(b + o1); D.cslot = (int8_t*)(b + o2); D.eslot = (int8_t*)(b + o3);
+  D.envbits = (uint32_t*)(b + o4); D.set_list = (int*)(b + o5); D.nsets = (int*)(b + o6); D.kvals = (int*)(b + o7);
+  return PP_OK;
+}
+
+Cloud* get_cloud(pp_ctx* ctx, int id) {
+  if (id < 0 || id >= (int)ctx->clouds.size()) return nullptr;
+  return ctx->clouds[id].get();
+}
+
+void fill_scan_common(pp::ScanArgs& a, const Cloud& cl, const RunPlan& P, const DevTables& D, const Tables& t) {
+  a.ions = cl.ions.as<float4>();
+  a.cell_start = cl.cell_start.as<uint32_t>();
+  a.g = cl.g;
+  a.R = t.rmax;
+  a.R2 = t.rmax * t.rmax;
+  const float Rm = t.rmax + cl.g.margin;
+  a.Rm2 = Rm * Rm;
+  a.H = P.H;
+  a.cat_T = D.catT;
+  a.guess_start = t.rmin;
+  a.guess_scale = (float)t.hscale;
+  a.cat_miss = P.cat_miss;
+  a.cslot_of = D.cslot;
+  a.eslot_of = D.eslot;
+  a.nC = P.nC;
+  a.nE = P.nE;
+  a.envbits = D.envbits;
+  a.set_list = D.set_list;
+  a.nsets = D.nsets;
+  a.nS = P.nS;
+  a.kvals = D.kvals;
+  a.nkI = (int)P.kvals.size();
+  a.kmax = std::max(P.kmax, 1);
+}
+
+// Fold per-type cores into per-task histograms (pp_fetch layout).
+void finalize(const Result& R, int r, uint64_t* out) {
+  const RunPlan& P = R.plan;
+  const int H = P.H, nt = R.ntasks;
+  const size_t rdf_sz = (size_t)P.nC * P.nE * H;
+  const size_t knn_sz = (size_t)P.nC * P.nS * P.kvals.size() * H;
+  const unsigned long long* rdf = R.rdf_h.data() + (size_t)r * rdf_sz;
+  const unsigned long long* knn = R.knn_h.empty() ? nullptr : R.knn_h.data() + (size_t)r * knn_sz;
+  uint64_t o = 0;
+  auto kidx = [&](uint32_t k) { return (int)(std::lower_bound(P.kvals.begin(), P.kvals.end(), k) - P.kvals.begin()); };
+  auto rdf_task = [&](int t) {
+    for (int b = 0; b < H; ++b) {
+      unsigned long long s = 0;
+      for (int c = 0; c < P.nC; ++c) {
+        if (!has_type(&R.trg[8 * t], P.ctype[c])) continue;
+        for (int e = 0; e < P.nE; ++e)
+          if (has_type(&R.env[8 * t], P.etype[e])) s += rdf[((size_t)c * P.nE + e) * H + b];
+      }
+      out[o++] = s;
+    }
+  };
+  auto knn_task = [&](int t, int ki) {
+    const int Sg = P.task_set[t];
+    for (int b = 0; b < H; ++b) {
+      unsigned long long s = 0;
+      for (int c = 0; c < P.nC; ++c)
+        if (has_type(&R.trg[8 * t], P.ctype[c])) s += knn[(((size_t)c * P.nS + Sg) * P.kvals.size() + ki) * H + b];
+      out[o++] = s;
+    }
+  };
+  if (P.flags & PP_RDF) for (int t = 0; t < nt; ++t) rdf_task(t);
+  if (P.flags & PP_1NN) for (int t = 0; t < nt; ++t) knn_task(t, kidx(1));
+  if (P.flags & PP_RIPK) for (int t = 0; t < nt; ++t) rdf_task(t);
+  if ((P.flags & PP_MKNN) && !P.k_out.empty())
+    for (int t = 0; t < nt; ++t)
+      for (uint32_t k : P.k_out) knn_task(t, kidx(k));
+}
+
+uint64_t result_len(const Result& R) {
+  const RunPlan& P = R.plan;
+  uint64_t g = 0;
+  if (P.flags & PP_RDF) g += R.ntasks;
+  if (P.flags & PP_1NN) g += R.ntasks;
+  if (P.flags & PP_RIPK) g += R.ntasks;
+  if (P.flags & PP_MKNN) g += (uint64_t)R.ntasks * P.k_out.size();
+  return g * P.H;
+}
+
+int fetch_cores(pp_ctx* ctx) {
+  Result& R = ctx->res;
+  if (!R.valid) return fail(ctx, PP_ERR_STATE, "no run to fetch");
+  if (R.fetched) return PP_OK;
+  CK(cudaStreamSynchronize(R.stream));
+  int status = 0;
+  CK(cudaMemcpy(&status, R.status.p, 4, cudaMemcpyDeviceToHost));
+  const RunPlan& P = R.plan;
+  const size_t rdf_sz = (size_t)P.nC * P.nE * P.H * R.nreal;
+  const size_t knn_sz = (size_t)P.nC * P.nS * P.kvals.size() * P.H * R.nreal;
+  R.rdf_h.assign(rdf_sz, 0);
+  R.knn_h.assign(P.kr ? knn_sz : 0, 0);
+  if ((P.flags & (PP_RDF | PP_RIPK)) && rdf_sz) CK(cudaMemcpy(R.rdf_h.data(), R.rdf.p, rdf_sz * 8, cudaMemcpyDeviceToHost));
+  if (P.kr && knn_sz) CK(cudaMemcpy(R.knn_h.data(), R.knn.p, knn_sz * 8, cudaMemcpyDeviceToHost));
+  if ((P.flags & PP_CNTNB) && !R.batched) {
+    const size_t cs = (size_t)P.nC * P.nE * (P.cmax + 1);
+    R.cnt_h.assign(cs, 0);
+    CK(cudaMemcpy(R.cnt_h.data(), R.cnt.p, cs * 8, cudaMemcpyDeviceToHost));
+  }
+  R.counters_h.assign(2 * R.nreal, 0);
+  CK(cudaMemcpy(R.counters_h.data(), R.counters.p, 16 * R.nreal, cudaMemcpyDeviceToHost));
+  R.fetched = true;
+  if (status & pp::ST_CNT_OVERFLOW) return fail(ctx, PP_ERR_OVERFLOW, "a neighbour count exceeded the CNTNB capacity");
+  if (status & pp::ST_LIST_OVERFLOW) return fail(ctx, PP_ERR_OVERFLOW, "a pair list exceeded its allocation");
+  if (status) return fail(ctx, PP_ERR_DEVICE, "device status word 0x%x", status);
+  return PP_OK;
+}
+
+int alloc_result(pp_ctx* ctx, const RunPlan& P, int nreal, bool batched, cudaStream_t s) {
+  Result& R = ctx->res;
+  R.valid = false;
+  R.fetched = false;
+  R.plan = P;
+  R.nreal = nreal;
+  R.batched = batched;
+  R.ntasks = ctx->ntasks;
+  R.trg = ctx->trg;
+  R.env = ctx->env;
+  R.nbins = ctx->tab.nbins;
+  R.stream = s;
+  const size_t rdf_sz = std::max<size_t>((size_t)P.nC * P.nE * P.H * nreal, 1);
+  const size_t knn_sz = std::max<size_t>((size_t)P.nC * P.nS * std::max<size_t>(P.kvals.size(), 1) * P.H * nreal, 1);
+  const size_t cnt_sz = std::max<size_t>((size_t)P.nC * P.nE * (P.cmax + 1), 1);
+  CK(R.rdf.ensure(rdf_sz * 8));
+  CK(cudaMemsetAsync(R.rdf.p, 0, rdf_sz * 8, s));
+  if (P.kr) {
+    CK(R.knn.ensure(knn_sz * 8));
+    CK(cudaMemsetAsync(R.knn.p, 0, knn_sz * 8, s));
+  }
+  if (P.flags & PP_CNTNB) {
+    CK(R.cnt.ensure(cnt_sz * 8));
+    CK(cudaMemsetAsync(R.cnt.p, 0, cnt_sz * 8, s));
+  }
+  CK(R.counters.ensure(16 * (size_t)nreal));
+  CK(cudaMemsetAsync(R.counters.p, 0, 16 * (size_t)nreal, s));
+  CK(R.status.ensure(4));
+  CK(cudaMemsetAsync(R.status.p, 0, 4, s));
+  return PP_OK;
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+const char* pp_strerror(int code) {
+  switch (code) {
+    case PP_OK: return "ok";
+    case PP_ERR_INVALID: return "invalid argument";
+    case PP_ERR_CUDA: return "CUDA error";
+    case PP_ERR_NOMEM: return "out of memory";
+    case PP_ERR_UNSUPPORTED: return "unsupported";
+    case PP_ERR_STATE: return "call order violated";
+    case PP_ERR_OVERFLOW: return "capacity exceeded";
+    case PP_ERR_DEVICE: return "device reported a failure";
+    case PP_ERR_IO: return "file error";
+    default: return "unknown error";
+  }
+}
+
+const char* pp_last_error(pp_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int pp_create(pp_ctx** out, int device) {
+  if (!out) return PP_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PP_ERR_CUDA;
+  if (device < 0 || device >= ndev) return PP_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return PP_ERR_CUDA;
+  pp_ctx* c = new (std::nothrow) pp_ctx();
+  if (!c) return PP_ERR_NOMEM;
+  c->device = device;
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  *out = c;
+  return PP_OK;
+}
+
+void pp_destroy(pp_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  delete ctx;
+}
+
+int pp_device_info(pp_ctx* ctx, int* device, int* sm_count) {
+  if (!ctx) return PP_ERR_INVALID;
+  if (device) *device = ctx->device;
+  if (sm_count) *sm_count = ctx->sm_count;
+  return PP_OK;
+}
+
+static int new_cloud(pp_ctx* ctx, uint64_t n, int* cloud, Cloud** out) {
+  if (n > 0xfffffff0ull) return fail(ctx, PP_ERR_UNSUPPORTED, "clouds are limited to 2^32-16 ions");
+  auto c = std::make_unique<Cloud>();
+  c->n = n;
+  CK(c->xyz.ensure(std::max<uint64_t>(n, 1) * 12));
+  CK(c->label.ensure(std::max<uint64_t>(n, 1)));
+  *out = c.get();
+  ctx->clouds.push_back(std::move(c));
+  *cloud = (int)ctx->clouds.size() - 1;
+  return PP_OK;
+}
+
+int pp_cloud_upload(pp_ctx* ctx, const float* xyz, const uint8_t* label, const uint32_t* ion_id, uint64_t n,
+                    int* cloud) {
+  if (!ctx || !cloud || (n && (!xyz || !label))) return fail(ctx, PP_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  Cloud* c = nullptr;
+  int rc = new_cloud(ctx, n, cloud, &c);
+  if (rc) return rc;
+  CK(cudaMemcpy(c->xyz.p, xyz, n * 12, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(c->label.p, label, n, cudaMemcpyHostToDevice));
+  if (ion_id) c->ids.assign(ion_id, ion_id + n);
+  return PP_OK;
+}
+
+int pp_cloud_upload_device(pp_ctx* ctx, const float* d_xyz, const uint8_t* d_label, uint64_t n, int* cloud,
+                           void* stream) {
+  if (!ctx || !cloud || (n && (!d_xyz || !d_label))) return fail(ctx, PP_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  Cloud* c = nullptr;
+  int rc = new_cloud(ctx, n, cloud, &c);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  CK(cudaMemcpyAsync(c->xyz.p, d_xyz, n * 12, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(c->label.p, d_label, n, cudaMemcpyDeviceToDevice, s));
+  return PP_OK;
+}
+
+int pp_cloud_upload_pos(pp_ctx* ctx, const void* pos_bytes, uint64_t n, const float* range_lo, const float* range_hi,
+                        const uint8_t* range_type, int nranges, int* cloud) {
+  if (!ctx || !cloud || (n && !pos_bytes) || nranges < 0 || (nranges && (!range_lo || !range_hi || !range_type)))
+    return fail(ctx, PP_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(ctx->device));
+  Cloud* c = nullptr;
+  int rc = new_cloud(ctx, n, cloud, &c);
+  if (rc) return rc;
+  CK(ctx->gather_src.ensure(std::max<uint64_t>(n, 1) * 16));
+  CK(cudaMemcpy(ctx->gather_src.p, pos_bytes, n * 16, cudaMemcpyHostToDevice));
+  DevBuf rng;
+  const size_t nr = (size_t)nranges;
+  CK(rng.ensure(std::max<size_t>(nr, 1) * 9 + 64));
+  float* dlo = rng.as<float>();
+  float* dhi = dlo + std::max<size_t>(nr, 1);
+  uint8_t* dty = (uint8_t*)(dhi + std::max<size_t>(nr, 1));
+  if (nr) {
+    CK(cudaMemcpy(dlo, range_lo, nr * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dhi, range_hi, nr * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dty, range_type, nr, cudaMemcpyHostToDevice));
+  }
+  pp::launch_decode_pos(ctx->gather_src.as<uint32_t>(), n, dlo, dhi, dty, nranges, c->xyz.as<float>(),
+                        c->label.as<uint8_t>(), 0);
+  CK(cudaGetLastError());
+  CK(cudaDeviceSynchronize());
+  return PP_OK;
+}
+
+int pp_cloud_free(pp_ctx* ctx, int cloud) {
+  if (!ctx || !get_cloud(ctx, cloud)) return fail(ctx, PP_ERR_INVALID, "bad cloud");
+  cudaSetDevice(ctx->device);
+  cudaDeviceSynchronize();
+  ctx->clouds[cloud].reset();
+  if (ctx->geo_cloud == cloud) ctx->geo_cloud = -1;
+  return PP_OK;
+}
+
+int pp_cloud_labels(pp_ctx* ctx, int cloud, uint8_t* out, uint64_t n) {
+  Cloud* c = ctx ? get_cloud(ctx, cloud) : nullptr;
+  if (!c || !out || n < c->n) return fail(ctx, PP_ERR_INVALID, "bad argument");
+  CK(cudaMemcpy(out, c->label.p, c->n, cudaMemcpyDeviceToHost));
+  return PP_OK;
+}
+
+int pp_hull_upload(pp_ctx* ctx, int cloud, const float* tri, uint64_t ntri, float carve_radius) {
+  Cloud* c = ctx ? get_cloud(ctx, cloud) : nullptr;
+  if (!c || (ntri && !tri) || !(carve_radius >= 0.f)) return fail(ctx, PP_ERR_INVALID, "bad argument");
+  c->hull.tri.assign(tri, tri + 9 * ntri);
+  for (float v : c->hull.tri)
+    if (!std::isfinite(v)) return fail(ctx, PP_ERR_INVALID, "hull has non-finite vertices");
+  c->hull.carve = carve_radius;
+  c->hull.present = ntri > 0;
+  c->has_user_surf = false;
+  c->surf_version = ~0ull;
+  return PP_OK;
+}
+
+int pp_surfdist_upload(pp_ctx* ctx, int cloud, const float* d2) {
+  Cloud* c = ctx ? get_cloud(ctx, cloud) : nullptr;
+  if (!c || (c->n && !d2)) return fail(ctx, PP_ERR_INVALID, "bad argument");
+  CK(c->user_surf.ensure(std::max<uint64_t>(c->n, 1) * 4));
+  CK(cudaMemcpy(c->user_surf.p, d2, c->n * 4, cudaMemcpyHostToDevice));
+  c->has_user_surf = true;
+  c->surf_version = ~0ull;
+  return PP_OK;
+}
+
+int pp_surfdist_fetch(pp_ctx* ctx, int cloud, float* out, uint64_t n) {
+  Cloud* c = ctx ? get_cloud(ctx, cloud) : nullptr;
+  if (!c || !out || n < c->n) return fail(ctx, PP_ERR_INVALID, "bad argument");
+  if (!c->grid_ok || c->surf_version != c->grid_version) return fail(ctx, PP_ERR_STATE, "no ion2surf computed yet");
+  CK(cudaDeviceSynchronize());
+  std::vector<float> sorted(c->n);
+  std::vector<uint32_t> slot(c->n);
+  CK(cudaMemcpy(sorted.data(), c->surf.p, c->n * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(slot.data(), c->slot_of_id.p, c->n * 4, cudaMemcpyDeviceToHost));
+  for (uint64_t i = 0; i < c->n; ++i) out[i] = sorted[slot[i]];
+  return PP_OK;
+}
+
+int pp_tasks_set(pp_ctx* ctx, const uint32_t* trg_mask, const uint32_t* env_mask, int ntasks) {
+  if (!ctx || ntasks < 0 || (ntasks && (!trg_mask || !env_mask))) return fail(ctx, PP_ERR_INVALID, "bad argument");
+  ctx->trg.assign(trg_mask, trg_mask + 8 * (size_t)ntasks);
+  ctx->env.assign(env_mask, env_mask + 8 * (size_t)ntasks);
+  ctx->ntasks = ntasks;
+  ctx->tasks_ok = true;
+  ctx->geo_cloud = -1;
+  return PP_OK;
+}
+
+int pp_hist_params(pp_ctx* ctx, float rmin, float rincr, float rmax) {
+  if (!ctx) return PP_ERR_INVALID;
+  if (!(rmax > 0.f) || !(rincr > 0.f) || !(rmin >= 0.f) || !(rmin < rmax) || !std::isfinite(rmax))
+    return fail(ctx, PP_ERR_INVALID, "need 0 <= rmin < rmax and rincr > 0 (src/PARAPROBE_Settings.cpp:871-885)");
+  set_tables(ctx->tab, rmin, rincr, rmax);
+  ctx->hist_ok = true;
+  return PP_OK;
+}
+
+int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk, const uint32_t* label_perm,
+           void* stream) {
+  if (!ctx) return PP_ERR_INVALID;
+  Cloud* cl = get_cloud(ctx, cloud);
+  if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  RunPlan P;
+  int rc = make_plan(ctx, flags, k_list, nk, P);
+  if (rc) return rc;
+  const float R = ctx->tab.rmax;
+  if ((rc = ensure_grid(ctx, *cl, R, s))) return rc;
+  if ((rc = ensure_surface(ctx, *cl, R, s))) return rc;
+  const uint64_t n = cl->n;
+  // neighbour-count capacity: the largest possible ball is bounded by the
+  // ions of the densest cell times the stencil's cell count
+  P.cmax = 0;
+  if (flags & PP_CNTNB) P.cmax = 4095;
+  DevTables D{};
+  if ((rc = upload_tables(ctx, P, D, s))) return rc;
+  if ((rc = alloc_result(ctx, P, 1, false, s))) return rc;
+  // labels of this run
+  const uint8_t* labels = nullptr;
+  if (label_perm) {
+    CK(ctx->perm_dev.ensure(std::max<uint64_t>(n, 1) * 4));
+    CK(cudaMemcpyAsync(ctx->perm_dev.p, label_perm, n * 4, cudaMemcpyHostToDevice, s));
+    CK(ctx->labels_run.ensure(std::max<uint64_t>(n, 1)));
+    pp::launch_permute_labels(cl->label.as<uint8_t>(), ctx->perm_dev.as<uint32_t>(), cl->id_of_slot.as<uint32_t>(), n,
+                              ctx->labels_run.as<uint8_t>(), s);
+    labels = ctx->labels_run.as<uint8_t>();
+  }
+  // centres
+  CK(ctx->centres.ensure(std::max<uint64_t>(n, 1) * 4));
+  CK(ctx->centre_count.ensure(8));
+  CK(cudaMemsetAsync(ctx->centre_count.p, 0, 8, s));
+  pp::launch_select_centres(labels ? labels : cl->label_sorted.as<uint8_t>(), cl->surf.as<float>(), n, R * R,
+                            D.cslot, nullptr, ctx->centres.as<uint32_t>(), ctx->centre_count.as<uint32_t>(), s);
+  uint32_t ncent = 0;
+  CK(cudaMemcpyAsync(&ncent, ctx->centre_count.p, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  ctx->res.ncentres_total = ncent;
+  ctx->res.n_ions = n;
+  CK(ctx->work.ensure(16));
+  CK(cudaMemsetAsync(ctx->work.p, 0, 16, s));
+  pp::ScanArgs a{};
+  fill_scan_common(a, *cl, P, D, ctx->tab);
+  a.labels = labels;
+  a.centres = ctx->centres.as<uint32_t>();
+  a.ncentres = ncent;
+  a.flags = flags & (PP_RDF | PP_RIPK | PP_CNTNB);
+  if (flags & PP_RIPK) a.flags |= PP_RDF;
+  a.rdf_core = ctx->res.rdf.as<unsigned long long>();
+  a.knn_core = ctx->res.knn.as<unsigned long long>();
+  a.cnt_core = ctx->res.cnt.as<unsigned long long>();
+  a.cmax = P.cmax;
+  a.counters = ctx->res.counters.as<unsigned long long>();
+  a.work = ctx->work.as<uint32_t>();
+  a.status = ctx->res.status.as<int>();
+  a.mode = 0;
+  a.rdf_in_smem = ((size_t)P.nC * P.nE * P.H * 4 <= 96 * 1024) ? 1 : 0;
+  if (ncent > 0) {
+    size_t smem = 0;
+    rc = pp::launch_scan(a, P.kr, P.emax, ctx->sm_count, &smem, s);
+    if (rc == -2) return fail(ctx, PP_ERR_UNSUPPORTED, "no kernel variant for k=%d with %d environment sets", P.kmax, P.emax);
+    if (rc) {
+      cudaError_t e = cudaGetLastError();
+      return fail(ctx, PP_ERR_CUDA, "scan launch failed (%s, %zu B shared)", cudaGetErrorString(e), smem);
+    }
+  }
+  ctx->res.valid = true;
+  ctx->res.centres_sel.assign(1, ncent);
+  return PP_OK;
+}
+
+int pp_result_size(pp_ctx* ctx, uint64_t* total, uint64_t* nbins) {
+  if (!ctx || !ctx->res.valid) return fail(ctx, PP_ERR_STATE, "no run");
+  if (total) *total = result_len(ctx->res);
+  if (nbins) *nbins = ctx->res.nbins;
+  return PP_OK;
+}
+
+int pp_fetch(pp_ctx* ctx, uint64_t* bins, size_t cap) {
+  if (!ctx) return PP_ERR_INVALID;
+  int rc = fetch_cores(ctx);
+  if (rc) return rc;
+  const uint64_t need = result_len(ctx->res);
+  if (!bins || cap < need) return fail(ctx, PP_ERR_INVALID, "result needs %llu uint64", (unsigned long long)need);
+  finalize(ctx->res, 0, bins);
+  return PP_OK;
+}
+
+int pp_fetch_cntnb(pp_ctx* ctx, uint64_t* bins, size_t cap, uint64_t* len) {
+  if (!ctx || !len) return PP_ERR_INVALID;
+  int rc = fetch_cores(ctx);
+  if (rc) return rc;
+  const Result& R = ctx->res;
+  const RunPlan& P = R.plan;
+  if (!(P.flags & PP_CNTNB) || R.batched) return fail(ctx, PP_ERR_STATE, "last run had no PP_CNTNB");
+  const int W = P.cmax + 1;
+  // common length: largest nonzero count + 1 over all tasks
+  uint64_t L = 0;
+  std::vector<std::vector<unsigned long long>> per(R.ntasks, std::vector<unsigned long long>(W, 0));
+  for (int t = 0; t < R.ntasks; ++t) {
+    for (int c = 0; c < P.nC; ++c) {
+      if (!has_type(&R.trg[8 * t], P.ctype[c])) continue;
+      for (int e = 0; e < P.nE; ++e) {
+        if (!has_type(&R.env[8 * t], P.etype[e])) continue;
+        const unsigned long long* src = R.cnt_h.data() + ((size_t)c * P.nE + e) * W;
+        for (int v = 0; v < W; ++v) per[t][v] += src[v];
+      }
+    }
+    for (int v = W - 1; v >= 0; --v)
+      if (per[t][v]) { L = std::max<uint64_t>(L, (uint64_t)v + 1); break; }
+  }
+  *len = L;
+  if (!bins) return PP_OK;
+  if (cap < L * (uint64_t)R.ntasks) return fail(ctx, PP_ERR_INVALID, "cntnb needs %llu uint64", (unsigned long long)(L * R.ntasks));
+  for (int t = 0; t < R.ntasks; ++t)
+    for (uint64_t v = 0; v < L; ++v) bins[(uint64_t)t * L + v] = per[t][v];
+  return PP_OK;
+}
+
+int pp_run_stats(pp_ctx* ctx, uint64_t* centres, uint64_t* discarded, uint64_t* pairs) {
+  if (!ctx) return PP_ERR_INVALID;
+  int rc = fetch_cores(ctx);
+  if (rc) return rc;
+  const Result& R = ctx->res;
+  if (centres) *centres = R.counters_h[1];
+  if (discarded) *discarded = R.n_ions - R.counters_h[1];
+  if (pairs) *pairs = R.counters_h[0];
+  return PP_OK;
+}
+
+int pp_neighbors(pp_ctx* ctx, int cloud, uint64_t ion, float r, uint64_t* ids, float* d2, uint64_t cap,
+                 uint64_t* count) {
+  Cloud* cl = ctx ? get_cloud(ctx, cloud) : nullptr;
+  if (!cl || ion >= cl->n || !count || !(r > 0.f)) return fail(ctx, PP_ERR_INVALID, "bad argument");
+  CK(cudaSetDevice(ctx->device));
+  int rc = ensure_grid(ctx, *cl, r, 0);
+  if (rc) return rc;
+  uint32_t self = 0;
+  CK(cudaMemcpy(&self, cl->slot_of_id.as<uint32_t>() + ion, 4, cudaMemcpyDeviceToHost));
+  const uint32_t dcap = 1u << 22;
+  DevBuf bs, bd, bc;
+  CK(bs.ensure(dcap * 4));
+  CK(bd.ensure(dcap * 4));
+  CK(bc.ensure(4));
+  CK(cudaMemset(bc.p, 0, 4));
+  pp::launch_neighbors(cl->ions.as<float4>(), cl->cell_start.as<uint32_t>(), cl->g, self, r, nullptr,
+                       bs.as<uint32_t>(), bd.as<float>(), dcap, bc.as<uint32_t>(), 0);
+  CK(cudaGetLastError());
+  uint32_t cnt = 0;
+  CK(cudaMemcpy(&cnt, bc.p, 4, cudaMemcpyDeviceToHost));
+  if (cnt > dcap) return fail(ctx, PP_ERR_OVERFLOW, "more than %u neighbours", dcap);
+  std::vector<uint32_t> slots(cnt), id_of(cl->n);
+  std::vector<float> dd(cnt);
+  CK(cudaMemcpy(slots.data(), bs.p, cnt * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(dd.data(), bd.p, cnt * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(id_of.data(), cl->id_of_slot.p, cl->n * 4, cudaMemcpyDeviceToHost));
+  std::vector<std::pair<float, uint64_t>> v(cnt);
+  for (uint32_t k = 0; k < cnt; ++k) {
+    const uint32_t idx = id_of[slots[k]];
+    v[k] = {dd[k], cl->ids.empty() ? (uint64_t)idx : (uint64_t)cl->ids[idx]};
+  }
+  std::sort(v.begin(), v.end());
+  *count = cnt;
+  for (uint64_t k = 0; k < cnt && k < cap; ++k) {
+    if (ids) ids[k] = v[k].second;
+    if (d2) d2[k] = v[k].first;
+  }
+  return PP_OK;
+}
+
+int pp_shuffle_labels(const uint8_t* label, uint64_t n, uint64_t seed, uint8_t* out) {
+  if ((n && (!label || !out))) return PP_ERR_INVALID;
+  pp_host::shuffle_labels(label, n, seed, out);
+  return PP_OK;
+}
+
+// ------------------------------------------------------------- batched
+int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk, int include_original,
+                   const uint8_t* label_sets, int n_label_sets, const float* rois, int n_rois, void* stream) {
+  if (!ctx) return PP_ERR_INVALID;
+  Cloud* cl = get_cloud(ctx, cloud);
+  if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
+  if (n_label_sets < 0 || n_rois < 0 || (n_label_sets && !label_sets) || (n_rois && !rois))
+    return fail(ctx, PP_ERR_INVALID, "bad realisation arguments");
+  if (flags & PP_CNTNB) return fail(ctx, PP_ERR_UNSUPPORTED, "PP_CNTNB is provided by pp_run only");
+  const int nreal = (include_original ? 1 : 0) + n_label_sets + n_rois;
+  if (nreal == 0) return fail(ctx, PP_ERR_INVALID, "no realisation requested");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  RunPlan P;
+  int rc = make_plan(ctx, flags, k_list, nk, P);
+  if (rc) return rc;
+  if (P.H > 65535) return fail(ctx, PP_ERR_UNSUPPORTED, "batched runs hold categories in 16 bits");
+  const float R = ctx->tab.rmax;
+  if ((rc = ensure_grid(ctx, *cl, R, s))) return rc;
+  if ((rc = ensure_surface(ctx, *cl, R, s))) return rc;
+  const uint64_t n = cl->n;
+  DevTables D{};
+  if ((rc = upload_tables(ctx, P, D, s))) return rc;
+  if ((rc = alloc_result(ctx, P, nreal, true, s))) return rc;
+
+  // ---- geometry: per-centre pair lists sorted by category (cached)
+  const bool geo_hit = ctx->geo_cloud == cloud && ctx->geo_key_version == cl->grid_version && ctx->geo_R == R &&
+                       ctx->geo_H == P.H && ctx->geo_rmin == ctx->tab.rmin && ctx->geo_rincr == ctx->tab.rincr &&
+                       cl->surf_version == cl->grid_version;
+  if (!geo_hit) {
+    CK(ctx->geo_centres.ensure(std::max<uint64_t>(n, 1) * 4));
+    CK(ctx->centre_count.ensure(8));
+    CK(cudaMemsetAsync(ctx->centre_count.p, 0, 8, s));
+    pp::launch_select_centres(cl->label_sorted.as<uint8_t>(), cl->surf.as<float>(), n, R * R, nullptr, nullptr,
+                              ctx->geo_centres.as<uint32_t>(), ctx->centre_count.as<uint32_t>(), s);
+    uint32_t nc = 0;
+    CK(cudaMemcpyAsync(&nc, ctx->centre_count.p, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    pp::ScanArgs a{};
+    fill_scan_common(a, *cl, P, D, ctx->tab);
+    a.labels = cl->label_sorted.as<uint8_t>();
+    a.centres = ctx->geo_centres.as<uint32_t>();
+    a.ncentres = nc;
+    a.flags = 0;
+    a.counters = ctx->res.counters.as<unsigned long long>();
+    a.status = ctx->res.status.as<int>();
+    a.rdf_in_smem = 0;
+    CK(ctx->work.ensure(16));
+    CK(ctx->pair_count.ensure((std::max<uint64_t>(nc, 1)) * 4));
+    CK(ctx->pair_off.ensure((std::max<uint64_t>(nc, 1) + 1) * 8));
+    unsigned long long total = 0;
+    if (nc) {
+      CK(cudaMemsetAsync(ctx->work.p, 0, 16, s));
+      a.mode = 1;
+      a.pair_count = ctx->pair_count.as<uint32_t>();
+      a.work = ctx->work.as<uint32_t>();
+      if (pp::launch_scan(a, 0, 1, ctx->sm_count, nullptr, s)) return fail(ctx, PP_ERR_CUDA, "pair count launch failed");
+      const uint64_t tmp_elems = (uint64_t)(nc + 1) / 2048 + 64;
+      CK(ctx->scan_tmp.ensure(tmp_elems * 8 * 2));
+      CK(cudaMemsetAsync(ctx->pair_count.as<uint32_t>() + 0, 0, 0, s));
+      // offsets: exclusive scan of counts, plus the total in slot nc
+      DevBuf cnt1;
+      CK(cnt1.ensure(((uint64_t)nc + 1) * 4));
+      CK(cudaMemcpyAsync(cnt1.p, ctx->pair_count.p, (uint64_t)nc * 4, cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemsetAsync(cnt1.as<uint32_t>() + nc, 0, 4, s));
+      pp::launch_exclusive_scan_u64_from_u32(cnt1.as<uint32_t>(), (uint64_t)nc + 1,
+                                             ctx->pair_off.as<unsigned long long>(),
+                                             ctx->scan_tmp.as<unsigned long long>(), tmp_elems * 2, s);
+      CK(cudaMemcpyAsync(&total, ctx->pair_off.as<unsigned long long>() + nc, 8, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      CK(ctx->pair_slot.ensure(std::max<unsigned long long>(total, 1) * 4));
+      CK(ctx->pair_cat.ensure(std::max<unsigned long long>(total, 1) * 2));
+      CK(cudaMemsetAsync(ctx->work.p, 0, 16, s));
+      a.mode = 2;
+      a.pair_off = ctx->pair_off.as<unsigned long long>();
+      a.pair_slot = ctx->pair_slot.as<uint32_t>();
+      a.pair_cat = ctx->pair_cat.as<uint16_t>();
+      a.pair_cap = total;
+      if (pp::launch_scan(a, 0, 1, ctx->sm_count, nullptr, s)) return fail(ctx, PP_ERR_CUDA, "pair emit launch failed");
+      CK(cudaGetLastError());
+    }
+    ctx->geo_cloud = cloud;
+    ctx->geo_key_version = cl->grid_version;
+    ctx->geo_R = R;
+    ctx->geo_H = P.H;
+    ctx->geo_rmin = ctx->tab.rmin;
+    ctx->geo_rincr = ctx->tab.rincr;
+    ctx->geo_ncentres = nc;
+    ctx->geo_pairs = total;
+    // counters were used by the geometry passes; clear them for the apply
+    CK(cudaMemsetAsync(ctx->res.counters.p, 0, 16 * (size_t)nreal, s));
+  }
+  const uint32_t nc = ctx->geo_ncentres;
+  // ---- realisation labels (sorted-slot order) and centre masks
+  CK(ctx->real_labels.ensure(std::max<uint64_t>(n, 1) * nreal));
+  CK(ctx->centre_ok.ensure(std::max<uint64_t>(nc, 1) * nreal));
+  int r = 0;
+  uint8_t* RL = ctx->real_labels.as<uint8_t>();
+  uint8_t* OK = ctx->centre_ok.as<uint8_t>();
+  if (include_original) {
+    CK(cudaMemcpyAsync(RL, cl->label_sorted.p, n, cudaMemcpyDeviceToDevice, s));
+    pp::launch_perm_mask(RL, ctx->geo_centres.as<uint32_t>(), nc, D.cslot, OK, s);
+    ++r;
+  }
+  if (n_label_sets) {
+    cudaPointerAttributes attr{};
+    const bool on_dev = cudaPointerGetAttributes(&attr, label_sets) == cudaSuccess && attr.type == cudaMemoryTypeDevice;
+    cudaGetLastError();
+    const uint8_t* src = label_sets;
+    if (!on_dev) {
+      CK(ctx->gather_src.ensure(std::max<uint64_t>(n, 1) * n_label_sets));
+      CK(cudaMemcpyAsync(ctx->gather_src.p, label_sets, n * (uint64_t)n_label_sets, cudaMemcpyHostToDevice, s));
+      src = ctx->gather_src.as<uint8_t>();
+    }
+    pp::launch_gather_labels(src, cl->id_of_slot.as<uint32_t>(), n, RL + (uint64_t)r * n, n_label_sets, s);
+    for (int q = 0; q < n_label_sets; ++q)
+      pp::launch_perm_mask(RL + (uint64_t)(r + q) * n, ctx->geo_centres.as<uint32_t>(), nc, D.cslot,
+                           OK + (uint64_t)(r + q) * nc, s);
+    r += n_label_sets;
+  }
+  if (n_rois) {
+    for (int q = 0; q < n_rois; ++q)
+      CK(cudaMemcpyAsync(RL + (uint64_t)(r + q) * n, cl->label_sorted.p, n, cudaMemcpyDeviceToDevice, s));
+    CK(ctx->rois_dev.ensure((size_t)n_rois * 16));
+    CK(cudaMemcpyAsync(ctx->rois_dev.p, rois, (size_t)n_rois * 16, cudaMemcpyHostToDevice, s));
+    pp::launch_roi_mask(cl->ions.as<float4>(), ctx->geo_centres.as<uint32_t>(), nc, ctx->rois_dev.as<float>(), n_rois,
+                        R, cl->label_sorted.as<uint8_t>(), D.cslot, OK + (uint64_t)r * nc, s);
+    r += n_rois;
+  }
+  CK(cudaGetLastError());
+  // ---- apply every realisation in one persistent launch
+  if (nc) {
+    CK(ctx->work.ensure(16));
+    CK(cudaMemsetAsync(ctx->work.p, 0, 16, s));
+    pp::ApplyArgs b{};
+    b.centres = ctx->geo_centres.as<uint32_t>();
+    b.ncentres = nc;
+    b.pair_off = ctx->pair_off.as<unsigned long long>();
+    b.pair_slot = ctx->pair_slot.as<uint32_t>();
+    b.pair_cat = ctx->pair_cat.as<uint16_t>();
+    b.labels = RL;
+    b.centre_ok = OK;
+    b.n = n;
+    b.nreal = nreal;
+    b.H = P.H;
+    b.cat_miss = P.cat_miss;
+    b.cslot_of = D.cslot;
+    b.eslot_of = D.eslot;
+    b.nC = P.nC;
+    b.nE = P.nE;
+    b.envbits = D.envbits;
+    b.set_list = D.set_list;
+    b.nsets = D.nsets;
+    b.nS = P.nS;
+    b.kvals = D.kvals;
+    b.nkI = (int)P.kvals.size();
+    b.flags = ((flags & (PP_RDF | PP_RIPK)) ? PP_RDF : 0) | (P.kr ? PP_MKNN : 0);
+    b.rdf_core = ctx->res.rdf.as<unsigned long long>();
+    b.knn_core = ctx->res.knn.as<unsigned long long>();
+    b.counters = ctx->res.counters.as<unsigned long long>();
+    const double avg = nc ? (double)ctx->geo_pairs / nc : 1.0;
+    b.tile = (uint32_t)std::max(32.0, std::min(4096.0, 65536.0 / std::max(avg, 1.0)));
+    b.work = ctx->work.as<uint32_t>();
+    b.status = ctx->res.status.as<int>();
+    rc = pp::launch_apply(b, ctx->sm_count, s);
+    if (rc == -2) return fail(ctx, PP_ERR_UNSUPPORTED, "RDF bins of one realisation exceed shared memory");
+    if (rc) return fail(ctx, PP_ERR_CUDA, "apply launch failed");
+  }
+  ctx->res.valid = true;
+  return PP_OK;
+}
+
+int pp_batched_count(pp_ctx* ctx, int* n) {
+  if (!ctx || !n || !ctx->res.valid || !ctx->res.batched) return fail(ctx, PP_ERR_STATE, "no batched run");
+  *n = ctx->res.nreal;
+  return PP_OK;
+}
+
+int pp_fetch_batched(pp_ctx* ctx, int r, uint64_t* bins, size_t cap) {
+  if (!ctx || !ctx->res.valid || !ctx->res.batched) return fail(ctx, PP_ERR_STATE, "no batched run");
+  if (r < 0 || r >= ctx->res.nreal) return fail(ctx, PP_ERR_INVALID, "bad realisation");
+  int rc = fetch_cores(ctx);
+  if (rc) return rc;
+  const uint64_t need = result_len(ctx->res);
+  if (!bins || cap < need) return fail(ctx, PP_ERR_INVALID, "result needs %llu uint64", (unsigned long long)need);
+  finalize(ctx->res, r, bins);
+  return PP_OK;
+}
+
+int pp_batched_stats(pp_ctx* ctx, int r, uint64_t* centres, uint64_t* pairs) {
+  if (!ctx || !ctx->res.valid || !ctx->res.batched) return fail(ctx, PP_ERR_STATE, "no batched run");
+  if (r < 0 || r >= ctx->res.nreal) return fail(ctx, PP_ERR_INVALID, "bad realisation");
+  int rc = fetch_cores(ctx);
+  if (rc) return rc;
+  if (pairs) *pairs = ctx->res.counters_h[2 * r];
+  if (centres) *centres = ctx->res.counters_h[2 * r + 1];
+  return PP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+// pp_internal.h -- structures shared by the host side of the C ABI and the
+// CUDA kernels of the spatial-statistics path.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pp {
+
+// Device status word bits (kernels never trap; they record and return).
+enum StatusBits : int {
+  ST_CNT_OVERFLOW = 1,     // a neighbour count exceeded the CNTNB capacity
+  ST_LIST_OVERFLOW = 2,    // a pair list exceeded its allocation
+  ST_BAD_SLOT = 4,         // an index left its buffer (bounds check fired)
+  ST_TYPE_RANGE = 8,       // a type id had no slot where one was required
+};
+
+// Uniform cell grid over a cloud's bounding box.  Cells are stored x-fastest
+// (cell = (z * ny + y) * nx + x) so the cells of one (y, z) row are
+// contiguous: a row of the stencil is one contiguous run of ions.
+struct Grid {
+  float lox, loy, loz;   // grid origin
+  float h, inv_h;        // cell edge and its reciprocal
+  int nx, ny, nz;
+  uint64_t ncells;
+  float margin;          // conservative slack for cell-membership rounding
+};
+
+// Everything the fused stencil-scan kernel reads.  Pointers are device memory.
+struct ScanArgs {
+  // cloud
+  const float4* ions;          // sorted by cell: x, y, z, type id (as uint bits)
+  const uint32_t* cell_start;  // ncells + 1
+  Grid g;
+  // realisation
+  const uint8_t* labels;       // type per sorted slot (plain or permuted)
+  const uint32_t* centres;     // sorted slots of the centres
+  uint32_t ncentres;
+  // geometry of the query
+  float R, R2;                 // SpatStatRadiusMax and float(R*R)
+  float Rm2;                   // (R + margin)^2 for conservative row trimming
+  // bins: categories 0 = lowest, 1..nb = bins, nb+1 = highest
+  int H;                       // nb + 2
+  const float* cat_T;          // [H] smallest d^2 of each category (index 0 unused)
+  float guess_start, guess_scale;
+  int cat_miss;                // category of the float R + EPSILON
+  // type maps
+  const int8_t* cslot_of;      // [256] centre slot of a type or -1
+  const int8_t* eslot_of;      // [256] environment slot of a type or -1
+  int nC, nE;
+  const uint32_t* envbits;     // [nC][256] bit p: type is in the p-th env set of slot c
+  const int* set_list;         // [nC][32] global env-set id of the p-th local set
+  const int* nsets;            // [nC]
+  int nS;                      // global env sets
+  const int* kvals;            // [nkI] internal k list (1-based)
+  int nkI, kmax;
+  uint32_t flags;              // PP_RDF | PP_MKNN (1NN is k = 1) | PP_CNTNB
+  // outputs (uint64 atomics)
+  unsigned long long* rdf_core;  // [nC][nE][H]
+  unsigned long long* knn_core;  // [nC][nS][nkI][H]
+  unsigned long long* cnt_core;  // [nC][nE][cmax + 1]
+  int cmax;
+  unsigned long long* counters;  // [0] pairs [1] centres
+  uint32_t* work;                // dynamic work counter
+  int* status;
+  int rdf_in_smem;
+  // pair-list mode (batched geometry)
+  int mode;                      // 0 = fused bins, 1 = count pairs, 2 = emit lists
+  uint32_t* pair_count;          // [ncentres] (mode 1)
+  const unsigned long long* pair_off;  // [ncentres] (mode 2)
+  uint32_t* pair_slot;           // [total] (mode 2)
+  uint16_t* pair_cat;            // [total] (mode 2)
+  unsigned long long pair_cap;
+};
+
+// Realisation pass over stored pair lists (batched null models and ROIs).
+struct ApplyArgs {
+  const uint32_t* centres;       // sorted slots of the geometry centres
+  uint32_t ncentres;
+  const unsigned long long* pair_off;  // [ncentres + 1]
+  const uint32_t* pair_slot;
+  const uint16_t* pair_cat;
+  const uint8_t* labels;         // [nreal][n] type per sorted slot
+  const uint8_t* centre_ok;      // [nreal][ncentres] 1 if a centre in that realisation (nullable = all)
+  uint64_t n;
+  int nreal;
+  int H, cat_miss;
+  const int8_t* cslot_of;
+  const int8_t* eslot_of;
+  int nC, nE;
+  const uint32_t* envbits;
+  const int* set_list;
+  const int* nsets;
+  int nS;
+  const int* kvals;
+  int nkI;
+  uint32_t flags;
+  unsigned long long* rdf_core;  // [nreal][nC][nE][H]
+  unsigned long long* knn_core;  // [nreal][nC][nS][nkI][H]
+  unsigned long long* counters;  // [nreal][2] pairs, centres
+  uint32_t tile;                 // centres per work item
+  uint32_t* work;
+  int* status;
+};
+
+// kernel launchers (pp_kernels.cu)
+void launch_bbox(const float* xyz, uint64_t n, float* d_minmax, cudaStream_t s);
+void launch_bbox_pos(const uint32_t* be, uint64_t n, float* d_minmax, cudaStream_t s);
+void launch_decode_pos(const uint32_t* be, uint64_t n, const float* lo, const float* hi,
+                       const uint8_t* type, int nranges, float* xyz, uint8_t* label, cudaStream_t s);
+void launch_cell_count(const float* xyz, uint64_t n, Grid g, uint32_t* cell_of, uint32_t* rank,
+                       uint32_t* counts, cudaStream_t s);
+void launch_exclusive_scan_u32(uint32_t* data, uint64_t n, uint32_t* tmp, uint64_t tmp_elems,
+                               cudaStream_t s);
+void launch_scatter(const float* xyz, const uint8_t* label, uint64_t n, const uint32_t* cell_of,
+                    const uint32_t* rank, const uint32_t* cell_start, float4* ions,
+                    uint32_t* slot_of_id, uint32_t* id_of_slot, uint8_t* label_sorted,
+                    cudaStream_t s);
+void launch_gather_labels(const uint8_t* src_by_id, const uint32_t* id_of_slot, uint64_t n,
+                          uint8_t* dst_by_slot, int nsets, cudaStream_t s);
+void launch_permute_labels(const uint8_t* label_by_id, const uint32_t* perm, const uint32_t* id_of_slot,
+                           uint64_t n, uint8_t* dst_by_slot, cudaStream_t s);
+void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const float* tri,
+                    const uint32_t* tcell_start, const uint32_t* tcell_tri, Grid tg, float rprime,
+                    float* surf_d2, cudaStream_t s);
+void launch_select_centres(const uint8_t* labels, const float* surf_d2, uint64_t n, float R2,
+                           const int8_t* cslot_of, const uint8_t* extra_mask, uint32_t* out,
+                           uint32_t* count, cudaStream_t s);
+void launch_select_any(const float* surf_d2, const uint8_t* any_mask, uint64_t n, float R2,
+                       uint32_t* out, uint32_t* count, cudaStream_t s);
+int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s);
+int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s);
+void launch_roi_mask(const float4* ions, const uint32_t* centres, uint32_t ncentres, const float* rois,
+                     int nrois, float R, const uint8_t* labels, const int8_t* cslot_of,
+                     uint8_t* centre_ok, cudaStream_t s);
+void launch_perm_mask(const uint8_t* labels_r, const uint32_t* centres, uint32_t ncentres,
+                      const int8_t* cslot_of, uint8_t* centre_ok, cudaStream_t s);
+void launch_exclusive_scan_u64_from_u32(const uint32_t* in, uint64_t n, unsigned long long* out,
+                                        unsigned long long* tmp, uint64_t tmp_elems, cudaStream_t s);
+void launch_neighbors(const float4* ions, const uint32_t* cell_start, Grid g, uint32_t self,
+                      float R, const uint32_t* id_of_slot, uint32_t* out_slot, float* out_d2,
+                      uint32_t cap, uint32_t* count, cudaStream_t s);
+
+}  // namespace pp

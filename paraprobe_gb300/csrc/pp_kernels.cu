@@ -1,0 +1,968 @@
+// pp_kernels.cu -- sm_103a kernels of the GB300 spatial-statistics path.
+//
+//  K0 k_decode_pos     big-endian POS records -> xyz + ranged type ids
+//  K1 k_cell_count / k_scan_* / k_scatter
+//                      uniform-grid counting sort: ions -> cell-sorted float4
+//                      records (x-fastest cells, so stencil rows are contiguous)
+//  K2 k_surface        squared ion-to-hull distance, same candidate test and
+//                      float evaluation order as the reference
+//  K3 k_scan<KR,EMAX>  warp-per-centre scan of the trimmed cell stencil: RDF
+//                      bins in shared memory, kNN as register-resident sorted
+//                      lists, neighbour counts; or pair-list count / emit
+//  K5 k_apply          batched realisations over stored per-centre pair lists
+//
+// Floating-point rules.  Every quantity that decides a count is evaluated with
+// round-to-nearest intrinsics in the reference's source order and without
+// contraction (the library is built with --fmad=false as well):
+//   d^2 = ((xi-xj)^2 + (yi-yj)^2) + (zi-zj)^2   src/PARAPROBE_KDTree.h:55-58
+// Histogram bins are found by comparing d^2 with a host-built threshold table
+// (the smallest float d^2 of each category under histogram::add,
+// src/PARAPROBE_Histogram.h:97-117), so no double arithmetic runs per pair.
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "pp_internal.h"
+#include "pp_host.h"
+#include "../../include/paraprobe_gb300.h"
+
+namespace pp {
+
+#define FULL 0xffffffffu
+
+__device__ __forceinline__ float kInf() { return __int_as_float(0x7f800000); }
+
+__device__ __forceinline__ float dist2(float ax, float ay, float az, float bx, float by, float bz) {
+  const float dx = __fsub_rn(ax, bx), dy = __fsub_rn(ay, by), dz = __fsub_rn(az, bz);
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// ------------------------------------------------------------------ K0 / bbox
+__device__ __forceinline__ uint32_t f2o(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// d_minmax holds 6 order-preserving keys (min x,y,z as min keys, max x,y,z)
+// plus a count of non-finite coordinates.
+__global__ void k_bbox(const float* __restrict__ xyz, uint64_t n, uint32_t* out) {
+  uint32_t mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0, 0, 0};
+  uint32_t bad = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float v = xyz[3 * i + k];
+      if (!isfinite(v)) { ++bad; continue; }
+      const uint32_t o = f2o(v);
+      mn[k] = min(mn[k], o);
+      mx[k] = max(mx[k], o);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    for (int o = 16; o; o >>= 1) {
+      mn[k] = min(mn[k], __shfl_xor_sync(FULL, mn[k], o));
+      mx[k] = max(mx[k], __shfl_xor_sync(FULL, mx[k], o));
+    }
+  }
+  for (int o = 16; o; o >>= 1) bad += __shfl_xor_sync(FULL, bad, o);
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { atomicMin(&out[k], mn[k]); atomicMax(&out[3 + k], mx[k]); }
+    if (bad) atomicAdd(&out[6], bad);
+  }
+}
+
+__device__ __forceinline__ float be2f(uint32_t u) { return __uint_as_float(__byte_perm(u, 0, 0x0123)); }
+
+// POS ingest: byte swap (src/PARAPROBE_EPOSEndianness.h:54-79) and ranging
+// (PeriodicTable::mq2ionname, src/PARAPROBE_PeriodicTable.cpp:65-91: the first
+// range with !(mq < lo) && !(mq > hi) in type order wins, else type 0).
+__global__ void k_decode_pos(const uint4* __restrict__ rec, uint64_t n, const float* __restrict__ lo,
+                             const float* __restrict__ hi, const uint8_t* __restrict__ ty, int nr,
+                             float* __restrict__ xyz, uint8_t* __restrict__ label) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint4 r = rec[i];
+    xyz[3 * i] = be2f(r.x);
+    xyz[3 * i + 1] = be2f(r.y);
+    xyz[3 * i + 2] = be2f(r.z);
+    const float mq = be2f(r.w);
+    uint8_t t = 0;
+    for (int k = 0; k < nr; ++k) {
+      if (!(mq < lo[k]) && !(mq > hi[k])) { t = ty[k]; break; }
+    }
+    label[i] = t;
+  }
+}
+
+// -------------------------------------------------------------------- K1 grid
+__device__ __forceinline__ int cell_coord(float v, float lo, float inv_h, int n) {
+  int c = (int)floorf((v - lo) * inv_h);
+  return c < 0 ? 0 : (c >= n ? n - 1 : c);
+}
+
+__global__ void k_cell_count(const float* __restrict__ xyz, uint64_t n, Grid g, uint32_t* __restrict__ cell_of,
+                             uint32_t* __restrict__ rank, uint32_t* __restrict__ counts) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const int cx = cell_coord(xyz[3 * i], g.lox, g.inv_h, g.nx);
+    const int cy = cell_coord(xyz[3 * i + 1], g.loy, g.inv_h, g.ny);
+    const int cz = cell_coord(xyz[3 * i + 2], g.loz, g.inv_h, g.nz);
+    const uint32_t c = ((uint32_t)cz * (uint32_t)g.ny + (uint32_t)cy) * (uint32_t)g.nx + (uint32_t)cx;
+    cell_of[i] = c;
+    rank[i] = atomicAdd(&counts[c], 1u);
+  }
+}
+
+// Three-phase exclusive scan: per-block scan (4 items per thread), scan of the
+// block sums (recursively), add-back.
+constexpr int SCAN_T = 512, SCAN_I = 4, SCAN_B = SCAN_T * SCAN_I;
+
+template <typename T>
+__device__ T block_excl_scan(T v, T* warp_sums, T* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  T inc = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const T t = __shfl_up_sync(FULL, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) warp_sums[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    T s = (lane < (int)(blockDim.x >> 5)) ? warp_sums[lane] : T(0);
+    T si = s;
+    for (int o = 1; o < 32; o <<= 1) {
+      const T t = __shfl_up_sync(FULL, si, o);
+      if (lane >= o) si += t;
+    }
+    warp_sums[lane] = si - s;
+    if (lane == 31) *total = si;
+  }
+  __syncthreads();
+  return warp_sums[w] + inc - v;
+}
+
+template <typename T>
+__global__ void k_scan_blocks(T* data, uint64_t n, T* block_sums) {
+  __shared__ T ws[32];
+  __shared__ T tot;
+  const uint64_t base = (uint64_t)blockIdx.x * SCAN_B + (uint64_t)threadIdx.x * SCAN_I;
+  T v[SCAN_I];
+  T s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_I; ++k) { v[k] = (base + k < n) ? data[base + k] : T(0); s += v[k]; }
+  T off = block_excl_scan<T>(s, ws, &tot);
+#pragma unroll
+  for (int k = 0; k < SCAN_I; ++k) {
+    if (base + k < n) data[base + k] = off;
+    off += v[k];
+  }
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+
+template <typename T>
+__global__ void k_scan_add(T* data, uint64_t n, const T* block_off) {
+  const uint64_t base = (uint64_t)blockIdx.x * SCAN_B + (uint64_t)threadIdx.x * SCAN_I;
+  const T o = block_off[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < SCAN_I; ++k)
+    if (base + k < n) data[base + k] += o;
+}
+
+template <typename T>
+static void excl_scan(T* data, uint64_t n, T* tmp, uint64_t tmp_elems, cudaStream_t s) {
+  const uint64_t nb = (n + SCAN_B - 1) / SCAN_B;
+  if (nb == 0) return;
+  k_scan_blocks<T><<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp);
+  if (nb > 1) {
+    excl_scan<T>(tmp, nb, tmp + nb, tmp_elems - nb, s);
+    k_scan_add<T><<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp);
+  }
+}
+
+__global__ void k_u32_to_u64(const uint32_t* in, uint64_t n, unsigned long long* out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = in[i];
+}
+
+__global__ void k_scatter(const float* __restrict__ xyz, const uint8_t* __restrict__ label, uint64_t n,
+                          const uint32_t* __restrict__ cell_of, const uint32_t* __restrict__ rank,
+                          const uint32_t* __restrict__ cell_start, float4* __restrict__ ions,
+                          uint32_t* __restrict__ slot_of_id, uint32_t* __restrict__ id_of_slot,
+                          uint8_t* __restrict__ label_sorted) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t slot = cell_start[cell_of[i]] + rank[i];
+    const uint32_t lab = label[i];
+    ions[slot] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], __uint_as_float(lab));
+    slot_of_id[i] = slot;
+    id_of_slot[slot] = (uint32_t)i;
+    label_sorted[slot] = (uint8_t)lab;
+  }
+}
+
+// label sets given in input order -> sorted-slot order, nsets arrays at once
+__global__ void k_gather_labels(const uint8_t* __restrict__ src, const uint32_t* __restrict__ id_of_slot,
+                                uint64_t n, uint8_t* __restrict__ dst, int nsets) {
+  const uint64_t total = n * (uint64_t)nsets;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t r = t / n, slot = t - r * n;
+    dst[t] = src[r * n + id_of_slot[slot]];
+  }
+}
+
+// shuffled label of ion i = label[perm[i]]; written in sorted-slot order
+__global__ void k_permute_labels(const uint8_t* __restrict__ label_by_id, const uint32_t* __restrict__ perm,
+                                 const uint32_t* __restrict__ id_of_slot, uint64_t n, uint8_t* __restrict__ dst) {
+  for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t id = id_of_slot[s];
+    const uint32_t src = perm[id];
+    dst[s] = (src < n) ? label_by_id[src] : 0;
+  }
+}
+
+// ------------------------------------------------------------------- K2 hull
+__device__ __forceinline__ float clamp01(float x) {
+  const float lo = (x < 0.f) ? 0.f : x;  // MAX(x, 0.f) of src/PARAPROBE_Abinitio.h:48
+  return (lo < 1.f) ? lo : 1.f;           // MIN(., 1.f)
+}
+
+// Squared distance to the closest point of a triangle: the region analysis of
+// D. Eberly, "Distance Between Point and Triangle in 3D", evaluated in the
+// order of src/PARAPROBE_Math.cpp:88-184 (region-6 fallback included).
+__device__ float tri_dist2(const float* __restrict__ t, float px, float py, float pz) {
+  const float e0x = __fsub_rn(t[3], t[0]), e0y = __fsub_rn(t[4], t[1]), e0z = __fsub_rn(t[5], t[2]);
+  const float e1x = __fsub_rn(t[6], t[0]), e1y = __fsub_rn(t[7], t[1]), e1z = __fsub_rn(t[8], t[2]);
+  const float vx = __fsub_rn(t[0], px), vy = __fsub_rn(t[1], py), vz = __fsub_rn(t[2], pz);
+  const float a = __fadd_rn(__fadd_rn(__fmul_rn(e0x, e0x), __fmul_rn(e0y, e0y)), __fmul_rn(e0z, e0z));
+  const float b = __fadd_rn(__fadd_rn(__fmul_rn(e0x, e1x), __fmul_rn(e0y, e1y)), __fmul_rn(e0z, e1z));
+  const float c = __fadd_rn(__fadd_rn(__fmul_rn(e1x, e1x), __fmul_rn(e1y, e1y)), __fmul_rn(e1z, e1z));
+  const float d = __fadd_rn(__fadd_rn(__fmul_rn(e0x, vx), __fmul_rn(e0y, vy)), __fmul_rn(e0z, vz));
+  const float e = __fadd_rn(__fadd_rn(__fmul_rn(e1x, vx), __fmul_rn(e1y, vy)), __fmul_rn(e1z, vz));
+  const float det = __fsub_rn(__fmul_rn(a, c), __fmul_rn(b, b));
+  float s = __fsub_rn(__fmul_rn(b, e), __fmul_rn(c, d));
+  float u = __fsub_rn(__fmul_rn(b, d), __fmul_rn(a, e));
+  if (__fadd_rn(s, u) < det) {
+    if (s < 0.f) {
+      if (u < 0.f) {
+        if (d < 0.f) { s = clamp01(__fdiv_rn(-d, a)); u = 0.f; }
+        else { s = 0.f; u = clamp01(__fdiv_rn(-e, c)); }
+      } else { s = 0.f; u = clamp01(__fdiv_rn(-e, c)); }
+    } else if (u < 0.f) {
+      s = clamp01(__fdiv_rn(-d, a)); u = 0.f;
+    } else {
+      const float inv = __fdiv_rn(1.f, det);
+      s = __fmul_rn(s, inv); u = __fmul_rn(u, inv);
+    }
+  } else {
+    const float den = __fadd_rn(__fsub_rn(a, __fmul_rn(2.f, b)), c);
+    if (s < 0.f) {
+      const float t0 = __fadd_rn(b, d), t1 = __fadd_rn(c, e);
+      if (t1 > t0) { s = clamp01(__fdiv_rn(__fsub_rn(t1, t0), den)); u = __fsub_rn(1.f, s); }
+      else { u = clamp01(__fdiv_rn(-e, c)); s = 0.f; }
+    } else if (u < 0.f) {
+      if (__fadd_rn(a, d) > __fadd_rn(b, e)) {
+        const float num = __fsub_rn(__fsub_rn(__fadd_rn(c, e), b), d);
+        s = clamp01(__fdiv_rn(num, den)); u = __fsub_rn(1.f, s);
+      } else { s = clamp01(__fdiv_rn(-e, c)); u = 0.f; }
+    } else {
+      const float num = __fsub_rn(__fsub_rn(__fadd_rn(c, e), b), d);
+      s = clamp01(__fdiv_rn(num, den)); u = __fsub_rn(1.f, s);
+    }
+  }
+  const float cx = __fadd_rn(__fadd_rn(t[0], __fmul_rn(s, e0x)), __fmul_rn(u, e1x));
+  const float cy = __fadd_rn(__fadd_rn(t[1], __fmul_rn(s, e0y)), __fmul_rn(u, e1y));
+  const float cz = __fadd_rn(__fadd_rn(t[2], __fmul_rn(s, e0z)), __fmul_rn(u, e1z));
+  const float qx = __fsub_rn(cx, px), qy = __fsub_rn(cy, py), qz = __fsub_rn(cz, pz);
+  return __fadd_rn(__fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy)), __fmul_rn(qz, qz));
+}
+
+// ion2surf per sorted slot: R'^2, lowered to the smallest tri_dist2 over the
+// triangles whose float AABB overlaps [p - R', p + R'] (touching counts,
+// src/PARAPROBE_AABBTree.cpp:112-124).  Triangles are pre-binned (host) into
+// every cell of `tg` that their AABB grown by R' reaches.
+__global__ void k_surface(const float4* __restrict__ ions, uint64_t n, const float* __restrict__ tbox,
+                          const float* __restrict__ tri, const uint32_t* __restrict__ tstart,
+                          const uint32_t* __restrict__ tlist, Grid tg, float rp, float* __restrict__ out) {
+  const float rp2 = __fmul_rn(rp, rp);
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const float4 p = ions[i];
+    float best = rp2;
+    const int cx = (int)floorf((p.x - tg.lox) * tg.inv_h), cy = (int)floorf((p.y - tg.loy) * tg.inv_h),
+              cz = (int)floorf((p.z - tg.loz) * tg.inv_h);
+    if (cx >= 0 && cy >= 0 && cz >= 0 && cx < tg.nx && cy < tg.ny && cz < tg.nz) {
+      const uint64_t c = ((uint64_t)cz * tg.ny + cy) * tg.nx + cx;
+      const float lx = __fsub_rn(p.x, rp), ly = __fsub_rn(p.y, rp), lz = __fsub_rn(p.z, rp);
+      const float hx = __fadd_rn(p.x, rp), hy = __fadd_rn(p.y, rp), hz = __fadd_rn(p.z, rp);
+      for (uint32_t k = tstart[c]; k < tstart[c + 1]; ++k) {
+        const uint32_t t = tlist[k];
+        const float* b = tbox + 6 * (uint64_t)t;
+        if (b[3] < lx || b[0] > hx || b[4] < ly || b[1] > hy || b[5] < lz || b[2] > hz) continue;
+        const float v = tri_dist2(tri + 9 * (uint64_t)t, p.x, p.y, p.z);
+        if (!(v > best)) best = v;
+      }
+    }
+    out[i] = best;
+  }
+}
+
+// --------------------------------------------------------- centre selection
+// Centre filter of src/PARAPROBE_SolverHdl.cpp:3847-3859: the type is a target
+// of some task and ion2surf >= R^2 (plus an optional extra mask).  Output is
+// compacted per warp; order across warps is not preserved (results are
+// integer counts, independent of the order).
+__global__ void k_select(const uint8_t* __restrict__ labels, const float* __restrict__ surf, uint64_t n,
+                         float R2, const int8_t* __restrict__ cslot_of, const uint8_t* __restrict__ extra,
+                         uint32_t* __restrict__ out, uint32_t* __restrict__ count) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < n; base += stride) {
+    const uint64_t i = base + threadIdx.x;
+    bool ok = false;
+    if (i < n) {
+      const bool target = cslot_of ? (cslot_of[labels[i]] >= 0) : true;
+      ok = target && (surf[i] >= R2) && (extra ? extra[i] != 0 : true);
+    }
+    const uint32_t m = __ballot_sync(FULL, ok);
+    uint32_t pos = 0;
+    if (lane == 0 && m) pos = atomicAdd(count, (uint32_t)__popc(m));
+    pos = __shfl_sync(FULL, pos, 0);
+    if (ok) out[pos + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+  }
+}
+
+// --------------------------------------------------------------- K3 the scan
+__device__ __forceinline__ int category(float d2, const float* __restrict__ sT, int H, float gs, float gk) {
+  int g = (int)((sqrtf(d2) - gs) * gk) + 1;
+  g = g < 0 ? 0 : (g > H - 1 ? H - 1 : g);
+  while (g + 1 < H && sT[g + 1] <= d2) ++g;
+  while (g > 0 && sT[g] > d2) --g;
+  return g;
+}
+
+template <int KR>
+__device__ __forceinline__ void list_insert(float (&l)[KR], float x, int lane) {
+  int pos = 0;
+#pragma unroll
+  for (int r = 0; r < KR; ++r) pos += __popc(__ballot_sync(FULL, l[r] <= x));
+  float prev[KR];
+#pragma unroll
+  for (int r = 0; r < KR; ++r) {
+    const float up = __shfl_up_sync(FULL, l[r], 1);
+    const float carry = (r > 0) ? __shfl_sync(FULL, l[r > 0 ? r - 1 : 0], 31) : 0.f;
+    prev[r] = (lane == 0) ? carry : up;
+  }
+#pragma unroll
+  for (int r = 0; r < KR; ++r) {
+    const int idx = r * 32 + lane;
+    if (idx > pos) l[r] = prev[r];
+    else if (idx == pos) l[r] = x;
+  }
+}
+
+// element e = row * 32 + src of the distributed list (row, src may differ per lane)
+template <int KR>
+__device__ __forceinline__ float list_get(const float (&l)[KR], int row, int src) {
+  float v = 0.f;
+#pragma unroll
+  for (int r = 0; r < KR; ++r) {
+    const float t = __shfl_sync(FULL, l[r], src);
+    if (r == row) v = t;
+  }
+  return v;
+}
+
+struct ScanShared {
+  float* T;
+  int8_t* cs;
+  int8_t* es;
+  uint32_t* env;
+  uint32_t* rdf;
+  uint32_t* cnt;
+  int* hist;  // mode 2: per-warp category histogram
+  unsigned long long* since_flush;
+};
+
+// Iterates the candidates of one centre: every ion of every stencil row
+// (y, z) whose cells can hold a point within R + margin, with the row's x
+// range trimmed to the ball.  Rows are compacted and their ions streamed 32 at
+// a time across the warp; f(valid, slot, d2, inball, type) is called
+// warp-uniformly once per 32 candidates.
+template <class F>
+__device__ __forceinline__ void for_each_candidate(const ScanArgs& a, float4 cp, uint32_t self, int lane, F&& f) {
+  const Grid& g = a.g;
+  const float ext = a.R + g.margin;
+  auto clampc = [](int c, int n) { return c < 0 ? 0 : (c >= n ? n - 1 : c); };
+  const int y0 = clampc((int)floorf((cp.y - ext - g.loy) * g.inv_h), g.ny);
+  const int y1 = clampc((int)floorf((cp.y + ext - g.loy) * g.inv_h), g.ny);
+  const int z0 = clampc((int)floorf((cp.z - ext - g.loz) * g.inv_h), g.nz);
+  const int z1 = clampc((int)floorf((cp.z + ext - g.loz) * g.inv_h), g.nz);
+  const int nyr = y1 - y0 + 1;
+  const int nrows = nyr * (z1 - z0 + 1);
+  const uint32_t lemask = (2u << lane) - 1u;
+  for (int r0 = 0; r0 < nrows; r0 += 32) {
+    const int r = r0 + lane;
+    uint32_t st = 0, len = 0;
+    if (r < nrows) {
+      const int yy = y0 + r % nyr, zz = z0 + r / nyr;
+      const float ylo = g.loy + (float)yy * g.h - g.margin, yhi = g.loy + (float)(yy + 1) * g.h + g.margin;
+      const float zlo = g.loz + (float)zz * g.h - g.margin, zhi = g.loz + (float)(zz + 1) * g.h + g.margin;
+      const float dy = fmaxf(0.f, fmaxf(ylo - cp.y, cp.y - yhi));
+      const float dz = fmaxf(0.f, fmaxf(zlo - cp.z, cp.z - zhi));
+      const float rem = a.Rm2 - dy * dy - dz * dz;
+      if (rem >= 0.f) {
+        const float half = sqrtf(rem) + g.margin;
+        const int x0 = clampc((int)floorf((cp.x - half - g.lox) * g.inv_h), g.nx);
+        const int x1 = clampc((int)floorf((cp.x + half - g.lox) * g.inv_h), g.nx);
+        const uint64_t cb = ((uint64_t)zz * g.ny + yy) * g.nx;
+        st = a.cell_start[cb + x0];
+        len = a.cell_start[cb + x1 + 1] - st;
+      }
+    }
+    const uint32_t ne = __ballot_sync(FULL, len > 0);
+    const int cnt = __popc(ne);
+    if (cnt == 0) continue;
+    const int src = (lane < cnt) ? (int)__fns(ne, 0, lane + 1) : 0;
+    const uint32_t rst = __shfl_sync(FULL, st, src);
+    uint32_t rlen = __shfl_sync(FULL, len, src);
+    if (lane >= cnt) rlen = 0;
+    uint32_t inc = rlen;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(FULL, inc, o);
+      if (lane >= o) inc += t;
+    }
+    const uint32_t exc = inc - rlen;
+    const uint32_t total = __shfl_sync(FULL, inc, 31);
+    int before = 0;
+    for (uint32_t b = 0; b < total; b += 32) {
+      const uint32_t bitv = (lane < cnt && rlen > 0 && exc >= b && exc < b + 32) ? (1u << (exc - b)) : 0u;
+      const uint32_t sm = __reduce_or_sync(FULL, bitv);
+      const int row = before + __popc(sm & lemask) - 1;
+      before += __popc(sm);
+      const int rowc = row < 0 ? 0 : (row > 31 ? 31 : row);
+      const uint32_t rs = __shfl_sync(FULL, rst, rowc);
+      const uint32_t rp = __shfl_sync(FULL, exc, rowc);
+      const uint32_t t = b + lane;
+      const bool valid = t < total;
+      const uint32_t slot = rs + (t - rp);
+      float d2 = kInf();
+      uint32_t m = 0;
+      bool inball = false;
+      if (valid) {
+        const float4 q = __ldg(a.ions + slot);
+        d2 = dist2(cp.x, cp.y, cp.z, q.x, q.y, q.z);
+        inball = (d2 <= a.R2) && (slot != self);
+        m = a.labels ? (uint32_t)a.labels[slot] : __float_as_uint(q.w);
+      }
+      f(valid, slot, d2, inball, m);
+    }
+  }
+}
+
+template <int KR, int EMAX>
+__global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int H = a.H;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  ScanShared S;
+  {
+    unsigned char* p = smem;
+    S.since_flush = (unsigned long long*)p; p += 16;
+    S.T = (float*)p; p += ((H + 3) & ~3) * 4;
+    S.cs = (int8_t*)p; p += 256;
+    S.es = (int8_t*)p; p += 256;
+    S.env = (uint32_t*)p; p += (KR > 0 ? a.nC * 256 * 4 : 0);
+    S.rdf = (uint32_t*)p; p += (a.rdf_in_smem ? a.nC * a.nE * H * 4 : 0);
+    S.cnt = (uint32_t*)p; p += ((a.flags & PP_CNTNB) ? nwarps * a.nE * 4 : 0);
+    S.hist = (int*)p;
+  }
+  for (int i = threadIdx.x; i < H; i += blockDim.x) S.T[i] = a.cat_T[i];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) { S.cs[i] = a.cslot_of[i]; S.es[i] = a.eslot_of[i]; }
+  if (KR > 0) for (int i = threadIdx.x; i < a.nC * 256; i += blockDim.x) S.env[i] = a.envbits[i];
+  if (a.rdf_in_smem) for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) S.rdf[i] = 0;
+  if (a.flags & PP_CNTNB) for (int i = threadIdx.x; i < nwarps * a.nE; i += blockDim.x) S.cnt[i] = 0;
+  if (a.mode == 2) for (int i = threadIdx.x; i < nwarps * H; i += blockDim.x) S.hist[i] = 0;
+  if (threadIdx.x == 0) *S.since_flush = 0ull;
+  __syncthreads();
+
+  const bool doR = (a.flags & PP_RDF) && a.mode == 0;
+  const bool doC = (a.flags & PP_CNTNB) && a.mode == 0;
+  const bool doK = KR > 0 && a.mode == 0;
+  const int krow = (a.kmax - 1) >> 5, klane = (a.kmax - 1) & 31;
+  unsigned long long pairs_lane = 0, centres = 0;
+  constexpr uint32_t CHUNK = 4;
+  constexpr unsigned long long FLUSH = 1ull << 30;
+
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(a.work, CHUNK);
+    base = __shfl_sync(FULL, base, 0);
+    if (base >= a.ncentres) break;
+    const uint32_t end = min(base + CHUNK, a.ncentres);
+    for (uint32_t ci = base; ci < end; ++ci) {
+      const uint32_t self = a.centres[ci];
+      const float4 cp = a.ions[self];
+      const uint32_t ct = a.labels ? (uint32_t)a.labels[self] : __float_as_uint(cp.w);
+      const int cs = (a.mode == 0) ? S.cs[ct & 255] : 0;
+      if (cs < 0) {  // selection guarantees a slot; record and skip otherwise
+        if (lane == 0) atomicOr(a.status, ST_TYPE_RANGE);
+        continue;
+      }
+      uint32_t inb = 0;
+      if (a.mode == 0) {
+        float lst[EMAX][KR > 0 ? KR : 1];
+        float thr[EMAX];
+        int nset = 0;
+        if (doK) {
+          nset = a.nsets[cs];
+#pragma unroll
+          for (int p = 0; p < EMAX; ++p) {
+            thr[p] = kInf();
+#pragma unroll
+            for (int r = 0; r < (KR > 0 ? KR : 1); ++r) lst[p][r] = kInf();
+          }
+        }
+        for_each_candidate(a, cp, self, lane, [&](bool valid, uint32_t slot, float d2, bool inball, uint32_t m) {
+          (void)valid; (void)slot;
+          if (inball) {
+            ++inb;
+            const int es = S.es[m & 255];
+            if (doR && es >= 0) {
+              const int cat = category(d2, S.T, H, a.guess_start, a.guess_scale);
+              const uint32_t idx = ((uint32_t)cs * a.nE + es) * H + cat;
+              if (a.rdf_in_smem) atomicAdd(&S.rdf[idx], 1u);
+              else atomicAdd(&a.rdf_core[idx], 1ull);
+            }
+            if (doC && es >= 0) atomicAdd(&S.cnt[warp * a.nE + es], 1u);
+          }
+          if constexpr (KR > 0) {
+            if (doK) {
+              const uint32_t eb = inball ? S.env[cs * 256 + (m & 255)] : 0u;
+#pragma unroll
+              for (int p = 0; p < EMAX; ++p) {
+                if (p < nset) {
+                  uint32_t mask = __ballot_sync(FULL, ((eb >> p) & 1u) && d2 < thr[p]);
+                  while (mask) {
+                    const int srcl = __ffs(mask) - 1;
+                    const float x = __shfl_sync(FULL, d2, srcl);
+                    list_insert<KR>(lst[p], x, lane);
+                    thr[p] = list_get<KR>(lst[p], krow, klane);
+                    mask &= ~(1u << srcl);
+                    mask &= __ballot_sync(FULL, d2 < thr[p]);
+                  }
+                }
+              }
+            }
+          }
+        });
+        if constexpr (KR > 0) {
+          if (doK) {
+#pragma unroll
+            for (int p = 0; p < EMAX; ++p) {
+              if (p < nset) {
+                const int Sg = a.set_list[cs * 32 + p];
+                for (int k0 = 0; k0 < a.nkI; k0 += 32) {
+                  const int kk = k0 + lane;
+                  const int e = (kk < a.nkI) ? a.kvals[kk] - 1 : 0;
+                  const float v = list_get<KR>(lst[p], e >> 5, e & 31);
+                  if (kk < a.nkI) {
+                    const int cat = (v == kInf()) ? a.cat_miss : category(v, S.T, H, a.guess_start, a.guess_scale);
+                    atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
+                  }
+                }
+              }
+            }
+          }
+        }
+        if (doC) {
+          __syncwarp();
+          for (int es = lane; es < a.nE; es += 32) {
+            uint32_t c = S.cnt[warp * a.nE + es];
+            S.cnt[warp * a.nE + es] = 0;
+            if ((int)c > a.cmax) { atomicOr(a.status, ST_CNT_OVERFLOW); c = a.cmax; }
+            atomicAdd(&a.cnt_core[((uint64_t)cs * a.nE + es) * (a.cmax + 1) + c], 1ull);
+          }
+          __syncwarp();
+        }
+      } else if (a.mode == 1) {
+        for_each_candidate(a, cp, self, lane, [&](bool, uint32_t, float, bool inball, uint32_t) { inb += inball; });
+        uint32_t tot = inb;
+        for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+        if (lane == 0) a.pair_count[ci] = tot;
+      } else {
+        // mode 2: counting sort of the ball by category into the pair list
+        int* hist = S.hist + warp * H;
+        for_each_candidate(a, cp, self, lane, [&](bool, uint32_t, float d2, bool inball, uint32_t) {
+          if (inball) atomicAdd(&hist[category(d2, S.T, H, a.guess_start, a.guess_scale)], 1);
+        });
+        __syncwarp();
+        int run = 0;
+        for (int h0 = 0; h0 < H; h0 += 32) {
+          const int h = h0 + lane;
+          const int v = (h < H) ? hist[h] : 0;
+          int inc = v;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc += t;
+          }
+          if (h < H) hist[h] = run + inc - v;
+          run += __shfl_sync(FULL, inc, 31);
+        }
+        __syncwarp();
+        const unsigned long long off = a.pair_off[ci];
+        const unsigned long long lim = a.pair_off[ci + 1];
+        for_each_candidate(a, cp, self, lane, [&](bool, uint32_t slot, float d2, bool inball, uint32_t) {
+          if (inball) {
+            const int cat = category(d2, S.T, H, a.guess_start, a.guess_scale);
+            const unsigned long long at = off + (unsigned long long)atomicAdd(&hist[cat], 1);
+            if (at < lim && at < a.pair_cap) { a.pair_slot[at] = slot; a.pair_cat[at] = (uint16_t)cat; }
+            else atomicOr(a.status, ST_LIST_OVERFLOW);
+            ++inb;
+          }
+        });
+        __syncwarp();
+        for (int h = lane; h < H; h += 32) hist[h] = 0;
+        __syncwarp();
+      }
+      pairs_lane += inb;
+      if (lane == 0) ++centres;
+      if (a.rdf_in_smem && doR) {
+        // Exchange-based flush keeps every shared bin below 2^32: each time
+        // the block's pair count crosses a multiple of 2^30 the warp that
+        // crossed it moves all bins to the global uint64 core.
+        uint32_t tot = inb;
+        for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+        unsigned long long old = 0;
+        if (lane == 0) old = atomicAdd(S.since_flush, (unsigned long long)tot);
+        old = __shfl_sync(FULL, old, 0);
+        if (old / FLUSH != (old + tot) / FLUSH) {
+          for (int i = lane; i < a.nC * a.nE * H; i += 32) {
+            const uint32_t v = atomicExch(&S.rdf[i], 0u);
+            if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
+          }
+        }
+      }
+    }
+  }
+  for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
+  if (lane == 0) {
+    atomicAdd(&a.counters[0], pairs_lane);
+    atomicAdd(&a.counters[1], centres);
+  }
+  __syncthreads();
+  if (a.rdf_in_smem && doR) {
+    for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) {
+      const uint32_t v = S.rdf[i];
+      if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
+    }
+  }
+}
+
+// --------------------------------------------------------------- K5 batched
+// One work item = a tile of geometry centres; the block applies every
+// realisation to the tile's stored (slot, category) lists, which are sorted
+// by category per centre.  RDF bins of the current realisation accumulate in
+// shared memory and are flushed before the next realisation; the k-th nearest
+// member of an environment set is the k-th member met walking the sorted list.
+__global__ void __launch_bounds__(256) k_apply(ApplyArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int H = a.H;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  int8_t* sC = (int8_t*)smem;
+  int8_t* sE = sC + 256;
+  uint32_t* sEnv = (uint32_t*)(sE + 256);
+  const int nenv = (a.flags & PP_MKNN) ? a.nC * 256 : 0;
+  uint32_t* sRdf = sEnv + nenv;
+  const int nrdf = (a.flags & PP_RDF) ? a.nC * a.nE * H : 0;
+  __shared__ uint32_t s_item;
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) { sC[i] = a.cslot_of[i]; sE[i] = a.eslot_of[i]; }
+  for (int i = threadIdx.x; i < nenv; i += blockDim.x) sEnv[i] = a.envbits[i];
+  for (int i = threadIdx.x; i < nrdf; i += blockDim.x) sRdf[i] = 0;
+  __syncthreads();
+  const uint32_t ntiles = (a.ncentres + a.tile - 1) / a.tile;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(a.work, 1u);
+    __syncthreads();
+    const uint32_t item = s_item;
+    __syncthreads();
+    if (item >= ntiles) break;
+    const uint32_t c0 = item * a.tile, c1 = min(c0 + a.tile, a.ncentres);
+    for (int r = 0; r < a.nreal; ++r) {
+      const uint8_t* lab = a.labels + (uint64_t)r * a.n;
+      const uint8_t* ok = a.centre_ok ? a.centre_ok + (uint64_t)r * a.ncentres : nullptr;
+      unsigned long long pairs_lane = 0, cen = 0;
+      for (uint32_t ci = c0 + warp; ci < c1; ci += nwarps) {
+        if (ok && !ok[ci]) continue;
+        const uint32_t self = a.centres[ci];
+        const int cs = sC[lab[self]];
+        if (cs < 0) continue;
+        const unsigned long long o0 = a.pair_off[ci], o1 = a.pair_off[ci + 1];
+        if (lane == 0) ++cen;
+        // RDF: every list entry of an environment type
+        if (a.flags & PP_RDF) {
+          for (unsigned long long k = o0 + lane; k < o1; k += 32) {
+            const int es = sE[lab[a.pair_slot[k]]];
+            if (es >= 0) atomicAdd(&sRdf[((uint32_t)cs * a.nE + es) * H + a.pair_cat[k]], 1u);
+          }
+        }
+        if (lane == 0) pairs_lane += (o1 - o0);
+        // kNN: walk the category-sorted list, counting members of each set
+        if (a.flags & PP_MKNN) {
+          const int nset = a.nsets[cs];
+          for (int p = 0; p < nset; ++p) {
+            const int Sg = a.set_list[cs * 32 + p];
+            // lane kk looks for the kvals[kk]-th member of set p
+            for (int k0 = 0; k0 < a.nkI; k0 += 32) {
+              const int kk = k0 + lane;
+              const uint32_t want = (kk < a.nkI) ? (uint32_t)a.kvals[kk] : 0u;
+              bool done = (kk >= a.nkI);
+              int found = -1;
+              uint32_t seen = 0;
+              for (unsigned long long k = o0; k < o1; k += 32) {
+                const unsigned long long e = k + lane;
+                uint32_t bit = 0;
+                int cat = 0;
+                if (e < o1) {
+                  cat = a.pair_cat[e];
+                  bit = (sEnv[cs * 256 + lab[a.pair_slot[e]]] >> p) & 1u;
+                }
+                const uint32_t mem = __ballot_sync(FULL, bit);
+                const uint32_t c = __popc(mem);
+                const bool here = !done && want > seen && want <= seen + c;
+                const int at = here ? (int)__fns(mem, 0, want - seen) : 0;
+                const int cv = __shfl_sync(FULL, cat, at);
+                if (here) { found = cv; done = true; }
+                seen += c;
+                if (__all_sync(FULL, done)) break;
+              }
+              if (kk < a.nkI) {
+                const int cat = (found >= 0) ? found : a.cat_miss;
+                atomicAdd(&a.knn_core[((((uint64_t)r * a.nC + cs) * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
+              }
+            }
+          }
+        }
+      }
+      for (int o = 16; o; o >>= 1) {
+        pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
+        cen += __shfl_xor_sync(FULL, cen, o);
+      }
+      if (lane == 0 && (pairs_lane || cen)) {
+        atomicAdd(&a.counters[2 * r], pairs_lane);
+        atomicAdd(&a.counters[2 * r + 1], cen);
+      }
+      __syncthreads();
+      if (nrdf) {
+        unsigned long long* dst = a.rdf_core + (uint64_t)r * a.nC * a.nE * H;
+        for (int i = threadIdx.x; i < nrdf; i += blockDim.x) {
+          const uint32_t v = sRdf[i];
+          if (v) { atomicAdd(&dst[i], (unsigned long long)v); sRdf[i] = 0; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// centre_ok for ROI realisations: type is a target, and r_roi - |p - c| >= R
+// evaluated in float as sqrt((px-cx)^2 + (py-cy)^2 + (pz-cz)^2).
+__global__ void k_roi_mask(const float4* __restrict__ ions, const uint32_t* __restrict__ centres, uint32_t nc,
+                           const float* __restrict__ rois, int nrois, float R, const uint8_t* __restrict__ labels,
+                           const int8_t* __restrict__ cslot_of, uint8_t* __restrict__ ok) {
+  const uint64_t total = (uint64_t)nc * nrois;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t q = (uint32_t)(t / nc), ci = (uint32_t)(t - (uint64_t)q * nc);
+    const uint32_t s = centres[ci];
+    const float4 p = ions[s];
+    const float* c = rois + 4 * q;
+    const float dd = sqrtf(dist2(p.x, p.y, p.z, c[0], c[1], c[2]));
+    ok[t] = (cslot_of[labels[s]] >= 0) && (__fsub_rn(c[3], dd) >= R);
+  }
+}
+
+__global__ void k_perm_mask(const uint8_t* __restrict__ lab, const uint32_t* __restrict__ centres, uint32_t nc,
+                            const int8_t* __restrict__ cslot_of, uint8_t* __restrict__ ok) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < nc; t += (uint64_t)gridDim.x * blockDim.x)
+    ok[t] = cslot_of[lab[centres[t]]] >= 0;
+}
+
+// all ions j != self with d^2 <= R^2 in the full 3-D stencil (debug / parity)
+__global__ void k_neighbors(const float4* __restrict__ ions, const uint32_t* __restrict__ cell_start, Grid g,
+                            uint32_t self, float R, uint32_t* out_slot, float* out_d2, uint32_t cap,
+                            uint32_t* count) {
+  const float4 cp = ions[self];
+  const float R2 = __fmul_rn(R, R);
+  const float ext = R + g.margin;
+  auto cl = [](int c, int n) { return c < 0 ? 0 : (c >= n ? n - 1 : c); };
+  const int x0 = cl((int)floorf((cp.x - ext - g.lox) * g.inv_h), g.nx), x1 = cl((int)floorf((cp.x + ext - g.lox) * g.inv_h), g.nx);
+  const int y0 = cl((int)floorf((cp.y - ext - g.loy) * g.inv_h), g.ny), y1 = cl((int)floorf((cp.y + ext - g.loy) * g.inv_h), g.ny);
+  const int z0 = cl((int)floorf((cp.z - ext - g.loz) * g.inv_h), g.nz), z1 = cl((int)floorf((cp.z + ext - g.loz) * g.inv_h), g.nz);
+  const int ny = y1 - y0 + 1, nz = z1 - z0 + 1;
+  for (int r = blockIdx.x; r < ny * nz; r += gridDim.x) {
+    const int yy = y0 + r % ny, zz = z0 + r / ny;
+    const uint64_t cb = ((uint64_t)zz * g.ny + yy) * g.nx;
+    const uint32_t s0 = cell_start[cb + x0], s1 = cell_start[cb + x1 + 1];
+    for (uint32_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+      const float4 q = ions[s];
+      const float d2 = dist2(cp.x, cp.y, cp.z, q.x, q.y, q.z);
+      if (d2 <= R2 && s != self) {
+        const uint32_t at = atomicAdd(count, 1u);
+        if (at < cap) { out_slot[at] = s; out_d2[at] = d2; }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+inline unsigned grid_for(uint64_t n, int threads, unsigned cap = 152u * 16u) {
+  uint64_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  return (unsigned)(b > cap ? cap : b);
+}
+
+void launch_bbox(const float* xyz, uint64_t n, float* d_minmax, cudaStream_t s) {
+  k_bbox<<<grid_for(n, 256), 256, 0, s>>>(xyz, n, reinterpret_cast<uint32_t*>(d_minmax));
+}
+
+void launch_decode_pos(const uint32_t* be, uint64_t n, const float* lo, const float* hi, const uint8_t* type,
+                       int nranges, float* xyz, uint8_t* label, cudaStream_t s) {
+  k_decode_pos<<<grid_for(n, 256), 256, 0, s>>>(reinterpret_cast<const uint4*>(be), n, lo, hi, type, nranges, xyz, label);
+}
+
+void launch_cell_count(const float* xyz, uint64_t n, Grid g, uint32_t* cell_of, uint32_t* rank, uint32_t* counts,
+                       cudaStream_t s) {
+  k_cell_count<<<grid_for(n, 256), 256, 0, s>>>(xyz, n, g, cell_of, rank, counts);
+}
+
+void launch_exclusive_scan_u32(uint32_t* data, uint64_t n, uint32_t* tmp, uint64_t tmp_elems, cudaStream_t s) {
+  excl_scan<uint32_t>(data, n, tmp, tmp_elems, s);
+}
+
+void launch_exclusive_scan_u64_from_u32(const uint32_t* in, uint64_t n, unsigned long long* out,
+                                        unsigned long long* tmp, uint64_t tmp_elems, cudaStream_t s) {
+  k_u32_to_u64<<<grid_for(n, 256), 256, 0, s>>>(in, n, out);
+  excl_scan<unsigned long long>(out, n, tmp, tmp_elems, s);
+}
+
+void launch_scatter(const float* xyz, const uint8_t* label, uint64_t n, const uint32_t* cell_of, const uint32_t* rank,
+                    const uint32_t* cell_start, float4* ions, uint32_t* slot_of_id, uint32_t* id_of_slot,
+                    uint8_t* label_sorted, cudaStream_t s) {
+  k_scatter<<<grid_for(n, 256), 256, 0, s>>>(xyz, label, n, cell_of, rank, cell_start, ions, slot_of_id, id_of_slot,
+                                             label_sorted);
+}
+
+void launch_gather_labels(const uint8_t* src, const uint32_t* id_of_slot, uint64_t n, uint8_t* dst, int nsets,
+                          cudaStream_t s) {
+  k_gather_labels<<<grid_for(n * (uint64_t)nsets, 256), 256, 0, s>>>(src, id_of_slot, n, dst, nsets);
+}
+
+void launch_permute_labels(const uint8_t* label_by_id, const uint32_t* perm, const uint32_t* id_of_slot, uint64_t n,
+                           uint8_t* dst, cudaStream_t s) {
+  k_permute_labels<<<grid_for(n, 256), 256, 0, s>>>(label_by_id, perm, id_of_slot, n, dst);
+}
+
+void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const float* tri, const uint32_t* tcs,
+                    const uint32_t* tct, Grid tg, float rprime, float* surf, cudaStream_t s) {
+  k_surface<<<grid_for(n, 256), 256, 0, s>>>(ions, n, tri_box, tri, tcs, tct, tg, rprime, surf);
+}
+
+void launch_select_centres(const uint8_t* labels, const float* surf, uint64_t n, float R2, const int8_t* cslot_of,
+                           const uint8_t* extra, uint32_t* out, uint32_t* count, cudaStream_t s) {
+  k_select<<<grid_for(n, 256), 256, 0, s>>>(labels, surf, n, R2, cslot_of, extra, out, count);
+}
+
+void launch_select_any(const float* surf, const uint8_t* any_mask, uint64_t n, float R2, uint32_t* out,
+                       uint32_t* count, cudaStream_t s) {
+  k_select<<<grid_for(n, 256), 256, 0, s>>>(any_mask, surf, n, R2, nullptr, any_mask, out, count);
+}
+
+template <int KR, int EMAX>
+static int launch_scan_t(const ScanArgs& a, int sm_count, size_t smem, cudaStream_t s) {
+  auto kern = k_scan<KR, EMAX>;
+  if (smem > 48 * 1024) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem) != cudaSuccess || per_sm < 1) return -1;
+  const int blocks = sm_count * per_sm;
+  kern<<<blocks, 256, smem, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s) {
+  const int nwarps = 8;
+  size_t smem = 16 + (size_t)((a.H + 3) & ~3) * 4 + 512;
+  if (kr > 0) smem += (size_t)a.nC * 256 * 4;
+  if (a.rdf_in_smem) smem += (size_t)a.nC * a.nE * a.H * 4;
+  if (a.flags & PP_CNTNB) smem += (size_t)nwarps * a.nE * 4;
+  if (a.mode == 2) smem += (size_t)nwarps * a.H * 4;
+  if (smem_used) *smem_used = smem;
+  if (kr == 0) return launch_scan_t<0, 1>(a, sm_count, smem, s);
+  if (kr == 1) {
+    if (emax <= 1) return launch_scan_t<1, 1>(a, sm_count, smem, s);
+    if (emax <= 8) return launch_scan_t<1, 8>(a, sm_count, smem, s);
+    return launch_scan_t<1, 32>(a, sm_count, smem, s);
+  }
+  if (kr <= 4) {
+    if (emax <= 1) return launch_scan_t<4, 1>(a, sm_count, smem, s);
+    if (emax <= 8) return launch_scan_t<4, 8>(a, sm_count, smem, s);
+  }
+  return -2;
+}
+
+int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s) {
+  size_t smem = 512;
+  if (a.flags & PP_MKNN) smem += (size_t)a.nC * 256 * 4;
+  if (a.flags & PP_RDF) smem += (size_t)a.nC * a.nE * a.H * 4;
+  if (smem > 200 * 1024) return -2;
+  if (smem > 48 * 1024) {
+    if (cudaFuncSetAttribute(k_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply, 256, smem) != cudaSuccess || per_sm < 1) return -1;
+  k_apply<<<sm_count * per_sm, 256, smem, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+void launch_roi_mask(const float4* ions, const uint32_t* centres, uint32_t nc, const float* rois, int nrois, float R,
+                     const uint8_t* labels, const int8_t* cslot_of, uint8_t* ok, cudaStream_t s) {
+  k_roi_mask<<<grid_for((uint64_t)nc * nrois, 256), 256, 0, s>>>(ions, centres, nc, rois, nrois, R, labels, cslot_of, ok);
+}
+
+void launch_perm_mask(const uint8_t* lab, const uint32_t* centres, uint32_t nc, const int8_t* cslot_of, uint8_t* ok,
+                      cudaStream_t s) {
+  k_perm_mask<<<grid_for(nc, 256), 256, 0, s>>>(lab, centres, nc, cslot_of, ok);
+}
+
+void launch_neighbors(const float4* ions, const uint32_t* cell_start, Grid g, uint32_t self, float R,
+                      const uint32_t* id_of_slot, uint32_t* out_slot, float* out_d2, uint32_t cap, uint32_t* count,
+                      cudaStream_t s) {
+  (void)id_of_slot;
+  k_neighbors<<<64, 256, 0, s>>>(ions, cell_start, g, self, R, out_slot, out_d2, cap, count);
+}
+
+}  // namespace pp
+
+// ------------------------------------------------------------- small helpers
+namespace pp_host {
+
+__global__ void k_gather_f32(const float* __restrict__ src, const uint32_t* __restrict__ id_of_slot, uint64_t n,
+                             float* __restrict__ dst) {
+  for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x)
+    dst[s] = src[id_of_slot[s]];
+}
+
+__global__ void k_fill_f32(float* __restrict__ dst, uint64_t n, float v) {
+  for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x)
+    dst[s] = v;
+}
+
+void gather_f32_sorted(const float* src, const uint32_t* id_of_slot, uint64_t n, float* dst, cudaStream_t s) {
+  k_gather_f32<<<pp::grid_for(n, 256), 256, 0, s>>>(src, id_of_slot, n, dst);
+}
+
+void fill_f32(float* dst, uint64_t n, float v, cudaStream_t s) {
+  k_fill_f32<<<pp::grid_for(n, 256), 256, 0, s>>>(dst, n, v);
+}
+
+}  // namespace pp_host

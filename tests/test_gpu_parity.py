@@ -1,0 +1,147 @@
+"""GPU path (through the C ABI) against the CPU oracle on seeded clouds.
+
+Counts must be bit-identical: the oracle restates the reference's float
+arithmetic, and the device evaluates the same expressions without
+contraction, binning through an exact threshold table.
+"""
+import numpy as np
+import pytest
+
+from paraprobe_gb300 import native as N
+from paraprobe_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+ALL = N.PP_RDF | N.PP_1NN | N.PP_RIPK | N.PP_MKNN
+
+
+def _run_both(ctx, oracle, spec, rmin, rincr, rmax, flags, trg, env, ks, surf=None, perm_labels=None, carve=2.0):
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, carve)
+    ctx.tasks(trg, env)
+    ctx.hist(rmin, rincr, rmax)
+    perm = None
+    labels = spec.labels
+    if perm_labels is not None:
+        perm, labels = perm_labels
+    ctx.run(cid, flags, ks, label_perm=perm)
+    gpu = ctx.fetch()
+    st = ctx.stats()
+    gs = ctx.surfdist_fetch(cid, spec.xyz.shape[0])
+    rp = max(np.float32(rmax), np.float32(carve))
+    cs = oracle.surface_distance(spec.xyz, spec.hull, rp)
+    assert np.array_equal(gs.view(np.uint32), cs.view(np.uint32)), "ion2surf differs"
+    ref = oracle.spatstat(spec.xyz, labels, cs, rmin, rincr, rmax, flags, trg, env, ks)
+    cnt = None
+    if flags & N.PP_CNTNB:
+        cnt = ctx.fetch_cntnb()
+    ctx.free(cid)
+    return gpu, st, ref, cnt
+
+
+def test_cylinder_all_analyses(ctx, oracle):
+    spec = synth.cylinder_specimen(n=40000, radius=6.0, height=24.0, seed=11, nseg=96, stack=4.0)
+    trg = [[2], [1], [2, 3]]
+    env = [[1, 2, 3], [2], [3]]
+    gpu, st, ref, _ = _run_both(ctx, oracle, spec, 0.0, 0.01, 1.0, ALL, trg, env, [10, 5, 1])
+    assert st["centres"] == ref["centres"]
+    assert st["pairs"] == ref["pairs"]
+    assert gpu.shape == ref["bins"].shape
+    bad = np.nonzero(gpu != ref["bins"])[0]
+    assert bad.size == 0, f"{bad.size} bins differ, first {bad[:10]}"
+
+
+def test_cone_all_pairs_knn(ctx, oracle):
+    spec = synth.cone_specimen(n=60000, r_apex=8.0, half_angle_deg=10.0, length=20.0, n_clusters=30,
+                               members=40, nspecies=4, seed=5, nseg=96, stack=4.0)
+    types = [1, 2, 3, 4]
+    trg = [[a] for a in types for b in types]
+    env = [[b] for a in types for b in types]
+    gpu, st, ref, _ = _run_both(ctx, oracle, spec, 0.0, 0.005, 1.5, ALL, trg, env, [8, 3, 1])
+    assert st["pairs"] == ref["pairs"]
+    assert np.array_equal(gpu, ref["bins"])
+
+
+def test_cntnb(ctx, oracle):
+    spec = synth.cylinder_specimen(n=20000, radius=5.0, height=16.0, seed=3, nseg=64, stack=4.0)
+    trg, env = [[2], [1, 2]], [[1, 2, 3], [3]]
+    gpu, st, ref, cnt = _run_both(ctx, oracle, spec, 0.0, 0.02, 1.2, N.PP_RDF | N.PP_CNTNB, trg, env, [])
+    L = cnt.shape[1]
+    assert np.array_equal(cnt, ref["cntnb"][:, :L])
+    assert ref["cntnb"][:, L:].sum() == 0
+
+
+def test_nonzero_rmin_and_coarse_bins(ctx, oracle):
+    spec = synth.cylinder_specimen(n=20000, radius=5.0, height=16.0, seed=4, nseg=64, stack=4.0)
+    trg, env = [[1], [2]], [[1, 2, 3], [1]]
+    # 0.1 nm bins over [0.3, 1.3]: (1.0/0.1f) truncates to 9 bins, d == R goes to the upper dump
+    gpu, st, ref, _ = _run_both(ctx, oracle, spec, 0.3, 0.1, 1.3, ALL, trg, env, [40, 2])
+    assert ref["nbins"] == 9
+    assert np.array_equal(gpu, ref["bins"])
+
+
+def test_large_k_register_rows(ctx, oracle):
+    spec = synth.cylinder_specimen(n=30000, radius=5.0, height=20.0, seed=8, nseg=64, stack=4.0)
+    trg, env = [[1], [2]], [[1, 2, 3], [1, 2]]
+    gpu, st, ref, _ = _run_both(ctx, oracle, spec, 0.0, 0.01, 1.3, N.PP_MKNN | N.PP_1NN, trg, env, [100, 64, 33, 7])
+    assert np.array_equal(gpu, ref["bins"])
+
+
+def test_label_permutation(ctx, oracle):
+    spec = synth.cylinder_specimen(n=20000, radius=5.0, height=16.0, seed=9, nseg=64, stack=4.0)
+    rng = np.random.default_rng(1)
+    perm = rng.permutation(spec.xyz.shape[0]).astype(np.uint32)
+    shuffled = spec.labels[perm]
+    trg, env = [[2]], [[1, 2, 3]]
+    gpu, st, ref, _ = _run_both(ctx, oracle, spec, 0.0, 0.01, 1.0, ALL, trg, env, [5, 1],
+                                perm_labels=(perm, shuffled))
+    assert np.array_equal(gpu, ref["bins"])
+
+
+def test_neighbor_sets(ctx, oracle):
+    spec = synth.cylinder_specimen(n=20000, radius=5.0, height=16.0, seed=2, nseg=64, stack=4.0)
+    cid = ctx.upload(spec.xyz, spec.labels)
+    for ion in (0, 17, 12345):
+        ids, d2 = ctx.neighbors(cid, ion, 1.0)
+        rid, rd2 = oracle.neighbors(spec.xyz, ion, 1.0)
+        assert np.array_equal(ids, rid)
+        assert np.array_equal(d2.view(np.uint32), rd2.view(np.uint32))
+    ctx.free(cid)
+
+
+def test_batched_matches_plain(ctx, oracle):
+    spec = synth.cone_specimen(n=40000, r_apex=8.0, half_angle_deg=10.0, length=16.0, n_clusters=20,
+                               members=40, nspecies=3, seed=13, nseg=64, stack=4.0)
+    types = [1, 2, 3]
+    trg = [[a] for a in types for b in types]
+    env = [[b] for a in types for b in types]
+    rmin, rincr, rmax = 0.0, 0.01, 1.2
+    ks = [8, 2, 1]
+    flags = N.PP_RDF | N.PP_1NN | N.PP_MKNN
+    sets = np.stack([N.shuffle_labels(spec.labels, 100 + s) for s in range(3)])
+    rois = np.array([[0.0, 0.0, 8.0, 6.0], [2.0, -1.0, 5.0, 3.5]], dtype=np.float32)
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks(trg, env)
+    ctx.hist(rmin, rincr, rmax)
+    ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets, rois=rois)
+    assert ctx.batched_count() == 1 + 3 + 2
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    outs = [ctx.fetch_batched(r) for r in range(6)]
+    ref0 = oracle.spatstat(spec.xyz, spec.labels, surf, rmin, rincr, rmax, flags, trg, env, ks)
+    assert np.array_equal(outs[0], ref0["bins"])
+    for q in range(3):
+        refq = oracle.spatstat(spec.xyz, sets[q], surf, rmin, rincr, rmax, flags, trg, env, ks)
+        assert np.array_equal(outs[1 + q], refq["bins"]), f"label set {q}"
+    for q in range(2):
+        c = rois[q]
+        d = np.sqrt(((spec.xyz - c[:3]) ** 2).sum(axis=1, dtype=np.float32)).astype(np.float32)
+        # the device evaluates |p-c| from the float d^2 expression; recompute it the same way
+        dx = (spec.xyz[:, 0] - c[0]).astype(np.float32)
+        dy = (spec.xyz[:, 1] - c[1]).astype(np.float32)
+        dz = (spec.xyz[:, 2] - c[2]).astype(np.float32)
+        d = np.sqrt((dx * dx + dy * dy) + dz * dz).astype(np.float32)
+        mask = ((np.float32(c[3]) - d) >= np.float32(rmax)).astype(np.uint8)
+        refq = oracle.spatstat(spec.xyz, spec.labels, surf, rmin, rincr, rmax, flags, trg, env, ks, centre_mask=mask)
+        assert np.array_equal(outs[4 + q], refq["bins"]), f"roi {q}"
+    ctx.free(cid)
