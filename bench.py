@@ -1,0 +1,421 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 spatial-statistics path: neighbour pairs/s.
+
+Default workload ("tip20m", the plain-method tip configuration): 20,000,000
+ions in a truncated cone (apex radius 30 nm, half-angle 10 deg, length 200 nm;
+density follows from N and the geometry, 13.42 nm^-3), Poisson matrix plus
+2,000 Gaussian solute clusters (sigma 1.5 nm, 50 members, species 1/2 at
+70/30 %), three iid minority species -- six species in all.  One step is the
+two passes the reference needs for that configuration (it has one bin width
+per run): all 36 pairwise RDFs to R = 2.0 nm in 0.01 nm bins, then kNN
+k = 1..10 for all 36 pairs in 0.005 nm bins, both with centres excluded within
+R of the triangulated cone surface.  A neighbour pair is one in-ball
+(centre, neighbour) pair of one pass.
+
+`value` times the passes on a resident cloud (CUDA events on the launching
+stream); `e2e` times the public C ABI from pinned host buffers (upload, hull,
+both passes, result fetch).  The cloud (320 MB of cell-sorted records) is
+larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Under torchrun each rank runs an independent replica (the path does not
+shard); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "neighbour pairs/s"
+UNIT = "pairs/s"
+BYTES_PER_PAIR = 16  # one float4 {x, y, z, type} neighbour record per in-ball pair
+
+
+# ------------------------------------------------------------------ workloads
+def workload(name):
+    from paraprobe_gb300 import synth
+    if name in ("tip20m", "tip10m"):
+        n = 20_000_000 if name == "tip20m" else 10_000_000
+        rho = 20_000_000 / synth.cone_volume(30.0, 10.0, 200.0)
+        length = 200.0 if name == "tip20m" else synth.cone_length_for(n, rho, 30.0, 10.0)
+        spec = synth.cone_specimen(n=n, r_apex=30.0, half_angle_deg=10.0, length=length,
+                                   n_clusters=2000 * n // 20_000_000, sigma=1.5, members=50,
+                                   cluster_p=(0.7, 0.3), iid=(0.02, 0.01, 0.005), nspecies=6,
+                                   seed=20261205)
+        types = list(range(1, 7))
+        trg = [[a] for a in types for b in types]
+        env = [[b] for a in types for b in types]
+        runs = [dict(flags=1, hist=(0.0, 0.01, 2.0), k=[]),
+                dict(flags=8, hist=(0.0, 0.005, 2.0), k=list(range(10, 0, -1)))]
+        cfg = {"workload": f"{name}: {n // 1_000_000}M-ion clustered truncated cone (r_apex 30 nm, 10 deg, "
+                           f"L {length:.1f} nm), 6 species, 36 pair tasks; pass 1 RDF R=2.0/0.01, pass 2 kNN "
+                           "k=1..10 R=2.0/0.005, hull-distance exclusion",
+               "ions": n, "tasks": 36, "R_nm": 2.0}
+    elif name == "cyl1m":
+        spec = synth.cylinder_specimen(n=1_000_000, radius=10.0, height=63.66, fractions=(0.90, 0.08, 0.02),
+                                       seed=20261204)
+        trg, env = [[2]], [[1, 2, 3]]
+        runs = [dict(flags=1 | 8, hist=(0.0, 0.01, 1.0), k=[10, 5, 1])]
+        cfg = {"workload": "cyl1m: 1M uniform ions in a cylinder (r 10 nm, h 63.66 nm), species 1 centres, "
+                           "RDF R=1.0/0.01 + kNN k=1,5,10 against all species",
+               "ions": 1_000_000, "tasks": 1, "R_nm": 1.0}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return spec, trg, env, runs, cfg
+
+
+# --------------------------------------------------------------------- helpers
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_bytes(workload_name):
+    """DRAM bytes per scan launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_scan_dram_traffic.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.strip().strip("|").split("|")
+        parts = [x.strip() for x in parts]
+        if len(parts) >= 3 and parts[0] == workload_name:
+            try:
+                return [float(x) for x in parts[1:3]]  # per pass
+            except ValueError:
+                continue
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = list(csv.reader(io.StringIO(open(self.path).read())))
+        os.unlink(self.path)
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def reduce_max(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------ CPU (oracle)
+def cpu_measure(spec, trg, env, runs, target_s, threads):
+    """Oracle port on a bounded sample: a random subset of centre candidates
+    (centre mask), same cloud, tasks and passes.  Returns pairs/s of the
+    statistics phase (DescrStatsThreadparallelCompute) and a description."""
+    from oracle import oracle as O
+    surf = O.surface_distance(spec.xyz, spec.hull, max(2.0, runs[0]["hist"][2]), nthreads=threads)
+    n = spec.xyz.shape[0]
+    rng = np.random.default_rng(7)
+    keys = rng.random(n)
+
+    def one(frac):
+        mask = (keys < frac).astype(np.uint8)
+        pairs = 0
+        secs = 0.0
+        for r in runs:
+            out = O.spatstat(spec.xyz, spec.labels, surf, *r["hist"], r["flags"], trg, env, r["k"],
+                             centre_mask=mask, nthreads=threads)
+            pairs += out["pairs"]
+            secs += out["compute_s"]
+        return pairs, secs
+
+    p0, s0 = one(min(1.0, 2e5 / n))
+    rate = p0 / max(s0, 1e-6)
+    frac = min(1.0, max(1e-4, (min(1.0, 2e5 / n)) * target_s / max(s0, 1e-3)))
+    p1, s1 = one(frac)
+    return p1 / max(s1, 1e-9), frac, p1, s1, rate
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args):
+    import torch
+    from paraprobe_gb300 import build as B
+    B.build()
+    from paraprobe_gb300 import native as N
+
+    world, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    spec, trg, env, runs, cfg = workload(args.workload)
+    n = spec.xyz.shape[0]
+    ctx = N.Context(local)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    # untimed: the project autotuner picks cell edge and block tile on a
+    # sample of centres of the heaviest pass
+    heavy = runs[-1]
+    ctx.tasks(trg, env)
+    ctx.hist(*heavy["hist"])
+    ratio, tile = ctx.autotune(cid, heavy["flags"], heavy["k"], sample=200000)
+
+    def step():
+        pairs = 0
+        kms = []
+        for r in runs:
+            ctx.tasks(trg, env)
+            ctx.hist(*r["hist"])
+            ctx.run(cid, r["flags"], r["k"], stream=sh)
+            ctx.fetch()
+            pairs += ctx.stats()["pairs"]
+            kms.append(ctx.last_kernel_ms())
+        return pairs, kms
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clk = Clocks(local)
+    clk.start()
+    barrier(pg)
+    launches0 = N.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    tot_pairs = 0
+    per_pass_ms = [[] for _ in runs]
+    per_pass_pairs = [0 for _ in runs]
+    for _ in range(args.steps):
+        p, kms = step()
+        tot_pairs += p
+        for i, m in enumerate(kms):
+            per_pass_ms[i].append(m)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = N.kernel_launches() - launches0
+    elapsed = e0.elapsed_time(e1) / 1e3
+    barrier(pg)
+    clocks = clk.stop()
+    # pairs per pass (same every step)
+    for i, r in enumerate(runs):
+        ctx.tasks(trg, env)
+        ctx.hist(*r["hist"])
+        ctx.run(cid, r["flags"], r["k"], stream=sh)
+        ctx.fetch()
+        per_pass_pairs[i] = ctx.stats()["pairs"]
+    t_max = reduce_max(pg, elapsed)
+    value = tot_pairs * world / t_max
+
+    # ---- end to end through the C ABI from pinned host memory
+    xyz_pin = torch.empty((n, 3), dtype=torch.float32, pin_memory=True)
+    xyz_pin.numpy()[:] = spec.xyz
+    lab_pin = torch.empty((n,), dtype=torch.uint8, pin_memory=True)
+    lab_pin.numpy()[:] = spec.labels
+    tri = np.ascontiguousarray(spec.hull, dtype=np.float32)
+
+    def e2e_step():
+        c = ctx.upload(xyz_pin.numpy(), lab_pin.numpy())
+        ctx.tuning(c, ratio, tile)
+        ctx.hull(c, tri, 2.0)
+        pairs = 0
+        d2h = 0
+        for r in runs:
+            ctx.tasks(trg, env)
+            ctx.hist(*r["hist"])
+            ctx.run(c, r["flags"], r["k"], stream=sh)
+            out = ctx.fetch()
+            d2h += out.nbytes
+            pairs += ctx.stats()["pairs"]
+        ctx.free(c)
+        return pairs, d2h
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier(pg)
+    t0 = time.perf_counter()
+    e_pairs = 0
+    d2h = 0
+    e_steps = max(1, min(args.steps, 3))
+    for _ in range(e_steps):
+        p, d2h = e2e_step()
+        e_pairs += p
+    torch.cuda.synchronize()
+    e_el = reduce_max(pg, time.perf_counter() - t0)
+    e2e = {"value": e_pairs * world / e_el, "unit": UNIT,
+           "h2d_bytes_per_step": int(n * 12 + n + tri.nbytes + 2 * len(trg) * 8 * 4 * len(runs)),
+           "d2h_bytes_per_step": int(d2h), "steps": e_steps,
+           "includes": "upload + device grid build + hull distance + all passes + result fetch"}
+
+    # ---- roofline of the dominant kernel (k_scan), measured live
+    peak, kind = peaks()
+    scan_s = sum(sum(m) for m in per_pass_ms) / 1e3
+    alg_bytes = sum(BYTES_PER_PAIR * per_pass_pairs[i] * len(per_pass_ms[i]) for i in range(len(runs)))
+    achieved = alg_bytes / scan_s / 1e9
+    tb = traffic_bytes(args.workload)
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": kind,
+            "traffic": (None if tb is None else int(sum(tb) / len(tb))),
+            "kernel": "k_scan", "kernel_ms_per_pass": [round(statistics.mean(m), 3) for m in per_pass_ms],
+            "algorithmic_bytes_per_pair": BYTES_PER_PAIR}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(cfg, passes=len(runs), pairs_per_step=int(tot_pairs // args.steps),
+                           tuning={"cell_edge_nm": round(cfg["R_nm"] / ratio, 4), "tile": tile},
+                           l2="inputs larger than L2 (cell-sorted cloud 16 B/ion), no flush",
+                           parallelism=f"replicas x{world}"),
+            "roofline": roof, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, frac, p, s, _ = cpu_measure(spec, trg, env, runs, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"oracle port (KD-tree + OpenMP, restating the reference), "
+                                          f"{frac * 100:.3f}% of ions eligible as centres "
+                                          f"({p} pairs, {s:.1f} s statistics phase)"}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference(args):
+    world, rank, local, pg = dist_setup()
+    if rank != 0:
+        if pg is not None:
+            pg.barrier()
+            pg.destroy_process_group()
+        return
+    spec, trg, env, runs, cfg = workload(args.workload)
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    surf = O.surface_distance(spec.xyz, spec.hull, max(2.0, runs[0]["hist"][2]), nthreads=threads)
+    n = spec.xyz.shape[0]
+    keys = np.random.default_rng(7).random(n)
+    frac = min(1.0, 4e5 / n) if args.workload.startswith("tip") else min(1.0, 2e5 / n)
+    mask = (keys < frac).astype(np.uint8)
+
+    def step():
+        pairs, secs = 0, 0.0
+        for r in runs:
+            out = O.spatstat(spec.xyz, spec.labels, surf, *r["hist"], r["flags"], trg, env, r["k"],
+                             centre_mask=mask, nthreads=threads)
+            pairs += out["pairs"]
+            secs += out["compute_s"]
+        return pairs, secs
+
+    for _ in range(args.warmup):
+        step()
+    tp, ts = 0, 0.0
+    for _ in range(args.steps):
+        p, s = step()
+        tp += p
+        ts += s
+    value = tp / ts
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ts / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": dict(cfg, passes=len(runs)),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"oracle port on {frac * 100:.2f}% of ions eligible as centres per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="tip20m", choices=["tip20m", "tip10m", "cyl1m"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -122,6 +122,17 @@ int pp_hist_params(pp_ctx* ctx, float rmin, float rincr, float rmax);
  * null model of rndlabeler, src/PARAPROBE_SolverHdl.cpp:2809-3003). */
 int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk,
            const uint32_t* label_perm, void* stream);
+/* Project-written autotuner: times the scan on the first `sample` centres
+ * (0 = 200000) for cell edges R/2 .. R/5 and block tiles of 32, 128 and 512
+ * centres, keeps the fastest for this cloud and rebuilds its cell grid.  Uses
+ * the current tasks and histogram settings; results of the trial runs are
+ * discarded.  Has no counterpart in the reference (its KD-tree has no tuning). */
+int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk,
+                uint32_t sample, float* best_ratio, uint32_t* best_tile);
+/* Set the tuning of a cloud directly: cell edge R / cell_ratio, tile centres
+ * per block work item. */
+int pp_cloud_tuning(pp_ctx* ctx, int cloud, float cell_ratio, uint32_t tile);
+
 /* Results of the last pp_run (synchronises). cap = capacity in uint64. */
 int pp_fetch(pp_ctx* ctx, uint64_t* bins, size_t cap);
 /* Neighbour-count histograms (PP_CNTNB): ntasks x len counts; *len returns
@@ -160,6 +171,13 @@ int pp_neighbors(pp_ctx* ctx, int cloud, uint64_t ion, float r, uint64_t* ids,
  * implementation-defined and depends on its thread count, so both sides of a
  * comparison take the permuted labels this produces. */
 int pp_shuffle_labels(const uint8_t* label, uint64_t n, uint64_t seed, uint8_t* out);
+
+/* Number of kernels this library has launched in the process so far. */
+int pp_kernel_launches(uint64_t* count);
+/* Device time of the last run's main kernel (the stencil scan of pp_run, the
+ * realisation pass of pp_run_batched), measured with CUDA events recorded
+ * around that launch on the run's stream.  Synchronises. */
+int pp_last_kernel_ms(pp_ctx* ctx, float* ms);
 
 /* Device the context runs on and its SM count. */
 int pp_device_info(pp_ctx* ctx, int* device, int* sm_count);

@@ -111,7 +111,7 @@ def spatstat(xyz, labels, ion2surf, rmin, rincr, rmax, analyses, trg, env, k_lis
     ngroups = sum(1 for a in (RDF, NN1, RIPK) if analyses & a) + nk
     out = np.zeros(max(1, ngroups * nt * (nb + 2)), dtype=np.uint64)
     cnt = np.zeros(max(1, nt * cntnb_len), dtype=np.uint64)
-    stats = np.zeros(3, dtype=np.uint64)
+    stats = np.zeros(5, dtype=np.uint64)
     rc = lib().ppo_spatstat(xyz.reshape(-1), labels, _ptr(surf), xyz.shape[0], np.float32(rmin),
                             np.float32(rincr), np.float32(rmax), analyses, _ptr(ks), nk, nt,
                             tm.reshape(-1), em.reshape(-1), _ptr(cm), nthreads, out, out.size,
@@ -119,7 +119,8 @@ def spatstat(xyz, labels, ion2surf, rmin, rincr, rmax, analyses, trg, env, k_lis
     if rc:
         raise RuntimeError(f"ppo_spatstat failed ({rc})")
     return dict(bins=out[: ngroups * nt * (nb + 2)], cntnb=cnt[: nt * cntnb_len].reshape(nt, cntnb_len),
-                centres=int(stats[0]), discarded=int(stats[1]), pairs=int(stats[2]), nbins=nb)
+                centres=int(stats[0]), discarded=int(stats[1]), pairs=int(stats[2]), nbins=nb,
+                build_s=float(stats[3]) * 1e-9, compute_s=float(stats[4]) * 1e-9)
 
 
 def neighbors(xyz, centre, R):

@@ -388,7 +388,10 @@ int ppo_surface_distance(const float* xyz, uint64_t n, const float* tri, uint64_
 //   removes that ion from the centre set only).
 //   trg_mask / env_mask: ntasks x 8 words, bit t set when type t is listed.
 //   k_list: MKNN orders (1-based) in output order.
-//   stats (nullable): [0] centres, [1] discarded ions, [2] in-ball pairs.
+//   stats (nullable): [0] centres, [1] discarded ions, [2] in-ball pairs,
+//   [3] nanoseconds spent in decomposition + KD-tree builds (the reference's
+//   Loadpartitioning / ThreadparallelKDTreeConstruct phases), [4] nanoseconds
+//   in the statistics pass (DescrStatsThreadparallelCompute).
 int ppo_spatstat(const float* xyz, const uint8_t* label, const float* ion2surf, uint64_t n,
                  float rmin, float rincr, float rmax, uint32_t analyses,
                  const uint32_t* k_list, int nk, int ntasks,
@@ -411,8 +414,10 @@ int ppo_spatstat(const float* xyz, const uint8_t* label, const float* ion2surf, 
   const float RSQR = R * R;
   const float missing = (float)(R + kEpsilon);  // add(R + EPSILON) takes an apt_real
 
+  const double t_build0 = omp_get_wtime();
   std::vector<Slab> slabs;
   decompose(xyz, label, ion2surf, centre_mask, n, nthreads, slabs);
+  const double t_build1 = omp_get_wtime();
   uint32_t maxtype = 0;
   for (uint64_t i = 0; i < n; ++i) maxtype = std::max<uint32_t>(maxtype, label[i]);
   for (int t = 0; t < ntasks; ++t)
@@ -511,6 +516,7 @@ int ppo_spatstat(const float* xyz, const uint8_t* label, const float* ion2surf, 
       if (doM) for (size_t h = 0; h < gM.size(); ++h) gM[h].merge(mM[h]);
     }
   }
+  const double t_comp1 = omp_get_wtime();
   if (err) return err;
   uint64_t o = 0;
   auto put = [&](const Hist& h) { for (uint64_t b = 0; b < H; ++b) out_bins[o++] = (uint64_t)h.cnt[b]; };
@@ -519,7 +525,11 @@ int ppo_spatstat(const float* xyz, const uint8_t* label, const float* ion2surf, 
   if (doK) for (auto& h : gK) put(h);
   if (doM) for (auto& h : gM) put(h);
   if (doC) for (int t = 0; t < ntasks; ++t) std::memcpy(out_cntnb + (uint64_t)t * cntnb_len, gC[t].data(), cntnb_len * 8);
-  if (stats) { stats[0] = n_centre; stats[1] = n_disc; stats[2] = n_pairs; }
+  if (stats) {
+    stats[0] = n_centre; stats[1] = n_disc; stats[2] = n_pairs;
+    stats[3] = (uint64_t)((t_build1 - t_build0) * 1e9);
+    stats[4] = (uint64_t)((t_comp1 - t_build1) * 1e9);
+  }
   return 0;
 }
 

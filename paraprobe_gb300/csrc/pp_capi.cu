@@ -72,6 +72,9 @@ struct Cloud {
   uint64_t grid_version = 0;
   DevBuf ions, cell_start, slot_of_id, id_of_slot, label_sorted;
   // hull / ion2surf
+  // tuning (pp_autotune): cell edge = R / cell_ratio, centres per block tile
+  float cell_ratio = 3.0f;
+  uint32_t tile = 128;
   Hull hull;
   DevBuf user_surf;             // input order, when given
   bool has_user_surf = false;
@@ -105,6 +108,8 @@ struct RunPlan {
   int cmax = 0;
   int cat_miss = 0;
   std::vector<float> catT;
+  int disjoint = 0;
+  std::vector<int8_t> setidx;      // [nC][256]
 };
 
 struct Result {
@@ -138,7 +143,7 @@ struct pp_ctx {
   Tables tab;
   Result res;
   // scratch
-  DevBuf tmp_cell_of, tmp_rank, scan_tmp, bbox, centres, centre_count, work, tables_dev;
+  DevBuf tmp_cell_of, tmp_rank, scan_tmp, bbox, centres, centre_count, work, tables_dev, sel_flags, sel_tmp;
   DevBuf labels_run, perm_dev, gather_src;
   // batched geometry cache
   DevBuf pair_count, pair_off, pair_slot, pair_cat, geo_centres, centre_ok, real_labels, rois_dev;
@@ -150,6 +155,8 @@ struct pp_ctx {
   int geo_H = 0;
   float geo_rmin = 0, geo_rincr = 0;
   uint64_t grid_counter = 1;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool ev_recorded = false;
 };
 
 namespace {
@@ -247,9 +254,9 @@ int build_grid(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
     lo[k] = n ? o2f(bb[k]) : 0.f;
     hi[k] = n ? o2f(bb[3 + k]) : 0.f;
   }
-  // cell edge R/2 (stencil rows of about five cells), coarsened if the grid
-  // would hold more than max(4 n, 2^20) cells
-  double h = std::max((double)R * 0.5, 1e-3);
+  // cell edge R / cell_ratio (3 by default, tuned by pp_autotune), coarsened
+  // if the grid would hold more than max(4 n, 2^20) cells
+  double h = std::max((double)R / std::max(cl.cell_ratio, 0.5f), 1e-3);
   const double ext[3] = {(double)hi[0] - lo[0], (double)hi[1] - lo[1], (double)hi[2] - lo[2]};
   const double maxcells = std::max(4.0 * (double)n, (double)(1 << 20));
   for (;;) {
@@ -294,11 +301,10 @@ int build_grid(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
   return PP_OK;
 }
 
+// A grid serves every radius with R / h in [1, 6] (stencils of 3..13 cells a
+// side); outside that range it is rebuilt with h = R / cell_ratio.
 int ensure_grid(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
   if (cl.grid_ok && cl.g.h <= R * 1.0001f && cl.g.h >= R / 6.f) return PP_OK;
-  if (cl.grid_ok && cl.g.h <= R * 1.0001f && cl.g.h < R / 6.f) {
-    // very fine grid relative to R: acceptable only if coarsening was forced
-  }
   return build_grid(ctx, cl, R, s);
 }
 
@@ -481,6 +487,16 @@ int make_plan(pp_ctx* ctx, uint32_t flags, const uint32_t* k_list, int nk, RunPl
     P.emax = std::max(P.emax, (int)local.size());
   }
   if (P.kr == 4 && P.emax > 8) return fail(ctx, PP_ERR_UNSUPPORTED, "k > 32 with more than 8 environment sets per centre type");
+  // disjoint sets: no type in two environment sets of one centre type (the
+  // usual "A-B" task lists); then a type names its set directly
+  P.disjoint = 1;
+  P.setidx.assign((size_t)std::max(P.nC, 1) * 256, (int8_t)-1);
+  for (int c = 0; c < P.nC; ++c)
+    for (int ty = 0; ty < 256; ++ty) {
+      const uint32_t b = P.envbits[c * 256 + ty];
+      if (__builtin_popcount(b) > 1) P.disjoint = 0;
+      if (b) P.setidx[c * 256 + ty] = (int8_t)__builtin_ctz(b);
+    }
   P.catT = threshold_table(t);
   P.cat_miss = category_of_distance(t, (float)((double)t.rmax + kEpsilon));
   return PP_OK;
@@ -489,6 +505,7 @@ int make_plan(pp_ctx* ctx, uint32_t flags, const uint32_t* k_list, int nk, RunPl
 // Upload the plan's tables into one device block; returns device pointers.
 struct DevTables {
   float* catT; int8_t* cslot; int8_t* eslot; uint32_t* envbits; int* set_list; int* nsets; int* kvals;
+  int8_t* setidx;
 };
 
 int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
@@ -508,12 +525,14 @@ int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
   std::vector<int> kv(P.kvals.begin(), P.kvals.end());
   if (kv.empty()) kv.push_back(1);
   const size_t o7 = put(kv.data(), kv.size() * 4);
+  const size_t o8 = put(P.setidx.data(), P.setidx.size());
   CK(ctx->tables_dev.ensure(blob.size()));
   CK(cudaMemcpyAsync(ctx->tables_dev.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));  // blob is a host temporary
   unsigned char* b = ctx->tables_dev.as<unsigned char>();
   D.catT = (float*)(b + o1); D.cslot = (int8_t*)(b + o2); D.eslot = (int8_t*)(b + o3);
   D.envbits = (uint32_t*)(b + o4); D.set_list = (int*)(b + o5); D.nsets = (int*)(b + o6); D.kvals = (int*)(b + o7);
+  D.setidx = (int8_t*)(b + o8);
   return PP_OK;
 }
 
@@ -546,6 +565,9 @@ void fill_scan_common(pp::ScanArgs& a, const Cloud& cl, const RunPlan& P, const 
   a.kvals = D.kvals;
   a.nkI = (int)P.kvals.size();
   a.kmax = std::max(P.kmax, 1);
+  a.disjoint = P.disjoint;
+  a.setidx = D.setidx;
+  a.tile = std::max<uint32_t>(cl.tile, 1);
 }
 
 // Fold per-type cores into per-task histograms (pp_fetch layout).
@@ -689,6 +711,10 @@ int pp_create(pp_ctx** out, int device) {
   if (!c) return PP_ERR_NOMEM;
   c->device = device;
   cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    delete c;
+    return PP_ERR_CUDA;
+  }
   *out = c;
   return PP_OK;
 }
@@ -697,6 +723,8 @@ void pp_destroy(pp_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   delete ctx;
 }
 
@@ -844,13 +872,33 @@ int pp_hist_params(pp_ctx* ctx, float rmin, float rincr, float rmax) {
   return PP_OK;
 }
 
-int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk, const uint32_t* label_perm,
-           void* stream) {
-  if (!ctx) return PP_ERR_INVALID;
-  Cloud* cl = get_cloud(ctx, cloud);
-  if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
-  CK(cudaSetDevice(ctx->device));
-  cudaStream_t s = (cudaStream_t)stream;
+}  // extern "C"
+
+namespace {
+
+// Select the centres of a plain run into ctx->centres (cell order); returns
+// their number.  Synchronises the stream once to learn the count.
+int select_centres(pp_ctx* ctx, Cloud& cl, const uint8_t* labels, const int8_t* cslot, float R, uint32_t* ncent,
+                   cudaStream_t s) {
+  const uint64_t n = cl.n;
+  CK(ctx->centres.ensure(std::max<uint64_t>(n, 1) * 4));
+  CK(ctx->centre_count.ensure(8));
+  CK(ctx->sel_flags.ensure((n + 1) * 4));
+  const uint64_t tmp_elems = (n + 1) / 2048 + 64;
+  CK(ctx->sel_tmp.ensure(tmp_elems * 4 * 2));
+  pp::launch_select_centres(labels ? labels : cl.label_sorted.as<uint8_t>(), cl.surf.as<float>(), n, R * R, cslot,
+                            nullptr, ctx->sel_flags.as<uint32_t>(), ctx->sel_tmp.as<uint32_t>(), tmp_elems * 2,
+                            ctx->centres.as<uint32_t>(), ctx->centre_count.as<uint32_t>(), s);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ncent, ctx->centre_count.p, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return PP_OK;
+}
+
+// One pass of compute_generic_spatstat3 on the device.  centre_limit > 0
+// restricts the pass to the first centres (cell order), for tuning.
+int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, int nk, const uint32_t* label_perm,
+              cudaStream_t s, uint32_t centre_limit) {
   RunPlan P;
   int rc = make_plan(ctx, flags, k_list, nk, P);
   if (rc) return rc;
@@ -858,10 +906,7 @@ int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int n
   if ((rc = ensure_grid(ctx, *cl, R, s))) return rc;
   if ((rc = ensure_surface(ctx, *cl, R, s))) return rc;
   const uint64_t n = cl->n;
-  // neighbour-count capacity: the largest possible ball is bounded by the
-  // ions of the densest cell times the stencil's cell count
-  P.cmax = 0;
-  if (flags & PP_CNTNB) P.cmax = 4095;
+  P.cmax = (flags & PP_CNTNB) ? 4095 : 0;  // neighbour counts above 4095 set PP_ERR_OVERFLOW
   DevTables D{};
   if ((rc = upload_tables(ctx, P, D, s))) return rc;
   if ((rc = alloc_result(ctx, P, 1, false, s))) return rc;
@@ -875,15 +920,9 @@ int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int n
                               ctx->labels_run.as<uint8_t>(), s);
     labels = ctx->labels_run.as<uint8_t>();
   }
-  // centres
-  CK(ctx->centres.ensure(std::max<uint64_t>(n, 1) * 4));
-  CK(ctx->centre_count.ensure(8));
-  CK(cudaMemsetAsync(ctx->centre_count.p, 0, 8, s));
-  pp::launch_select_centres(labels ? labels : cl->label_sorted.as<uint8_t>(), cl->surf.as<float>(), n, R * R,
-                            D.cslot, nullptr, ctx->centres.as<uint32_t>(), ctx->centre_count.as<uint32_t>(), s);
   uint32_t ncent = 0;
-  CK(cudaMemcpyAsync(&ncent, ctx->centre_count.p, 4, cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  if ((rc = select_centres(ctx, *cl, labels, D.cslot, R, &ncent, s))) return rc;
+  if (centre_limit && ncent > centre_limit) ncent = centre_limit;
   ctx->res.ncentres_total = ncent;
   ctx->res.n_ions = n;
   CK(ctx->work.ensure(16));
@@ -903,10 +942,14 @@ int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int n
   a.work = ctx->work.as<uint32_t>();
   a.status = ctx->res.status.as<int>();
   a.mode = 0;
-  a.rdf_in_smem = ((size_t)P.nC * P.nE * P.H * 4 <= 96 * 1024) ? 1 : 0;
+  a.rdf_in_smem = ((a.flags & PP_RDF) && (size_t)P.nC * P.nE * P.H * 4 <= 96 * 1024) ? 1 : 0;
+  ctx->ev_recorded = false;
   if (ncent > 0) {
     size_t smem = 0;
+    CK(cudaEventRecord(ctx->ev0, s));
     rc = pp::launch_scan(a, P.kr, P.emax, ctx->sm_count, &smem, s);
+    CK(cudaEventRecord(ctx->ev1, s));
+    ctx->ev_recorded = true;
     if (rc == -2) return fail(ctx, PP_ERR_UNSUPPORTED, "no kernel variant for k=%d with %d environment sets", P.kmax, P.emax);
     if (rc) {
       cudaError_t e = cudaGetLastError();
@@ -915,6 +958,70 @@ int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int n
   }
   ctx->res.valid = true;
   ctx->res.centres_sel.assign(1, ncent);
+  return PP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk, const uint32_t* label_perm,
+           void* stream) {
+  if (!ctx) return PP_ERR_INVALID;
+  Cloud* cl = get_cloud(ctx, cloud);
+  if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
+  CK(cudaSetDevice(ctx->device));
+  return run_plain(ctx, cl, flags, k_list, nk, label_perm, (cudaStream_t)stream, 0);
+}
+
+// Times the scan on the first `sample` centres for each candidate cell ratio
+// (R / h) and block tile, keeps the fastest pair for this cloud and rebuilds
+// its grid.  Uses the current tasks and histogram settings.
+int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk, uint32_t sample,
+                float* best_ratio, uint32_t* best_tile) {
+  if (!ctx) return PP_ERR_INVALID;
+  Cloud* cl = get_cloud(ctx, cloud);
+  if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
+  CK(cudaSetDevice(ctx->device));
+  if (sample == 0) sample = 200000;
+  const float ratios[] = {2.0f, 3.0f, 4.0f, 5.0f};
+  const uint32_t tiles[] = {32, 128, 512};
+  float bestr = cl->cell_ratio, bestms = 1e30f;
+  uint32_t bestt = cl->tile;
+  const float R = ctx->tab.rmax;
+  for (float r : ratios) {
+    cl->cell_ratio = r;
+    int rc = build_grid(ctx, *cl, R, 0);
+    if (rc) return rc;
+    for (uint32_t t : tiles) {
+      cl->tile = t;
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; ++rep) {  // first repetition warms caches and lazy state
+        rc = run_plain(ctx, cl, flags, k_list, nk, nullptr, 0, sample);
+        if (rc) return rc;
+        rc = pp_last_kernel_ms(ctx, &ms);
+        if (rc) return rc;
+      }
+      if (ms < bestms) { bestms = ms; bestr = r; bestt = t; }
+    }
+  }
+  cl->cell_ratio = bestr;
+  cl->tile = bestt;
+  int rc = build_grid(ctx, *cl, R, 0);
+  if (rc) return rc;
+  ctx->res.valid = false;
+  if (best_ratio) *best_ratio = bestr;
+  if (best_tile) *best_tile = bestt;
+  return PP_OK;
+}
+
+int pp_cloud_tuning(pp_ctx* ctx, int cloud, float cell_ratio, uint32_t tile) {
+  Cloud* cl = ctx ? get_cloud(ctx, cloud) : nullptr;
+  if (!cl || !(cell_ratio >= 1.0f && cell_ratio <= 8.0f) || tile == 0 || tile > 65536)
+    return fail(ctx, PP_ERR_INVALID, "cell_ratio in [1, 8] and tile in [1, 65536] required");
+  if (cl->cell_ratio != cell_ratio) cl->grid_ok = false;
+  cl->cell_ratio = cell_ratio;
+  cl->tile = tile;
   return PP_OK;
 }
 
@@ -1052,15 +1159,12 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
   const bool geo_hit = ctx->geo_cloud == cloud && ctx->geo_key_version == cl->grid_version && ctx->geo_R == R &&
                        ctx->geo_H == P.H && ctx->geo_rmin == ctx->tab.rmin && ctx->geo_rincr == ctx->tab.rincr &&
                        cl->surf_version == cl->grid_version;
+  ctx->ev_recorded = false;
   if (!geo_hit) {
-    CK(ctx->geo_centres.ensure(std::max<uint64_t>(n, 1) * 4));
-    CK(ctx->centre_count.ensure(8));
-    CK(cudaMemsetAsync(ctx->centre_count.p, 0, 8, s));
-    pp::launch_select_centres(cl->label_sorted.as<uint8_t>(), cl->surf.as<float>(), n, R * R, nullptr, nullptr,
-                              ctx->geo_centres.as<uint32_t>(), ctx->centre_count.as<uint32_t>(), s);
     uint32_t nc = 0;
-    CK(cudaMemcpyAsync(&nc, ctx->centre_count.p, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    if ((rc = select_centres(ctx, *cl, nullptr, nullptr, R, &nc, s))) return rc;
+    CK(ctx->geo_centres.ensure(std::max<uint64_t>(n, 1) * 4));
+    CK(cudaMemcpyAsync(ctx->geo_centres.p, ctx->centres.p, (uint64_t)nc * 4, cudaMemcpyDeviceToDevice, s));
     pp::ScanArgs a{};
     fill_scan_common(a, *cl, P, D, ctx->tab);
     a.labels = cl->label_sorted.as<uint8_t>();
@@ -1082,7 +1186,6 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
       if (pp::launch_scan(a, 0, 1, ctx->sm_count, nullptr, s)) return fail(ctx, PP_ERR_CUDA, "pair count launch failed");
       const uint64_t tmp_elems = (uint64_t)(nc + 1) / 2048 + 64;
       CK(ctx->scan_tmp.ensure(tmp_elems * 8 * 2));
-      CK(cudaMemsetAsync(ctx->pair_count.as<uint32_t>() + 0, 0, 0, s));
       // offsets: exclusive scan of counts, plus the total in slot nc
       DevBuf cnt1;
       CK(cnt1.ensure(((uint64_t)nc + 1) * 4));
@@ -1187,11 +1290,28 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     b.tile = (uint32_t)std::max(32.0, std::min(4096.0, 65536.0 / std::max(avg, 1.0)));
     b.work = ctx->work.as<uint32_t>();
     b.status = ctx->res.status.as<int>();
+    CK(cudaEventRecord(ctx->ev0, s));
     rc = pp::launch_apply(b, ctx->sm_count, s);
+    CK(cudaEventRecord(ctx->ev1, s));
+    ctx->ev_recorded = true;
     if (rc == -2) return fail(ctx, PP_ERR_UNSUPPORTED, "RDF bins of one realisation exceed shared memory");
     if (rc) return fail(ctx, PP_ERR_CUDA, "apply launch failed");
   }
   ctx->res.valid = true;
+  return PP_OK;
+}
+
+int pp_kernel_launches(uint64_t* count) {
+  if (!count) return PP_ERR_INVALID;
+  *count = pp::kernel_launches();
+  return PP_OK;
+}
+
+int pp_last_kernel_ms(pp_ctx* ctx, float* ms) {
+  if (!ctx || !ms) return PP_ERR_INVALID;
+  if (!ctx->ev_recorded) { *ms = 0.f; return PP_OK; }
+  CK(cudaEventSynchronize(ctx->ev1));
+  CK(cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
   return PP_OK;
 }
 

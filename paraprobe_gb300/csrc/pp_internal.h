@@ -64,6 +64,9 @@ struct ScanArgs {
   uint32_t* work;                // dynamic work counter
   int* status;
   int rdf_in_smem;
+  int disjoint;                  // every type is in at most one env set per centre slot
+  const int8_t* setidx;          // [nC][256] that set's local index or -1 (disjoint only)
+  uint32_t tile;                 // centres per block work item
   // pair-list mode (batched geometry)
   int mode;                      // 0 = fused bins, 1 = count pairs, 2 = emit lists
   uint32_t* pair_count;          // [ncentres] (mode 1)
@@ -123,11 +126,12 @@ void launch_permute_labels(const uint8_t* label_by_id, const uint32_t* perm, con
 void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const float* tri,
                     const uint32_t* tcell_start, const uint32_t* tcell_tri, Grid tg, float rprime,
                     float* surf_d2, cudaStream_t s);
+// Order-preserving centre compaction; flags needs n + 1 words, scan_tmp the
+// exclusive-scan scratch for n + 1 elements.
 void launch_select_centres(const uint8_t* labels, const float* surf_d2, uint64_t n, float R2,
-                           const int8_t* cslot_of, const uint8_t* extra_mask, uint32_t* out,
+                           const int8_t* cslot_of, const uint8_t* extra_mask, uint32_t* flags,
+                           uint32_t* scan_tmp, uint64_t scan_tmp_elems, uint32_t* out,
                            uint32_t* count, cudaStream_t s);
-void launch_select_any(const float* surf_d2, const uint8_t* any_mask, uint64_t n, float R2,
-                       uint32_t* out, uint32_t* count, cudaStream_t s);
 int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s);
 int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s);
 void launch_roi_mask(const float4* ions, const uint32_t* centres, uint32_t ncentres, const float* rois,
@@ -140,5 +144,7 @@ void launch_exclusive_scan_u64_from_u32(const uint32_t* in, uint64_t n, unsigned
 void launch_neighbors(const float4* ions, const uint32_t* cell_start, Grid g, uint32_t self,
                       float R, const uint32_t* id_of_slot, uint32_t* out_slot, float* out_d2,
                       uint32_t cap, uint32_t* count, cudaStream_t s);
+
+unsigned long long kernel_launches();
 
 }  // namespace pp

@@ -168,14 +168,18 @@ __global__ void k_scan_add(T* data, uint64_t n, const T* block_off) {
     if (base + k < n) data[base + k] += o;
 }
 
+void scan_launched(int k);
+
 template <typename T>
 static void excl_scan(T* data, uint64_t n, T* tmp, uint64_t tmp_elems, cudaStream_t s) {
   const uint64_t nb = (n + SCAN_B - 1) / SCAN_B;
   if (nb == 0) return;
   k_scan_blocks<T><<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp);
+  scan_launched(1);
   if (nb > 1) {
     excl_scan<T>(tmp, nb, tmp + nb, tmp_elems - nb, s);
     k_scan_add<T><<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp);
+    scan_launched(1);
   }
 }
 
@@ -306,27 +310,29 @@ __global__ void k_surface(const float4* __restrict__ ions, uint64_t n, const flo
 
 // --------------------------------------------------------- centre selection
 // Centre filter of src/PARAPROBE_SolverHdl.cpp:3847-3859: the type is a target
-// of some task and ion2surf >= R^2 (plus an optional extra mask).  Output is
-// compacted per warp; order across warps is not preserved (results are
-// integer counts, independent of the order).
-__global__ void k_select(const uint8_t* __restrict__ labels, const float* __restrict__ surf, uint64_t n,
-                         float R2, const int8_t* __restrict__ cslot_of, const uint8_t* __restrict__ extra,
-                         uint32_t* __restrict__ out, uint32_t* __restrict__ count) {
-  const int lane = threadIdx.x & 31;
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < n; base += stride) {
-    const uint64_t i = base + threadIdx.x;
-    bool ok = false;
-    if (i < n) {
-      const bool target = cslot_of ? (cslot_of[labels[i]] >= 0) : true;
-      ok = target && (surf[i] >= R2) && (extra ? extra[i] != 0 : true);
-    }
-    const uint32_t m = __ballot_sync(FULL, ok);
-    uint32_t pos = 0;
-    if (lane == 0 && m) pos = atomicAdd(count, (uint32_t)__popc(m));
-    pos = __shfl_sync(FULL, pos, 0);
-    if (ok) out[pos + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
-  }
+// of some task and ion2surf >= R^2 (plus an optional extra mask).  The
+// compaction keeps cell order (flags, exclusive scan, write), so consecutive
+// centres are spatial neighbours and a block's warps share stencil rows in L1.
+__device__ __forceinline__ bool centre_ok(const uint8_t* labels, const float* surf, uint64_t i, float R2,
+                                          const int8_t* cslot_of, const uint8_t* extra) {
+  const bool target = cslot_of ? (cslot_of[labels[i]] >= 0) : true;
+  return target && (surf[i] >= R2) && (extra ? extra[i] != 0 : true);
+}
+
+__global__ void k_select_flags(const uint8_t* __restrict__ labels, const float* __restrict__ surf, uint64_t n,
+                               float R2, const int8_t* __restrict__ cslot_of, const uint8_t* __restrict__ extra,
+                               uint32_t* __restrict__ flags) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= n; i += (uint64_t)gridDim.x * blockDim.x)
+    flags[i] = (i < n && centre_ok(labels, surf, i, R2, cslot_of, extra)) ? 1u : 0u;
+}
+
+__global__ void k_select_write(const uint8_t* __restrict__ labels, const float* __restrict__ surf, uint64_t n,
+                               float R2, const int8_t* __restrict__ cslot_of, const uint8_t* __restrict__ extra,
+                               const uint32_t* __restrict__ pos, uint32_t* __restrict__ out,
+                               uint32_t* __restrict__ count) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    if (centre_ok(labels, surf, i, R2, cslot_of, extra)) out[pos[i]] = (uint32_t)i;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *count = pos[n];
 }
 
 // --------------------------------------------------------------- K3 the scan
@@ -374,6 +380,8 @@ struct ScanShared {
   float* T;
   int8_t* cs;
   int8_t* es;
+  int8_t* sidx;   // [nC][256] the only env set of a type, or -1 (disjoint sets)
+  float* thr;     // [warps][32] current k-th smallest d^2 per set (disjoint sets)
   uint32_t* env;
   uint32_t* rdf;
   uint32_t* cnt;
@@ -471,13 +479,16 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
     S.cs = (int8_t*)p; p += 256;
     S.es = (int8_t*)p; p += 256;
     S.env = (uint32_t*)p; p += (KR > 0 ? a.nC * 256 * 4 : 0);
+    S.thr = (float*)p; p += (KR > 0 ? nwarps * 32 * 4 : 0);
     S.rdf = (uint32_t*)p; p += (a.rdf_in_smem ? a.nC * a.nE * H * 4 : 0);
     S.cnt = (uint32_t*)p; p += ((a.flags & PP_CNTNB) ? nwarps * a.nE * 4 : 0);
-    S.hist = (int*)p;
+    S.hist = (int*)p; p += (a.mode == 2 ? nwarps * H * 4 : 0);
+    S.sidx = (int8_t*)p;
   }
   for (int i = threadIdx.x; i < H; i += blockDim.x) S.T[i] = a.cat_T[i];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) { S.cs[i] = a.cslot_of[i]; S.es[i] = a.eslot_of[i]; }
   if (KR > 0) for (int i = threadIdx.x; i < a.nC * 256; i += blockDim.x) S.env[i] = a.envbits[i];
+  if (KR > 0 && a.disjoint) for (int i = threadIdx.x; i < a.nC * 256; i += blockDim.x) S.sidx[i] = a.setidx[i];
   if (a.rdf_in_smem) for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) S.rdf[i] = 0;
   if (a.flags & PP_CNTNB) for (int i = threadIdx.x; i < nwarps * a.nE; i += blockDim.x) S.cnt[i] = 0;
   if (a.mode == 2) for (int i = threadIdx.x; i < nwarps * H; i += blockDim.x) S.hist[i] = 0;
@@ -489,16 +500,26 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
   const bool doK = KR > 0 && a.mode == 0;
   const int krow = (a.kmax - 1) >> 5, klane = (a.kmax - 1) & 31;
   unsigned long long pairs_lane = 0, centres = 0;
-  constexpr uint32_t CHUNK = 4;
   constexpr unsigned long long FLUSH = 1ull << 30;
+  __shared__ uint32_t s_tile, s_next;
+  const uint32_t T = a.tile;
+  const uint32_t ntiles = (a.ncentres + T - 1) / T;
 
+  // Work: a block takes a tile of consecutive (cell-ordered) centres from a
+  // global counter; its warps take centres of the tile one at a time.
   for (;;) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(a.work, CHUNK);
-    base = __shfl_sync(FULL, base, 0);
-    if (base >= a.ncentres) break;
-    const uint32_t end = min(base + CHUNK, a.ncentres);
-    for (uint32_t ci = base; ci < end; ++ci) {
+    if (threadIdx.x == 0) { s_tile = atomicAdd(a.work, 1u); s_next = 0; }
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= ntiles) break;
+    const uint32_t c0 = tile * T, clen = min(T, a.ncentres - c0);
+    for (;;) {
+    uint32_t kk = 0;
+    if (lane == 0) kk = atomicAdd(&s_next, 1u);
+    kk = __shfl_sync(FULL, kk, 0);
+    if (kk >= clen) break;
+    {
+      const uint32_t ci = c0 + kk;
       const uint32_t self = a.centres[ci];
       const float4 cp = a.ions[self];
       const uint32_t ct = a.labels ? (uint32_t)a.labels[self] : __float_as_uint(cp.w);
@@ -520,6 +541,11 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
 #pragma unroll
             for (int r = 0; r < (KR > 0 ? KR : 1); ++r) lst[p][r] = kInf();
           }
+          if (KR > 0) {
+            __syncwarp();
+            S.thr[warp * 32 + lane] = kInf();
+            __syncwarp();
+          }
         }
         for_each_candidate(a, cp, self, lane, [&](bool valid, uint32_t slot, float d2, bool inball, uint32_t m) {
           (void)valid; (void)slot;
@@ -535,7 +561,32 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
             if (doC && es >= 0) atomicAdd(&S.cnt[warp * a.nE + es], 1u);
           }
           if constexpr (KR > 0) {
-            if (doK) {
+            if (doK && a.disjoint) {
+              // every type belongs to at most one environment set of this
+              // centre type: one ballot per 32 candidates, thresholds of the
+              // warp's sets in shared memory
+              float* thr_w = S.thr + warp * 32;
+              const int p = inball ? (int)S.sidx[cs * 256 + (m & 255)] : -1;
+              uint32_t mask = __ballot_sync(FULL, p >= 0 && d2 < thr_w[p < 0 ? 0 : p]);
+              while (mask) {
+                const int srcl = __ffs(mask) - 1;
+                const float x = __shfl_sync(FULL, d2, srcl);
+                const int ps = __shfl_sync(FULL, p, srcl);
+                float nt = 0.f;
+#pragma unroll
+                for (int q = 0; q < EMAX; ++q) {
+                  if (q == ps) {
+                    list_insert<KR>(lst[q], x, lane);
+                    nt = list_get<KR>(lst[q], krow, klane);
+                  }
+                }
+                __syncwarp();
+                if (lane == 0) thr_w[ps] = nt;
+                __syncwarp();
+                mask &= ~(1u << srcl);
+                mask &= __ballot_sync(FULL, p >= 0 && d2 < thr_w[p < 0 ? 0 : p]);
+              }
+            } else if (doK) {
               const uint32_t eb = inball ? S.env[cs * 256 + (m & 255)] : 0u;
 #pragma unroll
               for (int p = 0; p < EMAX; ++p) {
@@ -643,6 +694,8 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
         }
       }
     }
+    }
+    __syncthreads();
   }
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
   if (lane == 0) {
@@ -814,6 +867,13 @@ __global__ void k_neighbors(const float4* __restrict__ ions, const uint32_t* __r
 }
 
 // ------------------------------------------------------------------ launchers
+// Every kernel this library launches is counted here (read via
+// pp_kernel_launches), so a caller can verify that its work ran on the device.
+static unsigned long long g_launches = 0;
+void counted() { __atomic_fetch_add(&g_launches, 1ull, __ATOMIC_RELAXED); }
+void scan_launched(int k) { __atomic_fetch_add(&g_launches, (unsigned long long)k, __ATOMIC_RELAXED); }
+unsigned long long kernel_launches() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+
 inline unsigned grid_for(uint64_t n, int threads, unsigned cap = 152u * 16u) {
   uint64_t b = (n + threads - 1) / threads;
   if (b < 1) b = 1;
@@ -821,16 +881,19 @@ inline unsigned grid_for(uint64_t n, int threads, unsigned cap = 152u * 16u) {
 }
 
 void launch_bbox(const float* xyz, uint64_t n, float* d_minmax, cudaStream_t s) {
+  counted();
   k_bbox<<<grid_for(n, 256), 256, 0, s>>>(xyz, n, reinterpret_cast<uint32_t*>(d_minmax));
 }
 
 void launch_decode_pos(const uint32_t* be, uint64_t n, const float* lo, const float* hi, const uint8_t* type,
                        int nranges, float* xyz, uint8_t* label, cudaStream_t s) {
+  counted();
   k_decode_pos<<<grid_for(n, 256), 256, 0, s>>>(reinterpret_cast<const uint4*>(be), n, lo, hi, type, nranges, xyz, label);
 }
 
 void launch_cell_count(const float* xyz, uint64_t n, Grid g, uint32_t* cell_of, uint32_t* rank, uint32_t* counts,
                        cudaStream_t s) {
+  counted();
   k_cell_count<<<grid_for(n, 256), 256, 0, s>>>(xyz, n, g, cell_of, rank, counts);
 }
 
@@ -840,6 +903,7 @@ void launch_exclusive_scan_u32(uint32_t* data, uint64_t n, uint32_t* tmp, uint64
 
 void launch_exclusive_scan_u64_from_u32(const uint32_t* in, uint64_t n, unsigned long long* out,
                                         unsigned long long* tmp, uint64_t tmp_elems, cudaStream_t s) {
+  counted();
   k_u32_to_u64<<<grid_for(n, 256), 256, 0, s>>>(in, n, out);
   excl_scan<unsigned long long>(out, n, tmp, tmp_elems, s);
 }
@@ -847,33 +911,37 @@ void launch_exclusive_scan_u64_from_u32(const uint32_t* in, uint64_t n, unsigned
 void launch_scatter(const float* xyz, const uint8_t* label, uint64_t n, const uint32_t* cell_of, const uint32_t* rank,
                     const uint32_t* cell_start, float4* ions, uint32_t* slot_of_id, uint32_t* id_of_slot,
                     uint8_t* label_sorted, cudaStream_t s) {
+  counted();
   k_scatter<<<grid_for(n, 256), 256, 0, s>>>(xyz, label, n, cell_of, rank, cell_start, ions, slot_of_id, id_of_slot,
                                              label_sorted);
 }
 
 void launch_gather_labels(const uint8_t* src, const uint32_t* id_of_slot, uint64_t n, uint8_t* dst, int nsets,
                           cudaStream_t s) {
+  counted();
   k_gather_labels<<<grid_for(n * (uint64_t)nsets, 256), 256, 0, s>>>(src, id_of_slot, n, dst, nsets);
 }
 
 void launch_permute_labels(const uint8_t* label_by_id, const uint32_t* perm, const uint32_t* id_of_slot, uint64_t n,
                            uint8_t* dst, cudaStream_t s) {
+  counted();
   k_permute_labels<<<grid_for(n, 256), 256, 0, s>>>(label_by_id, perm, id_of_slot, n, dst);
 }
 
 void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const float* tri, const uint32_t* tcs,
                     const uint32_t* tct, Grid tg, float rprime, float* surf, cudaStream_t s) {
+  counted();
   k_surface<<<grid_for(n, 256), 256, 0, s>>>(ions, n, tri_box, tri, tcs, tct, tg, rprime, surf);
 }
 
 void launch_select_centres(const uint8_t* labels, const float* surf, uint64_t n, float R2, const int8_t* cslot_of,
-                           const uint8_t* extra, uint32_t* out, uint32_t* count, cudaStream_t s) {
-  k_select<<<grid_for(n, 256), 256, 0, s>>>(labels, surf, n, R2, cslot_of, extra, out, count);
-}
-
-void launch_select_any(const float* surf, const uint8_t* any_mask, uint64_t n, float R2, uint32_t* out,
-                       uint32_t* count, cudaStream_t s) {
-  k_select<<<grid_for(n, 256), 256, 0, s>>>(any_mask, surf, n, R2, nullptr, any_mask, out, count);
+                           const uint8_t* extra, uint32_t* flags, uint32_t* scan_tmp, uint64_t scan_tmp_elems,
+                           uint32_t* out, uint32_t* count, cudaStream_t s) {
+  counted();
+  k_select_flags<<<grid_for(n + 1, 256), 256, 0, s>>>(labels, surf, n, R2, cslot_of, extra, flags);
+  excl_scan<uint32_t>(flags, n + 1, scan_tmp, scan_tmp_elems, s);
+  counted();
+  k_select_write<<<grid_for(n, 256), 256, 0, s>>>(labels, surf, n, R2, cslot_of, extra, flags, out, count);
 }
 
 template <int KR, int EMAX>
@@ -885,6 +953,7 @@ static int launch_scan_t(const ScanArgs& a, int sm_count, size_t smem, cudaStrea
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem) != cudaSuccess || per_sm < 1) return -1;
   const int blocks = sm_count * per_sm;
+  counted();
   kern<<<blocks, 256, smem, s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -892,10 +961,11 @@ static int launch_scan_t(const ScanArgs& a, int sm_count, size_t smem, cudaStrea
 int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s) {
   const int nwarps = 8;
   size_t smem = 16 + (size_t)((a.H + 3) & ~3) * 4 + 512;
-  if (kr > 0) smem += (size_t)a.nC * 256 * 4;
+  if (kr > 0) smem += (size_t)a.nC * 256 * 4 + (size_t)nwarps * 32 * 4;
   if (a.rdf_in_smem) smem += (size_t)a.nC * a.nE * a.H * 4;
   if (a.flags & PP_CNTNB) smem += (size_t)nwarps * a.nE * 4;
   if (a.mode == 2) smem += (size_t)nwarps * a.H * 4;
+  if (kr > 0 && a.disjoint) smem += (size_t)a.nC * 256;
   if (smem_used) *smem_used = smem;
   if (kr == 0) return launch_scan_t<0, 1>(a, sm_count, smem, s);
   if (kr == 1) {
@@ -920,17 +990,20 @@ int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s) {
   }
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply, 256, smem) != cudaSuccess || per_sm < 1) return -1;
+  counted();
   k_apply<<<sm_count * per_sm, 256, smem, s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 void launch_roi_mask(const float4* ions, const uint32_t* centres, uint32_t nc, const float* rois, int nrois, float R,
                      const uint8_t* labels, const int8_t* cslot_of, uint8_t* ok, cudaStream_t s) {
+  counted();
   k_roi_mask<<<grid_for((uint64_t)nc * nrois, 256), 256, 0, s>>>(ions, centres, nc, rois, nrois, R, labels, cslot_of, ok);
 }
 
 void launch_perm_mask(const uint8_t* lab, const uint32_t* centres, uint32_t nc, const int8_t* cslot_of, uint8_t* ok,
                       cudaStream_t s) {
+  counted();
   k_perm_mask<<<grid_for(nc, 256), 256, 0, s>>>(lab, centres, nc, cslot_of, ok);
 }
 
@@ -938,6 +1011,7 @@ void launch_neighbors(const float4* ions, const uint32_t* cell_start, Grid g, ui
                       const uint32_t* id_of_slot, uint32_t* out_slot, float* out_d2, uint32_t cap, uint32_t* count,
                       cudaStream_t s) {
   (void)id_of_slot;
+  counted();
   k_neighbors<<<64, 256, 0, s>>>(ions, cell_start, g, self, R, out_slot, out_d2, cap, count);
 }
 
@@ -958,10 +1032,12 @@ __global__ void k_fill_f32(float* __restrict__ dst, uint64_t n, float v) {
 }
 
 void gather_f32_sorted(const float* src, const uint32_t* id_of_slot, uint64_t n, float* dst, cudaStream_t s) {
+  pp::counted();
   k_gather_f32<<<pp::grid_for(n, 256), 256, 0, s>>>(src, id_of_slot, n, dst);
 }
 
 void fill_f32(float* dst, uint64_t n, float v, cudaStream_t s) {
+  pp::counted();
   k_fill_f32<<<pp::grid_for(n, 256), 256, 0, s>>>(dst, n, v);
 }
 

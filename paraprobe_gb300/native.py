@@ -22,7 +22,8 @@ EXPORTS = (
     "pp_cloud_upload_pos", "pp_cloud_free", "pp_cloud_labels", "pp_hull_upload", "pp_surfdist_upload",
     "pp_surfdist_fetch", "pp_tasks_set", "pp_hist_params", "pp_run", "pp_fetch", "pp_fetch_cntnb",
     "pp_result_size", "pp_run_stats", "pp_run_batched", "pp_batched_count", "pp_fetch_batched",
-    "pp_batched_stats", "pp_neighbors", "pp_shuffle_labels", "pp_device_info",
+    "pp_batched_stats", "pp_neighbors", "pp_shuffle_labels", "pp_device_info", "pp_kernel_launches",
+    "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning",
 )
 
 _lib = None
@@ -69,6 +70,10 @@ def load():
         "pp_neighbors": ([vp, i32, u64, f32, vp, vp, u64, C.POINTER(u64)], i32),
         "pp_shuffle_labels": ([vp, u64, u64, vp], i32),
         "pp_device_info": ([vp, C.POINTER(i32), C.POINTER(i32)], i32),
+        "pp_kernel_launches": ([C.POINTER(u64)], i32),
+        "pp_last_kernel_ms": ([vp, C.POINTER(f32)], i32),
+        "pp_autotune": ([vp, i32, u32, vp, i32, u32, C.POINTER(f32), C.POINTER(u32)], i32),
+        "pp_cloud_tuning": ([vp, i32, f32, u32], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -89,6 +94,12 @@ def type_masks(sets) -> np.ndarray:
         for t in s:
             m[i, int(t) >> 5] |= np.uint32(1 << (int(t) & 31))
     return m
+
+
+def kernel_launches() -> int:
+    n = C.c_uint64()
+    load().pp_kernel_launches(C.byref(n))
+    return n.value
 
 
 def shuffle_labels(labels, seed):
@@ -126,6 +137,11 @@ class Context:
         if rc:
             msg = self.L.pp_last_error(self.h).decode(errors="replace")
             raise PPError(rc, f"{what}: {self.L.pp_strerror(rc).decode()}: {msg}")
+
+    def last_kernel_ms(self) -> float:
+        ms = C.c_float()
+        self._ck(self.L.pp_last_kernel_ms(self.h, C.byref(ms)), "pp_last_kernel_ms")
+        return ms.value
 
     def sm_count(self):
         d, s = C.c_int(), C.c_int()
@@ -195,6 +211,16 @@ class Context:
         perm = None if label_perm is None else np.ascontiguousarray(label_perm, dtype=np.uint32)
         self._ck(self.L.pp_run(self.h, cloud, flags, _p(ks) if ks.size else None, ks.size, _p(perm),
                                C.c_void_p(stream)), "pp_run")
+
+    def autotune(self, cloud, flags, k_list=(), sample=0):
+        ks = np.ascontiguousarray(np.asarray(k_list, dtype=np.uint32))
+        r, t = C.c_float(), C.c_uint32()
+        self._ck(self.L.pp_autotune(self.h, cloud, flags, _p(ks) if ks.size else None, ks.size, sample,
+                                    C.byref(r), C.byref(t)), "pp_autotune")
+        return r.value, t.value
+
+    def tuning(self, cloud, cell_ratio, tile):
+        self._ck(self.L.pp_cloud_tuning(self.h, cloud, cell_ratio, tile), "pp_cloud_tuning")
 
     def result_size(self):
         t, nb = C.c_uint64(), C.c_uint64()

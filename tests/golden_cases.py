@@ -1,0 +1,29 @@
+"""Loader for the reference-generated golden fixtures in tests/golden/."""
+import glob
+import json
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+FLAG_OF_DIGIT = {"1": 1, "2": 2, "3": 4, "4": 8, "6": 32}
+
+
+def names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(str(z["meta"]))
+    c = meta["case"]
+    flags = 0
+    for d in c["analyses"]:
+        flags |= FLAG_OF_DIGIT.get(d, 0)
+    rmin, rincr, rmax = (np.float32(float(x)) for x in c["r"])
+    return dict(xyz=z["xyz"], mq=z["mq"], labels=z["labels"], hull=z["hull"], surf=z["surf"], bins=z["bins"],
+                cntnb=z["cntnb"], meta=meta, csv=json.loads(str(z["csv"])), flags=flags,
+                rmin=rmin, rincr=rincr, rmax=rmax, trg=meta["trg"], env=meta["env"], k=meta["k"],
+                stats=meta["stats"])

@@ -1,0 +1,30 @@
+"""The CUDA path against the reference-generated golden fixtures."""
+import numpy as np
+import pytest
+
+import golden_cases as G
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", G.names())
+def test_gpu_matches_reference(ctx, name):
+    c = G.load(name)
+    cid = ctx.upload(c["xyz"], c["labels"])
+    if c["hull"].shape[0]:
+        ctx.hull(cid, c["hull"], 2.0)
+    ctx.tasks(c["trg"], c["env"])
+    ctx.hist(c["rmin"], c["rincr"], c["rmax"])
+    ctx.run(cid, c["flags"], c["k"])
+    out = ctx.fetch()
+    st = ctx.stats()
+    surf = ctx.surfdist_fetch(cid, c["xyz"].shape[0])
+    assert np.array_equal(surf.view(np.uint32), c["surf"].view(np.uint32))
+    assert st["centres"] == c["stats"]["centres"]
+    assert st["pairs"] == c["stats"]["pairs"]
+    assert np.array_equal(out, c["bins"])
+    L = c["stats"]["cntnb_len"]
+    if L:
+        cn = ctx.fetch_cntnb()
+        assert np.array_equal(cn, c["cntnb"].reshape(len(c["trg"]), L))
+    ctx.free(cid)

@@ -145,3 +145,30 @@ def test_batched_matches_plain(ctx, oracle):
         refq = oracle.spatstat(spec.xyz, spec.labels, surf, rmin, rincr, rmax, flags, trg, env, ks, centre_mask=mask)
         assert np.array_equal(outs[4 + q], refq["bins"]), f"roi {q}"
     ctx.free(cid)
+
+
+def test_results_independent_of_tuning(ctx, oracle):
+    spec = synth.cone_specimen(n=50000, r_apex=8.0, half_angle_deg=10.0, length=20.0, n_clusters=25,
+                               members=40, nspecies=3, seed=21, nseg=64, stack=4.0)
+    types = [1, 2, 3]
+    trg = [[a] for a in types for b in types]
+    env = [[b] for a in types for b in types]
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks(trg, env)
+    ctx.hist(0.0, 0.01, 1.4)
+    outs = []
+    for ratio, tile in ((2.0, 1), (3.5, 64), (5.0, 7), (1.0, 1000)):
+        ctx.tuning(cid, ratio, tile)
+        ctx.run(cid, ALL, [6, 2, 1])
+        outs.append(ctx.fetch())
+    r, t = ctx.autotune(cid, ALL, [6, 2, 1], sample=2000)
+    assert 2.0 <= r <= 5.0 and t in (32, 128, 512)
+    ctx.run(cid, ALL, [6, 2, 1])
+    outs.append(ctx.fetch())
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    ref = oracle.spatstat(spec.xyz, spec.labels, surf, 0.0, 0.01, 1.4, ALL, trg, env, [6, 2, 1])
+    assert np.array_equal(outs[0], ref["bins"])
+    ctx.free(cid)
