@@ -144,6 +144,7 @@ struct pp_ctx {
   Result res;
   // scratch
   DevBuf tmp_cell_of, tmp_rank, scan_tmp, bbox, centres, centre_count, work, tables_dev, sel_flags, sel_tmp;
+  DevBuf tri_fill, cflag, rowtab;
   DevBuf labels_run, perm_dev, gather_src;
   // batched geometry cache
   DevBuf pair_count, pair_off, pair_slot, pair_cat, geo_centres, centre_ok, real_labels, rois_dev;
@@ -155,6 +156,7 @@ struct pp_ctx {
   int geo_H = 0;
   float geo_rmin = 0, geo_rincr = 0;
   uint64_t grid_counter = 1;
+  bool no_sym = false;  // testing hook: force the one-sided scan
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ev_recorded = false;
 };
@@ -366,47 +368,29 @@ int ensure_surface(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
   tg.ny = (int)std::floor((ghi[1] - glo[1]) / h) + 1;
   tg.nz = (int)std::floor((ghi[2] - glo[2]) / h) + 1;
   tg.ncells = (uint64_t)tg.nx * tg.ny * tg.nz;
-  std::vector<uint32_t> cnt(tg.ncells + 1, 0);
-  auto range = [&](uint64_t t, int k, int& c0, int& c1, int nmax, float org) {
-    const float l = box[6 * t + k] - rp - slack, u = box[6 * t + 3 + k] + rp + slack;
-    c0 = std::max(0, (int)std::floor((l - org) / h) - 1);
-    c1 = std::min(nmax - 1, (int)std::floor((u - org) / h) + 1);
-  };
-  for (int pass = 0; pass < 2; ++pass) {
-    std::vector<uint32_t> list;
-    if (pass == 1) {
-      uint64_t acc = 0;
-      for (uint64_t c = 0; c < tg.ncells; ++c) { const uint32_t v = cnt[c]; cnt[c] = (uint32_t)acc; acc += v; }
-      cnt[tg.ncells] = (uint32_t)acc;
-      list.assign(acc, 0);
-    }
-    std::vector<uint32_t> fillp;
-    if (pass == 1) fillp.assign(cnt.begin(), cnt.end() - 1);
-    for (uint64_t t = 0; t < nt; ++t) {
-      int x0, x1, y0, y1, z0, z1;
-      range(t, 0, x0, x1, tg.nx, tg.lox);
-      range(t, 1, y0, y1, tg.ny, tg.loy);
-      range(t, 2, z0, z1, tg.nz, tg.loz);
-      for (int z = z0; z <= z1; ++z)
-        for (int y = y0; y <= y1; ++y)
-          for (int x = x0; x <= x1; ++x) {
-            const uint64_t c = ((uint64_t)z * tg.ny + y) * tg.nx + x;
-            if (pass == 0) cnt[c]++;
-            else list[fillp[c]++] = (uint32_t)t;
-          }
-    }
-    if (pass == 1) {
-      CK(cl.tcell_list.ensure(std::max<size_t>(list.size(), 1) * 4));
-      CK(cudaMemcpyAsync(cl.tcell_list.p, list.data(), list.size() * 4, cudaMemcpyHostToDevice, s));
-      CK(cl.tcell_start.ensure(cnt.size() * 4));
-      CK(cudaMemcpyAsync(cl.tcell_start.p, cnt.data(), cnt.size() * 4, cudaMemcpyHostToDevice, s));
-      CK(cl.tri_dev.ensure(std::max<size_t>(tri.size(), 1) * 4));
-      CK(cudaMemcpyAsync(cl.tri_dev.p, tri.data(), tri.size() * 4, cudaMemcpyHostToDevice, s));
-      CK(cl.tri_box.ensure(std::max<size_t>(box.size(), 1) * 4));
-      CK(cudaMemcpyAsync(cl.tri_box.p, box.data(), box.size() * 4, cudaMemcpyHostToDevice, s));
-      CK(cudaStreamSynchronize(s));  // host vectors die at scope end
-    }
+  // triangles and boxes to the device, binned there (count, scan, fill)
+  CK(cl.tri_dev.ensure(std::max<size_t>(tri.size(), 1) * 4));
+  CK(cudaMemcpyAsync(cl.tri_dev.p, tri.data(), tri.size() * 4, cudaMemcpyHostToDevice, s));
+  CK(cl.tri_box.ensure(std::max<size_t>(box.size(), 1) * 4));
+  CK(cudaMemcpyAsync(cl.tri_box.p, box.data(), box.size() * 4, cudaMemcpyHostToDevice, s));
+  CK(cl.tcell_start.ensure((tg.ncells + 1) * 4));
+  CK(ctx->tri_fill.ensure((tg.ncells + 1) * 4));
+  const uint64_t tmp_elems = (tg.ncells + 1) / 2048 + 64;
+  CK(ctx->scan_tmp.ensure(tmp_elems * 8 * 2));
+  const float grow = rp + slack;
+  uint64_t total = 0;
+  uint64_t cap = cl.tcell_list.bytes / 4;
+  int brc = pp::launch_tri_bins(cl.tri_box.as<float>(), nt, tg, grow, cl.tcell_start.as<uint32_t>(),
+                                ctx->tri_fill.as<uint32_t>(), cl.tcell_list.as<uint32_t>(), cap,
+                                ctx->scan_tmp.as<uint32_t>(), tmp_elems * 4, &total, s);
+  if (brc == 1) {
+    CK(cl.tcell_list.ensure(std::max<uint64_t>(total, 1) * 4));
+    cap = cl.tcell_list.bytes / 4;
+    brc = pp::launch_tri_bins(cl.tri_box.as<float>(), nt, tg, grow, cl.tcell_start.as<uint32_t>(),
+                              ctx->tri_fill.as<uint32_t>(), cl.tcell_list.as<uint32_t>(), cap,
+                              ctx->scan_tmp.as<uint32_t>(), tmp_elems * 4, &total, s);
   }
+  if (brc) return fail(ctx, PP_ERR_CUDA, "triangle binning failed");
   pp::launch_surface(cl.ions.as<float4>(), n, cl.tri_box.as<float>(), cl.tri_dev.as<float>(),
                      cl.tcell_start.as<uint32_t>(), cl.tcell_list.as<uint32_t>(), tg, rp, cl.surf.as<float>(), s);
   CK(cudaGetLastError());
@@ -506,6 +490,7 @@ int make_plan(pp_ctx* ctx, uint32_t flags, const uint32_t* k_list, int nk, RunPl
 struct DevTables {
   float* catT; int8_t* cslot; int8_t* eslot; uint32_t* envbits; int* set_list; int* nsets; int* kvals;
   int8_t* setidx;
+  int8_t* rowtab;
 };
 
 int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
@@ -526,6 +511,9 @@ int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
   if (kv.empty()) kv.push_back(1);
   const size_t o7 = put(kv.data(), kv.size() * 4);
   const size_t o8 = put(P.setidx.data(), P.setidx.size());
+  int nrow = 0;
+  const int8_t* rows = pp::row_table_host(&nrow);
+  const size_t o9 = put(rows, (size_t)nrow * 2);
   CK(ctx->tables_dev.ensure(blob.size()));
   CK(cudaMemcpyAsync(ctx->tables_dev.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));  // blob is a host temporary
@@ -533,6 +521,7 @@ int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
   D.catT = (float*)(b + o1); D.cslot = (int8_t*)(b + o2); D.eslot = (int8_t*)(b + o3);
   D.envbits = (uint32_t*)(b + o4); D.set_list = (int*)(b + o5); D.nsets = (int*)(b + o6); D.kvals = (int*)(b + o7);
   D.setidx = (int8_t*)(b + o8);
+  D.rowtab = (int8_t*)(b + o9);
   return PP_OK;
 }
 
@@ -568,6 +557,8 @@ void fill_scan_common(pp::ScanArgs& a, const Cloud& cl, const RunPlan& P, const 
   a.disjoint = P.disjoint;
   a.setidx = D.setidx;
   a.tile = std::max<uint32_t>(cl.tile, 1);
+  a.rowtab = D.rowtab;
+  a.sym = 0;
 }
 
 // Fold per-type cores into per-task histograms (pp_fetch layout).
@@ -886,9 +877,10 @@ int select_centres(pp_ctx* ctx, Cloud& cl, const uint8_t* labels, const int8_t* 
   CK(ctx->sel_flags.ensure((n + 1) * 4));
   const uint64_t tmp_elems = (n + 1) / 2048 + 64;
   CK(ctx->sel_tmp.ensure(tmp_elems * 4 * 2));
+  CK(ctx->cflag.ensure(std::max<uint64_t>(n, 1)));
   pp::launch_select_centres(labels ? labels : cl.label_sorted.as<uint8_t>(), cl.surf.as<float>(), n, R * R, cslot,
                             nullptr, ctx->sel_flags.as<uint32_t>(), ctx->sel_tmp.as<uint32_t>(), tmp_elems * 2,
-                            ctx->centres.as<uint32_t>(), ctx->centre_count.as<uint32_t>(), s);
+                            ctx->centres.as<uint32_t>(), ctx->centre_count.as<uint32_t>(), ctx->cflag.as<uint8_t>(), s);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(ncent, ctx->centre_count.p, 4, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -943,6 +935,10 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   a.status = ctx->res.status.as<int>();
   a.mode = 0;
   a.rdf_in_smem = ((a.flags & PP_RDF) && (size_t)P.nC * P.nE * P.H * 4 <= 96 * 1024) ? 1 : 0;
+  // RDF / RIPK alone: each pair of two centres is computed once and credited
+  // to both (the counts are the same as the per-centre ball scan's)
+  a.sym = (P.kr == 0 && !(flags & PP_CNTNB) && (a.flags & PP_RDF) && !ctx->no_sym) ? 1 : 0;
+  a.cflag = ctx->cflag.as<uint8_t>();
   ctx->ev_recorded = false;
   if (ncent > 0) {
     size_t smem = 0;

@@ -67,6 +67,9 @@ struct ScanArgs {
   int disjoint;                  // every type is in at most one env set per centre slot
   const int8_t* setidx;          // [nC][256] that set's local index or -1 (disjoint only)
   uint32_t tile;                 // centres per block work item
+  const int8_t* rowtab;          // stencil row offsets in distance order (row_table_offset)
+  int sym;                       // symmetric pass: pairs of two centres are taken once
+  const uint8_t* cflag;          // [n] 1 if the sorted slot is a centre (sym only)
   // pair-list mode (batched geometry)
   int mode;                      // 0 = fused bins, 1 = count pairs, 2 = emit lists
   uint32_t* pair_count;          // [ncentres] (mode 1)
@@ -131,7 +134,14 @@ void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const 
 void launch_select_centres(const uint8_t* labels, const float* surf_d2, uint64_t n, float R2,
                            const int8_t* cslot_of, const uint8_t* extra_mask, uint32_t* flags,
                            uint32_t* scan_tmp, uint64_t scan_tmp_elems, uint32_t* out,
-                           uint32_t* count, cudaStream_t s);
+                           uint32_t* count, uint8_t* cflag, cudaStream_t s);
+// (dy, dz) stencil row offsets, [ROW_TABLE_ENTRIES][2], for ScanArgs::rowtab
+const int8_t* row_table_host(int* entries);
+// Bin triangles (boxes tbox[6 t]) into every cell of tg their box grown by
+// rp + slack reaches; fills tstart (ncells + 1) and tlist (returns the count).
+int launch_tri_bins(const float* tbox, uint64_t ntri, Grid tg, float grow, uint32_t* tstart, uint32_t* tfill,
+                    uint32_t* tlist, uint64_t list_cap, uint32_t* scan_tmp, uint64_t scan_tmp_elems,
+                    uint64_t* total_out, cudaStream_t s);
 int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s);
 int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s);
 void launch_roi_mask(const float4* ions, const uint32_t* centres, uint32_t ncentres, const float* rois,

@@ -321,9 +321,52 @@ __device__ __forceinline__ bool centre_ok(const uint8_t* labels, const float* su
 
 __global__ void k_select_flags(const uint8_t* __restrict__ labels, const float* __restrict__ surf, uint64_t n,
                                float R2, const int8_t* __restrict__ cslot_of, const uint8_t* __restrict__ extra,
-                               uint32_t* __restrict__ flags) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= n; i += (uint64_t)gridDim.x * blockDim.x)
-    flags[i] = (i < n && centre_ok(labels, surf, i, R2, cslot_of, extra)) ? 1u : 0u;
+                               uint32_t* __restrict__ flags, uint8_t* __restrict__ cflag) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const bool ok = i < n && centre_ok(labels, surf, i, R2, cslot_of, extra);
+    flags[i] = ok ? 1u : 0u;
+    if (cflag && i < n) cflag[i] = ok ? 1 : 0;
+  }
+}
+
+// Triangle binning for the hull distance: every cell of tg that a triangle's
+// box grown by `grow` touches lists the triangle (count, scan, fill).
+__device__ __forceinline__ void tri_cell_range(const float* b, Grid tg, float grow, int* c0, int* c1) {
+  const float org[3] = {tg.lox, tg.loy, tg.loz};
+  const int nmax[3] = {tg.nx, tg.ny, tg.nz};
+  for (int k = 0; k < 3; ++k) {
+    int lo = (int)floorf((b[k] - grow - org[k]) * tg.inv_h);
+    int hi = (int)floorf((b[3 + k] + grow - org[k]) * tg.inv_h);
+    c0[k] = lo < 0 ? 0 : (lo >= nmax[k] ? nmax[k] - 1 : lo);
+    c1[k] = hi < 0 ? 0 : (hi >= nmax[k] ? nmax[k] - 1 : hi);
+  }
+}
+
+__global__ void k_tri_count(const float* __restrict__ tbox, uint64_t ntri, Grid tg, float grow,
+                            uint32_t* __restrict__ cnt) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ntri; t += (uint64_t)gridDim.x * blockDim.x) {
+    int c0[3], c1[3];
+    tri_cell_range(tbox + 6 * t, tg, grow, c0, c1);
+    for (int z = c0[2]; z <= c1[2]; ++z)
+      for (int y = c0[1]; y <= c1[1]; ++y)
+        for (int x = c0[0]; x <= c1[0]; ++x) atomicAdd(&cnt[((uint64_t)z * tg.ny + y) * tg.nx + x], 1u);
+  }
+}
+
+__global__ void k_tri_fill(const float* __restrict__ tbox, uint64_t ntri, Grid tg, float grow,
+                           uint32_t* __restrict__ fill, uint32_t* __restrict__ list, uint64_t cap,
+                           int* __restrict__ status) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ntri; t += (uint64_t)gridDim.x * blockDim.x) {
+    int c0[3], c1[3];
+    tri_cell_range(tbox + 6 * t, tg, grow, c0, c1);
+    for (int z = c0[2]; z <= c1[2]; ++z)
+      for (int y = c0[1]; y <= c1[1]; ++y)
+        for (int x = c0[0]; x <= c1[0]; ++x) {
+          const uint32_t at = atomicAdd(&fill[((uint64_t)z * tg.ny + y) * tg.nx + x], 1u);
+          if (at < cap) list[at] = (uint32_t)t;
+          else if (status) atomicOr(status, ST_LIST_OVERFLOW);
+        }
+  }
 }
 
 __global__ void k_select_write(const uint8_t* __restrict__ labels, const float* __restrict__ surf, uint64_t n,
@@ -336,6 +379,13 @@ __global__ void k_select_write(const uint8_t* __restrict__ labels, const float* 
 }
 
 // --------------------------------------------------------------- K3 the scan
+// Row offsets (dy, dz) of stencils with half-width s = 0..ROW_SMAX, each table
+// sorted by dy^2 + dz^2; table s starts at entry row_table_offset(s) =
+// sum_{t<s} (2t+1)^2 (built on the host, copied to shared memory).
+constexpr int ROW_SMAX = 7;
+__host__ __device__ constexpr int row_table_offset(int s) { return s * (4 * s * s - 1) / 3; }
+constexpr int ROW_TABLE_ENTRIES = row_table_offset(ROW_SMAX + 1);
+
 __device__ __forceinline__ int category(float d2, const float* __restrict__ sT, int H, float gs, float gk) {
   int g = (int)((sqrtf(d2) - gs) * gk) + 1;
   g = g < 0 ? 0 : (g > H - 1 ? H - 1 : g);
@@ -377,6 +427,7 @@ __device__ __forceinline__ float list_get(const float (&l)[KR], int row, int src
 }
 
 struct ScanShared {
+  int8_t* rowtab; // [ROW_TABLE_ENTRIES][2]
   float* T;
   int8_t* cs;
   int8_t* es;
@@ -395,7 +446,8 @@ struct ScanShared {
 // a time across the warp; f(valid, slot, d2, inball, type) is called
 // warp-uniformly once per 32 candidates.
 template <class F>
-__device__ __forceinline__ void for_each_candidate(const ScanArgs& a, float4 cp, uint32_t self, int lane, F&& f) {
+__device__ __forceinline__ void for_each_candidate(const ScanArgs& a, const int8_t* __restrict__ rowtab, float4 cp,
+                                                   uint32_t self, int lane, F&& f) {
   const Grid& g = a.g;
   const float ext = a.R + g.margin;
   auto clampc = [](int c, int n) { return c < 0 ? 0 : (c >= n ? n - 1 : c); };
@@ -403,14 +455,24 @@ __device__ __forceinline__ void for_each_candidate(const ScanArgs& a, float4 cp,
   const int y1 = clampc((int)floorf((cp.y + ext - g.loy) * g.inv_h), g.ny);
   const int z0 = clampc((int)floorf((cp.z - ext - g.loz) * g.inv_h), g.nz);
   const int z1 = clampc((int)floorf((cp.z + ext - g.loz) * g.inv_h), g.nz);
-  const int nyr = y1 - y0 + 1;
-  const int nrows = nyr * (z1 - z0 + 1);
+  const int yc = clampc((int)floorf((cp.y - g.loy) * g.inv_h), g.ny);
+  const int zc = clampc((int)floorf((cp.z - g.loz) * g.inv_h), g.nz);
+  // rows are visited in order of increasing offset from the centre's row, so
+  // the nearest candidates come first (the kNN lists settle early)
+  int sr = max(max(yc - y0, y1 - yc), max(zc - z0, z1 - zc));
+  if (sr > ROW_SMAX) {  // cannot happen for cell edges >= R / 6; recorded, never silent
+    if (lane == 0) atomicOr(a.status, ST_BAD_SLOT);
+    sr = ROW_SMAX;
+  }
+  const int nrows = (2 * sr + 1) * (2 * sr + 1);
+  const int8_t* tab = rowtab + 2 * row_table_offset(sr);
   const uint32_t lemask = (2u << lane) - 1u;
   for (int r0 = 0; r0 < nrows; r0 += 32) {
     const int r = r0 + lane;
     uint32_t st = 0, len = 0;
-    if (r < nrows) {
-      const int yy = y0 + r % nyr, zz = z0 + r / nyr;
+    const int yy = (r < nrows) ? yc + tab[2 * r] : -1;
+    const int zz = (r < nrows) ? zc + tab[2 * r + 1] : -1;
+    if (r < nrows && yy >= y0 && yy <= y1 && zz >= z0 && zz <= z1) {
       const float ylo = g.loy + (float)yy * g.h - g.margin, yhi = g.loy + (float)(yy + 1) * g.h + g.margin;
       const float zlo = g.loz + (float)zz * g.h - g.margin, zhi = g.loz + (float)(zz + 1) * g.h + g.margin;
       const float dy = fmaxf(0.f, fmaxf(ylo - cp.y, cp.y - yhi));
@@ -454,14 +516,16 @@ __device__ __forceinline__ void for_each_candidate(const ScanArgs& a, float4 cp,
       const uint32_t slot = rs + (t - rp);
       float d2 = kInf();
       uint32_t m = 0;
-      bool inball = false;
+      bool inball = false, jcentre = false;
       if (valid) {
         const float4 q = __ldg(a.ions + slot);
         d2 = dist2(cp.x, cp.y, cp.z, q.x, q.y, q.z);
-        inball = (d2 <= a.R2) && (slot != self);
+        // symmetric mode: a pair of two centres is taken once, by the lower slot
+        if (a.sym) jcentre = a.cflag[slot] != 0;
+        inball = (d2 <= a.R2) && (slot != self) && !(jcentre && slot < self);
         m = a.labels ? (uint32_t)a.labels[slot] : __float_as_uint(q.w);
       }
-      f(valid, slot, d2, inball, m);
+      f(valid, slot, d2, inball, m, jcentre && slot > self);
     }
   }
 }
@@ -475,6 +539,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
   {
     unsigned char* p = smem;
     S.since_flush = (unsigned long long*)p; p += 16;
+    S.rowtab = (int8_t*)p; p += ROW_TABLE_ENTRIES * 2;
     S.T = (float*)p; p += ((H + 3) & ~3) * 4;
     S.cs = (int8_t*)p; p += 256;
     S.es = (int8_t*)p; p += 256;
@@ -486,6 +551,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
     S.sidx = (int8_t*)p;
   }
   for (int i = threadIdx.x; i < H; i += blockDim.x) S.T[i] = a.cat_T[i];
+  for (int i = threadIdx.x; i < ROW_TABLE_ENTRIES * 2; i += blockDim.x) S.rowtab[i] = a.rowtab[i];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) { S.cs[i] = a.cslot_of[i]; S.es[i] = a.eslot_of[i]; }
   if (KR > 0) for (int i = threadIdx.x; i < a.nC * 256; i += blockDim.x) S.env[i] = a.envbits[i];
   if (KR > 0 && a.disjoint) for (int i = threadIdx.x; i < a.nC * 256; i += blockDim.x) S.sidx[i] = a.setidx[i];
@@ -547,16 +613,29 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
             __syncwarp();
           }
         }
-        for_each_candidate(a, cp, self, lane, [&](bool valid, uint32_t slot, float d2, bool inball, uint32_t m) {
+        for_each_candidate(a, S.rowtab, cp, self, lane,
+                           [&](bool valid, uint32_t slot, float d2, bool inball, uint32_t m, bool jside) {
           (void)valid; (void)slot;
           if (inball) {
             ++inb;
             const int es = S.es[m & 255];
+            int cat = -1;
             if (doR && es >= 0) {
-              const int cat = category(d2, S.T, H, a.guess_start, a.guess_scale);
+              cat = category(d2, S.T, H, a.guess_start, a.guess_scale);
               const uint32_t idx = ((uint32_t)cs * a.nE + es) * H + cat;
               if (a.rdf_in_smem) atomicAdd(&S.rdf[idx], 1u);
               else atomicAdd(&a.rdf_core[idx], 1ull);
+            }
+            if (jside) {
+              // the same pair seen from neighbour j, which is a centre too
+              ++inb;
+              const int csj = S.cs[m & 255], esi = S.es[ct & 255];
+              if (doR && esi >= 0 && csj >= 0) {
+                if (cat < 0) cat = category(d2, S.T, H, a.guess_start, a.guess_scale);
+                const uint32_t idx = ((uint32_t)csj * a.nE + esi) * H + cat;
+                if (a.rdf_in_smem) atomicAdd(&S.rdf[idx], 1u);
+                else atomicAdd(&a.rdf_core[idx], 1ull);
+              }
             }
             if (doC && es >= 0) atomicAdd(&S.cnt[warp * a.nE + es], 1u);
           }
@@ -635,14 +714,15 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
           __syncwarp();
         }
       } else if (a.mode == 1) {
-        for_each_candidate(a, cp, self, lane, [&](bool, uint32_t, float, bool inball, uint32_t) { inb += inball; });
+        for_each_candidate(a, S.rowtab, cp, self, lane,
+                           [&](bool, uint32_t, float, bool inball, uint32_t, bool) { inb += inball; });
         uint32_t tot = inb;
         for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
         if (lane == 0) a.pair_count[ci] = tot;
       } else {
         // mode 2: counting sort of the ball by category into the pair list
         int* hist = S.hist + warp * H;
-        for_each_candidate(a, cp, self, lane, [&](bool, uint32_t, float d2, bool inball, uint32_t) {
+        for_each_candidate(a, S.rowtab, cp, self, lane, [&](bool, uint32_t, float d2, bool inball, uint32_t, bool) {
           if (inball) atomicAdd(&hist[category(d2, S.T, H, a.guess_start, a.guess_scale)], 1);
         });
         __syncwarp();
@@ -662,7 +742,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
         __syncwarp();
         const unsigned long long off = a.pair_off[ci];
         const unsigned long long lim = a.pair_off[ci + 1];
-        for_each_candidate(a, cp, self, lane, [&](bool, uint32_t slot, float d2, bool inball, uint32_t) {
+        for_each_candidate(a, S.rowtab, cp, self, lane, [&](bool, uint32_t slot, float d2, bool inball, uint32_t, bool) {
           if (inball) {
             const int cat = category(d2, S.T, H, a.guess_start, a.guess_scale);
             const unsigned long long at = off + (unsigned long long)atomicAdd(&hist[cat], 1);
@@ -934,11 +1014,49 @@ void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const 
   k_surface<<<grid_for(n, 256), 256, 0, s>>>(ions, n, tri_box, tri, tcs, tct, tg, rprime, surf);
 }
 
+// Stencil rows (dy, dz), |dy|, |dz| <= s, per half-width s, sorted by
+// dy^2 + dz^2 (ties by dz then dy) so a warp visits the nearest rows first.
+const int8_t* row_table_host(int* entries) {
+  static int8_t tab[ROW_TABLE_ENTRIES * 2];
+  static bool built = false;
+  if (!built) {
+    for (int sr = 0; sr <= ROW_SMAX; ++sr) {
+      int8_t* t = tab + 2 * row_table_offset(sr);
+      int k = 0;
+      for (int d2 = 0; d2 <= 2 * sr * sr; ++d2)
+        for (int dz = -sr; dz <= sr; ++dz)
+          for (int dy = -sr; dy <= sr; ++dy)
+            if (dy * dy + dz * dz == d2) { t[2 * k] = (int8_t)dy; t[2 * k + 1] = (int8_t)dz; ++k; }
+    }
+    built = true;
+  }
+  if (entries) *entries = ROW_TABLE_ENTRIES;
+  return tab;
+}
+
+int launch_tri_bins(const float* tbox, uint64_t ntri, Grid tg, float grow, uint32_t* tstart, uint32_t* tfill,
+                    uint32_t* tlist, uint64_t list_cap, uint32_t* scan_tmp, uint64_t scan_tmp_elems,
+                    uint64_t* total_out, cudaStream_t s) {
+  if (cudaMemsetAsync(tstart, 0, (tg.ncells + 1) * 4, s) != cudaSuccess) return -1;
+  counted();
+  k_tri_count<<<grid_for(ntri, 128), 128, 0, s>>>(tbox, ntri, tg, grow, tstart);
+  excl_scan<uint32_t>(tstart, tg.ncells + 1, scan_tmp, scan_tmp_elems, s);
+  uint32_t total = 0;
+  if (cudaMemcpyAsync(&total, tstart + tg.ncells, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return -1;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+  *total_out = total;
+  if (total > list_cap) return 1;  // caller grows the list and calls again
+  if (cudaMemcpyAsync(tfill, tstart, (tg.ncells + 1) * 4, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return -1;
+  counted();
+  k_tri_fill<<<grid_for(ntri, 128), 128, 0, s>>>(tbox, ntri, tg, grow, tfill, tlist, list_cap, nullptr);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 void launch_select_centres(const uint8_t* labels, const float* surf, uint64_t n, float R2, const int8_t* cslot_of,
                            const uint8_t* extra, uint32_t* flags, uint32_t* scan_tmp, uint64_t scan_tmp_elems,
-                           uint32_t* out, uint32_t* count, cudaStream_t s) {
+                           uint32_t* out, uint32_t* count, uint8_t* cflag, cudaStream_t s) {
   counted();
-  k_select_flags<<<grid_for(n + 1, 256), 256, 0, s>>>(labels, surf, n, R2, cslot_of, extra, flags);
+  k_select_flags<<<grid_for(n + 1, 256), 256, 0, s>>>(labels, surf, n, R2, cslot_of, extra, flags, cflag);
   excl_scan<uint32_t>(flags, n + 1, scan_tmp, scan_tmp_elems, s);
   counted();
   k_select_write<<<grid_for(n, 256), 256, 0, s>>>(labels, surf, n, R2, cslot_of, extra, flags, out, count);
@@ -960,7 +1078,7 @@ static int launch_scan_t(const ScanArgs& a, int sm_count, size_t smem, cudaStrea
 
 int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s) {
   const int nwarps = 8;
-  size_t smem = 16 + (size_t)((a.H + 3) & ~3) * 4 + 512;
+  size_t smem = 16 + ROW_TABLE_ENTRIES * 2 + (size_t)((a.H + 3) & ~3) * 4 + 512;
   if (kr > 0) smem += (size_t)a.nC * 256 * 4 + (size_t)nwarps * 32 * 4;
   if (a.rdf_in_smem) smem += (size_t)a.nC * a.nE * a.H * 4;
   if (a.flags & PP_CNTNB) smem += (size_t)nwarps * a.nE * 4;

@@ -47,6 +47,8 @@ CASES = [
          tasks="Al,Sc,Zr-Al,Sc,Zr", r=("0.0", "0.01", "0.8"), mknn="1;2;3;4;5", threads=2, hull=False),
     dict(name="bigk", geom="cyl", n=15000, radius=5.0, height=14.0, seed=107, analyses="4",
          tasks="Al-Al,Sc,Zr;Sc-Sc,Zr", r=("0.0", "0.01", "1.3"), mknn="1;33;64;100", threads=3),
+    dict(name="rdf_sym", geom="cone", n=20000, seed=108, nspecies=4, analyses="13",
+         tasks="Al-Al,Sc;Sc,Zr-Al,Sc,Zr;Si-Al", r=("0.1", "0.02", "1.6"), mknn="", threads=3),
 ]
 
 

@@ -1,0 +1,34 @@
+"""The drop-in CLI (settings -> POS -> device ranging -> hull -> tasks -> C ABI
+-> CSV) writes the same CSV files, byte for byte, as the reference harness."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import golden_cases as G
+from host_inputs import write_case
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "paraprobe_gb300", "_lib", "paraprobe_gpu")
+
+
+@pytest.mark.parametrize("name", G.names())
+def test_cli_csv_identical(ctx, tmp_path, name):
+    c = G.load(name)
+    write_case(c, str(tmp_path))
+    out = tmp_path / "out"
+    out.mkdir()
+    cmd = [CLI, "7", "settings.xml", "--outdir", str(out), "--inside", str(c["meta"]["nions_inside"]),
+           repr(c["meta"]["volume_inside"])]
+    if name == "shuffled":
+        np.ascontiguousarray(c["labels"], dtype=np.uint8).tofile(tmp_path / "labels.u8")
+        cmd += ["--labels", "labels.u8"]
+    r = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr + r.stdout
+    produced = sorted(os.listdir(out))
+    assert produced == sorted(c["csv"].keys())
+    for f in produced:
+        assert (out / f).read_text() == c["csv"][f], f

@@ -172,3 +172,21 @@ def test_results_independent_of_tuning(ctx, oracle):
     ref = oracle.spatstat(spec.xyz, spec.labels, surf, 0.0, 0.01, 1.4, ALL, trg, env, [6, 2, 1])
     assert np.array_equal(outs[0], ref["bins"])
     ctx.free(cid)
+
+
+def test_symmetric_rdf_pass(ctx, oracle):
+    """RDF/RIPK-only passes take each pair of two centres once; counts must equal
+    the per-centre scan's, including non-centre neighbours, a label
+    permutation and a non-zero lower radius."""
+    spec = synth.cone_specimen(n=60000, r_apex=8.0, half_angle_deg=10.0, length=20.0, n_clusters=30,
+                               members=40, nspecies=4, seed=31, nseg=96, stack=4.0)
+    trg = [[1], [2, 3], [4]]
+    env = [[1, 2], [1, 2, 3], [1]]
+    rng = np.random.default_rng(5)
+    perm = rng.permutation(spec.xyz.shape[0]).astype(np.uint32)
+    for p in (None, perm):
+        labels = spec.labels if p is None else spec.labels[p]
+        gpu, st, ref, _ = _run_both(ctx, oracle, spec, 0.1, 0.02, 1.6, N.PP_RDF | N.PP_RIPK, trg, env, [],
+                                    perm_labels=None if p is None else (p, labels))
+        assert st["pairs"] == ref["pairs"]
+        assert np.array_equal(gpu, ref["bins"])
