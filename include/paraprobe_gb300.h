@@ -133,6 +133,12 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
  * per block work item. */
 int pp_cloud_tuning(pp_ctx* ctx, int cloud, float cell_ratio, uint32_t tile);
 
+/* Context options (value 0 or 1):
+ *   "symmetric"  RDF/RIPK-only passes take each pair of two centres once and
+ *                credit both (default 1); 0 scans every centre's full ball.
+ * Results are identical either way; the option exists to compare the two. */
+int pp_set_option(pp_ctx* ctx, const char* name, int value);
+
 /* Results of the last pp_run (synchronises). cap = capacity in uint64. */
 int pp_fetch(pp_ctx* ctx, uint64_t* bins, size_t cap);
 /* Neighbour-count histograms (PP_CNTNB): ntasks x len counts; *len returns

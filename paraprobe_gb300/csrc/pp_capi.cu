@@ -144,7 +144,7 @@ struct pp_ctx {
   Result res;
   // scratch
   DevBuf tmp_cell_of, tmp_rank, scan_tmp, bbox, centres, centre_count, work, tables_dev, sel_flags, sel_tmp;
-  DevBuf tri_fill, cflag, rowtab;
+  DevBuf tri_fill, cflag, rowtab, nc_pre;
   DevBuf labels_run, perm_dev, gather_src;
   // batched geometry cache
   DevBuf pair_count, pair_off, pair_slot, pair_cat, geo_centres, centre_ok, real_labels, rois_dev;
@@ -554,7 +554,9 @@ void fill_scan_common(pp::ScanArgs& a, const Cloud& cl, const RunPlan& P, const 
   a.kvals = D.kvals;
   a.nkI = (int)P.kvals.size();
   a.kmax = std::max(P.kmax, 1);
-  a.disjoint = P.disjoint;
+  // shared-memory kNN lists when every type names one set and they fit
+  a.disjoint = (P.disjoint && (size_t)8 * std::max(P.emax, 1) * (P.kr * 32 + 1) * 4 <= 64 * 1024) ? 1 : 0;
+  a.emax = std::max(P.emax, 1);
   a.setidx = D.setidx;
   a.tile = std::max<uint32_t>(cl.tile, 1);
   a.rowtab = D.rowtab;
@@ -939,6 +941,14 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   // to both (the counts are the same as the per-centre ball scan's)
   a.sym = (P.kr == 0 && !(flags & PP_CNTNB) && (a.flags & PP_RDF) && !ctx->no_sym) ? 1 : 0;
   a.cflag = ctx->cflag.as<uint8_t>();
+  if (a.sym) {
+    CK(ctx->nc_pre.ensure((cl->g.ncells + 1) * 4));
+    const uint64_t tmp_elems = (cl->g.ncells + 1) / 2048 + 64;
+    CK(ctx->scan_tmp.ensure(tmp_elems * 8 * 2));
+    pp::launch_nc_prefix(cl->cell_start.as<uint32_t>(), cl->g.ncells, a.cflag, ctx->nc_pre.as<uint32_t>(),
+                         ctx->scan_tmp.as<uint32_t>(), tmp_elems * 4, s);
+    a.nc_pre = ctx->nc_pre.as<uint32_t>();
+  }
   ctx->ev_recorded = false;
   if (ncent > 0) {
     size_t smem = 0;
@@ -1009,6 +1019,12 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
   if (best_ratio) *best_ratio = bestr;
   if (best_tile) *best_tile = bestt;
   return PP_OK;
+}
+
+int pp_set_option(pp_ctx* ctx, const char* name, int value) {
+  if (!ctx || !name) return PP_ERR_INVALID;
+  if (std::strcmp(name, "symmetric") == 0) { ctx->no_sym = (value == 0); return PP_OK; }
+  return fail(ctx, PP_ERR_INVALID, "unknown option %s", name);
 }
 
 int pp_cloud_tuning(pp_ctx* ctx, int cloud, float cell_ratio, uint32_t tile) {

@@ -65,11 +65,13 @@ struct ScanArgs {
   int* status;
   int rdf_in_smem;
   int disjoint;                  // every type is in at most one env set per centre slot
+  int emax;                      // most env sets of one centre slot (shared kNN lists)
   const int8_t* setidx;          // [nC][256] that set's local index or -1 (disjoint only)
   uint32_t tile;                 // centres per block work item
   const int8_t* rowtab;          // stencil row offsets in distance order (row_table_offset)
   int sym;                       // symmetric pass: pairs of two centres are taken once
   const uint8_t* cflag;          // [n] 1 if the sorted slot is a centre (sym only)
+  const uint32_t* nc_pre;        // [ncells + 1] exclusive prefix of non-centre ions per cell (sym only)
   // pair-list mode (batched geometry)
   int mode;                      // 0 = fused bins, 1 = count pairs, 2 = emit lists
   uint32_t* pair_count;          // [ncentres] (mode 1)
@@ -135,6 +137,9 @@ void launch_select_centres(const uint8_t* labels, const float* surf_d2, uint64_t
                            const int8_t* cslot_of, const uint8_t* extra_mask, uint32_t* flags,
                            uint32_t* scan_tmp, uint64_t scan_tmp_elems, uint32_t* out,
                            uint32_t* count, uint8_t* cflag, cudaStream_t s);
+// Exclusive prefix over cells of the non-centre ion count (ncells + 1 words).
+void launch_nc_prefix(const uint32_t* cell_start, uint64_t ncells, const uint8_t* cflag, uint32_t* out,
+                      uint32_t* scan_tmp, uint64_t scan_tmp_elems, cudaStream_t s);
 // (dy, dz) stencil row offsets, [ROW_TABLE_ENTRIES][2], for ScanArgs::rowtab
 const int8_t* row_table_host(int* entries);
 // Bin triangles (boxes tbox[6 t]) into every cell of tg their box grown by

@@ -142,7 +142,7 @@ __device__ T block_excl_scan(T v, T* warp_sums, T* total) {
 }
 
 template <typename T>
-__global__ void k_scan_blocks(T* data, uint64_t n, T* block_sums) {
+__global__ void k_prefix_blocks(T* data, uint64_t n, T* block_sums) {
   __shared__ T ws[32];
   __shared__ T tot;
   const uint64_t base = (uint64_t)blockIdx.x * SCAN_B + (uint64_t)threadIdx.x * SCAN_I;
@@ -160,7 +160,7 @@ __global__ void k_scan_blocks(T* data, uint64_t n, T* block_sums) {
 }
 
 template <typename T>
-__global__ void k_scan_add(T* data, uint64_t n, const T* block_off) {
+__global__ void k_prefix_add(T* data, uint64_t n, const T* block_off) {
   const uint64_t base = (uint64_t)blockIdx.x * SCAN_B + (uint64_t)threadIdx.x * SCAN_I;
   const T o = block_off[blockIdx.x];
 #pragma unroll
@@ -174,11 +174,11 @@ template <typename T>
 static void excl_scan(T* data, uint64_t n, T* tmp, uint64_t tmp_elems, cudaStream_t s) {
   const uint64_t nb = (n + SCAN_B - 1) / SCAN_B;
   if (nb == 0) return;
-  k_scan_blocks<T><<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp);
+  k_prefix_blocks<T><<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp);
   scan_launched(1);
   if (nb > 1) {
     excl_scan<T>(tmp, nb, tmp + nb, tmp_elems - nb, s);
-    k_scan_add<T><<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp);
+    k_prefix_add<T><<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp);
     scan_launched(1);
   }
 }
@@ -329,6 +329,17 @@ __global__ void k_select_flags(const uint8_t* __restrict__ labels, const float* 
   }
 }
 
+// Number of non-centre ions per cell (for the symmetric pass's row skipping).
+__global__ void k_nc_count(const uint32_t* __restrict__ cell_start, uint64_t ncells, const uint8_t* __restrict__ cflag,
+                           uint32_t* __restrict__ out) {
+  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c <= ncells; c += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t k = 0;
+    if (c < ncells)
+      for (uint32_t j = cell_start[c]; j < cell_start[c + 1]; ++j) k += cflag[j] ? 0u : 1u;
+    out[c] = k;
+  }
+}
+
 // Triangle binning for the hull distance: every cell of tg that a triangle's
 // box grown by `grow` touches lists the triangle (count, scan, fill).
 __device__ __forceinline__ void tri_cell_range(const float* b, Grid tg, float grow, int* c0, int* c1) {
@@ -428,11 +439,11 @@ __device__ __forceinline__ float list_get(const float (&l)[KR], int row, int src
 
 struct ScanShared {
   int8_t* rowtab; // [ROW_TABLE_ENTRIES][2]
+  float* lst;     // [warps][emax][LS] sorted kNN lists (disjoint sets)
   float* T;
   int8_t* cs;
   int8_t* es;
   int8_t* sidx;   // [nC][256] the only env set of a type, or -1 (disjoint sets)
-  float* thr;     // [warps][32] current k-th smallest d^2 per set (disjoint sets)
   uint32_t* env;
   uint32_t* rdf;
   uint32_t* cnt;
@@ -457,6 +468,7 @@ __device__ __forceinline__ void for_each_candidate(const ScanArgs& a, const int8
   const int z1 = clampc((int)floorf((cp.z + ext - g.loz) * g.inv_h), g.nz);
   const int yc = clampc((int)floorf((cp.y - g.loy) * g.inv_h), g.ny);
   const int zc = clampc((int)floorf((cp.z - g.loz) * g.inv_h), g.nz);
+  const int xc = clampc((int)floorf((cp.x - g.lox) * g.inv_h), g.nx);
   // rows are visited in order of increasing offset from the centre's row, so
   // the nearest candidates come first (the kNN lists settle early)
   int sr = max(max(yc - y0, y1 - yc), max(zc - z0, z1 - zc));
@@ -483,8 +495,20 @@ __device__ __forceinline__ void for_each_candidate(const ScanArgs& a, const int8
         const int x0 = clampc((int)floorf((cp.x - half - g.lox) * g.inv_h), g.nx);
         const int x1 = clampc((int)floorf((cp.x + half - g.lox) * g.inv_h), g.nx);
         const uint64_t cb = ((uint64_t)zz * g.ny + yy) * g.nx;
-        st = a.cell_start[cb + x0];
-        len = a.cell_start[cb + x1 + 1] - st;
+        int xs = x0;
+        if (a.sym) {
+          // cells that precede the centre in slot order and hold only centres
+          // are skipped: each of those pairs is taken by the other centre
+          const bool own = (zz == zc && yy == yc);
+          if (own || zz < zc || (zz == zc && yy < yc)) {
+            const int xe = own ? min(x1, xc - 1) : x1;
+            if (xe >= x0 && a.nc_pre[cb + xe + 1] == a.nc_pre[cb + x0]) xs = xe + 1;
+          }
+        }
+        if (xs <= x1) {
+          st = a.cell_start[cb + xs];
+          len = a.cell_start[cb + x1 + 1] - st;
+        }
       }
     }
     const uint32_t ne = __ballot_sync(FULL, len > 0);
@@ -532,6 +556,9 @@ __device__ __forceinline__ void for_each_candidate(const ScanArgs& a, const int8
 
 template <int KR, int EMAX>
 __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
+  // shared kNN list stride: one padding word keeps set p's k-th entry in bank
+  // (p + k) % 32, so lanes testing different sets do not collide
+  constexpr int LS = (KR > 0 ? KR : 1) * 32 + 1;
   extern __shared__ __align__(16) unsigned char smem[];
   const int H = a.H;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -544,7 +571,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
     S.cs = (int8_t*)p; p += 256;
     S.es = (int8_t*)p; p += 256;
     S.env = (uint32_t*)p; p += (KR > 0 ? a.nC * 256 * 4 : 0);
-    S.thr = (float*)p; p += (KR > 0 ? nwarps * 32 * 4 : 0);
+    S.lst = (float*)p; p += ((KR > 0 && a.disjoint) ? nwarps * a.emax * LS * 4 : 0);
     S.rdf = (uint32_t*)p; p += (a.rdf_in_smem ? a.nC * a.nE * H * 4 : 0);
     S.cnt = (uint32_t*)p; p += ((a.flags & PP_CNTNB) ? nwarps * a.nE * 4 : 0);
     S.hist = (int*)p; p += (a.mode == 2 ? nwarps * H * 4 : 0);
@@ -607,9 +634,9 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
 #pragma unroll
             for (int r = 0; r < (KR > 0 ? KR : 1); ++r) lst[p][r] = kInf();
           }
-          if (KR > 0) {
-            __syncwarp();
-            S.thr[warp * 32 + lane] = kInf();
+          if (KR > 0 && a.disjoint) {
+            float* L = S.lst + warp * a.emax * LS;
+            for (int e = lane; e < nset * LS; e += 32) L[e] = kInf();
             __syncwarp();
           }
         }
@@ -642,28 +669,27 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
           if constexpr (KR > 0) {
             if (doK && a.disjoint) {
               // every type belongs to at most one environment set of this
-              // centre type: one ballot per 32 candidates, thresholds of the
-              // warp's sets in shared memory
-              float* thr_w = S.thr + warp * 32;
+              // centre type: the warp's sorted lists live in shared memory
+              // (set p at L + p * LS, element e at [e]), one ballot per 32
+              // candidates tests each lane against its own set's k-th value
+              float* L = S.lst + warp * a.emax * LS;
               const int p = inball ? (int)S.sidx[cs * 256 + (m & 255)] : -1;
-              uint32_t mask = __ballot_sync(FULL, p >= 0 && d2 < thr_w[p < 0 ? 0 : p]);
+              const int kix = a.kmax - 1;
+              uint32_t mask = __ballot_sync(FULL, p >= 0 && d2 < L[(p < 0 ? 0 : p) * LS + kix]);
               while (mask) {
                 const int srcl = __ffs(mask) - 1;
                 const float x = __shfl_sync(FULL, d2, srcl);
                 const int ps = __shfl_sync(FULL, p, srcl);
-                float nt = 0.f;
+                float* lp = L + ps * LS;
+                float v[KR];
 #pragma unroll
-                for (int q = 0; q < EMAX; ++q) {
-                  if (q == ps) {
-                    list_insert<KR>(lst[q], x, lane);
-                    nt = list_get<KR>(lst[q], krow, klane);
-                  }
-                }
-                __syncwarp();
-                if (lane == 0) thr_w[ps] = nt;
+                for (int r = 0; r < KR; ++r) v[r] = lp[r * 32 + lane];
+                list_insert<KR>(v, x, lane);
+#pragma unroll
+                for (int r = 0; r < KR; ++r) lp[r * 32 + lane] = v[r];
                 __syncwarp();
                 mask &= ~(1u << srcl);
-                mask &= __ballot_sync(FULL, p >= 0 && d2 < thr_w[p < 0 ? 0 : p]);
+                mask &= __ballot_sync(FULL, p >= 0 && d2 < L[(p < 0 ? 0 : p) * LS + kix]);
               }
             } else if (doK) {
               const uint32_t eb = inball ? S.env[cs * 256 + (m & 255)] : 0u;
@@ -693,7 +719,8 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
                 for (int k0 = 0; k0 < a.nkI; k0 += 32) {
                   const int kk = k0 + lane;
                   const int e = (kk < a.nkI) ? a.kvals[kk] - 1 : 0;
-                  const float v = list_get<KR>(lst[p], e >> 5, e & 31);
+                  float v = list_get<KR>(lst[p], e >> 5, e & 31);
+                  if (a.disjoint) v = S.lst[(warp * a.emax + p) * LS + e];
                   if (kk < a.nkI) {
                     const int cat = (v == kInf()) ? a.cat_miss : category(v, S.T, H, a.guess_start, a.guess_scale);
                     atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
@@ -1014,6 +1041,13 @@ void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const 
   k_surface<<<grid_for(n, 256), 256, 0, s>>>(ions, n, tri_box, tri, tcs, tct, tg, rprime, surf);
 }
 
+void launch_nc_prefix(const uint32_t* cell_start, uint64_t ncells, const uint8_t* cflag, uint32_t* out,
+                      uint32_t* scan_tmp, uint64_t scan_tmp_elems, cudaStream_t s) {
+  counted();
+  k_nc_count<<<grid_for(ncells + 1, 256), 256, 0, s>>>(cell_start, ncells, cflag, out);
+  excl_scan<uint32_t>(out, ncells + 1, scan_tmp, scan_tmp_elems, s);
+}
+
 // Stencil rows (dy, dz), |dy|, |dz| <= s, per half-width s, sorted by
 // dy^2 + dz^2 (ties by dz then dy) so a warp visits the nearest rows first.
 const int8_t* row_table_host(int* entries) {
@@ -1079,7 +1113,8 @@ static int launch_scan_t(const ScanArgs& a, int sm_count, size_t smem, cudaStrea
 int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s) {
   const int nwarps = 8;
   size_t smem = 16 + ROW_TABLE_ENTRIES * 2 + (size_t)((a.H + 3) & ~3) * 4 + 512;
-  if (kr > 0) smem += (size_t)a.nC * 256 * 4 + (size_t)nwarps * 32 * 4;
+  if (kr > 0) smem += (size_t)a.nC * 256 * 4;
+  if (kr > 0 && a.disjoint) smem += (size_t)nwarps * a.emax * (kr * 32 + 1) * 4;
   if (a.rdf_in_smem) smem += (size_t)a.nC * a.nE * a.H * 4;
   if (a.flags & PP_CNTNB) smem += (size_t)nwarps * a.nE * 4;
   if (a.mode == 2) smem += (size_t)nwarps * a.H * 4;

@@ -23,7 +23,7 @@ EXPORTS = (
     "pp_surfdist_fetch", "pp_tasks_set", "pp_hist_params", "pp_run", "pp_fetch", "pp_fetch_cntnb",
     "pp_result_size", "pp_run_stats", "pp_run_batched", "pp_batched_count", "pp_fetch_batched",
     "pp_batched_stats", "pp_neighbors", "pp_shuffle_labels", "pp_device_info", "pp_kernel_launches",
-    "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning",
+    "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option",
 )
 
 _lib = None
@@ -74,6 +74,7 @@ def load():
         "pp_last_kernel_ms": ([vp, C.POINTER(f32)], i32),
         "pp_autotune": ([vp, i32, u32, vp, i32, u32, C.POINTER(f32), C.POINTER(u32)], i32),
         "pp_cloud_tuning": ([vp, i32, f32, u32], i32),
+        "pp_set_option": ([vp, C.c_char_p, i32], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -218,6 +219,9 @@ class Context:
         self._ck(self.L.pp_autotune(self.h, cloud, flags, _p(ks) if ks.size else None, ks.size, sample,
                                     C.byref(r), C.byref(t)), "pp_autotune")
         return r.value, t.value
+
+    def set_option(self, name, value):
+        self._ck(self.L.pp_set_option(self.h, name.encode(), int(value)), "pp_set_option")
 
     def tuning(self, cloud, cell_ratio, tile):
         self._ck(self.L.pp_cloud_tuning(self.h, cloud, cell_ratio, tile), "pp_cloud_tuning")
