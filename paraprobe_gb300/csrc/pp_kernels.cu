@@ -623,21 +623,27 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
       }
       uint32_t inb = 0;
       if (a.mode == 0) {
-        float lst[EMAX][KR > 0 ? KR : 1];
-        float thr[EMAX];
+        // SL: shared-memory lists (disjoint environment sets, EMAX == 0);
+        // otherwise register lists, one per local environment set
+        constexpr bool SL = (EMAX == 0);
+        constexpr int EM = SL ? 1 : EMAX;
+        constexpr int KRR = KR > 0 ? KR : 1;
+        float lst[EM][KRR];
+        float thr[EM];
         int nset = 0;
         if (doK) {
           nset = a.nsets[cs];
-#pragma unroll
-          for (int p = 0; p < EMAX; ++p) {
-            thr[p] = kInf();
-#pragma unroll
-            for (int r = 0; r < (KR > 0 ? KR : 1); ++r) lst[p][r] = kInf();
-          }
-          if (KR > 0 && a.disjoint) {
+          if constexpr (SL) {
             float* L = S.lst + warp * a.emax * LS;
             for (int e = lane; e < nset * LS; e += 32) L[e] = kInf();
             __syncwarp();
+          } else {
+#pragma unroll
+            for (int p = 0; p < EM; ++p) {
+              thr[p] = kInf();
+#pragma unroll
+              for (int r = 0; r < KRR; ++r) lst[p][r] = kInf();
+            }
           }
         }
         for_each_candidate(a, S.rowtab, cp, self, lane,
@@ -666,8 +672,8 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
             }
             if (doC && es >= 0) atomicAdd(&S.cnt[warp * a.nE + es], 1u);
           }
-          if constexpr (KR > 0) {
-            if (doK && a.disjoint) {
+          if constexpr (KR > 0 && SL) {
+            if (doK) {
               // every type belongs to at most one environment set of this
               // centre type: the warp's sorted lists live in shared memory
               // (set p at L + p * LS, element e at [e]), one ballot per 32
@@ -691,10 +697,13 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
                 mask &= ~(1u << srcl);
                 mask &= __ballot_sync(FULL, p >= 0 && d2 < L[(p < 0 ? 0 : p) * LS + kix]);
               }
-            } else if (doK) {
+            }
+          }
+          if constexpr (KR > 0 && !SL) {
+            if (doK) {
               const uint32_t eb = inball ? S.env[cs * 256 + (m & 255)] : 0u;
 #pragma unroll
-              for (int p = 0; p < EMAX; ++p) {
+              for (int p = 0; p < EM; ++p) {
                 if (p < nset) {
                   uint32_t mask = __ballot_sync(FULL, ((eb >> p) & 1u) && d2 < thr[p]);
                   while (mask) {
@@ -712,18 +721,25 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
         });
         if constexpr (KR > 0) {
           if (doK) {
+            // the k-th smallest d^2 of each set -> its bin (or the miss bin)
+            auto emit = [&](int p, int kk, float v) {
+              const int Sg = a.set_list[cs * 32 + p];
+              const int cat = (v == kInf()) ? a.cat_miss : category(v, S.T, H, a.guess_start, a.guess_scale);
+              atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
+            };
+            if constexpr (SL) {
+              for (int p = 0; p < nset; ++p)
+                for (int kk = lane; kk < a.nkI; kk += 32)
+                  emit(p, kk, S.lst[(warp * a.emax + p) * LS + a.kvals[kk] - 1]);
+            } else {
 #pragma unroll
-            for (int p = 0; p < EMAX; ++p) {
-              if (p < nset) {
-                const int Sg = a.set_list[cs * 32 + p];
-                for (int k0 = 0; k0 < a.nkI; k0 += 32) {
-                  const int kk = k0 + lane;
-                  const int e = (kk < a.nkI) ? a.kvals[kk] - 1 : 0;
-                  float v = list_get<KR>(lst[p], e >> 5, e & 31);
-                  if (a.disjoint) v = S.lst[(warp * a.emax + p) * LS + e];
-                  if (kk < a.nkI) {
-                    const int cat = (v == kInf()) ? a.cat_miss : category(v, S.T, H, a.guess_start, a.guess_scale);
-                    atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
+              for (int p = 0; p < EM; ++p) {
+                if (p < nset) {
+                  for (int k0 = 0; k0 < a.nkI; k0 += 32) {
+                    const int kk = k0 + lane;
+                    const int e = (kk < a.nkI) ? a.kvals[kk] - 1 : 0;
+                    const float v = list_get<KR>(lst[p], e >> 5, e & 31);
+                    if (kk < a.nkI) emit(p, kk, v);
                   }
                 }
               }
@@ -1121,6 +1137,10 @@ int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_
   if (kr > 0 && a.disjoint) smem += (size_t)a.nC * 256;
   if (smem_used) *smem_used = smem;
   if (kr == 0) return launch_scan_t<0, 1>(a, sm_count, smem, s);
+  if (a.disjoint) {
+    if (kr == 1) return launch_scan_t<1, 0>(a, sm_count, smem, s);
+    if (kr <= 4) return launch_scan_t<4, 0>(a, sm_count, smem, s);
+  }
   if (kr == 1) {
     if (emax <= 1) return launch_scan_t<1, 1>(a, sm_count, smem, s);
     if (emax <= 8) return launch_scan_t<1, 8>(a, sm_count, smem, s);
