@@ -185,6 +185,35 @@ int pp_kernel_launches(uint64_t* count);
  * around that launch on the run's stream.  Synchronises. */
 int pp_last_kernel_ms(pp_ctx* ctx, float* ms);
 
+/* Prepare a cloud for queries with r_lo <= rmax <= r_hi (r_hi <= 6 r_lo):
+ * builds its cell grid with edge r_lo, the hull lists for R' up to
+ * max(r_hi, carve radius) and the cached ion2surf for R' = max(r_lo, carve).
+ * Required before a cloud is served. */
+int pp_cloud_prepare(pp_ctx* ctx, int cloud, float r_lo, float r_hi);
+
+/* ---- serving loop (no counterpart in the reference, which runs one task per
+ * process): clouds stay resident in the context; queries are admitted by
+ * estimated HBM footprint as worker slots and memory free up, and run
+ * concurrently on the workers' own streams. */
+typedef struct pp_server pp_server;
+/* `slots` worker threads, each with its own stream and run buffers;
+ * `budget_bytes` caps the estimated device memory of admitted queries. */
+int pp_server_create(pp_ctx* ctx, int slots, uint64_t budget_bytes, pp_server** out);
+/* Queue one query (tasks as for pp_tasks_set, histogram as for
+ * pp_hist_params, flags/k_list as for pp_run).  Returns PP_ERR_NOMEM (and
+ * counts a rejection) when the query could never fit the budget. */
+int pp_server_submit(pp_server* srv, int cloud, uint32_t flags, float rmin, float rincr, float rmax,
+                     const uint32_t* trg_mask, const uint32_t* env_mask, int ntasks,
+                     const uint32_t* k_list, int nk, uint64_t* ticket);
+/* Wait for a query and take its results (pp_fetch layout).  len returns the
+ * number of uint64 written; latency_ms is submit-to-completion time. */
+int pp_server_wait(pp_server* srv, uint64_t ticket, uint64_t* bins, size_t cap, uint64_t* len,
+                   uint64_t* pairs, double* latency_ms);
+/* stats[0..7]: submitted, admitted, rejected, completed, in flight,
+ * p50 ms, p99 ms, total pairs of completed queries (as doubles). */
+int pp_server_stats(pp_server* srv, double* stats);
+void pp_server_destroy(pp_server* srv);
+
 /* Device the context runs on and its SM count. */
 int pp_device_info(pp_ctx* ctx, int* device, int* sm_count);
 

@@ -82,6 +82,9 @@ struct Cloud {
   float surf_rp = -1.f;
   uint64_t surf_version = ~0ull;
   DevBuf tri_dev, tri_box, tcell_start, tcell_list;
+  Grid tg{};
+  float tri_grow = -1.f, tri_slack = 0.f;
+  bool tri_ok = false;
 };
 
 struct Tables {
@@ -157,6 +160,9 @@ struct pp_ctx {
   float geo_rmin = 0, geo_rincr = 0;
   uint64_t grid_counter = 1;
   bool no_sym = false;  // testing hook: force the one-sided scan
+  pp_ctx* parent = nullptr;     // serving workers share the parent's clouds
+  bool readonly_clouds = false; // ... and never rebuild them
+  DevBuf surf_own;              // ion2surf for an R' the cloud does not cache
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ev_recorded = false;
 };
@@ -304,37 +310,22 @@ int build_grid(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
 }
 
 // A grid serves every radius with R / h in [1, 6] (stencils of 3..13 cells a
-// side); outside that range it is rebuilt with h = R / cell_ratio.
+// side); outside that range it is rebuilt with h = R / cell_ratio.  Contexts
+// that share a parent's clouds (serving workers) may not rebuild.
 int ensure_grid(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
   if (cl.grid_ok && cl.g.h <= R * 1.0001f && cl.g.h >= R / 6.f) return PP_OK;
+  if (ctx->readonly_clouds)
+    return fail(ctx, PP_ERR_STATE, "cloud was not prepared for R = %g (pp_cloud_prepare)", (double)R);
   return build_grid(ctx, cl, R, s);
 }
 
 // ------------------------------------------------------------- ion2surf
-int ensure_surface(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
-  const uint64_t n = cl.n;
-  if (cl.has_user_surf) {
-    if (cl.surf_version == cl.grid_version && cl.surf_rp < 0.f) return PP_OK;
-    CK(cl.surf.ensure(std::max<uint64_t>(n, 1) * 4));
-    // sorted[slot] = user[id_of_slot[slot]] : reuse the label gather on 4-byte words
-    std::vector<uint32_t> dummy;
-    (void)dummy;
-    pp_host::gather_f32_sorted(cl.user_surf.as<float>(), cl.id_of_slot.as<uint32_t>(), n, cl.surf.as<float>(), s);
-    cl.surf_rp = -1.f;
-    cl.surf_version = cl.grid_version;
-    return PP_OK;
-  }
-  const float rp = std::max(R, cl.hull.carve);  // max(SpatStatRadiusMax, SurfaceCellsCarvingRadius)
-  if (cl.surf_version == cl.grid_version && cl.surf_rp == rp) return PP_OK;
-  CK(cl.surf.ensure(std::max<uint64_t>(n, 1) * 4));
-  if (!cl.hull.present) {
-    // no hull: every ion keeps the initial R'^2 (src/PARAPROBE_SolverHdl.cpp:335-348)
-    const float rp2 = rp * rp;
-    pp_host::fill_f32(cl.surf.as<float>(), n, rp2, s);
-    cl.surf_rp = rp;
-    cl.surf_version = cl.grid_version;
-    return PP_OK;
-  }
+// Triangle boxes (fmin/fmax of the vertices, src/PARAPROBE_SolverHdl.cpp:
+// 2712-2717) and per-cell triangle lists of a hull grid.  A triangle is listed
+// in every cell its box grown by `grow` reaches, so the lists serve every
+// query radius R' with R' + slack <= grow.
+int ensure_tri_bins(pp_ctx* ctx, Cloud& cl, float rp, cudaStream_t s) {
+  if (cl.tri_ok && cl.tri_grow >= rp + cl.tri_slack) return PP_OK;
   const std::vector<float>& tri = cl.hull.tri;
   const uint64_t nt = tri.size() / 9;
   std::vector<float> box(6 * nt);
@@ -342,20 +333,21 @@ int ensure_surface(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
   for (uint64_t t = 0; t < nt; ++t) {
     const float* v = &tri[9 * t];
     for (int k = 0; k < 3; ++k) {
-      // src/PARAPROBE_SolverHdl.cpp:2712-2717: fmin/fmax of the three vertices
       const float l = std::fmin(std::fmin(v[k], v[3 + k]), v[6 + k]);
       const float h = std::fmax(std::fmax(v[k], v[3 + k]), v[6 + k]);
       box[6 * t + k] = l; box[6 * t + 3 + k] = h;
       glo[k] = std::min(glo[k], l); ghi[k] = std::max(ghi[k], h);
     }
   }
-  // triangle grid: cell edge about R', every triangle listed in each cell its
-  // box grown by R' (+ slack) reaches
-  Grid tg{};
   const float slack = 1e-3f + 1e-5f * std::max({std::fabs(glo[0]), std::fabs(ghi[0]), std::fabs(glo[1]),
                                                  std::fabs(ghi[1]), std::fabs(glo[2]), std::fabs(ghi[2])});
+  const float grow = rp + slack;
+  if (cl.tri_ok && cl.tri_grow >= grow) return PP_OK;
+  if (ctx->readonly_clouds)
+    return fail(ctx, PP_ERR_STATE, "hull lists were not prepared for R' = %g (pp_cloud_prepare)", (double)rp);
+  Grid tg{};
   double h = std::max((double)rp, 0.25);
-  for (int k = 0; k < 3; ++k) { glo[k] -= rp + 2 * slack; ghi[k] += rp + 2 * slack; }
+  for (int k = 0; k < 3; ++k) { glo[k] -= grow + slack; ghi[k] += grow + slack; }
   for (;;) {
     double c = 1;
     for (int k = 0; k < 3; ++k) c *= std::floor((ghi[k] - glo[k]) / h) + 1;
@@ -368,7 +360,6 @@ int ensure_surface(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
   tg.ny = (int)std::floor((ghi[1] - glo[1]) / h) + 1;
   tg.nz = (int)std::floor((ghi[2] - glo[2]) / h) + 1;
   tg.ncells = (uint64_t)tg.nx * tg.ny * tg.nz;
-  // triangles and boxes to the device, binned there (count, scan, fill)
   CK(cl.tri_dev.ensure(std::max<size_t>(tri.size(), 1) * 4));
   CK(cudaMemcpyAsync(cl.tri_dev.p, tri.data(), tri.size() * 4, cudaMemcpyHostToDevice, s));
   CK(cl.tri_box.ensure(std::max<size_t>(box.size(), 1) * 4));
@@ -377,7 +368,6 @@ int ensure_surface(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
   CK(ctx->tri_fill.ensure((tg.ncells + 1) * 4));
   const uint64_t tmp_elems = (tg.ncells + 1) / 2048 + 64;
   CK(ctx->scan_tmp.ensure(tmp_elems * 8 * 2));
-  const float grow = rp + slack;
   uint64_t total = 0;
   uint64_t cap = cl.tcell_list.bytes / 4;
   int brc = pp::launch_tri_bins(cl.tri_box.as<float>(), nt, tg, grow, cl.tcell_start.as<uint32_t>(),
@@ -391,11 +381,53 @@ int ensure_surface(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
                               ctx->scan_tmp.as<uint32_t>(), tmp_elems * 4, &total, s);
   }
   if (brc) return fail(ctx, PP_ERR_CUDA, "triangle binning failed");
-  pp::launch_surface(cl.ions.as<float4>(), n, cl.tri_box.as<float>(), cl.tri_dev.as<float>(),
-                     cl.tcell_start.as<uint32_t>(), cl.tcell_list.as<uint32_t>(), tg, rp, cl.surf.as<float>(), s);
-  CK(cudaGetLastError());
-  cl.surf_rp = rp;
-  cl.surf_version = cl.grid_version;
+  CK(cudaStreamSynchronize(s));  // host box vector dies here
+  cl.tg = tg;
+  cl.tri_grow = grow;
+  cl.tri_slack = slack;
+  cl.tri_ok = true;
+  return PP_OK;
+}
+
+// ion2surf of the run in sorted-slot order: from the caller's values, or R'^2
+// without a hull (src/PARAPROBE_SolverHdl.cpp:335-348), or computed against
+// the hull with R' = max(R, SurfaceCellsCarvingRadius).  The cloud caches one
+// R'; a serving worker computes other R' into its own buffer.
+int ensure_surface(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s, const float** surf_out) {
+  const uint64_t n = cl.n;
+  if (cl.has_user_surf) {
+    if (!(cl.surf_version == cl.grid_version && cl.surf_rp < 0.f)) {
+      if (ctx->readonly_clouds) return fail(ctx, PP_ERR_STATE, "cloud was not prepared (pp_cloud_prepare)");
+      CK(cl.surf.ensure(std::max<uint64_t>(n, 1) * 4));
+      pp_host::gather_f32_sorted(cl.user_surf.as<float>(), cl.id_of_slot.as<uint32_t>(), n, cl.surf.as<float>(), s);
+      cl.surf_rp = -1.f;
+      cl.surf_version = cl.grid_version;
+    }
+    *surf_out = cl.surf.as<float>();
+    return PP_OK;
+  }
+  const float rp = std::max(R, cl.hull.carve);  // max(SpatStatRadiusMax, SurfaceCellsCarvingRadius)
+  if (cl.surf_version == cl.grid_version && cl.surf_rp == rp) {
+    *surf_out = cl.surf.as<float>();
+    return PP_OK;
+  }
+  DevBuf* dst = &cl.surf;
+  if (ctx->readonly_clouds) dst = &ctx->surf_own;
+  CK(dst->ensure(std::max<uint64_t>(n, 1) * 4));
+  if (!cl.hull.present) {
+    pp_host::fill_f32(dst->as<float>(), n, rp * rp, s);
+  } else {
+    int rc = ensure_tri_bins(ctx, cl, rp, s);
+    if (rc) return rc;
+    pp::launch_surface(cl.ions.as<float4>(), n, cl.tri_box.as<float>(), cl.tri_dev.as<float>(),
+                       cl.tcell_start.as<uint32_t>(), cl.tcell_list.as<uint32_t>(), cl.tg, rp, dst->as<float>(), s);
+    CK(cudaGetLastError());
+  }
+  if (!ctx->readonly_clouds) {
+    cl.surf_rp = rp;
+    cl.surf_version = cl.grid_version;
+  }
+  *surf_out = dst->as<float>();
   return PP_OK;
 }
 
@@ -526,8 +558,9 @@ int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
 }
 
 Cloud* get_cloud(pp_ctx* ctx, int id) {
-  if (id < 0 || id >= (int)ctx->clouds.size()) return nullptr;
-  return ctx->clouds[id].get();
+  std::vector<std::unique_ptr<Cloud>>& v = ctx->parent ? ctx->parent->clouds : ctx->clouds;
+  if (id < 0 || id >= (int)v.size()) return nullptr;
+  return v[id].get();
 }
 
 void fill_scan_common(pp::ScanArgs& a, const Cloud& cl, const RunPlan& P, const DevTables& D, const Tables& t) {
@@ -818,6 +851,7 @@ int pp_hull_upload(pp_ctx* ctx, int cloud, const float* tri, uint64_t ntri, floa
     if (!std::isfinite(v)) return fail(ctx, PP_ERR_INVALID, "hull has non-finite vertices");
   c->hull.carve = carve_radius;
   c->hull.present = ntri > 0;
+  c->tri_ok = false;
   c->has_user_surf = false;
   c->surf_version = ~0ull;
   return PP_OK;
@@ -871,8 +905,8 @@ namespace {
 
 // Select the centres of a plain run into ctx->centres (cell order); returns
 // their number.  Synchronises the stream once to learn the count.
-int select_centres(pp_ctx* ctx, Cloud& cl, const uint8_t* labels, const int8_t* cslot, float R, uint32_t* ncent,
-                   cudaStream_t s) {
+int select_centres(pp_ctx* ctx, Cloud& cl, const uint8_t* labels, const float* surf, const int8_t* cslot, float R,
+                   uint32_t* ncent, cudaStream_t s) {
   const uint64_t n = cl.n;
   CK(ctx->centres.ensure(std::max<uint64_t>(n, 1) * 4));
   CK(ctx->centre_count.ensure(8));
@@ -880,7 +914,7 @@ int select_centres(pp_ctx* ctx, Cloud& cl, const uint8_t* labels, const int8_t* 
   const uint64_t tmp_elems = (n + 1) / 2048 + 64;
   CK(ctx->sel_tmp.ensure(tmp_elems * 4 * 2));
   CK(ctx->cflag.ensure(std::max<uint64_t>(n, 1)));
-  pp::launch_select_centres(labels ? labels : cl.label_sorted.as<uint8_t>(), cl.surf.as<float>(), n, R * R, cslot,
+  pp::launch_select_centres(labels ? labels : cl.label_sorted.as<uint8_t>(), surf, n, R * R, cslot,
                             nullptr, ctx->sel_flags.as<uint32_t>(), ctx->sel_tmp.as<uint32_t>(), tmp_elems * 2,
                             ctx->centres.as<uint32_t>(), ctx->centre_count.as<uint32_t>(), ctx->cflag.as<uint8_t>(), s);
   CK(cudaGetLastError());
@@ -898,7 +932,8 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   if (rc) return rc;
   const float R = ctx->tab.rmax;
   if ((rc = ensure_grid(ctx, *cl, R, s))) return rc;
-  if ((rc = ensure_surface(ctx, *cl, R, s))) return rc;
+  const float* surf = nullptr;
+  if ((rc = ensure_surface(ctx, *cl, R, s, &surf))) return rc;
   const uint64_t n = cl->n;
   P.cmax = (flags & PP_CNTNB) ? 4095 : 0;  // neighbour counts above 4095 set PP_ERR_OVERFLOW
   DevTables D{};
@@ -915,7 +950,7 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
     labels = ctx->labels_run.as<uint8_t>();
   }
   uint32_t ncent = 0;
-  if ((rc = select_centres(ctx, *cl, labels, D.cslot, R, &ncent, s))) return rc;
+  if ((rc = select_centres(ctx, *cl, labels, surf, D.cslot, R, &ncent, s))) return rc;
   if (centre_limit && ncent > centre_limit) ncent = centre_limit;
   ctx->res.ncentres_total = ncent;
   ctx->res.n_ions = n;
@@ -1161,7 +1196,8 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
   if (P.H > 65535) return fail(ctx, PP_ERR_UNSUPPORTED, "batched runs hold categories in 16 bits");
   const float R = ctx->tab.rmax;
   if ((rc = ensure_grid(ctx, *cl, R, s))) return rc;
-  if ((rc = ensure_surface(ctx, *cl, R, s))) return rc;
+  const float* surf = nullptr;
+  if ((rc = ensure_surface(ctx, *cl, R, s, &surf))) return rc;
   const uint64_t n = cl->n;
   DevTables D{};
   if ((rc = upload_tables(ctx, P, D, s))) return rc;
@@ -1174,7 +1210,7 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
   ctx->ev_recorded = false;
   if (!geo_hit) {
     uint32_t nc = 0;
-    if ((rc = select_centres(ctx, *cl, nullptr, nullptr, R, &nc, s))) return rc;
+    if ((rc = select_centres(ctx, *cl, nullptr, surf, nullptr, R, &nc, s))) return rc;
     CK(ctx->geo_centres.ensure(std::max<uint64_t>(n, 1) * 4));
     CK(cudaMemcpyAsync(ctx->geo_centres.p, ctx->centres.p, (uint64_t)nc * 4, cudaMemcpyDeviceToDevice, s));
     pp::ScanArgs a{};
@@ -1352,6 +1388,251 @@ int pp_batched_stats(pp_ctx* ctx, int r, uint64_t* centres, uint64_t* pairs) {
   if (pairs) *pairs = ctx->res.counters_h[2 * r];
   if (centres) *centres = ctx->res.counters_h[2 * r + 1];
   return PP_OK;
+}
+
+}  // extern "C"
+
+// ================================================================ serving
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+#include <unordered_map>
+
+namespace {
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct ServerRequest {
+  uint64_t ticket = 0;
+  int cloud = -1;
+  uint32_t flags = 0;
+  float rmin = 0, rincr = 0, rmax = 0;
+  std::vector<uint32_t> trg, env, ks;
+  int ntasks = 0;
+  uint64_t footprint = 0;
+  int rc = PP_OK;
+  std::string err;
+  std::vector<uint64_t> bins;
+  uint64_t pairs = 0;
+  double t_submit = 0, t_end = 0;
+  bool done = false;
+};
+
+}  // namespace
+
+struct pp_server {
+  pp_ctx* ctx = nullptr;
+  std::vector<pp_ctx*> workers;
+  std::vector<cudaStream_t> streams;
+  std::vector<std::thread> threads;
+  std::mutex mu;
+  std::condition_variable cv_queue, cv_done;
+  std::deque<std::shared_ptr<ServerRequest>> queue;
+  std::unordered_map<uint64_t, std::shared_ptr<ServerRequest>> reqs;
+  uint64_t next_ticket = 1;
+  uint64_t budget = 0, inflight = 0;
+  bool stop = false;
+  uint64_t submitted = 0, admitted = 0, rejected = 0, completed = 0;
+  double pairs_done = 0;
+  std::vector<double> latencies;
+};
+
+namespace {
+
+// One query on a worker context: the plain path on the worker's stream.
+void serve_one(pp_ctx* w, cudaStream_t st, ServerRequest& q) {
+  int rc = pp_tasks_set(w, q.trg.data(), q.env.data(), q.ntasks);
+  if (!rc) rc = pp_hist_params(w, q.rmin, q.rincr, q.rmax);
+  if (!rc) rc = pp_run(w, q.cloud, q.flags, q.ks.empty() ? nullptr : q.ks.data(), (int)q.ks.size(), nullptr, st);
+  uint64_t total = 0, nb = 0;
+  if (!rc) rc = pp_result_size(w, &total, &nb);
+  if (!rc) {
+    q.bins.assign(std::max<uint64_t>(total, 1), 0);
+    rc = pp_fetch(w, q.bins.data(), q.bins.size());
+    q.bins.resize(total);
+  }
+  if (!rc) rc = pp_run_stats(w, nullptr, nullptr, &q.pairs);
+  q.rc = rc;
+  if (rc) q.err = w->err;
+}
+
+void worker_loop(pp_server* S, int k) {
+  pp_ctx* w = S->workers[k];
+  cudaSetDevice(w->device);
+  for (;;) {
+    std::shared_ptr<ServerRequest> q;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_queue.wait(lk, [&] {
+        return S->stop || (!S->queue.empty() && S->inflight + S->queue.front()->footprint <= S->budget);
+      });
+      if (S->queue.empty()) return;  // stop requested and nothing left
+      q = S->queue.front();
+      S->queue.pop_front();
+      S->inflight += q->footprint;
+      S->admitted++;
+    }
+    serve_one(w, S->streams[k], *q);
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->inflight -= q->footprint;
+      q->t_end = now_ms();
+      q->done = true;
+      S->completed++;
+      S->pairs_done += (double)q->pairs;
+      S->latencies.push_back(q->t_end - q->t_submit);
+    }
+    S->cv_done.notify_all();
+    S->cv_queue.notify_all();
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int pp_cloud_prepare(pp_ctx* ctx, int cloud, float r_lo, float r_hi) {
+  Cloud* cl = ctx ? get_cloud(ctx, cloud) : nullptr;
+  if (!cl || ctx->readonly_clouds || !(r_lo > 0.f) || !(r_hi >= r_lo) || r_hi > 6.f * r_lo)
+    return fail(ctx, PP_ERR_INVALID, "need 0 < r_lo <= r_hi <= 6 r_lo on an owned cloud");
+  CK(cudaSetDevice(ctx->device));
+  const float keep = cl->cell_ratio;
+  cl->cell_ratio = 1.0f;  // cell edge r_lo serves every R in [r_lo, 6 r_lo]
+  int rc = build_grid(ctx, *cl, r_lo, 0);
+  cl->cell_ratio = keep;
+  if (rc) return rc;
+  if (cl->hull.present && !cl->has_user_surf) {
+    if ((rc = ensure_tri_bins(ctx, *cl, std::max(r_hi, cl->hull.carve), 0))) return rc;
+  }
+  const float* surf = nullptr;
+  if ((rc = ensure_surface(ctx, *cl, r_lo, 0, &surf))) return rc;
+  CK(cudaDeviceSynchronize());
+  return PP_OK;
+}
+
+int pp_server_create(pp_ctx* ctx, int slots, uint64_t budget_bytes, pp_server** out) {
+  if (!ctx || !out || slots < 1 || slots > 64 || ctx->parent) return fail(ctx, PP_ERR_INVALID, "bad server arguments");
+  CK(cudaSetDevice(ctx->device));
+  auto S = new (std::nothrow) pp_server();
+  if (!S) return PP_ERR_NOMEM;
+  S->ctx = ctx;
+  S->budget = budget_bytes;
+  for (int k = 0; k < slots; ++k) {
+    pp_ctx* w = new (std::nothrow) pp_ctx();
+    cudaStream_t st = nullptr;
+    if (!w || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&w->ev0) != cudaSuccess || cudaEventCreate(&w->ev1) != cudaSuccess) {
+      delete w;
+      pp_server_destroy(S);
+      return fail(ctx, PP_ERR_CUDA, "cannot create a serving worker");
+    }
+    w->device = ctx->device;
+    w->sm_count = ctx->sm_count;
+    w->parent = ctx;
+    w->readonly_clouds = true;
+    w->no_sym = ctx->no_sym;
+    S->workers.push_back(w);
+    S->streams.push_back(st);
+  }
+  for (int k = 0; k < slots; ++k) S->threads.emplace_back(worker_loop, S, k);
+  *out = S;
+  return PP_OK;
+}
+
+int pp_server_submit(pp_server* S, int cloud, uint32_t flags, float rmin, float rincr, float rmax,
+                     const uint32_t* trg_mask, const uint32_t* env_mask, int ntasks, const uint32_t* k_list, int nk,
+                     uint64_t* ticket) {
+  if (!S || !ticket || ntasks < 1 || !trg_mask || !env_mask || nk < 0 || (nk && !k_list)) return PP_ERR_INVALID;
+  Cloud* cl = get_cloud(S->ctx, cloud);
+  if (!cl || !cl->grid_ok) return PP_ERR_STATE;
+  auto q = std::make_shared<ServerRequest>();
+  q->cloud = cloud;
+  q->flags = flags;
+  q->rmin = rmin; q->rincr = rincr; q->rmax = rmax;
+  q->trg.assign(trg_mask, trg_mask + 8 * (size_t)ntasks);
+  q->env.assign(env_mask, env_mask + 8 * (size_t)ntasks);
+  q->ntasks = ntasks;
+  if (nk) q->ks.assign(k_list, k_list + nk);
+  // device footprint of one query: centre list, flags, scan scratch, centre
+  // flags, private ion2surf, per-cell prefix, result cores
+  const double nb = (rincr > 0.f) ? std::floor(((double)rmax - (double)rmin) / (double)rincr) + 2.0 : 1.0;
+  const double cores = 8.0 * nb * (double)ntasks * (3.0 + (double)nk);
+  q->footprint = (uint64_t)(13.0 * (double)cl->n + 4.0 * (double)cl->g.ncells + cores);
+  q->t_submit = now_ms();
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->submitted++;
+  if (q->footprint > S->budget) {
+    S->rejected++;
+    return PP_ERR_NOMEM;
+  }
+  q->ticket = S->next_ticket++;
+  S->reqs[q->ticket] = q;
+  S->queue.push_back(q);
+  *ticket = q->ticket;
+  S->cv_queue.notify_one();
+  return PP_OK;
+}
+
+int pp_server_wait(pp_server* S, uint64_t ticket, uint64_t* bins, size_t cap, uint64_t* len, uint64_t* pairs,
+                   double* latency_ms) {
+  if (!S) return PP_ERR_INVALID;
+  std::shared_ptr<ServerRequest> q;
+  {
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(ticket);
+    if (it == S->reqs.end()) return PP_ERR_INVALID;
+    q = it->second;
+    S->cv_done.wait(lk, [&] { return q->done; });
+    S->reqs.erase(ticket);
+  }
+  if (len) *len = q->bins.size();
+  if (pairs) *pairs = q->pairs;
+  if (latency_ms) *latency_ms = q->t_end - q->t_submit;
+  if (q->rc) return q->rc;
+  if (bins) {
+    if (cap < q->bins.size()) return PP_ERR_INVALID;
+    std::memcpy(bins, q->bins.data(), q->bins.size() * 8);
+  }
+  return PP_OK;
+}
+
+int pp_server_stats(pp_server* S, double* st) {
+  if (!S || !st) return PP_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(S->mu);
+  std::vector<double> l = S->latencies;
+  std::sort(l.begin(), l.end());
+  auto pct = [&](double p) {
+    if (l.empty()) return 0.0;
+    const size_t i = (size_t)std::min<double>((double)l.size() - 1, std::ceil(p * (double)l.size()) - 1);
+    return l[i];
+  };
+  st[0] = (double)S->submitted;
+  st[1] = (double)S->admitted;
+  st[2] = (double)S->rejected;
+  st[3] = (double)S->completed;
+  st[4] = (double)(S->admitted - S->completed);
+  st[5] = pct(0.50);
+  st[6] = pct(0.99);
+  st[7] = S->pairs_done;
+  return PP_OK;
+}
+
+void pp_server_destroy(pp_server* S) {
+  if (!S) return;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+  }
+  S->cv_queue.notify_all();
+  for (auto& t : S->threads) t.join();
+  for (size_t k = 0; k < S->workers.size(); ++k) {
+    if (S->streams[k]) cudaStreamDestroy(S->streams[k]);
+    pp_destroy(S->workers[k]);
+  }
+  delete S;
 }
 
 }  // extern "C"

@@ -1067,21 +1067,22 @@ void launch_nc_prefix(const uint32_t* cell_start, uint64_t ncells, const uint8_t
 // Stencil rows (dy, dz), |dy|, |dz| <= s, per half-width s, sorted by
 // dy^2 + dz^2 (ties by dz then dy) so a warp visits the nearest rows first.
 const int8_t* row_table_host(int* entries) {
-  static int8_t tab[ROW_TABLE_ENTRIES * 2];
-  static bool built = false;
-  if (!built) {
-    for (int sr = 0; sr <= ROW_SMAX; ++sr) {
-      int8_t* t = tab + 2 * row_table_offset(sr);
-      int k = 0;
-      for (int d2 = 0; d2 <= 2 * sr * sr; ++d2)
-        for (int dz = -sr; dz <= sr; ++dz)
-          for (int dy = -sr; dy <= sr; ++dy)
-            if (dy * dy + dz * dz == d2) { t[2 * k] = (int8_t)dy; t[2 * k + 1] = (int8_t)dz; ++k; }
+  struct Table {
+    int8_t v[ROW_TABLE_ENTRIES * 2];
+    Table() {
+      for (int sr = 0; sr <= ROW_SMAX; ++sr) {
+        int8_t* t = v + 2 * row_table_offset(sr);
+        int k = 0;
+        for (int d2 = 0; d2 <= 2 * sr * sr; ++d2)
+          for (int dz = -sr; dz <= sr; ++dz)
+            for (int dy = -sr; dy <= sr; ++dy)
+              if (dy * dy + dz * dz == d2) { t[2 * k] = (int8_t)dy; t[2 * k + 1] = (int8_t)dz; ++k; }
+      }
     }
-    built = true;
-  }
+  };
+  static const Table table;  // built once, thread-safe initialisation
   if (entries) *entries = ROW_TABLE_ENTRIES;
-  return tab;
+  return table.v;
 }
 
 int launch_tri_bins(const float* tbox, uint64_t ntri, Grid tg, float grow, uint32_t* tstart, uint32_t* tfill,

@@ -23,7 +23,8 @@ EXPORTS = (
     "pp_surfdist_fetch", "pp_tasks_set", "pp_hist_params", "pp_run", "pp_fetch", "pp_fetch_cntnb",
     "pp_result_size", "pp_run_stats", "pp_run_batched", "pp_batched_count", "pp_fetch_batched",
     "pp_batched_stats", "pp_neighbors", "pp_shuffle_labels", "pp_device_info", "pp_kernel_launches",
-    "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option",
+    "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option", "pp_cloud_prepare",
+    "pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_stats", "pp_server_destroy",
 )
 
 _lib = None
@@ -75,6 +76,12 @@ def load():
         "pp_autotune": ([vp, i32, u32, vp, i32, u32, C.POINTER(f32), C.POINTER(u32)], i32),
         "pp_cloud_tuning": ([vp, i32, f32, u32], i32),
         "pp_set_option": ([vp, C.c_char_p, i32], i32),
+        "pp_cloud_prepare": ([vp, i32, f32, f32], i32),
+        "pp_server_create": ([vp, i32, u64, C.POINTER(vp)], i32),
+        "pp_server_submit": ([vp, i32, u32, f32, f32, f32, vp, vp, i32, vp, i32, C.POINTER(u64)], i32),
+        "pp_server_wait": ([vp, u64, vp, C.c_size_t, C.POINTER(u64), C.POINTER(u64), C.POINTER(C.c_double)], i32),
+        "pp_server_stats": ([vp, C.POINTER(C.c_double)], i32),
+        "pp_server_destroy": ([vp], None),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -220,6 +227,9 @@ class Context:
                                     C.byref(r), C.byref(t)), "pp_autotune")
         return r.value, t.value
 
+    def prepare(self, cloud, r_lo, r_hi):
+        self._ck(self.L.pp_cloud_prepare(self.h, cloud, r_lo, r_hi), "pp_cloud_prepare")
+
     def set_option(self, name, value):
         self._ck(self.L.pp_set_option(self.h, name.encode(), int(value)), "pp_set_option")
 
@@ -282,3 +292,51 @@ class Context:
         d2 = np.zeros(max(cnt.value, 1), dtype=np.float32)
         self._ck(self.L.pp_neighbors(self.h, cloud, ion, r, _p(ids), _p(d2), cnt.value, C.byref(cnt)), "pp_neighbors")
         return ids[: cnt.value], d2[: cnt.value]
+
+
+class Server:
+    """Continuous-batching query server over the clouds of a Context."""
+
+    def __init__(self, ctx: Context, slots: int = 4, budget_bytes: int = 8 << 30):
+        self.ctx = ctx
+        self.L = ctx.L
+        h = C.c_void_p()
+        rc = self.L.pp_server_create(ctx.h, slots, budget_bytes, C.byref(h))
+        if rc:
+            raise PPError(rc, "pp_server_create failed: " + self.L.pp_last_error(ctx.h).decode())
+        self.h = h
+
+    def submit(self, cloud, flags, hist, trg, env, k_list=()):
+        tm, em = type_masks(trg), type_masks(env)
+        ks = np.ascontiguousarray(np.asarray(k_list, dtype=np.uint32))
+        t = C.c_uint64()
+        rc = self.L.pp_server_submit(self.h, cloud, flags, hist[0], hist[1], hist[2], _p(tm), _p(em), len(trg),
+                                     _p(ks) if ks.size else None, ks.size, C.byref(t))
+        if rc:
+            raise PPError(rc, "pp_server_submit rejected the query")
+        return t.value
+
+    def wait(self, ticket, cap=1 << 22):
+        out = np.zeros(cap, dtype=np.uint64)
+        ln, pairs, lat = C.c_uint64(), C.c_uint64(), C.c_double()
+        rc = self.L.pp_server_wait(self.h, ticket, _p(out), cap, C.byref(ln), C.byref(pairs), C.byref(lat))
+        if rc:
+            raise PPError(rc, "query failed")
+        return out[: ln.value].copy(), pairs.value, lat.value
+
+    def stats(self):
+        st = (C.c_double * 8)()
+        self.L.pp_server_stats(self.h, st)
+        keys = ("submitted", "admitted", "rejected", "completed", "in_flight", "p50_ms", "p99_ms", "pairs")
+        return dict(zip(keys, list(st)))
+
+    def close(self):
+        if self.h:
+            self.L.pp_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
