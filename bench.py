@@ -77,6 +77,17 @@ def workload(name):
     return spec, trg, env, runs, cfg
 
 
+def tip_cloud(n, seed):
+    """A clustered cone "as in configuration 2": same apex, angle, density
+    (13.42 nm^-3) and cluster density, length shortened to hold n ions."""
+    from paraprobe_gb300 import synth
+    rho = 20_000_000 / synth.cone_volume(30.0, 10.0, 200.0)
+    length = synth.cone_length_for(n, rho, 30.0, 10.0)
+    return synth.cone_specimen(n=n, r_apex=30.0, half_angle_deg=10.0, length=length,
+                               n_clusters=max(1, round(2000 * n / 20_000_000)), sigma=1.5, members=50,
+                               cluster_p=(0.7, 0.3), iid=(0.02, 0.01, 0.005), nspecies=6, seed=seed), length
+
+
 # --------------------------------------------------------------------- helpers
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -345,11 +356,164 @@ def run_gpu(args):
                                 "sample": f"oracle port (KD-tree + OpenMP, restating the reference), "
                                           f"{frac * 100:.3f}% of ions eligible as centres "
                                           f"({p} pairs, {s:.1f} s statistics phase)"}
+    if not args.no_batched:
+        ctx.free(cid)
+        line["batched"] = batched_leg(ctx, torch, stream)
+    if not args.no_served:
+        line["served"] = served_leg(ctx)
     ctx.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
+
+
+# ---------------------------------------------------- batched (null model + ROIs)
+def batched_leg(ctx, torch, stream):
+    """Configuration 3: a 5M-ion clustered tip, 256 label shuffles (own seeds)
+    and 64 spherical ROIs (radius log-uniform 5-40 nm, centres uniform in the
+    tip) plus the measured labels, RDF to R = 1.5 nm and kNN k = 1..8 in
+    0.01 nm bins for all 36 pair tasks -- every realisation in one persistent
+    launch.  Compared with the plain single-query path on the same cloud."""
+    from concurrent.futures import ThreadPoolExecutor
+    from paraprobe_gb300 import native as N
+    spec, length = tip_cloud(5_000_000, seed=20261206)
+    n = spec.xyz.shape[0]
+    types = list(range(1, 7))
+    trg = [[a] for a in types for b in types]
+    env = [[b] for a in types for b in types]
+    hist = (0.0, 0.01, 1.5)
+    ks = list(range(8, 0, -1))
+    flags = N.PP_RDF | N.PP_MKNN
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        sets = list(ex.map(lambda r: N.shuffle_labels(spec.labels, 1000 + r), range(256)))
+    sets_dev = torch.from_numpy(np.stack(sets)).to("cuda")  # resident in HBM
+    rng = np.random.default_rng(20261207)
+    rois = []
+    tn = np.tan(np.radians(10.0))
+    while len(rois) < 64:
+        z = rng.uniform(0, length)
+        rz = 30.0 + z * tn
+        x, y = rng.uniform(-rz, rz, 2)
+        if x * x + y * y <= rz * rz:
+            rois.append([x, y, z, float(np.exp(rng.uniform(np.log(5.0), np.log(40.0))))])
+    rois = np.asarray(rois, dtype=np.float32)
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks(trg, env)
+    ctx.hist(*hist)
+    ratio, tile = ctx.autotune(cid, flags, ks, sample=100000)
+    # plain single-query path, same cloud and passes (one realisation)
+    for _ in range(2):
+        ctx.run(cid, flags, ks, stream=stream.cuda_stream)
+        ctx.fetch()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 3
+    plain_pairs = 0
+    for _ in range(reps):
+        ctx.run(cid, flags, ks, stream=stream.cuda_stream)
+        ctx.fetch()
+        plain_pairs += ctx.stats()["pairs"]
+    plain = plain_pairs / (time.perf_counter() - t0)
+
+    def batched_call():
+        ctx.tasks(trg, env)  # drops the cached pair lists: geometry is rebuilt inside the timed call
+        ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets_dev.data_ptr(), nsets=len(sets),
+                        rois=rois, stream=stream.cuda_stream)
+        nreal = ctx.batched_count()
+        pairs = sum(ctx.batched_stats(r)["pairs"] for r in range(nreal))
+        return nreal, pairs
+
+    batched_call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nreal, pairs = batched_call()
+    cold = time.perf_counter() - t0
+    apply_ms = ctx.last_kernel_ms()
+    ctx.free(cid)
+    return {"workload": "5M-ion clustered tip (as configuration 2), 36 pair tasks, RDF + kNN k=1..8, "
+                        "R=1.5 nm, 0.01 nm bins; 1 measured + 256 shuffled label sets + 64 ROIs",
+            "realisations": nreal, "pairs": int(pairs), "value": pairs / cold, "unit": UNIT,
+            "seconds": round(cold, 4), "apply_kernel_ms": round(apply_ms, 3),
+            "plain_single_query": plain, "ratio_vs_plain": (pairs / cold) / plain,
+            "tuning": {"cell_edge_nm": round(1.5 / ratio, 4), "tile": tile},
+            "includes": "pair-list geometry, label gathers, masks, one persistent launch over all realisations, "
+                        "result fetch"}
+
+
+# ------------------------------------------------------------- served queries
+def served_leg(ctx, nq=240, rate=200.0):
+    """Configuration 4: six resident clouds (0.1M .. 50M ions, as
+    configuration 2); queries arrive as a Poisson stream at `rate`/s, each with
+    a random cloud, R ~ U[0.5, 3.0] nm, k ~ U[1, 20] and a random species pair
+    (RDF + kNN, 0.01 nm bins).  Continuous batching on 4 worker streams,
+    admission by HBM footprint; compared with the same queries run one at a
+    time through pp_run."""
+    from paraprobe_gb300 import native as N
+    sizes = (100_000, 1_000_000, 5_000_000, 10_000_000, 20_000_000, 50_000_000)
+    clouds = []
+    for i, n in enumerate(sizes):
+        spec, _ = tip_cloud(n, seed=20261300 + i)
+        c = ctx.upload(spec.xyz, spec.labels)
+        ctx.hull(c, spec.hull, 2.0)
+        ctx.prepare(c, 0.5, 3.0)
+        clouds.append(c)
+        del spec
+    rng = np.random.default_rng(20261208)
+    qs = []
+    for _ in range(nq):
+        c = clouds[rng.integers(0, len(clouds))]
+        R = float(np.float32(rng.uniform(0.5, 3.0)))
+        k = int(rng.integers(1, 21))
+        a, b = (int(x) for x in rng.integers(1, 7, size=2))
+        qs.append((c, N.PP_RDF | N.PP_MKNN, (0.0, 0.01, R), [[a]], [[b]], [k]))
+    gaps = rng.exponential(1.0 / rate, size=nq)
+    free = 0
+    try:
+        import torch
+        free = torch.cuda.mem_get_info()[0]
+    except Exception:
+        pass
+    budget = int(max(2 << 30, free * 0.6))
+    srv = N.Server(ctx, slots=4, budget_bytes=budget)
+    for q in qs[:4]:  # warm the workers
+        srv.wait(srv.submit(*q))
+    t0 = time.perf_counter()
+    tickets, t_next = [], t0
+    for q, g in zip(qs, gaps):
+        t_next += g
+        dt = t_next - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        try:
+            tickets.append(srv.submit(*q))
+        except N.PPError:
+            pass
+    pairs = 0
+    for t in tickets:
+        pairs += srv.wait(t)[1]
+    served_s = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    # the same queries one at a time through the plain path
+    t0 = time.perf_counter()
+    plain_pairs = 0
+    for (c, f, h, tr, en, k) in qs:
+        ctx.tasks(tr, en)
+        ctx.hist(*h)
+        ctx.run(c, f, k)
+        ctx.fetch()
+        plain_pairs += ctx.stats()["pairs"]
+    plain_s = time.perf_counter() - t0
+    for c in clouds:
+        ctx.free(c)
+    return {"workload": "6 resident tips (0.1M, 1M, 5M, 10M, 20M, 50M ions), Poisson 200/s, R~U[0.5,3] nm, "
+                        "k~U[1,20], random species pair, RDF + kNN",
+            "queries": len(tickets), "value": pairs / served_s, "unit": UNIT,
+            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "admitted": int(st["admitted"]) - 4,
+            "rejected": int(st["rejected"]), "slots": 4, "budget_bytes": budget,
+            "plain_single_query": plain_pairs / plain_s, "ratio_vs_plain": (pairs / served_s) / (plain_pairs / plain_s)}
 
 
 # ------------------------------------------------------------ reference arm
@@ -408,6 +572,8 @@ def main():
     ap.add_argument("--workload", default="tip20m", choices=["tip20m", "tip10m", "cyl1m"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched realisation leg")
+    ap.add_argument("--no-served", action="store_true", help="skip the serving leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -882,39 +882,44 @@ __global__ void __launch_bounds__(256) k_apply(ApplyArgs a) {
           }
         }
         if (lane == 0) pairs_lane += (o1 - o0);
-        // kNN: walk the category-sorted list, counting members of each set
+        // kNN: one walk over the category-sorted list serves every set; lane t
+        // looks for the kvals[t % nk]-th member of local set t / nk
         if (a.flags & PP_MKNN) {
           const int nset = a.nsets[cs];
-          for (int p = 0; p < nset; ++p) {
-            const int Sg = a.set_list[cs * 32 + p];
-            // lane kk looks for the kvals[kk]-th member of set p
-            for (int k0 = 0; k0 < a.nkI; k0 += 32) {
-              const int kk = k0 + lane;
-              const uint32_t want = (kk < a.nkI) ? (uint32_t)a.kvals[kk] : 0u;
-              bool done = (kk >= a.nkI);
-              int found = -1;
-              uint32_t seen = 0;
-              for (unsigned long long k = o0; k < o1; k += 32) {
-                const unsigned long long e = k + lane;
-                uint32_t bit = 0;
-                int cat = 0;
-                if (e < o1) {
-                  cat = a.pair_cat[e];
-                  bit = (sEnv[cs * 256 + lab[a.pair_slot[e]]] >> p) & 1u;
-                }
-                const uint32_t mem = __ballot_sync(FULL, bit);
-                const uint32_t c = __popc(mem);
-                const bool here = !done && want > seen && want <= seen + c;
-                const int at = here ? (int)__fns(mem, 0, want - seen) : 0;
-                const int cv = __shfl_sync(FULL, cat, at);
-                if (here) { found = cv; done = true; }
-                seen += c;
-                if (__all_sync(FULL, done)) break;
+          const int ntarget = nset * a.nkI;
+          for (int t0 = 0; t0 < ntarget; t0 += 32) {
+            const int t = t0 + lane;
+            const bool act = t < ntarget;
+            const int q = act ? t / a.nkI : 0, kk = act ? t - q * a.nkI : 0;
+            const uint32_t want = act ? (uint32_t)a.kvals[kk] : 0u;
+            bool done = !act;
+            int found = -1;
+            uint32_t seen = 0;
+            for (unsigned long long k = o0; k < o1; k += 32) {
+              const unsigned long long e = k + lane;
+              uint32_t eb = 0;
+              int cat = 0;
+              if (e < o1) {
+                cat = a.pair_cat[e];
+                eb = sEnv[cs * 256 + lab[a.pair_slot[e]]];
               }
-              if (kk < a.nkI) {
-                const int cat = (found >= 0) ? found : a.cat_miss;
-                atomicAdd(&a.knn_core[((((uint64_t)r * a.nC + cs) * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
+              uint32_t mine = 0;
+              for (int qq = 0; qq < nset; ++qq) {
+                const uint32_t m = __ballot_sync(FULL, (eb >> qq) & 1u);
+                if (qq == q) mine = m;
               }
+              const uint32_t c = __popc(mine);
+              const bool here = !done && want > seen && want <= seen + c;
+              const int at = here ? (int)__fns(mine, 0, want - seen) : 0;
+              const int cv = __shfl_sync(FULL, cat, at);
+              if (here) { found = cv; done = true; }
+              seen += c;
+              if (__all_sync(FULL, done)) break;
+            }
+            if (act) {
+              const int Sg = a.set_list[cs * 32 + q];
+              const int cat = (found >= 0) ? found : a.cat_miss;
+              atomicAdd(&a.knn_core[((((uint64_t)r * a.nC + cs) * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
             }
           }
         }

@@ -259,14 +259,20 @@ class Context:
         self._ck(self.L.pp_run_stats(self.h, C.byref(c), C.byref(d), C.byref(p)), "pp_run_stats")
         return dict(centres=c.value, discarded=d.value, pairs=p.value)
 
-    def run_batched(self, cloud, flags, k_list=(), include_original=True, label_sets=None, rois=None, stream=0):
+    def run_batched(self, cloud, flags, k_list=(), include_original=True, label_sets=None, rois=None, stream=0,
+                    nsets=None):
+        """label_sets: (nsets, n) uint8 array, or a device pointer (int) with nsets given."""
         ks = np.ascontiguousarray(np.asarray(k_list, dtype=np.uint32))
-        ls = None if label_sets is None else np.ascontiguousarray(label_sets, dtype=np.uint8)
-        nls = 0 if ls is None else (ls.shape[0] if ls.ndim == 2 else 1)
+        if isinstance(label_sets, int):
+            lp, nls = C.c_void_p(label_sets), int(nsets)
+        else:
+            ls = None if label_sets is None else np.ascontiguousarray(label_sets, dtype=np.uint8)
+            nls = 0 if ls is None else (ls.shape[0] if ls.ndim == 2 else 1)
+            lp = _p(ls)
         rr = None if rois is None else np.ascontiguousarray(rois, dtype=np.float32).reshape(-1, 4)
         nr = 0 if rr is None else rr.shape[0]
         self._ck(self.L.pp_run_batched(self.h, cloud, flags, _p(ks) if ks.size else None, ks.size,
-                                       1 if include_original else 0, _p(ls), nls, _p(rr), nr, C.c_void_p(stream)),
+                                       1 if include_original else 0, lp, nls, _p(rr), nr, C.c_void_p(stream)),
                  "pp_run_batched")
 
     def batched_count(self):
