@@ -133,6 +133,19 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
  * per block work item. */
 int pp_cloud_tuning(pp_ctx* ctx, int cloud, float cell_ratio, uint32_t tile);
 
+/* FP64 audit of the current tasks and histogram settings on up to
+ * max_centres centres (evenly spaced over the cell-ordered centre list; 0 =
+ * all): every candidate within R is recomputed in double precision from the
+ * same float coordinates.  Reports the largest absolute and relative error of
+ * the float distance, the number of pairs audited, the pairs whose float bin
+ * (the reference's arithmetic) differs from the exact double bin, and the pairs
+ * on which float and double disagree about d <= R; up to `cap` disagreements
+ * are listed as (centre id, neighbour id) with (d_float, d_double).  A
+ * diagnostic with no counterpart in the reference. */
+int pp_fp64_audit(pp_ctx* ctx, int cloud, uint32_t max_centres, double* max_abs, double* max_rel,
+                  uint64_t* pairs, uint64_t* bin_disagree, uint64_t* set_disagree,
+                  uint64_t* listing_ids, double* listing_d, uint64_t cap, uint64_t* nlisted);
+
 /* Context options (value 0 or 1):
  *   "symmetric"  RDF/RIPK-only passes take each pair of two centres once and
  *                credit both (default 1); 0 scans every centre's full ball.

@@ -151,6 +151,9 @@ struct pp_ctx {
   DevBuf labels_run, perm_dev, gather_src;
   // batched geometry cache
   DevBuf pair_count, pair_off, pair_slot, pair_cat, geo_centres, centre_ok, real_labels, rois_dev;
+  DevBuf labels_il, ok_il;  // group-major interleaved copies of real_labels / centre_ok
+  DevBuf maxlist;           // longest pair list (one uint32)
+  uint32_t geo_maxlist = 0;
   uint64_t geo_key_version = ~0ull;
   int geo_cloud = -1;
   float geo_R = -1.f;
@@ -1056,6 +1059,80 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
   return PP_OK;
 }
 
+int pp_fp64_audit(pp_ctx* ctx, int cloud, uint32_t max_centres, double* max_abs, double* max_rel, uint64_t* pairs,
+                  uint64_t* bin_disagree, uint64_t* set_disagree, uint64_t* listing_ids, double* listing_d,
+                  uint64_t cap, uint64_t* nlisted) {
+  if (!ctx) return PP_ERR_INVALID;
+  Cloud* cl = get_cloud(ctx, cloud);
+  if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
+  if (cap && (!listing_ids || !listing_d)) return fail(ctx, PP_ERR_INVALID, "listing buffers missing");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = 0;
+  RunPlan P;
+  int rc = make_plan(ctx, PP_RDF, nullptr, 0, P);
+  if (rc) return rc;
+  const float R = ctx->tab.rmax;
+  if ((rc = ensure_grid(ctx, *cl, R, s))) return rc;
+  const float* surf = nullptr;
+  if ((rc = ensure_surface(ctx, *cl, R, s, &surf))) return rc;
+  DevTables D{};
+  if ((rc = upload_tables(ctx, P, D, s))) return rc;
+  uint32_t ncent = 0;
+  if ((rc = select_centres(ctx, *cl, nullptr, surf, D.cslot, R, &ncent, s))) return rc;
+  const uint32_t take = (max_centres && max_centres < ncent) ? max_centres : ncent;
+  const uint32_t stride = take ? std::max<uint32_t>(1, ncent / std::max<uint32_t>(take, 1)) : 1;
+  pp::ScanArgs a{};
+  fill_scan_common(a, *cl, P, D, ctx->tab);
+  const float Rw = R * (1.0f + 1.0f / 1024.0f);  // candidates slightly beyond R (double may include them)
+  a.R = Rw;
+  a.Rm2 = (Rw + cl->g.margin) * (Rw + cl->g.margin);
+  a.centres = ctx->centres.as<uint32_t>();
+  a.ncentres = take;
+  a.status = nullptr;
+  a.sym = 0;
+  DevBuf out, ls, ld;
+  const uint64_t c = std::min<uint64_t>(cap, 1u << 20);
+  CK(out.ensure(8 * 8));
+  CK(cudaMemset(out.p, 0, 8 * 8));
+  CK(ls.ensure(std::max<uint64_t>(c, 1) * 8));
+  CK(ld.ensure(std::max<uint64_t>(c, 1) * 16));
+  int* status = nullptr;
+  CK(cudaMalloc(&status, 4));
+  CK(cudaMemset(status, 0, 4));
+  a.status = status;
+  pp::launch_audit(a, ctx->tab.hstart, ctx->tab.hscale, ctx->tab.hend, (double)R, (int)ctx->tab.nbins, stride,
+                   out.as<unsigned long long>(), ls.as<uint32_t>(), ld.as<double>(), (uint32_t)c, ctx->sm_count, s);
+  unsigned long long o[8];
+  const cudaError_t e = cudaMemcpy(o, out.p, sizeof o, cudaMemcpyDeviceToHost);
+  cudaFree(status);
+  CK(e);
+  double v;
+  std::memcpy(&v, &o[0], 8);
+  if (max_abs) *max_abs = v;
+  std::memcpy(&v, &o[1], 8);
+  if (max_rel) *max_rel = v;
+  if (pairs) *pairs = o[2];
+  if (bin_disagree) *bin_disagree = o[3];
+  if (set_disagree) *set_disagree = o[4];
+  const uint64_t nl = std::min<uint64_t>(o[5], c);
+  if (nlisted) *nlisted = nl;
+  if (nl) {
+    std::vector<uint32_t> slots(2 * nl), id_of(cl->n);
+    std::vector<double> dd(2 * nl);
+    CK(cudaMemcpy(slots.data(), ls.p, nl * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dd.data(), ld.p, nl * 16, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(id_of.data(), cl->id_of_slot.p, cl->n * 4, cudaMemcpyDeviceToHost));
+    for (uint64_t k = 0; k < nl; ++k) {
+      for (int j = 0; j < 2; ++j) {
+        const uint32_t idx = id_of[slots[2 * k + j]];
+        listing_ids[2 * k + j] = cl->ids.empty() ? (uint64_t)idx : (uint64_t)cl->ids[idx];
+        listing_d[2 * k + j] = dd[2 * k + j];
+      }
+    }
+  }
+  return PP_OK;
+}
+
 int pp_set_option(pp_ctx* ctx, const char* name, int value) {
   if (!ctx || !name) return PP_ERR_INVALID;
   if (std::strcmp(name, "symmetric") == 0) { ctx->no_sym = (value == 0); return PP_OK; }
@@ -1243,6 +1320,10 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
                                              ctx->pair_off.as<unsigned long long>(),
                                              ctx->scan_tmp.as<unsigned long long>(), tmp_elems * 2, s);
       CK(cudaMemcpyAsync(&total, ctx->pair_off.as<unsigned long long>() + nc, 8, cudaMemcpyDeviceToHost, s));
+      CK(ctx->maxlist.ensure(4));
+      CK(cudaMemsetAsync(ctx->maxlist.p, 0, 4, s));
+      pp::launch_max_u32(ctx->pair_count.as<uint32_t>(), nc, ctx->maxlist.as<uint32_t>(), s);
+      CK(cudaMemcpyAsync(&ctx->geo_maxlist, ctx->maxlist.p, 4, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       CK(ctx->pair_slot.ensure(std::max<unsigned long long>(total, 1) * 4));
       CK(ctx->pair_cat.ensure(std::max<unsigned long long>(total, 1) * 2));
@@ -1314,8 +1395,6 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     b.pair_off = ctx->pair_off.as<unsigned long long>();
     b.pair_slot = ctx->pair_slot.as<uint32_t>();
     b.pair_cat = ctx->pair_cat.as<uint16_t>();
-    b.labels = RL;
-    b.centre_ok = OK;
     b.n = n;
     b.nreal = nreal;
     b.H = P.H;
@@ -1330,19 +1409,45 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     b.nS = P.nS;
     b.kvals = D.kvals;
     b.nkI = (int)P.kvals.size();
+    b.kmax = std::max(P.kmax, 1);
     b.flags = ((flags & (PP_RDF | PP_RIPK)) ? PP_RDF : 0) | (P.kr ? PP_MKNN : 0);
     b.rdf_core = ctx->res.rdf.as<unsigned long long>();
     b.knn_core = ctx->res.knn.as<unsigned long long>();
     b.counters = ctx->res.counters.as<unsigned long long>();
-    const double avg = nc ? (double)ctx->geo_pairs / nc : 1.0;
-    b.tile = (uint32_t)std::max(32.0, std::min(4096.0, 65536.0 / std::max(avg, 1.0)));
     b.work = ctx->work.as<uint32_t>();
     b.status = ctx->res.status.as<int>();
+    b.nsmax = std::max(P.emax, 1);
+    b.disjoint = P.disjoint;
+    b.setidx = D.setidx;
+    if (pp::apply_configure(b)) return fail(ctx, PP_ERR_UNSUPPORTED, "RDF bins of one realisation exceed shared memory");
+    b.ngroups = (nreal + b.group - 1) / b.group;
+    // tile: enough pairs per item to amortise the per-item flush of the
+    // shared bins, enough items to balance the persistent blocks, at most
+    // 65535 centres (16-bit kNN bins) and fewer than 2^31 pairs (RDF bins)
+    {
+      const double avg = std::max((double)ctx->geo_pairs / std::max<uint32_t>(nc, 1), 1.0);
+      const double flush_words = ((b.flags & PP_RDF) ? (double)P.nC * P.nE * P.H * b.group : 0.0) +
+                                 (b.knn_smem ? (double)P.nC * P.nS * P.kvals.size() * P.H * b.group / 2 : 0.0);
+      double tile = std::max(1.0e6, 256.0 * flush_words) / (avg * b.group);
+      const double balance = (double)nc * b.ngroups / (8.0 * ctx->sm_count);
+      tile = std::min(tile, balance);
+      tile = std::min(tile, 2147483647.0 / std::max<uint32_t>(ctx->geo_maxlist, 1));
+      tile = std::min(tile, 65535.0);
+      b.tile = (uint32_t)std::max(32.0, std::floor(tile));
+      if ((double)b.tile * ctx->geo_maxlist >= 2147483648.0 && b.tile > 1)
+        b.tile = (uint32_t)std::max<uint64_t>(1, 2147483647ull / std::max<uint32_t>(ctx->geo_maxlist, 1));
+    }
+    const uint64_t nrg = (uint64_t)b.ngroups * b.group;
+    CK(ctx->labels_il.ensure(std::max<uint64_t>(n, 1) * nrg));
+    CK(ctx->ok_il.ensure(std::max<uint64_t>(nc, 1) * nrg));
+    pp::launch_interleave(RL, nreal, n, b.group, ctx->labels_il.as<uint8_t>(), s);
+    pp::launch_interleave(OK, nreal, nc, b.group, ctx->ok_il.as<uint8_t>(), s);
+    b.labels = ctx->labels_il.as<uint8_t>();
+    b.centre_ok = ctx->ok_il.as<uint8_t>();
     CK(cudaEventRecord(ctx->ev0, s));
     rc = pp::launch_apply(b, ctx->sm_count, s);
     CK(cudaEventRecord(ctx->ev1, s));
     ctx->ev_recorded = true;
-    if (rc == -2) return fail(ctx, PP_ERR_UNSUPPORTED, "RDF bins of one realisation exceed shared memory");
     if (rc) return fail(ctx, PP_ERR_CUDA, "apply launch failed");
   }
   ctx->res.valid = true;

@@ -88,10 +88,13 @@ struct ApplyArgs {
   const unsigned long long* pair_off;  // [ncentres + 1]
   const uint32_t* pair_slot;
   const uint16_t* pair_cat;
-  const uint8_t* labels;         // [nreal][n] type per sorted slot
-  const uint8_t* centre_ok;      // [nreal][ncentres] 1 if a centre in that realisation (nullable = all)
+  const uint8_t* labels;         // [ngroups][n][group] type per sorted slot
+  const uint8_t* centre_ok;      // [ngroups][ncentres][group] 1 if a centre in that realisation
   uint64_t n;
   int nreal;
+  int group, ngroups;            // realisations per work item (1, 2, 4, 8) and the number of groups
+  int knn_smem;                  // kNN bins of a work item held in shared memory
+  int nsmax;                     // most environment sets of one centre type
   int H, cat_miss;
   const int8_t* cslot_of;
   const int8_t* eslot_of;
@@ -101,6 +104,9 @@ struct ApplyArgs {
   const int* nsets;
   int nS;
   const int* kvals;
+  int kmax;                      // largest k requested
+  int disjoint;                  // no type in two environment sets of one centre type
+  const int8_t* setidx;          // [nC][256] set of a type (disjoint sets), -1 = none
   int nkI;
   uint32_t flags;
   unsigned long long* rdf_core;  // [nreal][nC][nE][H]
@@ -149,6 +155,11 @@ int launch_tri_bins(const float* tbox, uint64_t ntri, Grid tg, float grow, uint3
                     uint64_t* total_out, cudaStream_t s);
 int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s);
 int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s);
+constexpr int kApplyThreads = 1024;
+// picks the realisation group and where kNN bins accumulate; -2 = no fit
+int apply_configure(ApplyArgs& a);
+void launch_max_u32(const uint32_t* v, uint64_t n, uint32_t* out, cudaStream_t s);
+void launch_interleave(const uint8_t* src, uint64_t rows, uint64_t cols, int G, uint8_t* dst, cudaStream_t s);
 void launch_roi_mask(const float4* ions, const uint32_t* centres, uint32_t ncentres, const float* rois,
                      int nrois, float R, const uint8_t* labels, const int8_t* cslot_of,
                      uint8_t* centre_ok, cudaStream_t s);
@@ -161,5 +172,9 @@ void launch_neighbors(const float4* ions, const uint32_t* cell_start, Grid g, ui
                       uint32_t cap, uint32_t* count, cudaStream_t s);
 
 unsigned long long kernel_launches();
+// FP64 audit of the float distances and bins of the selected centres.
+void launch_audit(const ScanArgs& a, double start, double scale, double end, double R64, int nbins, uint32_t stride,
+                  unsigned long long* out, uint32_t* list_slots, double* list_d, uint32_t cap, int sm_count,
+                  cudaStream_t s);
 
 }  // namespace pp

@@ -835,113 +835,259 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
 }
 
 // --------------------------------------------------------------- K5 batched
-// One work item = a tile of geometry centres; the block applies every
-// realisation to the tile's stored (slot, category) lists, which are sorted
-// by category per centre.  RDF bins of the current realisation accumulate in
-// shared memory and are flushed before the next realisation; the k-th nearest
-// member of an environment set is the k-th member met walking the sorted list.
-__global__ void __launch_bounds__(256) k_apply(ApplyArgs a) {
+// One work item = (tile of geometry centres, group of G realisations).  Labels
+// and centre masks are stored group-major, G realisations interleaved per slot
+// -- realisation g*G + r of slot s at (g * n + s) * G + r -- so one G-byte load
+// gives a neighbour's type in every realisation of the group while neighbours
+// stay close in memory.  One warp walks one centre's category-sorted pair list
+// once for the whole group.  For kNN every list entry knows its rank among the
+// members of its environment set met so far, and the entry of rank k-1 is the
+// k-th nearest member (the list is ordered by category, which is all a
+// histogram of distances resolves).  RDF bins (32-bit) and, when KS, kNN bins
+// (16-bit, two per word) of the group live in shared memory, bin-major with G
+// counters per bin, and are added to the global cores once per item.  The host
+// sizes a tile so that no 16-bit bin can reach 65536 within one item (at most
+// one count per centre) and no RDF bin 2^32 (tile x longest list < 2^31).
+template <int G>
+struct LabelWord;
+template <> struct LabelWord<1> { using T = uint8_t; };
+template <> struct LabelWord<2> { using T = uint16_t; };
+template <> struct LabelWord<4> { using T = uint32_t; };
+template <> struct LabelWord<8> { using T = unsigned long long; };
+
+struct ApplyLayout {
+  int nrdf, nknn, nkw, nenv, nset8;
+  __host__ __device__ ApplyLayout(const ApplyArgs& a, int G, bool ks) {
+    const bool knn = (a.flags & PP_MKNN) != 0;
+    nrdf = (a.flags & PP_RDF) ? a.nC * a.nE * a.H : 0;
+    nknn = (ks && knn) ? a.nC * a.nS * a.nkI * a.H : 0;
+    nkw = (nknn * G + 1) / 2;
+    nenv = (knn && !a.disjoint) ? a.nC * 256 : 0;
+    nset8 = (knn && a.disjoint) ? a.nC * 256 : 0;
+  }
+  // per-warp set counters live in shared memory only for overlapping sets
+  __host__ __device__ int seen_words(int G, int nwarps, int nsmax) const { return nenv ? nwarps * G * nsmax : 0; }
+  __host__ __device__ size_t bytes(int G, int nwarps, int nsmax) const {
+    return (size_t)16 * G + (size_t)nrdf * G * 4 + (size_t)nkw * 4 + (size_t)seen_words(G, nwarps, nsmax) * 4 +
+           (size_t)nenv * 4 + nset8 + 768;
+  }
+};
+
+template <int G, bool KS>
+__global__ void __launch_bounds__(1024, 1) k_apply(ApplyArgs a) {
+  using W = typename LabelWord<G>::T;
   extern __shared__ __align__(16) unsigned char smem[];
   const int H = a.H;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  int8_t* sC = (int8_t*)smem;
-  int8_t* sE = sC + 256;
-  uint32_t* sEnv = (uint32_t*)(sE + 256);
-  const int nenv = (a.flags & PP_MKNN) ? a.nC * 256 : 0;
-  uint32_t* sRdf = sEnv + nenv;
-  const int nrdf = (a.flags & PP_RDF) ? a.nC * a.nE * H : 0;
+  const bool knn = (a.flags & PP_MKNN) != 0;
+  const ApplyLayout L(a, G, KS);
+  const int nsmax = max(a.nsmax, 1);
+  unsigned long long* sCnt = (unsigned long long*)smem;      // [G][2] pairs, centres
+  uint32_t* sRdf = (uint32_t*)(sCnt + 2 * G);                 // [nrdf][G]
+  uint32_t* sKnn = sRdf + L.nrdf * G;                         // [nknn][G] 16-bit
+  uint32_t* sSeen = sKnn + L.nkw;                             // [nwarps][G][nsmax]
+  uint32_t* sEnv = sSeen + L.seen_words(G, nwarps, nsmax);    // [nC][256] (overlapping sets)
+  int8_t* sSet = (int8_t*)(sEnv + L.nenv);                    // [nC][256] (disjoint sets)
+  int8_t* sC = sSet + L.nset8;                                // 256
+  int8_t* sE = sC + 256;                                      // 256
+  int8_t* sK = sE + 256;                                      // 256: k -> index into kvals, -1
   __shared__ uint32_t s_item;
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) { sC[i] = a.cslot_of[i]; sE[i] = a.eslot_of[i]; }
-  for (int i = threadIdx.x; i < nenv; i += blockDim.x) sEnv[i] = a.envbits[i];
-  for (int i = threadIdx.x; i < nrdf; i += blockDim.x) sRdf[i] = 0;
+  for (int i = threadIdx.x; i < 2 * G; i += blockDim.x) sCnt[i] = 0;
+  for (int i = threadIdx.x; i < L.nrdf * G + L.nkw; i += blockDim.x) sRdf[i] = 0;
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) { sC[i] = a.cslot_of[i]; sE[i] = a.eslot_of[i]; sK[i] = -1; }
+  for (int i = threadIdx.x; i < L.nenv; i += blockDim.x) sEnv[i] = a.envbits[i];
+  for (int i = threadIdx.x; i < L.nset8; i += blockDim.x) sSet[i] = a.setidx[i];
   __syncthreads();
+  if (knn)
+    for (int i = threadIdx.x; i < a.nkI; i += blockDim.x)
+      if (a.kvals[i] >= 1 && a.kvals[i] <= 255) sK[a.kvals[i]] = (int8_t)i;
+  __syncthreads();
+  uint32_t* seen = sSeen + warp * G * nsmax;
+  const uint32_t lt = (1u << lane) - 1u;
   const uint32_t ntiles = (a.ncentres + a.tile - 1) / a.tile;
+  const uint32_t nitems = ntiles * (uint32_t)a.ngroups;
+  const uint64_t knn_real = (uint64_t)a.nC * a.nS * a.nkI * H;   // global kNN bins per realisation
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(a.work, 1u);
     __syncthreads();
     const uint32_t item = s_item;
     __syncthreads();
-    if (item >= ntiles) break;
-    const uint32_t c0 = item * a.tile, c1 = min(c0 + a.tile, a.ncentres);
-    for (int r = 0; r < a.nreal; ++r) {
-      const uint8_t* lab = a.labels + (uint64_t)r * a.n;
-      const uint8_t* ok = a.centre_ok ? a.centre_ok + (uint64_t)r * a.ncentres : nullptr;
-      unsigned long long pairs_lane = 0, cen = 0;
-      for (uint32_t ci = c0 + warp; ci < c1; ci += nwarps) {
-        if (ok && !ok[ci]) continue;
-        const uint32_t self = a.centres[ci];
-        const int cs = sC[lab[self]];
-        if (cs < 0) continue;
-        const unsigned long long o0 = a.pair_off[ci], o1 = a.pair_off[ci + 1];
-        if (lane == 0) ++cen;
-        // RDF: every list entry of an environment type
-        if (a.flags & PP_RDF) {
-          for (unsigned long long k = o0 + lane; k < o1; k += 32) {
-            const int es = sE[lab[a.pair_slot[k]]];
-            if (es >= 0) atomicAdd(&sRdf[((uint32_t)cs * a.nE + es) * H + a.pair_cat[k]], 1u);
+    if (item >= nitems) break;
+    const uint32_t tile = item / a.ngroups, grp = item - tile * a.ngroups;
+    const int rb = (int)grp * G;
+    const W* lab = (const W*)(a.labels + (uint64_t)grp * a.n * G);
+    const W* okw = (const W*)(a.centre_ok + (uint64_t)grp * a.ncentres * G);
+    const uint32_t c0 = tile * a.tile, c1 = min(c0 + a.tile, a.ncentres);
+    // one kNN count: bin (c, set q, order kk, category) of realisation rb + r
+    auto knn_add = [&](int c, int q, int kk, int cat, int r) {
+      const int Sg = a.set_list[c * 32 + q];
+      const uint32_t bin = (((uint32_t)c * a.nS + Sg) * a.nkI + kk) * H + cat;
+      if (KS) {
+        const uint32_t i16 = bin * G + r;
+        atomicAdd(&sKnn[i16 >> 1], 1u << ((i16 & 1u) * 16));
+      } else {
+        atomicAdd(&a.knn_core[(uint64_t)(rb + r) * knn_real + bin], 1ull);
+      }
+    };
+    for (uint32_t ci = c0 + warp; ci < c1; ci += nwarps) {
+      const uint32_t self = a.centres[ci];
+      const W lw = lab[self];
+      const W ow = okw[ci];
+      int cs[G];
+      uint32_t cnt[G];   // disjoint sets: lane q counts the members of set q met so far
+      uint32_t kn = 0;   // realisations whose kNN walk is still open
+      bool any = false;
+#pragma unroll
+      for (int r = 0; r < G; ++r) {
+        const bool ok = ((ow >> (8 * r)) & 0xff) != 0 && rb + r < a.nreal;
+        cs[r] = ok ? (int)sC[(lw >> (8 * r)) & 0xff] : -1;
+        any |= cs[r] >= 0;
+        if (knn && cs[r] >= 0 && a.nsets[cs[r]] > 0) kn |= 1u << r;
+        cnt[r] = 0;
+        if (L.nenv && lane < nsmax) seen[r * nsmax + lane] = 0;
+      }
+      if (!any) continue;
+      __syncwarp();
+      const unsigned long long o0 = a.pair_off[ci], o1 = a.pair_off[ci + 1];
+      if (lane == 0) {
+#pragma unroll
+        for (int r = 0; r < G; ++r)
+          if (cs[r] >= 0) { atomicAdd(&sCnt[2 * r], o1 - o0); atomicAdd(&sCnt[2 * r + 1], 1ull); }
+      }
+      for (unsigned long long k0 = o0; k0 < o1; k0 += 32) {
+        if (!L.nrdf && !kn) break;
+        const unsigned long long e = k0 + lane;
+        const bool valid = e < o1;
+        int cat = 0;
+        W nw = 0;
+        if (valid) {
+          cat = a.pair_cat[e];
+          nw = lab[a.pair_slot[e]];
+        }
+#pragma unroll
+        for (int r = 0; r < G; ++r) {
+          const int c = cs[r];
+          if (c < 0) continue;
+          const int t = (int)((nw >> (8 * r)) & 0xff);
+          if (L.nrdf && valid) {
+            const int es = sE[t];
+            if (es >= 0) atomicAdd(&sRdf[(((uint32_t)c * a.nE + es) * H + cat) * G + r], 1u);
           }
-        }
-        if (lane == 0) pairs_lane += (o1 - o0);
-        // kNN: one walk over the category-sorted list serves every set; lane t
-        // looks for the kvals[t % nk]-th member of local set t / nk
-        if (a.flags & PP_MKNN) {
-          const int nset = a.nsets[cs];
-          const int ntarget = nset * a.nkI;
-          for (int t0 = 0; t0 < ntarget; t0 += 32) {
-            const int t = t0 + lane;
-            const bool act = t < ntarget;
-            const int q = act ? t / a.nkI : 0, kk = act ? t - q * a.nkI : 0;
-            const uint32_t want = act ? (uint32_t)a.kvals[kk] : 0u;
-            bool done = !act;
-            int found = -1;
-            uint32_t seen = 0;
-            for (unsigned long long k = o0; k < o1; k += 32) {
-              const unsigned long long e = k + lane;
-              uint32_t eb = 0;
-              int cat = 0;
-              if (e < o1) {
-                cat = a.pair_cat[e];
-                eb = sEnv[cs * 256 + lab[a.pair_slot[e]]];
-              }
-              uint32_t mine = 0;
-              for (int qq = 0; qq < nset; ++qq) {
-                const uint32_t m = __ballot_sync(FULL, (eb >> qq) & 1u);
-                if (qq == q) mine = m;
-              }
-              const uint32_t c = __popc(mine);
-              const bool here = !done && want > seen && want <= seen + c;
-              const int at = here ? (int)__fns(mine, 0, want - seen) : 0;
-              const int cv = __shfl_sync(FULL, cat, at);
-              if (here) { found = cv; done = true; }
-              seen += c;
-              if (__all_sync(FULL, done)) break;
+          if (!((kn >> r) & 1u)) continue;
+          const int nset = a.nsets[c];
+          if (a.disjoint) {
+            // each type is in at most one set.  One ballot per bit of the set
+            // index gives every lane two masks: the lanes holding members of
+            // its entry's set, and the lanes holding members of set `lane`
+            const int q = valid ? (int)sSet[c * 256 + t] : -1;
+            const bool mem = q >= 0;
+            const uint32_t m0 = __ballot_sync(FULL, mem);
+            if (!m0) continue;
+            uint32_t mine = m0, own = m0;
+            const int nb = nset > 1 ? 32 - __clz(nset - 1) : 0;
+            for (int b = 0; b < nb; ++b) {
+              const uint32_t bb = __ballot_sync(FULL, (q >> b) & 1);
+              mine &= ((q >> b) & 1) ? bb : ~bb;
+              own &= ((lane >> b) & 1) ? bb : ~bb;
             }
-            if (act) {
-              const int Sg = a.set_list[cs * 32 + q];
-              const int cat = (found >= 0) ? found : a.cat_miss;
-              atomicAdd(&a.knn_core[((((uint64_t)r * a.nC + cs) * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
+            const uint32_t before = __shfl_sync(FULL, cnt[r], q & 31);
+            if (mem) {
+              const uint32_t rank = before + __popc(mine & lt);   // 0-based among set members
+              if (rank < (uint32_t)a.kmax) {
+                const int kk = sK[rank + 1];
+                if (kk >= 0) knn_add(c, q, kk, cat, r);
+              }
             }
+            cnt[r] += __popc(own);
+            if (!__any_sync(FULL, lane < nset && cnt[r] < (uint32_t)a.kmax)) kn &= ~(1u << r);
+            continue;
           }
+          uint32_t* sr = seen + r * nsmax;
+          const uint32_t eb = valid ? sEnv[c * 256 + t] : 0u;
+          bool open = false;
+          for (int q = 0; q < nset; ++q) {
+            const bool mem = (eb >> q) & 1u;
+            const uint32_t m = __ballot_sync(FULL, mem);
+            if (!m) { open |= sr[q] < (uint32_t)a.kmax; continue; }
+            const uint32_t before = sr[q];
+            if (mem) {
+              const uint32_t rank = before + __popc(m & lt);
+              if (rank < (uint32_t)a.kmax) {
+                const int kk = sK[rank + 1];
+                if (kk >= 0) knn_add(c, q, kk, cat, r);
+              }
+            }
+            const uint32_t after = before + __popc(m);
+            __syncwarp();
+            if (lane == 0) sr[q] = after;
+            __syncwarp();
+            open |= after < (uint32_t)a.kmax;
+          }
+          if (!open) kn &= ~(1u << r);
         }
       }
-      for (int o = 16; o; o >>= 1) {
-        pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
-        cen += __shfl_xor_sync(FULL, cen, o);
-      }
-      if (lane == 0 && (pairs_lane || cen)) {
-        atomicAdd(&a.counters[2 * r], pairs_lane);
-        atomicAdd(&a.counters[2 * r + 1], cen);
-      }
-      __syncthreads();
-      if (nrdf) {
-        unsigned long long* dst = a.rdf_core + (uint64_t)r * a.nC * a.nE * H;
-        for (int i = threadIdx.x; i < nrdf; i += blockDim.x) {
-          const uint32_t v = sRdf[i];
-          if (v) { atomicAdd(&dst[i], (unsigned long long)v); sRdf[i] = 0; }
+      // members not met within R: the remaining orders of each set are misses
+#pragma unroll
+      for (int r = 0; r < G; ++r) {
+        const int c = cs[r];
+        if (!knn || c < 0) continue;
+        const int nset = a.nsets[c];
+        for (int q = 0; q < nset; ++q) {
+          uint32_t got = __shfl_sync(FULL, cnt[r], q);
+          if (L.nenv) got = seen[r * nsmax + q];
+          if (got >= (uint32_t)a.kmax) continue;
+          for (int kk = lane; kk < a.nkI; kk += 32)
+            if (got < (uint32_t)a.kvals[kk]) knn_add(c, q, kk, a.cat_miss, r);
         }
       }
-      __syncthreads();
+      __syncwarp();
     }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 2 * G; i += blockDim.x) {
+      const unsigned long long v = sCnt[i];
+      if (v) { atomicAdd(&a.counters[2 * (uint64_t)rb + i], v); sCnt[i] = 0; }
+    }
+    for (int i = threadIdx.x; i < L.nrdf * G; i += blockDim.x) {
+      const uint32_t v = sRdf[i];
+      if (v) {
+        const int r = i % G, bin = i / G;
+        atomicAdd(&a.rdf_core[(uint64_t)(rb + r) * L.nrdf + bin], (unsigned long long)v);
+        sRdf[i] = 0;
+      }
+    }
+    if (KS) {
+      for (int w = threadIdx.x; w < L.nkw; w += blockDim.x) {
+        const uint32_t v = sKnn[w];
+        if (v) {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const uint32_t c16 = (v >> (16 * h)) & 0xffffu;
+            if (c16) {
+              const uint32_t i16 = 2 * w + h;
+              const int r = i16 % G;
+              const uint32_t bin = i16 / G;
+              atomicAdd(&a.knn_core[(uint64_t)(rb + r) * knn_real + bin], (unsigned long long)c16);
+            }
+          }
+          sKnn[w] = 0;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Realisation-major byte arrays src[rows][cols] to the group-major layout
+// k_apply reads: dst[((r / G) * cols + c) * G + r % G], rows padded to a
+// multiple of G with zeros.
+__global__ void k_interleave(const uint8_t* __restrict__ src, uint64_t rows, uint64_t cols, int G,
+                             uint8_t* __restrict__ dst) {
+  const uint64_t rows_pad = (rows + G - 1) / G * G;
+  const uint64_t total = cols * rows_pad;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t g = t / (cols * G), rem = t - g * cols * G;
+    const uint64_t c = rem / G, r = g * G + (rem - c * G);
+    dst[t] = r < rows ? src[r * cols + c] : 0;
   }
 }
 
@@ -965,6 +1111,86 @@ __global__ void k_perm_mask(const uint8_t* __restrict__ lab, const uint32_t* __r
                             const int8_t* __restrict__ cslot_of, uint8_t* __restrict__ ok) {
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < nc; t += (uint64_t)gridDim.x * blockDim.x)
     ok[t] = cslot_of[lab[centres[t]]] >= 0;
+}
+
+void counted();
+
+// FP64 audit: for each audited centre and each candidate within R (1 + 2^-10),
+// the float distance the reference computes (sqrtf of the float d^2) is
+// compared with the double-precision distance of the same coordinates, and
+// the float bin (threshold table) with the bin of exact double arithmetic,
+// floor((d64 - start) * nbins / (end - start)).  Out: [0] max |d32 - d64|,
+// [1] max relative error (as double bits, atomicMax on ordered uint64), [2]
+// pairs audited, [3] bin disagreements, [4] neighbour-set disagreements; up
+// to cap disagreements are listed as (centre slot, neighbour slot, d32, d64).
+struct AuditArgs {
+  double start, scale, end, R64;
+  int nbins;
+  uint32_t stride;
+  unsigned long long* out;
+  uint32_t* list_slots;
+  double* list_d;
+  uint32_t cap;
+};
+
+__device__ __forceinline__ int cat64(double d, const AuditArgs& x) {
+  if (d < x.start) return 0;
+  if (d > x.end) return x.nbins + 1;
+  const double b = floor((d - x.start) * x.scale);
+  return b < (double)x.nbins ? 1 + (int)b : x.nbins + 1;
+}
+
+__global__ void __launch_bounds__(256) k_audit(ScanArgs a, AuditArgs x) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  int8_t* rowtab = (int8_t*)smem;
+  float* T = (float*)(smem + ((ROW_TABLE_ENTRIES * 2 + 15) & ~15));
+  for (int i = threadIdx.x; i < ROW_TABLE_ENTRIES * 2; i += blockDim.x) rowtab[i] = a.rowtab[i];
+  for (int i = threadIdx.x; i < a.H; i += blockDim.x) T[i] = a.cat_T[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  const double R64 = x.R64;
+  for (uint32_t ci = gw; ci < a.ncentres; ci += nw) {
+    const uint32_t self = a.centres[(uint64_t)ci * x.stride];
+    const float4 cp = a.ions[self];
+    for_each_candidate(a, rowtab, cp, self, lane, [&](bool valid, uint32_t slot, float d2, bool inball, uint32_t,
+                                                      bool) {
+      if (!valid || slot == self) return;
+      const float4 q = __ldg(a.ions + slot);
+      const double dx = (double)cp.x - (double)q.x, dy = (double)cp.y - (double)q.y, dz = (double)cp.z - (double)q.z;
+      const double d64 = sqrt(dx * dx + dy * dy + dz * dz);
+      const bool in64 = d64 <= R64;
+      if (!inball && !in64) return;
+      if (inball != in64) {
+        atomicAdd(&x.out[4], 1ull);
+      } else {
+        atomicAdd(&x.out[2], 1ull);
+        const double d32 = (double)sqrtf(d2);
+        const double err = fabs(d32 - d64);
+        atomicMax(&x.out[0], (unsigned long long)__double_as_longlong(err));
+        if (d64 > 0) atomicMax(&x.out[1], (unsigned long long)__double_as_longlong(err / d64));
+        if (category(d2, T, a.H, a.guess_start, a.guess_scale) == cat64(d64, x)) return;
+        atomicAdd(&x.out[3], 1ull);
+      }
+      const unsigned long long at = atomicAdd(&x.out[5], 1ull);
+      if (at < x.cap) {
+        x.list_slots[2 * at] = self;
+        x.list_slots[2 * at + 1] = slot;
+        x.list_d[2 * at] = (double)sqrtf(d2);
+        x.list_d[2 * at + 1] = d64;
+      }
+    });
+  }
+}
+
+void launch_audit(const ScanArgs& a, double start, double scale, double end, double R64, int nbins, uint32_t stride,
+                  unsigned long long* out, uint32_t* list_slots, double* list_d, uint32_t cap, int sm_count,
+                  cudaStream_t s) {
+  AuditArgs x{start, scale, end, R64, nbins, stride, out, list_slots, list_d, cap};
+  const size_t smem = ((ROW_TABLE_ENTRIES * 2 + 15) & ~15) + (size_t)a.H * 4;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k_audit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  counted();
+  k_audit<<<sm_count * 4, 256, smem, s>>>(a, x);
 }
 
 // all ions j != self with d^2 <= R^2 in the full 3-D stencil (debug / parity)
@@ -1159,19 +1385,72 @@ int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_
   return -2;
 }
 
-int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s) {
-  size_t smem = 512;
-  if (a.flags & PP_MKNN) smem += (size_t)a.nC * 256 * 4;
-  if (a.flags & PP_RDF) smem += (size_t)a.nC * a.nE * a.H * 4;
-  if (smem > 200 * 1024) return -2;
+template <int G, bool KS>
+static int launch_apply_t(const ApplyArgs& a, int sm_count, size_t smem, cudaStream_t s) {
+  auto kern = k_apply<G, KS>;
   if (smem > 48 * 1024) {
-    if (cudaFuncSetAttribute(k_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
   }
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_apply, 256, smem) != cudaSuccess || per_sm < 1) return -1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kApplyThreads, smem) != cudaSuccess || per_sm < 1)
+    return -1;
   counted();
-  k_apply<<<sm_count * per_sm, 256, smem, s>>>(a);
+  kern<<<sm_count * per_sm, kApplyThreads, smem, s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+static size_t apply_bytes(const ApplyArgs& a, int G, bool ks) {
+  return ApplyLayout(a, G, ks).bytes(G, kApplyThreads / 32, std::max(a.nsmax, 1));
+}
+
+int apply_configure(ApplyArgs& a) {
+  const size_t cap = 220 * 1024;
+  const bool knn = (a.flags & PP_MKNN) != 0;
+  for (int pass = knn ? 0 : 1; pass < 2; ++pass) {
+    const bool ks = pass == 0;
+    for (int G = 8; G >= 1; G >>= 1) {
+      if (apply_bytes(a, G, ks) <= cap) {
+        a.group = G;
+        a.knn_smem = ks ? 1 : 0;
+        return 0;
+      }
+    }
+  }
+  return -2;
+}
+
+int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s) {
+  const int G = a.group;
+  const bool ks = a.knn_smem != 0;
+  const size_t smem = apply_bytes(a, G, ks);
+  if (ks) {
+    if (G == 8) return launch_apply_t<8, true>(a, sm_count, smem, s);
+    if (G == 4) return launch_apply_t<4, true>(a, sm_count, smem, s);
+    if (G == 2) return launch_apply_t<2, true>(a, sm_count, smem, s);
+    return launch_apply_t<1, true>(a, sm_count, smem, s);
+  }
+  if (G == 8) return launch_apply_t<8, false>(a, sm_count, smem, s);
+  if (G == 4) return launch_apply_t<4, false>(a, sm_count, smem, s);
+  if (G == 2) return launch_apply_t<2, false>(a, sm_count, smem, s);
+  return launch_apply_t<1, false>(a, sm_count, smem, s);
+}
+
+__global__ void k_max_u32(const uint32_t* __restrict__ v, uint64_t n, uint32_t* out) {
+  uint32_t m = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    m = max(m, v[i]);
+  for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(FULL, m, o));
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+void launch_max_u32(const uint32_t* v, uint64_t n, uint32_t* out, cudaStream_t s) {
+  counted();
+  k_max_u32<<<grid_for(n, 256), 256, 0, s>>>(v, n, out);
+}
+
+void launch_interleave(const uint8_t* src, uint64_t rows, uint64_t cols, int G, uint8_t* dst, cudaStream_t s) {
+  counted();
+  k_interleave<<<grid_for(cols * ((rows + G - 1) / G * G), 256), 256, 0, s>>>(src, rows, cols, G, dst);
 }
 
 void launch_roi_mask(const float4* ions, const uint32_t* centres, uint32_t nc, const float* rois, int nrois, float R,

@@ -25,6 +25,7 @@ EXPORTS = (
     "pp_batched_stats", "pp_neighbors", "pp_shuffle_labels", "pp_device_info", "pp_kernel_launches",
     "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option", "pp_cloud_prepare",
     "pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_stats", "pp_server_destroy",
+    "pp_fp64_audit",
 )
 
 _lib = None
@@ -82,6 +83,8 @@ def load():
         "pp_server_wait": ([vp, u64, vp, C.c_size_t, C.POINTER(u64), C.POINTER(u64), C.POINTER(C.c_double)], i32),
         "pp_server_stats": ([vp, C.POINTER(C.c_double)], i32),
         "pp_server_destroy": ([vp], None),
+        "pp_fp64_audit": ([vp, i32, u32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(u64),
+                           C.POINTER(u64), C.POINTER(u64), vp, vp, u64, C.POINTER(u64)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -226,6 +229,17 @@ class Context:
         self._ck(self.L.pp_autotune(self.h, cloud, flags, _p(ks) if ks.size else None, ks.size, sample,
                                     C.byref(r), C.byref(t)), "pp_autotune")
         return r.value, t.value
+
+    def fp64_audit(self, cloud, max_centres=0, cap=4096):
+        """FP64 recomputation of the current tasks' distances and bins."""
+        ma, mr = C.c_double(), C.c_double()
+        pairs, bd, sd, nl = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+        ids = np.zeros((max(cap, 1), 2), dtype=np.uint64)
+        dd = np.zeros((max(cap, 1), 2), dtype=np.float64)
+        self._ck(self.L.pp_fp64_audit(self.h, cloud, max_centres, C.byref(ma), C.byref(mr), C.byref(pairs),
+                                      C.byref(bd), C.byref(sd), _p(ids), _p(dd), cap, C.byref(nl)), "pp_fp64_audit")
+        return dict(max_abs_err=ma.value, max_rel_err=mr.value, pairs=pairs.value, bin_disagreements=bd.value,
+                    set_disagreements=sd.value, listed_ids=ids[: nl.value], listed_d=dd[: nl.value])
 
     def prepare(self, cloud, r_lo, r_hi):
         self._ck(self.L.pp_cloud_prepare(self.h, cloud, r_lo, r_hi), "pp_cloud_prepare")

@@ -147,6 +147,33 @@ def test_batched_matches_plain(ctx, oracle):
     ctx.free(cid)
 
 
+@pytest.mark.parametrize("rincr,nsets", [(0.001, 5), (0.02, 1), (0.0005, 2)])
+def test_batched_overlapping_sets(ctx, oracle, rincr, nsets):
+    """Overlapping environment sets, cumulative RIPK and an unsorted k list;
+    the bin widths select 2-, 4- and 1-realisation groups in the batched kernel."""
+    spec = synth.cone_specimen(n=30000, r_apex=8.0, half_angle_deg=10.0, length=14.0, n_clusters=15,
+                               members=40, nspecies=3, seed=31, nseg=64, stack=4.0)
+    trg = [[1], [2], [3, 1], [1, 2, 3]]
+    env = [[1, 2], [2, 3], [1, 2, 3], [3]]
+    rmin, rmax = 0.0, 1.2
+    ks = [3, 12, 1, 5]
+    flags = ALL
+    sets = np.stack([N.shuffle_labels(spec.labels, 700 + s) for s in range(nsets)])
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks(trg, env)
+    ctx.hist(rmin, rincr, rmax)
+    ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets)
+    assert ctx.batched_count() == 1 + nsets
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    ref0 = oracle.spatstat(spec.xyz, spec.labels, surf, rmin, rincr, rmax, flags, trg, env, ks)
+    assert np.array_equal(ctx.fetch_batched(0), ref0["bins"])
+    for q in range(nsets):
+        refq = oracle.spatstat(spec.xyz, sets[q], surf, rmin, rincr, rmax, flags, trg, env, ks)
+        assert np.array_equal(ctx.fetch_batched(1 + q), refq["bins"]), f"label set {q}"
+    ctx.free(cid)
+
+
 def test_results_independent_of_tuning(ctx, oracle):
     spec = synth.cone_specimen(n=50000, r_apex=8.0, half_angle_deg=10.0, length=20.0, n_clusters=25,
                                members=40, nspecies=3, seed=21, nseg=64, stack=4.0)
