@@ -106,6 +106,23 @@ int pp_surfdist_upload(pp_ctx* ctx, int cloud, const float* d2);
 /* The ion2surf values pp_run used last for this cloud (n floats, input order). */
 int pp_surfdist_fetch(pp_ctx* ctx, int cloud, float* d2_out, uint64_t n);
 
+/* ion2surf without any device allocation, for callers that cannot call
+ * cudaMalloc (a host whose own pool owns the device memory, a loop that may
+ * not take the synchronisation cudaFree implies).  No counterpart in the
+ * reference.  All pointers are device memory of the current device: xyz holds
+ * n packed (x, y, z) floats, tri ntri triangles of 9 floats, d2_out receives n
+ * floats in input order -- the same values pp_hull_upload + pp_run +
+ * pp_surfdist_fetch give for R' = max(rmax, carve radius).  The triangle
+ * boxes, grid and lists live in one static 64 MiB array per device, held from
+ * module load until exit; hulls above 2,000,000 triangles are rejected with
+ * PP_ERR_UNSUPPORTED, hulls whose lists still do not fit with PP_ERR_OVERFLOW.
+ * The first call on a device looks the array up (cudaGetSymbolAddress) and
+ * should come before any stream capture.  Calls share the array: calls whose
+ * GPU work overlaps (different streams, unordered threads) race.  A message
+ * goes to err (err_cap bytes) when it is not NULL.  stream may be NULL. */
+int pp_surfdist_noalloc(const float* xyz, uint64_t n, const float* tri, uint64_t ntri, float rp,
+                        float* d2_out, void* stream, char* err, size_t err_cap);
+
 /* Task list: ntasks x PP_TYPE_WORDS words each for the centre (trg) and the
  * environment (env) sets of TypeSpecDescrStat
  * (src/PARAPROBE_PeriodicTable.h:100-128). */

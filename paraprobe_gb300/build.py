@@ -42,7 +42,7 @@ NVFLAGS = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPI
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall",
             "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-I" + os.path.join(CUDA_HOME, "include")]
 
-CU_SOURCES = ["pp_kernels.cu", "pp_capi.cu"]
+CU_SOURCES = ["pp_kernels.cu", "pp_capi.cu", "pp_noalloc.cu"]
 CPP_SOURCES = [os.path.join(CSRC, "pp_shuffle.cpp")]
 
 

@@ -137,6 +137,13 @@ void launch_permute_labels(const uint8_t* label_by_id, const uint32_t* perm, con
 void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const float* tri,
                     const uint32_t* tcell_start, const uint32_t* tcell_tri, Grid tg, float rprime,
                     float* surf_d2, cudaStream_t s);
+// packed caller-order xyz in, ion2surf out in the same order (no cell sort)
+void launch_surface_xyz(const float* xyz, uint64_t n, const float* tbox, const float* tri, const uint32_t* tstart,
+                        const uint32_t* tlist, Grid tg, float rp, float* out, cudaStream_t s);
+void launch_tri_box(const float* tri, uint64_t ntri, float* box, cudaStream_t s);
+// adds the list entries binning into tg makes to *total (caller zeroes it)
+void launch_tri_entries(const float* tbox, uint64_t ntri, Grid tg, float grow, unsigned long long* total,
+                        cudaStream_t s);
 // Order-preserving centre compaction; flags needs n + 1 words, scan_tmp the
 // exclusive-scan scratch for n + 1 elements.
 void launch_select_centres(const uint8_t* labels, const float* surf_d2, uint64_t n, float R2,

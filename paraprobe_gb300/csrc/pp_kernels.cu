@@ -308,6 +308,48 @@ __global__ void k_surface(const float4* __restrict__ ions, uint64_t n, const flo
   }
 }
 
+// Caller-order variant for the entry point without allocations: positions as
+// packed xyz triples and ion2surf written in the same order.  The candidate
+// test and the minimum are those of k_surface, so both give the same bits.
+__global__ void k_surface_xyz(const float* __restrict__ xyz, uint64_t n, const float* __restrict__ tbox,
+                              const float* __restrict__ tri, const uint32_t* __restrict__ tstart,
+                              const uint32_t* __restrict__ tlist, Grid tg, float rp, float* __restrict__ out) {
+  const float rp2 = __fmul_rn(rp, rp);
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const float px = xyz[3 * i], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
+    float best = rp2;
+    const int cx = (int)floorf((px - tg.lox) * tg.inv_h), cy = (int)floorf((py - tg.loy) * tg.inv_h),
+              cz = (int)floorf((pz - tg.loz) * tg.inv_h);
+    if (cx >= 0 && cy >= 0 && cz >= 0 && cx < tg.nx && cy < tg.ny && cz < tg.nz) {
+      const uint64_t c = ((uint64_t)cz * tg.ny + cy) * tg.nx + cx;
+      const float lx = __fsub_rn(px, rp), ly = __fsub_rn(py, rp), lz = __fsub_rn(pz, rp);
+      const float hx = __fadd_rn(px, rp), hy = __fadd_rn(py, rp), hz = __fadd_rn(pz, rp);
+      const uint32_t k1 = tstart[c + 1];
+      for (uint32_t k = tstart[c]; k < k1; ++k) {
+        const uint32_t t = tlist[k];
+        const float* b = tbox + 6 * (uint64_t)t;
+        if (b[3] < lx || b[0] > hx || b[4] < ly || b[1] > hy || b[5] < lz || b[2] > hz) continue;
+        const float v = tri_dist2(tri + 9 * (uint64_t)t, px, py, pz);
+        if (!(v > best)) best = v;
+      }
+    }
+    out[i] = best;
+  }
+}
+
+// Triangle boxes on the device: per axis the smallest and largest vertex
+// coordinate (lo x,y,z then hi x,y,z), as the host builds them for k_surface.
+__global__ void k_tri_box(const float* __restrict__ tri, uint64_t ntri, float* __restrict__ box) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ntri; t += (uint64_t)gridDim.x * blockDim.x) {
+    const float* v = tri + 9 * t;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      box[6 * t + k] = fminf(fminf(v[k], v[3 + k]), v[6 + k]);
+      box[6 * t + 3 + k] = fmaxf(fmaxf(v[k], v[3 + k]), v[6 + k]);
+    }
+  }
+}
+
 // --------------------------------------------------------- centre selection
 // Centre filter of src/PARAPROBE_SolverHdl.cpp:3847-3859: the type is a target
 // of some task and ion2surf >= R^2 (plus an optional extra mask).  The
@@ -379,6 +421,21 @@ __global__ void k_tri_fill(const float* __restrict__ tbox, uint64_t ntri, Grid t
         }
   }
 }
+
+// Number of (triangle, cell) list entries binning into tg would make, in 64
+// bits, so that a grid is only filled when its lists fit the space at hand.
+__global__ void k_tri_entries(const float* __restrict__ tbox, uint64_t ntri, Grid tg, float grow,
+                              unsigned long long* total) {
+  unsigned long long sum = 0;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ntri; t += (uint64_t)gridDim.x * blockDim.x) {
+    int c0[3], c1[3];
+    tri_cell_range(tbox + 6 * t, tg, grow, c0, c1);
+    sum += (unsigned long long)(c1[0] - c0[0] + 1) * (c1[1] - c0[1] + 1) * (c1[2] - c0[2] + 1);
+  }
+  for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o);
+  if ((threadIdx.x & 31) == 0 && sum) atomicAdd(total, sum);
+}
+
 
 __global__ void k_select_write(const uint8_t* __restrict__ labels, const float* __restrict__ surf, uint64_t n,
                                float R2, const int8_t* __restrict__ cslot_of, const uint8_t* __restrict__ extra,
@@ -1332,6 +1389,23 @@ int launch_tri_bins(const float* tbox, uint64_t ntri, Grid tg, float grow, uint3
   counted();
   k_tri_fill<<<grid_for(ntri, 128), 128, 0, s>>>(tbox, ntri, tg, grow, tfill, tlist, list_cap, nullptr);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+void launch_tri_entries(const float* tbox, uint64_t ntri, Grid tg, float grow, unsigned long long* total,
+                        cudaStream_t s) {
+  counted();
+  k_tri_entries<<<grid_for(ntri, 256), 256, 0, s>>>(tbox, ntri, tg, grow, total);
+}
+
+void launch_tri_box(const float* tri, uint64_t ntri, float* box, cudaStream_t s) {
+  counted();
+  k_tri_box<<<grid_for(ntri, 256), 256, 0, s>>>(tri, ntri, box);
+}
+
+void launch_surface_xyz(const float* xyz, uint64_t n, const float* tbox, const float* tri, const uint32_t* tstart,
+                        const uint32_t* tlist, Grid tg, float rp, float* out, cudaStream_t s) {
+  counted();
+  k_surface_xyz<<<grid_for(n, 256), 256, 0, s>>>(xyz, n, tbox, tri, tstart, tlist, tg, rp, out);
 }
 
 void launch_select_centres(const uint8_t* labels, const float* surf, uint64_t n, float R2, const int8_t* cslot_of,

@@ -15,6 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libparaprobe_gb300.so")
 
 PP_RDF, PP_1NN, PP_RIPK, PP_MKNN, PP_NPCORR, PP_CNTNB = 1, 2, 4, 8, 16, 32
+PP_OK, PP_ERR_INVALID, PP_ERR_CUDA, PP_ERR_NOMEM, PP_ERR_UNSUPPORTED = 0, -1, -2, -3, -4
+PP_ERR_STATE, PP_ERR_OVERFLOW, PP_ERR_DEVICE, PP_ERR_IO = -5, -6, -7, -8
 
 # every symbol include/paraprobe_gb300.h declares
 EXPORTS = (
@@ -25,7 +27,7 @@ EXPORTS = (
     "pp_batched_stats", "pp_neighbors", "pp_shuffle_labels", "pp_device_info", "pp_kernel_launches",
     "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option", "pp_cloud_prepare",
     "pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_stats", "pp_server_destroy",
-    "pp_fp64_audit",
+    "pp_fp64_audit", "pp_surfdist_noalloc",
 )
 
 _lib = None
@@ -85,6 +87,7 @@ def load():
         "pp_server_destroy": ([vp], None),
         "pp_fp64_audit": ([vp, i32, u32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(u64),
                            C.POINTER(u64), C.POINTER(u64), vp, vp, u64, C.POINTER(u64)], i32),
+        "pp_surfdist_noalloc": ([vp, u64, vp, u64, f32, vp, vp, C.c_char_p, C.c_size_t], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
