@@ -195,6 +195,11 @@ int pp_batched_count(pp_ctx* ctx, int* n_realisations);
 /* Results of realisation r of the last batched run, pp_fetch layout. */
 int pp_fetch_batched(pp_ctx* ctx, int r, uint64_t* bins, size_t cap);
 int pp_batched_stats(pp_ctx* ctx, int r, uint64_t* centres, uint64_t* pairs);
+/* The device work of a batched run (the realisation passes after the pair
+ * lists and label layouts are built) runs as one CUDA graph: captured when
+ * its launch parameters change, replayed otherwise.  Nodes of the current
+ * graph, captures and launches so far.  No counterpart in the reference. */
+int pp_batched_graph(pp_ctx* ctx, uint64_t* nodes, uint64_t* captures, uint64_t* launches);
 
 /* Neighbour set of one ion (input index): every other ion with float
  * d^2 <= r^2, d^2 = (xi-xj)^2 + (yi-yj)^2 + (zi-zj)^2 evaluated left to right

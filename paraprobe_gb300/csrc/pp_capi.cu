@@ -152,6 +152,7 @@ struct pp_ctx {
   // batched geometry cache
   DevBuf pair_count, pair_off, pair_slot, pair_cat, geo_centres, centre_ok, real_labels, rois_dev;
   DevBuf labels_il, ok_il;  // group-major interleaved copies of real_labels / centre_ok
+  DevBuf knn_labels, knn_ok, knn_rec, knn_recc;  // 32-realisation kNN: layouts and records
   DevBuf maxlist;           // longest pair list (one uint32)
   uint32_t geo_maxlist = 0;
   uint64_t geo_key_version = ~0ull;
@@ -167,6 +168,12 @@ struct pp_ctx {
   bool readonly_clouds = false; // ... and never rebuild them
   DevBuf surf_own;              // ion2surf for an R' the cloud does not cache
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // batched apply as a CUDA graph: captured on a private stream, replayed
+  // while the launch parameters (buffers, sizes, tiles) stay the same
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t apply_exec = nullptr;
+  std::string apply_sig;
+  uint64_t graph_nodes = 0, graph_captures = 0, graph_launches = 0;
   bool ev_recorded = false;
 };
 
@@ -754,6 +761,8 @@ void pp_destroy(pp_ctx* ctx) {
   cudaDeviceSynchronize();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->apply_exec) cudaGraphExecDestroy(ctx->apply_exec);
+  if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
   delete ctx;
 }
 
@@ -1385,11 +1394,13 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     r += n_rois;
   }
   CK(cudaGetLastError());
-  // ---- apply every realisation in one persistent launch
+  // ---- apply every realisation: one persistent launch for RDF and the
+  // per-realisation counts, plus the 32-realisation kNN walk/bin launches,
+  // all captured once into a CUDA graph
   if (nc) {
     CK(ctx->work.ensure(16));
-    CK(cudaMemsetAsync(ctx->work.p, 0, 16, s));
-    pp::ApplyArgs b{};
+    pp::ApplyArgs b;
+    std::memset(&b, 0, sizeof b);
     b.centres = ctx->geo_centres.as<uint32_t>();
     b.ncentres = nc;
     b.pair_off = ctx->pair_off.as<unsigned long long>();
@@ -1419,6 +1430,37 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     b.nsmax = std::max(P.emax, 1);
     b.disjoint = P.disjoint;
     b.setidx = D.setidx;
+    // kNN of 32 realisations per warp (walk + bin) where its records and bins
+    // fit; the fused kernel then does RDF and the per-realisation counters
+    pp::KnnArgs kq;
+    std::memset(&kq, 0, sizeof kq);
+    bool knn32 = false;
+    if (b.flags & PP_MKNN) {
+      kq.centres = b.centres;
+      kq.ncentres = nc;
+      kq.pair_off = b.pair_off;
+      kq.pair_slot = b.pair_slot;
+      kq.pair_cat = b.pair_cat;
+      kq.n = n;
+      kq.nreal = nreal;
+      kq.cslot_of = D.cslot;
+      kq.envbits = D.envbits;
+      kq.disjoint = P.disjoint;
+      kq.setidx = D.setidx;
+      kq.nsets = D.nsets;
+      kq.set_list = D.set_list;
+      kq.kvals = D.kvals;
+      kq.nkI = b.nkI;
+      kq.kmax = b.kmax;
+      kq.nsmax = b.nsmax;
+      kq.nC = P.nC;
+      kq.nS = P.nS;
+      kq.H = P.H;
+      kq.cat_miss = P.cat_miss;
+      kq.knn_core = b.knn_core;
+      knn32 = pp::knn32_check(kq) == 0;
+      if (knn32) b.flags &= ~PP_MKNN;
+    }
     if (pp::apply_configure(b)) return fail(ctx, PP_ERR_UNSUPPORTED, "RDF bins of one realisation exceed shared memory");
     b.ngroups = (nreal + b.group - 1) / b.group;
     // tile: enough pairs per item to amortise the per-item flush of the
@@ -1444,11 +1486,80 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     pp::launch_interleave(OK, nreal, nc, b.group, ctx->ok_il.as<uint8_t>(), s);
     b.labels = ctx->labels_il.as<uint8_t>();
     b.centre_ok = ctx->ok_il.as<uint8_t>();
+    int ng32 = 0;
+    uint32_t chunk = 0;
+    const uint64_t NT = (uint64_t)kq.nsmax * kq.nkI;
+    if (knn32) {
+      ng32 = (nreal + 31) / 32;
+      CK(ctx->knn_labels.ensure(std::max<uint64_t>(n, 1) * 32 * ng32));
+      CK(ctx->knn_ok.ensure(std::max<uint64_t>(nc, 1) * 32 * ng32));
+      pp::launch_interleave(RL, nreal, n, 32, ctx->knn_labels.as<uint8_t>(), s);
+      pp::launch_interleave(OK, nreal, nc, 32, ctx->knn_ok.as<uint8_t>(), s);
+      kq.labels = ctx->knn_labels.as<uint8_t>();
+      kq.centre_ok = ctx->knn_ok.as<uint8_t>();
+      // records of one launch: at most 3 GiB
+      const uint64_t per_centre = NT * 64 + 32;
+      chunk = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(nc, (3ull << 30) / per_centre));
+      CK(ctx->knn_rec.ensure((uint64_t)chunk * NT * 64));
+      CK(ctx->knn_recc.ensure((uint64_t)chunk * 32));
+      kq.rec = ctx->knn_rec.as<uint16_t>();
+      kq.rec_c = ctx->knn_recc.as<uint8_t>();
+      kq.work = ctx->work.as<uint32_t>() + 1;
+    }
+    auto enqueue = [&](cudaStream_t st) -> int {
+      if (cudaMemsetAsync(ctx->work.p, 0, 16, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
+      if (pp::launch_apply(b, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "apply launch failed");
+      pp::KnnArgs k = kq;
+      for (int g = 0; g < ng32; ++g) {
+        for (uint32_t c0 = 0; c0 < nc; c0 += chunk) {
+          k.grp = g;
+          k.c0 = c0;
+          k.cn = std::min(chunk, nc - c0);
+          k.tile = 64;
+          if (cudaMemsetAsync(k.work, 0, 4, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
+          if (pp::launch_knn_walk(k, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "kNN walk launch failed");
+          const uint32_t nranges = (uint32_t)std::max<uint64_t>(1, (8ull * ctx->sm_count + NT - 1) / NT);
+          k.tile = std::max<uint32_t>(1, (k.cn + nranges - 1) / nranges);
+          if (cudaMemsetAsync(k.work, 0, 4, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
+          if (pp::launch_knn_bin(k, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "kNN bin launch failed");
+        }
+      }
+      return PP_OK;
+    };
+    std::string sig((const char*)&b, sizeof b);
+    sig.append((const char*)&kq, sizeof kq);
+    const uint64_t extra[4] = {(uint64_t)ng32, chunk, nc, (uint64_t)ctx->sm_count};
+    sig.append((const char*)extra, sizeof extra);
+    if (!ctx->apply_exec || sig != ctx->apply_sig) {
+      if (!ctx->cap_stream) CK(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+      if (ctx->apply_exec) {
+        cudaGraphExecDestroy(ctx->apply_exec);
+        ctx->apply_exec = nullptr;
+      }
+      ctx->apply_sig.clear();
+      CK(cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeRelaxed));
+      const int erc = enqueue(ctx->cap_stream);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(ctx->cap_stream, &graph);
+      if (erc) {
+        if (graph) cudaGraphDestroy(graph);
+        return erc;
+      }
+      CK(ce);
+      size_t nodes = 0;
+      cudaGraphGetNodes(graph, nullptr, &nodes);
+      const cudaError_t ie = cudaGraphInstantiate(&ctx->apply_exec, graph, 0);
+      cudaGraphDestroy(graph);
+      CK(ie);
+      ctx->apply_sig = sig;
+      ctx->graph_nodes = nodes;
+      ++ctx->graph_captures;
+    }
     CK(cudaEventRecord(ctx->ev0, s));
-    rc = pp::launch_apply(b, ctx->sm_count, s);
+    CK(cudaGraphLaunch(ctx->apply_exec, s));
     CK(cudaEventRecord(ctx->ev1, s));
+    ++ctx->graph_launches;
     ctx->ev_recorded = true;
-    if (rc) return fail(ctx, PP_ERR_CUDA, "apply launch failed");
   }
   ctx->res.valid = true;
   return PP_OK;
@@ -1492,6 +1603,14 @@ int pp_batched_stats(pp_ctx* ctx, int r, uint64_t* centres, uint64_t* pairs) {
   if (rc) return rc;
   if (pairs) *pairs = ctx->res.counters_h[2 * r];
   if (centres) *centres = ctx->res.counters_h[2 * r + 1];
+  return PP_OK;
+}
+
+int pp_batched_graph(pp_ctx* ctx, uint64_t* nodes, uint64_t* captures, uint64_t* launches) {
+  if (!ctx) return PP_ERR_INVALID;
+  if (nodes) *nodes = ctx->graph_nodes;
+  if (captures) *captures = ctx->graph_captures;
+  if (launches) *launches = ctx->graph_launches;
   return PP_OK;
 }
 

@@ -162,6 +162,41 @@ int launch_tri_bins(const float* tbox, uint64_t ntri, Grid tg, float grow, uint3
                     uint64_t* total_out, cudaStream_t s);
 int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s);
 int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s);
+// Batched kNN in two phases, 32 realisations per warp (one per lane).
+// Walk: per (centre, realisation) the category of the k-th member of every
+// environment set, as records rec[centre][slot][32] (slot = set * nkI + order,
+// 0xffff = no such slot) and rec_c[centre][32] (centre type slot, 0xff = not a
+// centre).  Bin: per (slot, centre range) a shared [nC][H][32] histogram.
+struct KnnArgs {
+  const uint32_t* centres;          // geometry centres (sorted slots)
+  uint32_t ncentres;                // all geometry centres
+  uint32_t c0, cn;                  // centres of this launch: [c0, c0 + cn)
+  const unsigned long long* pair_off;
+  const uint32_t* pair_slot;
+  const uint16_t* pair_cat;
+  const uint8_t* labels;            // [ngroups][n][32]
+  const uint8_t* centre_ok;         // [ngroups][ncentres][32]
+  uint64_t n;
+  int grp, nreal;
+  const int8_t* cslot_of;
+  const uint32_t* envbits;          // [nC][256]
+  int disjoint;                     // no type in two sets of one centre type
+  const int8_t* setidx;             // [nC][256] set of a type when disjoint, -1 = none
+  const int* nsets;                 // [nC]
+  const int* set_list;              // [nC][32]
+  const int* kvals;
+  int nkI, kmax, nsmax, nC, nS, H, cat_miss;
+  uint16_t* rec;                    // [cn][nsmax * nkI][32]
+  uint8_t* rec_c;                   // [cn][32]
+  uint32_t* work;
+  uint32_t tile;                    // centres per walk work item / per bin work item
+  unsigned long long* knn_core;     // [nreal][nC][nS][nkI][H]
+};
+// -2 when a warp's records or the bin histogram do not fit shared memory
+int knn32_check(const KnnArgs& k);
+int launch_knn_walk(const KnnArgs& k, int sm_count, cudaStream_t s);
+int launch_knn_bin(const KnnArgs& k, int sm_count, cudaStream_t s);
+
 constexpr int kApplyThreads = 1024;
 // picks the realisation group and where kNN bins accumulate; -2 = no fit
 int apply_configure(ApplyArgs& a);

@@ -1134,6 +1134,188 @@ __global__ void __launch_bounds__(1024, 1) k_apply(ApplyArgs a) {
   }
 }
 
+// --------------------------------------------------------- K5 batched kNN
+// Walk: one warp per centre, lane r = realisation grp * 32 + r.  All lanes
+// read the same pair-list entry (one broadcast load) and their own label of
+// the neighbour (32 consecutive bytes), so the walk costs a few instructions
+// per entry for 32 realisations.  Each lane counts the members of each set it
+// has met; the entry that makes a set's count k is its k-th nearest member
+// (the list is in category order).  The walk ends when every lane has k_max
+// members of every set, or the list ends (the rest are misses).
+template <bool DISJ>
+__global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int NT = a.nsmax * a.nkI;
+  // set table per centre type, plus a last row that matches nothing (lanes
+  // that are no centre in their realisation walk it without effect):
+  // DISJ: set index of a type (int8, -1 = none); else set bit mask (uint32)
+  const int nrow = (a.nC + 1) * 256;
+  unsigned char* sTab = smem;
+  int* sNs = (int*)(smem + (size_t)nrow * (DISJ ? 1 : 4));     // [nC]
+  int8_t* sC = (int8_t*)(sNs + a.nC);                          // 256
+  int8_t* sK = sC + 256;                                       // 256
+  uint16_t* sRes = (uint16_t*)(sK + 256);                      // [nwarps][NT][32]
+  uint8_t* sCnt = (uint8_t*)(sRes + (size_t)nwarps * NT * 32); // [nwarps][nsmax][32]
+  __shared__ uint32_t s_item;
+  for (int i = threadIdx.x; i < nrow; i += blockDim.x) {
+    const bool last = i >= a.nC * 256;
+    if (DISJ) ((int8_t*)sTab)[i] = last ? (int8_t)-1 : a.setidx[i];
+    else ((uint32_t*)sTab)[i] = last ? 0u : a.envbits[i];
+  }
+  for (int i = threadIdx.x; i < a.nC; i += blockDim.x) sNs[i] = a.nsets[i];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) { sC[i] = a.cslot_of[i]; sK[i] = -1; }
+  __syncthreads();
+  for (int i = threadIdx.x; i < a.nkI; i += blockDim.x)
+    if (a.kvals[i] >= 1 && a.kvals[i] <= 255) sK[a.kvals[i]] = (int8_t)i;
+  __syncthreads();
+  uint16_t* res = sRes + (size_t)warp * NT * 32 + lane;
+  uint8_t* cnt = sCnt + warp * a.nsmax * 32 + lane;
+  const uint8_t* lab = a.labels + (uint64_t)a.grp * a.n * 32 + lane;
+  const uint8_t* okp = a.centre_ok + (uint64_t)a.grp * a.ncentres * 32 + lane;
+  const bool real = a.grp * 32 + lane < a.nreal;
+  const int kmax = a.kmax, nkI = a.nkI;
+  const uint32_t ntiles = (a.cn + a.tile - 1) / a.tile;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(a.work, 1u);
+    __syncthreads();
+    const uint32_t item = s_item;
+    __syncthreads();
+    if (item >= ntiles) break;
+    const uint32_t l0 = item * a.tile, l1 = min(l0 + a.tile, a.cn);
+    for (uint32_t li = l0 + warp; li < l1; li += nwarps) {
+      const uint32_t ci = a.c0 + li;
+      const uint32_t self = a.centres[ci];
+      const bool ok = real && okp[(uint64_t)ci * 32] != 0;
+      const int c = ok ? (int)sC[lab[(uint64_t)self * 32]] : -1;
+      const int nset = c >= 0 ? sNs[c] : 0;
+      int unsat = nset;                   // sets with fewer than k_max members met
+      for (int q = 0; q < a.nsmax; ++q) cnt[q * 32] = 0;
+      const int row = (c >= 0 ? c : a.nC) * 256;
+      const unsigned long long o0 = a.pair_off[ci], o1 = a.pair_off[ci + 1];
+      // 32 entries per coalesced load, then neighbour labels 8 at a time
+      // (independent loads in flight), counted in list order
+      for (unsigned long long e0 = o0; e0 < o1; e0 += 32) {
+        if (!__any_sync(FULL, unsat > 0)) break;
+        const int ne = (int)min(32ull, o1 - e0);
+        uint32_t my_slot = 0, my_cat = 0;
+        if (lane < ne) {
+          my_slot = a.pair_slot[e0 + lane];
+          my_cat = a.pair_cat[e0 + lane];
+        }
+        for (int j0 = 0; j0 < ne; j0 += 8) {
+          uint32_t t8[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const uint32_t sl = __shfl_sync(FULL, my_slot, (j0 + u) & 31);
+            t8[u] = (j0 + u < ne) ? lab[(uint64_t)sl << 5] : 0u;
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const uint32_t cat = __shfl_sync(FULL, my_cat, (j0 + u) & 31);
+            if (j0 + u >= ne) break;
+            if (DISJ) {
+              const int q = ((const int8_t*)sTab)[row + t8[u]];
+              if (q >= 0) {
+                const int m = cnt[q * 32];
+                if (m < kmax) {
+                  const int kk = sK[m + 1];
+                  if (kk >= 0) res[(q * nkI + kk) * 32] = (uint16_t)cat;
+                  cnt[q * 32] = (uint8_t)(m + 1);
+                  unsat -= (m + 1 == kmax);
+                }
+              }
+            } else {
+              uint32_t eb = ((const uint32_t*)sTab)[row + t8[u]];
+              while (eb) {
+                const int q = __ffs(eb) - 1;
+                eb &= eb - 1;
+                const int m = cnt[q * 32];
+                if (m < kmax) {
+                  const int kk = sK[m + 1];
+                  if (kk >= 0) res[(q * nkI + kk) * 32] = (uint16_t)cat;
+                  cnt[q * 32] = (uint8_t)(m + 1);
+                  unsat -= (m + 1 == kmax);
+                }
+              }
+            }
+          }
+        }
+      }
+      // records: one 64-byte row per slot, realisations along the row
+      uint16_t* out = a.rec + (uint64_t)li * NT * 32 + lane;
+      for (int q = 0; q < a.nsmax; ++q) {
+        const int got = cnt[q * 32];
+        for (int kk = 0; kk < nkI; ++kk) {
+          uint16_t v = 0xffff;
+          if (q < nset) v = got >= a.kvals[kk] ? res[(q * nkI + kk) * 32] : (uint16_t)a.cat_miss;
+          out[(q * nkI + kk) * 32] = v;
+        }
+      }
+      a.rec_c[(uint64_t)li * 32 + lane] = c >= 0 ? (uint8_t)c : (uint8_t)0xff;
+    }
+  }
+}
+
+// Bin: one work item = (slot t = set q * nkI + order kk, range of centres).
+// The block histograms that slot for all 32 realisations at once in shared
+// memory laid out [nC][H][32], so lane r always hits bank r; the bins go to
+// knn_core of realisation grp * 32 + r, set set_list[c][q], order kk.
+__global__ void __launch_bounds__(1024, 1) k_knn_bin(KnnArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t* hist = (uint32_t*)smem;                  // [nC][H][32]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int NT = a.nsmax * a.nkI;
+  const uint32_t nh = (uint32_t)a.nC * a.H * 32;
+  __shared__ uint32_t s_item;
+  for (uint32_t i = threadIdx.x; i < nh; i += blockDim.x) hist[i] = 0;
+  const uint32_t nranges = (a.cn + a.tile - 1) / a.tile;
+  const uint32_t nitems = nranges * (uint32_t)NT;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(a.work, 1u);
+    __syncthreads();
+    const uint32_t item = s_item;
+    if (item >= nitems) break;
+    const uint32_t range = item / NT;
+    const int t = (int)(item - range * NT);
+    const uint32_t l0 = range * a.tile, l1 = min(l0 + a.tile, a.cn);
+    // 8 centres per step: their loads are in flight together
+    for (uint32_t lb = l0 + warp * 8; lb < l1; lb += nwarps * 8) {
+      uint32_t v8[8], c8[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const uint32_t li = lb + u;
+        v8[u] = 0xffff;
+        c8[u] = 0xff;
+        if (li < l1) {
+          v8[u] = a.rec[((uint64_t)li * NT + t) * 32 + lane];
+          c8[u] = a.rec_c[(uint64_t)li * 32 + lane];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (c8[u] != 0xff && v8[u] != 0xffff) atomicAdd(&hist[(c8[u] * a.H + v8[u]) * 32 + lane], 1u);
+    }
+    __syncthreads();
+    const int q = t / a.nkI, kk = t - q * a.nkI;
+    for (uint32_t i = threadIdx.x; i < nh; i += blockDim.x) {
+      const uint32_t v = hist[i];
+      if (v) {
+        hist[i] = 0;
+        const int rr = a.grp * 32 + (int)(i & 31);
+        const uint32_t cb = i >> 5;
+        const int c = (int)(cb / a.H), cat = (int)(cb - (uint32_t)c * a.H);
+        if (rr < a.nreal && q < a.nsets[c]) {
+          const int Sg = a.set_list[c * 32 + q];
+          atomicAdd(&a.knn_core[((((uint64_t)rr * a.nC + c) * a.nS + Sg) * a.nkI + kk) * a.H + cat],
+                    (unsigned long long)v);
+        }
+      }
+    }
+  }
+}
+
 // Realisation-major byte arrays src[rows][cols] to the group-major layout
 // k_apply reads: dst[((r / G) * cols + c) * G + r % G], rows padded to a
 // multiple of G with zeros.
@@ -1520,6 +1702,53 @@ __global__ void k_max_u32(const uint32_t* __restrict__ v, uint64_t n, uint32_t* 
 void launch_max_u32(const uint32_t* v, uint64_t n, uint32_t* out, cudaStream_t s) {
   counted();
   k_max_u32<<<grid_for(n, 256), 256, 0, s>>>(v, n, out);
+}
+
+static size_t knn_walk_bytes(const KnnArgs& k, int nwarps) {
+  return (size_t)(k.nC + 1) * 256 * (k.disjoint ? 1 : 4) + (size_t)k.nC * 4 + 512 +
+         (size_t)nwarps * k.nsmax * k.nkI * 64 + (size_t)nwarps * k.nsmax * 32;
+}
+
+static int knn_walk_warps(const KnnArgs& k) {
+  for (int w = 16; w >= 2; w /= 2)
+    if (knn_walk_bytes(k, w) <= 96 * 1024) return w;
+  return 0;
+}
+
+int knn32_check(const KnnArgs& k) {
+  if (k.nsmax > 32 || k.kmax > 254 || k.nC > 254) return -2;
+  if (!knn_walk_warps(k)) return -2;
+  if ((size_t)k.nC * k.H * 32 * 4 > 200 * 1024) return -2;
+  return 0;
+}
+
+int launch_knn_walk(const KnnArgs& k, int sm_count, cudaStream_t s) {
+  const int w = knn_walk_warps(k);
+  if (!w) return -2;
+  const size_t smem = knn_walk_bytes(k, w);
+  auto kern = k.disjoint ? k_knn_walk<true> : k_knn_walk<false>;
+  if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return -1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, w * 32, smem) != cudaSuccess || per_sm < 1)
+    return -1;
+  counted();
+  kern<<<sm_count * per_sm, w * 32, smem, s>>>(k);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_knn_bin(const KnnArgs& k, int sm_count, cudaStream_t s) {
+  const size_t smem = (size_t)k.nC * k.H * 32 * 4;
+  if (smem > 200 * 1024) return -2;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_knn_bin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return -1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_knn_bin, 1024, smem) != cudaSuccess || per_sm < 1)
+    return -1;
+  counted();
+  k_knn_bin<<<sm_count * per_sm, 1024, smem, s>>>(k);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 void launch_interleave(const uint8_t* src, uint64_t rows, uint64_t cols, int G, uint8_t* dst, cudaStream_t s) {

@@ -27,7 +27,7 @@ EXPORTS = (
     "pp_batched_stats", "pp_neighbors", "pp_shuffle_labels", "pp_device_info", "pp_kernel_launches",
     "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option", "pp_cloud_prepare",
     "pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_stats", "pp_server_destroy",
-    "pp_fp64_audit", "pp_surfdist_noalloc",
+    "pp_fp64_audit", "pp_surfdist_noalloc", "pp_batched_graph",
 )
 
 _lib = None
@@ -88,6 +88,7 @@ def load():
         "pp_fp64_audit": ([vp, i32, u32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(u64),
                            C.POINTER(u64), C.POINTER(u64), vp, vp, u64, C.POINTER(u64)], i32),
         "pp_surfdist_noalloc": ([vp, u64, vp, u64, f32, vp, vp, C.c_char_p, C.c_size_t], i32),
+        "pp_batched_graph": ([vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -307,6 +308,12 @@ class Context:
         c, p = C.c_uint64(), C.c_uint64()
         self._ck(self.L.pp_batched_stats(self.h, r, C.byref(c), C.byref(p)), "pp_batched_stats")
         return dict(centres=c.value, pairs=p.value)
+
+    def batched_graph(self):
+        nodes, caps, launches = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        self._ck(self.L.pp_batched_graph(self.h, C.byref(nodes), C.byref(caps), C.byref(launches)),
+                 "pp_batched_graph")
+        return dict(nodes=nodes.value, captures=caps.value, launches=launches.value)
 
     def neighbors(self, cloud, ion, r):
         cnt = C.c_uint64()

@@ -174,6 +174,39 @@ def test_batched_overlapping_sets(ctx, oracle, rincr, nsets):
     ctx.free(cid)
 
 
+def test_batched_graph_replay(ctx, oracle):
+    """A second batched run with the same plan replays the captured graph and
+    gives the same bins; new label sets in the same buffers replay it too."""
+    spec = synth.cone_specimen(n=30000, r_apex=8.0, half_angle_deg=10.0, length=14.0, n_clusters=15,
+                               members=40, nspecies=3, seed=37, nseg=64, stack=4.0)
+    types = [1, 2, 3]
+    trg = [[a] for a in types for b in types]
+    env = [[b] for a in types for b in types]
+    ks = [4, 2, 1]
+    flags = N.PP_RDF | N.PP_MKNN
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks(trg, env)
+    ctx.hist(0.0, 0.02, 1.2)
+    sets = np.stack([N.shuffle_labels(spec.labels, 900 + s) for s in range(5)])
+    ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets)
+    first = [ctx.fetch_batched(r) for r in range(6)]
+    g1 = ctx.batched_graph()
+    assert g1["nodes"] >= 1
+    ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets)
+    g2 = ctx.batched_graph()
+    assert g2["captures"] == g1["captures"] and g2["launches"] == g1["launches"] + 1
+    for r in range(6):
+        assert np.array_equal(ctx.fetch_batched(r), first[r])
+    sets2 = np.stack([N.shuffle_labels(spec.labels, 950 + s) for s in range(5)])
+    ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets2)
+    assert ctx.batched_graph()["captures"] == g1["captures"]
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    ref = oracle.spatstat(spec.xyz, sets2[3], surf, 0.0, 0.02, 1.2, flags, trg, env, ks)
+    assert np.array_equal(ctx.fetch_batched(4), ref["bins"])
+    ctx.free(cid)
+
+
 def test_results_independent_of_tuning(ctx, oracle):
     spec = synth.cone_specimen(n=50000, r_apex=8.0, half_angle_deg=10.0, length=20.0, n_clusters=25,
                                members=40, nspecies=3, seed=21, nseg=64, stack=4.0)
