@@ -279,13 +279,20 @@ def run_gpu(args):
     elapsed = e0.elapsed_time(e1) / 1e3
     barrier(pg)
     clocks = clk.stop()
-    # pairs per pass (same every step)
+    # pairs per pass (same every step); FP64 audit of each pass's bins on
+    # 20000 evenly spaced centres (untimed)
+    audits = []
     for i, r in enumerate(runs):
         ctx.tasks(trg, env)
         ctx.hist(*r["hist"])
         ctx.run(cid, r["flags"], r["k"], stream=sh)
         ctx.fetch()
         per_pass_pairs[i] = ctx.stats()["pairs"]
+        au = ctx.fp64_audit(cid, max_centres=20000, cap=1 << 16)
+        audits.append({"bins": f"{r['hist'][1]} nm", "pairs": au["pairs"],
+                       "max_abs_err_nm": au["max_abs_err"], "max_rel_err": au["max_rel_err"],
+                       "bin_disagreements": au["bin_disagreements"],
+                       "in_ball_disagreements": au["set_disagreements"]})
     t_max = reduce_max(pg, elapsed)
     value = tot_pairs * world / t_max
 
@@ -348,7 +355,8 @@ def run_gpu(args):
                            tuning={"cell_edge_nm": round(cfg["R_nm"] / ratio, 4), "tile": tile},
                            l2="inputs larger than L2 (cell-sorted cloud 16 B/ion), no flush",
                            parallelism=f"replicas x{world}"),
-            "roofline": roof, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks}
+            "roofline": roof, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
+            "fp64_audit": audits}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, frac, p, s, _ = cpu_measure(spec, trg, env, runs, args.cpu_seconds, threads)

@@ -3,6 +3,7 @@
 //
 //   paraprobe_gpu <simid> <settings.xml> [--outdir DIR] [--device N]
 //                 [--inside NIONS VOLUME] [--labels FILE] [--plan]
+//                 [--fp64-audit CENTRES]
 //
 // Follows the reference's flow for this task (src/PARAPROBE_Main.cpp:100-305
 // -> solver::characterize_spatstat, src/PARAPROBE_SolverHdl.cpp:745-776):
@@ -15,7 +16,13 @@
 // reference takes them from its voxeliser).  --labels replays a given label
 // assignment (one byte per ion, file order, e.g. a stored null-model shuffle)
 // and writes ".Rndmized" files.  --plan prints the parsed task plan as JSON
-// and runs nothing.
+// and runs nothing.  Every pass also recomputes the distances of a sample of
+// centres (--fp64-audit CENTRES, evenly spaced; 0 = all; default 20000) in
+// double precision, prints the largest error of the float arithmetic and
+// writes PARAPROBE.SimID.<id>.FP64Audit.<Original|Rndmized>.csv, which lists
+// every pair whose float bin or float in-ball decision differs from the
+// double one together with the bin edge (or the cut-off R) it sits on.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -46,12 +53,51 @@ int check(pp_ctx* ctx, int rc, const char* what) {
   return rc;
 }
 
+// FP64 audit of the current tasks and bins: summary on stdout, and a CSV of
+// every disagreement with the edge that explains it.  Bin edges are
+// rmin + b (rmax - rmin) / nbins in double, the reference's histogram grid.
+int fp64_audit(pp_ctx* ctx, int cloud, uint32_t centres, const ppio::Settings& S, uint64_t nbins,
+               const std::string& outdir, bool randomized) {
+  double max_abs = 0, max_rel = 0;
+  uint64_t pairs = 0, bin_dis = 0, set_dis = 0, listed = 0;
+  const uint64_t cap = 1u << 16;
+  std::vector<uint64_t> ids(2 * cap);
+  std::vector<double> dd(2 * cap);
+  if (check(ctx, pp_fp64_audit(ctx, cloud, centres, &max_abs, &max_rel, &pairs, &bin_dis, &set_dis, ids.data(),
+                               dd.data(), cap, &listed), "pp_fp64_audit"))
+    return 7;
+  std::cout << "FP64 audit (" << (centres ? std::to_string(centres) : std::string("all")) << " centres): " << pairs
+            << " pairs, max abs error " << max_abs << " nm, max rel error " << max_rel << ", " << bin_dis
+            << " bin and " << set_dis << " in-ball disagreements" << std::endl;
+  const std::string fn = outdir + "/PARAPROBE.SimID." + std::to_string(S.sim_id) + ".FP64Audit." +
+                         (randomized ? "Rndmized" : "Original") + ".csv";
+  FILE* f = std::fopen(fn.c_str(), "w");
+  if (!f) { stopping("cannot write " + fn); return 7; }
+  std::fprintf(f, "MaxAbsError;%.18g\nMaxRelError;%.18g\nPairs;%llu\nBinDisagreements;%llu\nInBallDisagreements;%llu\n",
+               max_abs, max_rel, (unsigned long long)pairs, (unsigned long long)bin_dis, (unsigned long long)set_dis);
+  std::fprintf(f, "CentreIonID;NeighbourIonID;DistanceFloat;DistanceDouble;Edge;EdgeValue;DistanceToEdge\n");
+  const double lo = (double)S.rmin, hi = (double)S.rmax, w = nbins ? (hi - lo) / (double)nbins : 0.0;
+  for (uint64_t i = 0; i < listed && i < cap; ++i) {
+    const double d64 = dd[2 * i + 1];
+    long b = w > 0 ? (long)std::floor((d64 - lo) / w + 0.5) : 0;
+    if (b < 0) b = 0;
+    if ((uint64_t)b > nbins) b = (long)nbins;
+    const double edge = lo + (double)b * w;
+    const bool cut = std::fabs(d64 - hi) <= std::fabs(d64 - edge);
+    std::fprintf(f, "%llu;%llu;%.18g;%.18g;%s;%.18g;%.18g\n", (unsigned long long)ids[2 * i],
+                 (unsigned long long)ids[2 * i + 1], dd[2 * i], d64, cut ? "cutoff R" : ("bin edge " + std::to_string(b)).c_str(),
+                 cut ? hi : edge, cut ? d64 - hi : d64 - edge);
+  }
+  std::fclose(f);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
   if (argc < 3) {
     std::cerr << "usage: paraprobe_gpu <simid> <settings.xml> [--outdir DIR] [--device N] "
-                 "[--inside NIONS VOLUME] [--plan]\n";
+                 "[--inside NIONS VOLUME] [--labels FILE] [--plan] [--fp64-audit CENTRES]\n";
     return 2;
   }
   std::string outdir = ".";
@@ -60,6 +106,7 @@ int main(int argc, char** argv) {
   double volume_inside = 0.0;
   bool plan_only = false;
   std::string labels_file;
+  uint32_t audit_centres = 20000;
   for (int a = 3; a < argc; ++a) {
     const std::string s = argv[a];
     if (s == "--outdir" && a + 1 < argc) outdir = argv[++a];
@@ -67,6 +114,7 @@ int main(int argc, char** argv) {
     else if (s == "--inside" && a + 2 < argc) { nions_inside = std::strtoull(argv[a + 1], nullptr, 10); volume_inside = std::strtod(argv[a + 2], nullptr); a += 2; }
     else if (s == "--plan") plan_only = true;
     else if (s == "--labels" && a + 1 < argc) labels_file = argv[++a];
+    else if (s == "--fp64-audit" && a + 1 < argc) audit_centres = (uint32_t)std::strtoul(argv[++a], nullptr, 10);
     else { std::cerr << "unknown option " << s << "\n"; return 2; }
   }
   ppio::Settings S;
@@ -174,6 +222,7 @@ int main(int argc, char** argv) {
     pp_run_stats(ctx, &centres, &discarded, &pairs);
     std::cout << "Descriptive spatial statistics considered/discarded " << centres << ";" << discarded << " ions, "
               << pairs << " neighbour pairs" << std::endl;
+    if (fp64_audit(ctx, cloud, audit_centres, S, nb, outdir, randomized)) return 7;
     const uint64_t H = nb + 2;
     uint64_t o = 0;
     auto hist = [&](uint64_t at) {

@@ -28,7 +28,17 @@ def test_cli_csv_identical(ctx, tmp_path, name):
         cmd += ["--labels", "labels.u8"]
     r = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr + r.stdout
-    produced = sorted(os.listdir(out))
+    produced = sorted(f for f in os.listdir(out) if ".FP64Audit." not in f)
     assert produced == sorted(c["csv"].keys())
     for f in produced:
         assert (out / f).read_text() == c["csv"][f], f
+    # the FP64 audit beside the reports: small errors, every listed pair on an edge
+    audits = [f for f in os.listdir(out) if ".FP64Audit." in f]
+    assert len(audits) == 1 and "FP64 audit" in r.stdout
+    lines = (out / audits[0]).read_text().splitlines()
+    head = dict(l.split(";", 1) for l in lines[:5])
+    assert float(head["MaxAbsError"]) < 1e-6 and int(head["Pairs"]) > 0
+    rows = [l.split(";") for l in lines[6:]]
+    assert len(rows) == min(int(head["BinDisagreements"]) + int(head["InBallDisagreements"]), 1 << 16)
+    for row in rows:
+        assert abs(float(row[6])) <= 1e-6 * max(float(row[3]), 1e-3), row
