@@ -139,15 +139,22 @@ int pp_hist_params(pp_ctx* ctx, float rmin, float rincr, float rmax);
  * null model of rndlabeler, src/PARAPROBE_SolverHdl.cpp:2809-3003). */
 int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk,
            const uint32_t* label_perm, void* stream);
-/* Project-written autotuner: times the scan on the first `sample` centres
- * (0 = 200000) for cell edges R/2 .. R/5 and block tiles of 32, 128 and 512
- * centres, keeps the fastest for this cloud and rebuilds its cell grid.  Uses
- * the current tasks and histogram settings; results of the trial runs are
- * discarded.  Has no counterpart in the reference (its KD-tree has no tuning). */
+/* Project-written autotuner: times the scan on about `sample` centres
+ * (0 = 200000) for cell edges R/2 .. R/5, with the per-centre scan at block
+ * tiles of 32, 128 and 512 centres and with the brick scan at bricks of 4, 8
+ * and 16 cells, keeps the fastest for this cloud and rebuilds its cell grid.
+ * best_tile comes back in the pp_cloud_tuning encoding.  Uses the current
+ * tasks and histogram settings; results of the trial runs are discarded.  Has
+ * no counterpart in the reference (its KD-tree has no tuning). */
 int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk,
                 uint32_t sample, float* best_ratio, uint32_t* best_tile);
-/* Set the tuning of a cloud directly: cell edge R / cell_ratio, tile centres
- * per block work item. */
+/* Set the tuning of a cloud directly: cell edge R / cell_ratio, and a tile
+ * code: 1..65535 = the per-centre scan with that many centres per block work
+ * item; (b << 16) | c with b in 1..64 and c in 1..32 = the brick scan, a warp
+ * taking up to c centres of b consecutive cells of a grid row together (used
+ * for passes without CNTNB whose kNN, if any, has k <= 32 and disjoint
+ * environment sets; other passes use the per-centre scan).  Results do not
+ * depend on the tuning. */
 int pp_cloud_tuning(pp_ctx* ctx, int cloud, float cell_ratio, uint32_t tile);
 
 /* FP64 audit of the current tasks and histogram settings on up to

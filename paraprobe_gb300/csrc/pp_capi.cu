@@ -75,6 +75,9 @@ struct Cloud {
   // tuning (pp_autotune): cell edge = R / cell_ratio, centres per block tile
   float cell_ratio = 3.0f;
   uint32_t tile = 128;
+  // brick scan: (cells per brick << 16) | centres per warp batch; 0 = the
+  // per-centre scan with `tile` centres per block work item
+  uint32_t brick = 0;
   Hull hull;
   DevBuf user_surf;             // input order, when given
   bool has_user_surf = false;
@@ -111,6 +114,9 @@ struct RunPlan {
   int cmax = 0;
   int cat_miss = 0;
   std::vector<float> catT;
+  std::vector<uint16_t> lut;       // category by high bits of d^2 (see build_lut)
+  int lut_shift = 0;
+  uint32_t lut_base = 0;
   int disjoint = 0;
   std::vector<int8_t> setidx;      // [nC][256]
 };
@@ -160,6 +166,9 @@ struct pp_ctx {
   float geo_R = -1.f;
   uint32_t geo_ncentres = 0;
   uint64_t geo_pairs = 0;
+  bool geo_emitted_all = false;  // the pair buffer holds every list (not one chunk's)
+  uint64_t pair_cap_opt = 0;     // option "batched_pair_cap": most pairs held at once (0 = by free memory)
+  DevBuf geo_counters;           // pair counters of the geometry passes
   int geo_H = 0;
   float geo_rmin = 0, geo_rincr = 0;
   uint64_t grid_counter = 1;
@@ -246,6 +255,42 @@ std::vector<float> threshold_table(const Tables& t) {
     std::memcpy(&T[k], &lo, 4);
   }
   return T;
+}
+
+// Category lookup table over the ordered bit patterns of d^2 in [0, R^2]:
+// cell c covers the patterns with (bits >> shift) == base + c and holds the
+// category of its smallest d^2 (cell 0 also takes every smaller d^2, all of
+// category T-count-at-0).  The device starts there and steps up through T, so
+// the result equals the threshold search for any shift; the shift is the
+// finest that keeps the table within max_cells, so a cell rarely spans more
+// than one threshold.
+void build_lut(const std::vector<float>& T, float r2, int max_cells, std::vector<uint16_t>& lut, int& shift,
+               uint32_t& base) {
+  const int H = (int)T.size();
+  auto bits = [](float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; };
+  auto cat = [&](float d2) {
+    int k = 0;
+    while (k + 1 < H && T[k + 1] <= d2) ++k;
+    return k;
+  };
+  float tmin = r2;
+  for (int k = 1; k < H; ++k)
+    if (T[k] > 0.f && T[k] < tmin) tmin = T[k];
+  const uint32_t top = bits(std::max(r2, 0.f));
+  for (shift = 0; shift < 31; ++shift) {
+    base = bits(tmin) >> shift;
+    if ((int64_t)(top >> shift) - (int64_t)base + 1 <= max_cells) break;
+  }
+  base = bits(tmin) >> shift;
+  const int n = (int)((top >> shift) - base + 1);
+  lut.assign(n, 0);
+  lut[0] = (uint16_t)cat(0.f);
+  for (int c = 1; c < n; ++c) {
+    const uint32_t u = (base + (uint32_t)c) << shift;
+    float f;
+    std::memcpy(&f, &u, 4);
+    lut[c] = (uint16_t)cat(f);
+  }
 }
 
 inline bool has_type(const uint32_t* m, int t) { return (m[t >> 5] >> (t & 31)) & 1u; }
@@ -524,6 +569,7 @@ int make_plan(pp_ctx* ctx, uint32_t flags, const uint32_t* k_list, int nk, RunPl
       if (b) P.setidx[c * 256 + ty] = (int8_t)__builtin_ctz(b);
     }
   P.catT = threshold_table(t);
+  build_lut(P.catT, t.rmax * t.rmax, 4096, P.lut, P.lut_shift, P.lut_base);
   P.cat_miss = category_of_distance(t, (float)((double)t.rmax + kEpsilon));
   return PP_OK;
 }
@@ -531,6 +577,7 @@ int make_plan(pp_ctx* ctx, uint32_t flags, const uint32_t* k_list, int nk, RunPl
 // Upload the plan's tables into one device block; returns device pointers.
 struct DevTables {
   float* catT; int8_t* cslot; int8_t* eslot; uint32_t* envbits; int* set_list; int* nsets; int* kvals;
+  uint16_t* lut;
   int8_t* setidx;
   int8_t* rowtab;
 };
@@ -556,6 +603,7 @@ int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
   int nrow = 0;
   const int8_t* rows = pp::row_table_host(&nrow);
   const size_t o9 = put(rows, (size_t)nrow * 2);
+  const size_t o10 = put(P.lut.data(), P.lut.size() * 2);
   CK(ctx->tables_dev.ensure(blob.size()));
   CK(cudaMemcpyAsync(ctx->tables_dev.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));  // blob is a host temporary
@@ -564,6 +612,7 @@ int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
   D.envbits = (uint32_t*)(b + o4); D.set_list = (int*)(b + o5); D.nsets = (int*)(b + o6); D.kvals = (int*)(b + o7);
   D.setidx = (int8_t*)(b + o8);
   D.rowtab = (int8_t*)(b + o9);
+  D.lut = (uint16_t*)(b + o10);
   return PP_OK;
 }
 
@@ -585,6 +634,10 @@ void fill_scan_common(pp::ScanArgs& a, const Cloud& cl, const RunPlan& P, const 
   a.cat_T = D.catT;
   a.guess_start = t.rmin;
   a.guess_scale = (float)t.hscale;
+  a.cat_lut = D.lut;
+  a.lut_n = (int)P.lut.size();
+  a.lut_shift = P.lut_shift;
+  a.lut_base = P.lut_base;
   a.cat_miss = P.cat_miss;
   a.cslot_of = D.cslot;
   a.eslot_of = D.eslot;
@@ -963,7 +1016,12 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   }
   uint32_t ncent = 0;
   if ((rc = select_centres(ctx, *cl, labels, surf, D.cslot, R, &ncent, s))) return rc;
-  if (centre_limit && ncent > centre_limit) ncent = centre_limit;
+  // a tuning sample: every stride-th centre (or brick) over the whole cloud
+  uint32_t stride = 1;
+  if (centre_limit && ncent > centre_limit) {
+    stride = ncent / centre_limit;
+    ncent = ncent / stride;
+  }
   ctx->res.ncentres_total = ncent;
   ctx->res.n_ions = n;
   CK(ctx->work.ensure(16));
@@ -983,6 +1041,7 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   a.work = ctx->work.as<uint32_t>();
   a.status = ctx->res.status.as<int>();
   a.mode = 0;
+  a.sample_stride = stride;
   a.rdf_in_smem = ((a.flags & PP_RDF) && (size_t)P.nC * P.nE * P.H * 4 <= 96 * 1024) ? 1 : 0;
   // RDF / RIPK alone: each pair of two centres is computed once and credited
   // to both (the counts are the same as the per-centre ball scan's)
@@ -1000,7 +1059,23 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   if (ncent > 0) {
     size_t smem = 0;
     CK(cudaEventRecord(ctx->ev0, s));
-    rc = pp::launch_scan(a, P.kr, P.emax, ctx->sm_count, &smem, s);
+    rc = -3;
+    const Grid& g = cl->g;
+    if (cl->brick && (int)std::floor((R + 3.f * g.margin) * g.inv_h) + 1 <= 7) {
+      a.bx = (int)(cl->brick >> 16);
+      a.bcap = (int)(cl->brick & 0xffffu);
+      const uint64_t nbx = ((uint64_t)g.nx + a.bx - 1) / a.bx;
+      uint64_t nb = nbx * g.ny * g.nz;
+      if (stride > 1) nb = std::max<uint64_t>(1, nb / stride);
+      if (nb < (1ull << 32)) {
+        a.nbricks = (uint32_t)nb;
+        const uint32_t keep = a.tile;
+        a.tile = 16;
+        rc = pp::launch_brick(a, P.kr, ctx->sm_count, &smem, s);
+        a.tile = keep;
+      }
+    }
+    if (rc == -3) rc = pp::launch_scan(a, P.kr, P.emax, ctx->sm_count, &smem, s);
     CK(cudaEventRecord(ctx->ev1, s));
     ctx->ev_recorded = true;
     if (rc == -2) return fail(ctx, PP_ERR_UNSUPPORTED, "no kernel variant for k=%d with %d environment sets", P.kmax, P.emax);
@@ -1038,16 +1113,18 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
   CK(cudaSetDevice(ctx->device));
   if (sample == 0) sample = 200000;
   const float ratios[] = {2.0f, 3.0f, 4.0f, 5.0f};
-  const uint32_t tiles[] = {32, 128, 512};
+  // per-centre tiles, then brick codes (cells per brick << 16 | batch)
+  const uint32_t tiles[] = {32, 128, 512, (4u << 16) | 16u, (8u << 16) | 16u, (8u << 16) | 32u, (16u << 16) | 32u};
   float bestr = cl->cell_ratio, bestms = 1e30f;
-  uint32_t bestt = cl->tile;
+  uint32_t bestt = cl->brick ? cl->brick : cl->tile;
   const float R = ctx->tab.rmax;
   for (float r : ratios) {
     cl->cell_ratio = r;
     int rc = build_grid(ctx, *cl, R, 0);
     if (rc) return rc;
     for (uint32_t t : tiles) {
-      cl->tile = t;
+      if (t >= 65536u) cl->brick = t;
+      else { cl->tile = t; cl->brick = 0; }
       float ms = 0.f;
       for (int rep = 0; rep < 2; ++rep) {  // first repetition warms caches and lazy state
         rc = run_plain(ctx, cl, flags, k_list, nk, nullptr, 0, sample);
@@ -1059,7 +1136,8 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
     }
   }
   cl->cell_ratio = bestr;
-  cl->tile = bestt;
+  if (bestt >= 65536u) cl->brick = bestt;
+  else { cl->tile = bestt; cl->brick = 0; }
   int rc = build_grid(ctx, *cl, R, 0);
   if (rc) return rc;
   ctx->res.valid = false;
@@ -1145,16 +1223,29 @@ int pp_fp64_audit(pp_ctx* ctx, int cloud, uint32_t max_centres, double* max_abs,
 int pp_set_option(pp_ctx* ctx, const char* name, int value) {
   if (!ctx || !name) return PP_ERR_INVALID;
   if (std::strcmp(name, "symmetric") == 0) { ctx->no_sym = (value == 0); return PP_OK; }
+  if (std::strcmp(name, "batched_pair_cap") == 0) {
+    if (value < 0) return fail(ctx, PP_ERR_INVALID, "batched_pair_cap must be >= 0");
+    ctx->pair_cap_opt = (uint64_t)value;
+    return PP_OK;
+  }
   return fail(ctx, PP_ERR_INVALID, "unknown option %s", name);
 }
 
 int pp_cloud_tuning(pp_ctx* ctx, int cloud, float cell_ratio, uint32_t tile) {
   Cloud* cl = ctx ? get_cloud(ctx, cloud) : nullptr;
-  if (!cl || !(cell_ratio >= 1.0f && cell_ratio <= 8.0f) || tile == 0 || tile > 65536)
-    return fail(ctx, PP_ERR_INVALID, "cell_ratio in [1, 8] and tile in [1, 65536] required");
+  if (!cl || !(cell_ratio >= 1.0f && cell_ratio <= 8.0f) || tile == 0)
+    return fail(ctx, PP_ERR_INVALID, "cell_ratio in [1, 8] and a tile code required");
+  if (tile >= 65536u) {
+    const uint32_t bx = tile >> 16, cap = tile & 0xffffu;
+    if (bx < 1 || bx > 64 || cap < 1 || cap > 32)
+      return fail(ctx, PP_ERR_INVALID, "brick code: cells per brick in [1, 64] << 16 | batch in [1, 32]");
+    cl->brick = tile;
+  } else {
+    cl->tile = tile;
+    cl->brick = 0;
+  }
   if (cl->cell_ratio != cell_ratio) cl->grid_ok = false;
   cl->cell_ratio = cell_ratio;
-  cl->tile = tile;
   return PP_OK;
 }
 
@@ -1305,7 +1396,8 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     a.centres = ctx->geo_centres.as<uint32_t>();
     a.ncentres = nc;
     a.flags = 0;
-    a.counters = ctx->res.counters.as<unsigned long long>();
+    CK(ctx->geo_counters.ensure(16));
+    a.counters = ctx->geo_counters.as<unsigned long long>();
     a.status = ctx->res.status.as<int>();
     a.rdf_in_smem = 0;
     CK(ctx->work.ensure(16));
@@ -1334,17 +1426,8 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
       pp::launch_max_u32(ctx->pair_count.as<uint32_t>(), nc, ctx->maxlist.as<uint32_t>(), s);
       CK(cudaMemcpyAsync(&ctx->geo_maxlist, ctx->maxlist.p, 4, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
-      CK(ctx->pair_slot.ensure(std::max<unsigned long long>(total, 1) * 4));
-      CK(ctx->pair_cat.ensure(std::max<unsigned long long>(total, 1) * 2));
-      CK(cudaMemsetAsync(ctx->work.p, 0, 16, s));
-      a.mode = 2;
-      a.pair_off = ctx->pair_off.as<unsigned long long>();
-      a.pair_slot = ctx->pair_slot.as<uint32_t>();
-      a.pair_cat = ctx->pair_cat.as<uint16_t>();
-      a.pair_cap = total;
-      if (pp::launch_scan(a, 0, 1, ctx->sm_count, nullptr, s)) return fail(ctx, PP_ERR_CUDA, "pair emit launch failed");
-      CK(cudaGetLastError());
     }
+    ctx->geo_emitted_all = false;
     ctx->geo_cloud = cloud;
     ctx->geo_key_version = cl->grid_version;
     ctx->geo_R = R;
@@ -1353,10 +1436,81 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     ctx->geo_rincr = ctx->tab.rincr;
     ctx->geo_ncentres = nc;
     ctx->geo_pairs = total;
-    // counters were used by the geometry passes; clear them for the apply
-    CK(cudaMemsetAsync(ctx->res.counters.p, 0, 16 * (size_t)nreal, s));
   }
   const uint32_t nc = ctx->geo_ncentres;
+  const unsigned long long total = ctx->geo_pairs;
+  // ---- pair lists: all at once when they fit, else per chunk of centres
+  // (each chunk's lists are emitted, then every realisation is applied)
+  uint64_t cap = ctx->pair_cap_opt;
+  if (!cap) {
+    size_t freeb = 0, totb = 0;
+    CK(cudaMemGetInfo(&freeb, &totb));
+    const uint64_t held = ctx->pair_slot.bytes + ctx->pair_cat.bytes;
+    const uint64_t reserve = (uint64_t)n * nreal * 3 + (uint64_t)nc * nreal * 3 + (4ull << 30);
+    const uint64_t avail = freeb + held > reserve ? freeb + held - reserve : 0;
+    cap = avail / 6 * 7 / 10;
+  }
+  cap = std::max<uint64_t>(cap, std::max<uint64_t>(ctx->geo_maxlist, 1));
+  const bool chunked = total > cap;
+  const uint64_t list_len = chunked ? cap : total;
+  CK(ctx->pair_slot.ensure(std::max<uint64_t>(list_len, 1) * 4));
+  CK(ctx->pair_cat.ensure(std::max<uint64_t>(list_len, 1) * 2));
+  pp::ScanArgs ea;  // the emit pass (category-sorted lists of a range of centres)
+  std::memset(&ea, 0, sizeof ea);
+  fill_scan_common(ea, *cl, P, D, ctx->tab);
+  ea.labels = cl->label_sorted.as<uint8_t>();
+  ea.flags = 0;
+  CK(ctx->geo_counters.ensure(16));
+  ea.counters = ctx->geo_counters.as<unsigned long long>();
+  ea.status = ctx->res.status.as<int>();
+  ea.rdf_in_smem = 0;
+  ea.mode = 2;
+  ea.pair_slot = ctx->pair_slot.as<uint32_t>();
+  ea.pair_cat = ctx->pair_cat.as<uint16_t>();
+  CK(ctx->work.ensure(16));
+  ea.work = ctx->work.as<uint32_t>() + 2;
+  const pp::ScanArgs ea_sig = ea;  // before any range is set: the graph's key
+  auto set_emit_range = [&](uint32_t c0, uint32_t c1, unsigned long long p0, unsigned long long p1) {
+    ea.centres = ctx->geo_centres.as<uint32_t>() + c0;
+    ea.ncentres = c1 - c0;
+    ea.pair_off = ctx->pair_off.as<unsigned long long>() + c0;
+    ea.pair_base = p0;
+    ea.pair_cap = p1 - p0;
+  };
+  if (!chunked && !ctx->geo_emitted_all && nc) {
+    set_emit_range(0, nc, 0, total);
+    CK(cudaMemsetAsync(ea.work, 0, 4, s));
+    if (pp::launch_scan(ea, 0, 1, ctx->sm_count, nullptr, s)) return fail(ctx, PP_ERR_CUDA, "pair emit launch failed");
+    CK(cudaGetLastError());
+    ctx->geo_emitted_all = true;
+  }
+  if (chunked) ctx->geo_emitted_all = false;
+  struct Chunk { uint32_t c0, c1; unsigned long long p0, p1; };
+  std::vector<Chunk> chunks;
+  if (!chunked) {
+    chunks.push_back({0, nc, 0, total});
+  } else {
+    auto off = [&](uint32_t i, unsigned long long* v) {
+      return cudaMemcpy(v, ctx->pair_off.as<unsigned long long>() + i, 8, cudaMemcpyDeviceToHost);
+    };
+    uint32_t c = 0;
+    unsigned long long pc = 0;
+    while (c < nc) {
+      // the last centre c1 with pair_off[c1] - pair_off[c] <= cap
+      uint32_t lo = c + 1, hi = nc;
+      while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo + 1) / 2;
+        unsigned long long v = 0;
+        CK(off(mid, &v));
+        if (v - pc <= cap) lo = mid; else hi = mid - 1;
+      }
+      unsigned long long pe = 0;
+      CK(off(lo, &pe));
+      chunks.push_back({c, lo, pc, pe});
+      c = lo;
+      pc = pe;
+    }
+  }
   // ---- realisation labels (sorted-slot order) and centre masks
   CK(ctx->real_labels.ensure(std::max<uint64_t>(n, 1) * nreal));
   CK(ctx->centre_ok.ensure(std::max<uint64_t>(nc, 1) * nreal));
@@ -1403,6 +1557,7 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     std::memset(&b, 0, sizeof b);
     b.centres = ctx->geo_centres.as<uint32_t>();
     b.ncentres = nc;
+    b.nc_total = nc;
     b.pair_off = ctx->pair_off.as<unsigned long long>();
     b.pair_slot = ctx->pair_slot.as<uint32_t>();
     b.pair_cat = ctx->pair_cat.as<uint16_t>();
@@ -1507,28 +1662,44 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
       kq.work = ctx->work.as<uint32_t>() + 1;
     }
     auto enqueue = [&](cudaStream_t st) -> int {
-      if (cudaMemsetAsync(ctx->work.p, 0, 16, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
-      if (pp::launch_apply(b, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "apply launch failed");
-      pp::KnnArgs k = kq;
-      for (int g = 0; g < ng32; ++g) {
-        for (uint32_t c0 = 0; c0 < nc; c0 += chunk) {
-          k.grp = g;
-          k.c0 = c0;
-          k.cn = std::min(chunk, nc - c0);
-          k.tile = 64;
-          if (cudaMemsetAsync(k.work, 0, 4, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
-          if (pp::launch_knn_walk(k, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "kNN walk launch failed");
-          const uint32_t nranges = (uint32_t)std::max<uint64_t>(1, (8ull * ctx->sm_count + NT - 1) / NT);
-          k.tile = std::max<uint32_t>(1, (k.cn + nranges - 1) / nranges);
-          if (cudaMemsetAsync(k.work, 0, 4, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
-          if (pp::launch_knn_bin(k, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "kNN bin launch failed");
+      for (const Chunk& ch : chunks) {
+        if (chunked) {
+          set_emit_range(ch.c0, ch.c1, ch.p0, ch.p1);
+          if (cudaMemsetAsync(ea.work, 0, 4, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
+          if (pp::launch_scan(ea, 0, 1, ctx->sm_count, nullptr, st)) return fail(ctx, PP_ERR_CUDA, "pair emit launch failed");
+        }
+        pp::ApplyArgs bc = b;
+        bc.centres = b.centres + ch.c0;
+        bc.ncentres = ch.c1 - ch.c0;
+        bc.pair_off = b.pair_off + ch.c0;
+        bc.cbase = ch.c0;
+        bc.pair_base = ch.p0;
+        if (cudaMemsetAsync(ctx->work.p, 0, 8, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
+        if (pp::launch_apply(bc, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "apply launch failed");
+        pp::KnnArgs k = kq;
+        k.pair_base = ch.p0;
+        for (int g = 0; g < ng32; ++g) {
+          for (uint32_t c0 = ch.c0; c0 < ch.c1; c0 += chunk) {
+            k.grp = g;
+            k.c0 = c0;
+            k.cn = std::min(chunk, ch.c1 - c0);
+            k.tile = 64;
+            if (cudaMemsetAsync(k.work, 0, 4, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
+            if (pp::launch_knn_walk(k, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "kNN walk launch failed");
+            const uint32_t nranges = (uint32_t)std::max<uint64_t>(1, (8ull * ctx->sm_count + NT - 1) / NT);
+            k.tile = std::max<uint32_t>(1, (k.cn + nranges - 1) / nranges);
+            if (cudaMemsetAsync(k.work, 0, 4, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
+            if (pp::launch_knn_bin(k, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "kNN bin launch failed");
+          }
         }
       }
       return PP_OK;
     };
     std::string sig((const char*)&b, sizeof b);
     sig.append((const char*)&kq, sizeof kq);
-    const uint64_t extra[4] = {(uint64_t)ng32, chunk, nc, (uint64_t)ctx->sm_count};
+    sig.append((const char*)&ea_sig, sizeof ea_sig);
+    sig.append((const char*)chunks.data(), chunks.size() * sizeof(Chunk));
+    const uint64_t extra[5] = {(uint64_t)ng32, chunk, nc, (uint64_t)ctx->sm_count, chunked ? 1u : 0u};
     sig.append((const char*)extra, sizeof extra);
     if (!ctx->apply_exec || sig != ctx->apply_sig) {
       if (!ctx->cap_stream) CK(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));

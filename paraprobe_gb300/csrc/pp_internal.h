@@ -43,6 +43,17 @@ struct ScanArgs {
   int H;                       // nb + 2
   const float* cat_T;          // [H] smallest d^2 of each category (index 0 unused)
   float guess_start, guess_scale;
+  // category lookup by the high bits of d^2: cell (bits(d2) >> lut_shift) -
+  // lut_base (clamped) holds the category of the cell's smallest d^2
+  const uint16_t* cat_lut;
+  int lut_n, lut_shift;
+  uint32_t lut_base;
+  // brick scan: cells per brick, centres per warp batch, bricks to process
+  int bx, bcap;
+  uint32_t nbricks;
+  // tuning samples: centre ci (brick b) of the pass is entry ci * stride
+  // (b * stride) of the full list; 0 or 1 = every entry
+  uint32_t sample_stride;
   int cat_miss;                // category of the float R + EPSILON
   // type maps
   const int8_t* cslot_of;      // [256] centre slot of a type or -1
@@ -79,6 +90,7 @@ struct ScanArgs {
   uint32_t* pair_slot;           // [total] (mode 2)
   uint16_t* pair_cat;            // [total] (mode 2)
   unsigned long long pair_cap;
+  unsigned long long pair_base;  // pair_slot/pair_cat hold positions [pair_base, pair_base + pair_cap)
 };
 
 // Realisation pass over stored pair lists (batched null models and ROIs).
@@ -89,7 +101,9 @@ struct ApplyArgs {
   const uint32_t* pair_slot;
   const uint16_t* pair_cat;
   const uint8_t* labels;         // [ngroups][n][group] type per sorted slot
-  const uint8_t* centre_ok;      // [ngroups][ncentres][group] 1 if a centre in that realisation
+  const uint8_t* centre_ok;      // [ngroups][nc_total][group] 1 if a centre in that realisation
+  uint32_t cbase, nc_total;      // this launch's centres are entries [cbase, cbase + ncentres) of nc_total
+  unsigned long long pair_base;  // pair_slot/pair_cat hold list positions from pair_base on
   uint64_t n;
   int nreal;
   int group, ngroups;            // realisations per work item (1, 2, 4, 8) and the number of groups
@@ -161,6 +175,8 @@ int launch_tri_bins(const float* tbox, uint64_t ntri, Grid tg, float grow, uint3
                     uint32_t* tlist, uint64_t list_cap, uint32_t* scan_tmp, uint64_t scan_tmp_elems,
                     uint64_t* total_out, cudaStream_t s);
 int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s);
+// the brick variant of k_scan; -3 when it does not apply to these arguments
+int launch_brick(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cudaStream_t s);
 int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s);
 // Batched kNN in two phases, 32 realisations per warp (one per lane).
 // Walk: per (centre, realisation) the category of the k-th member of every
@@ -174,6 +190,7 @@ struct KnnArgs {
   const unsigned long long* pair_off;
   const uint32_t* pair_slot;
   const uint16_t* pair_cat;
+  unsigned long long pair_base;     // pair_slot/pair_cat hold list positions from pair_base on
   const uint8_t* labels;            // [ngroups][n][32]
   const uint8_t* centre_ok;         // [ngroups][ncentres][32]
   uint64_t n;
@@ -190,10 +207,11 @@ struct KnnArgs {
   uint8_t* rec_c;                   // [cn][32]
   uint32_t* work;
   uint32_t tile;                    // centres per walk work item / per bin work item
+  int cblk;                         // centre types per bin histogram (set by knn32_check)
   unsigned long long* knn_core;     // [nreal][nC][nS][nkI][H]
 };
 // -2 when a warp's records or the bin histogram do not fit shared memory
-int knn32_check(const KnnArgs& k);
+int knn32_check(KnnArgs& k);
 int launch_knn_walk(const KnnArgs& k, int sm_count, cudaStream_t s);
 int launch_knn_bin(const KnnArgs& k, int sm_count, cudaStream_t s);
 

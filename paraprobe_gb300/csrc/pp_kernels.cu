@@ -462,6 +462,17 @@ __device__ __forceinline__ int category(float d2, const float* __restrict__ sT, 
   return g;
 }
 
+// The same category from the lookup table: start at the category of the
+// table cell's smallest d^2 and step up through the thresholds.
+__device__ __forceinline__ int category_lut(float d2, const uint16_t* __restrict__ lut, int lut_n, uint32_t lut_base,
+                                            int lut_shift, const float* __restrict__ sT, int H) {
+  int idx = (int)(__float_as_uint(d2) >> lut_shift) - (int)lut_base;
+  idx = idx < 0 ? 0 : (idx >= lut_n ? lut_n - 1 : idx);
+  int g = lut[idx];
+  while (g + 1 < H && sT[g + 1] <= d2) ++g;
+  return g;
+}
+
 template <int KR>
 __device__ __forceinline__ void list_insert(float (&l)[KR], float x, int lane) {
   int pos = 0;
@@ -496,6 +507,7 @@ __device__ __forceinline__ float list_get(const float (&l)[KR], int row, int src
 
 struct ScanShared {
   int8_t* rowtab; // [ROW_TABLE_ENTRIES][2]
+  uint16_t* lut;  // [lut_n] category lookup
   float* lst;     // [warps][emax][LS] sorted kNN lists (disjoint sets)
   float* T;
   int8_t* cs;
@@ -625,6 +637,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
     S.since_flush = (unsigned long long*)p; p += 16;
     S.rowtab = (int8_t*)p; p += ROW_TABLE_ENTRIES * 2;
     S.T = (float*)p; p += ((H + 3) & ~3) * 4;
+    S.lut = (uint16_t*)p; p += ((a.lut_n + 7) & ~7) * 2;
     S.cs = (int8_t*)p; p += 256;
     S.es = (int8_t*)p; p += 256;
     S.env = (uint32_t*)p; p += (KR > 0 ? a.nC * 256 * 4 : 0);
@@ -635,6 +648,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
     S.sidx = (int8_t*)p;
   }
   for (int i = threadIdx.x; i < H; i += blockDim.x) S.T[i] = a.cat_T[i];
+  for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) S.lut[i] = a.cat_lut[i];
   for (int i = threadIdx.x; i < ROW_TABLE_ENTRIES * 2; i += blockDim.x) S.rowtab[i] = a.rowtab[i];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) { S.cs[i] = a.cslot_of[i]; S.es[i] = a.eslot_of[i]; }
   if (KR > 0) for (int i = threadIdx.x; i < a.nC * 256; i += blockDim.x) S.env[i] = a.envbits[i];
@@ -670,7 +684,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
     if (kk >= clen) break;
     {
       const uint32_t ci = c0 + kk;
-      const uint32_t self = a.centres[ci];
+      const uint32_t self = a.centres[a.sample_stride > 1 ? (uint64_t)ci * a.sample_stride : ci];
       const float4 cp = a.ions[self];
       const uint32_t ct = a.labels ? (uint32_t)a.labels[self] : __float_as_uint(cp.w);
       const int cs = (a.mode == 0) ? S.cs[ct & 255] : 0;
@@ -711,7 +725,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
             const int es = S.es[m & 255];
             int cat = -1;
             if (doR && es >= 0) {
-              cat = category(d2, S.T, H, a.guess_start, a.guess_scale);
+              cat = category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H);
               const uint32_t idx = ((uint32_t)cs * a.nE + es) * H + cat;
               if (a.rdf_in_smem) atomicAdd(&S.rdf[idx], 1u);
               else atomicAdd(&a.rdf_core[idx], 1ull);
@@ -721,7 +735,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
               ++inb;
               const int csj = S.cs[m & 255], esi = S.es[ct & 255];
               if (doR && esi >= 0 && csj >= 0) {
-                if (cat < 0) cat = category(d2, S.T, H, a.guess_start, a.guess_scale);
+                if (cat < 0) cat = category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H);
                 const uint32_t idx = ((uint32_t)csj * a.nE + esi) * H + cat;
                 if (a.rdf_in_smem) atomicAdd(&S.rdf[idx], 1u);
                 else atomicAdd(&a.rdf_core[idx], 1ull);
@@ -781,7 +795,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
             // the k-th smallest d^2 of each set -> its bin (or the miss bin)
             auto emit = [&](int p, int kk, float v) {
               const int Sg = a.set_list[cs * 32 + p];
-              const int cat = (v == kInf()) ? a.cat_miss : category(v, S.T, H, a.guess_start, a.guess_scale);
+              const int cat = (v == kInf()) ? a.cat_miss : category_lut(v, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H);
               atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
             };
             if constexpr (SL) {
@@ -823,7 +837,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
         // mode 2: counting sort of the ball by category into the pair list
         int* hist = S.hist + warp * H;
         for_each_candidate(a, S.rowtab, cp, self, lane, [&](bool, uint32_t, float d2, bool inball, uint32_t, bool) {
-          if (inball) atomicAdd(&hist[category(d2, S.T, H, a.guess_start, a.guess_scale)], 1);
+          if (inball) atomicAdd(&hist[category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H)], 1);
         });
         __syncwarp();
         int run = 0;
@@ -844,9 +858,12 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
         const unsigned long long lim = a.pair_off[ci + 1];
         for_each_candidate(a, S.rowtab, cp, self, lane, [&](bool, uint32_t slot, float d2, bool inball, uint32_t, bool) {
           if (inball) {
-            const int cat = category(d2, S.T, H, a.guess_start, a.guess_scale);
+            const int cat = category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H);
             const unsigned long long at = off + (unsigned long long)atomicAdd(&hist[cat], 1);
-            if (at < lim && at < a.pair_cap) { a.pair_slot[at] = slot; a.pair_cat[at] = (uint16_t)cat; }
+            if (at < lim && at - a.pair_base < a.pair_cap) {
+              a.pair_slot[at - a.pair_base] = slot;
+              a.pair_cat[at - a.pair_base] = (uint16_t)cat;
+            }
             else atomicOr(a.status, ST_LIST_OVERFLOW);
             ++inb;
           }
@@ -886,6 +903,294 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
   if (a.rdf_in_smem && doR) {
     for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) {
       const uint32_t v = S.rdf[i];
+      if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
+    }
+  }
+}
+
+// -------------------------------------------------------- K3' brick scan
+// The same pass as k_scan, organised around bricks: a brick is up to bx
+// consecutive cells of one grid row, and a warp takes the centres of a brick
+// (up to `bcap` at a time, in slot order) together.  The stencil rows of the
+// brick (every row whose cells can hold a point within R of a point of the
+// brick, trimmed in x to the brick's reach) are set up once and their ions
+// streamed 32 per step; each candidate is then tested against every centre
+// of the batch, whose positions sit in shared memory.  Row set-up and
+// candidate loads are shared by the batch instead of paid per centre.  The
+// pair set, its distances and bins are those of k_scan: same d^2 expression,
+// same in-ball test, same symmetric rule (a pair of two centres is taken by
+// the lower slot and credited to both).
+template <bool KNN>
+__global__ void __launch_bounds__(256) k_brick(ScanArgs a) {
+  constexpr int NW = 8;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int H = a.H;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int K = KNN ? a.kmax : 1, CB = a.bcap;
+  unsigned char* sp = smem;
+  unsigned long long* since_flush = (unsigned long long*)sp; sp += 16;
+  float4* cposA = (float4*)sp; sp += NW * 32 * 16;
+  uint32_t* cslA = (uint32_t*)sp; sp += NW * 32 * 4;
+  float* sT = (float*)sp; sp += ((H + 3) & ~3) * 4;
+  uint16_t* slut = (uint16_t*)sp; sp += ((a.lut_n + 7) & ~7) * 2;
+  uint32_t* srdf = (uint32_t*)sp; sp += (a.rdf_in_smem ? (size_t)a.nC * a.nE * H * 4 : 0);
+  float* lists = (float*)sp; sp += (KNN ? (size_t)NW * a.emax * CB * K * 4 : 0);
+  int8_t* rowtab = (int8_t*)sp; sp += ROW_TABLE_ENTRIES * 2;
+  int8_t* scs = (int8_t*)sp; sp += 256;
+  int8_t* ses = (int8_t*)sp; sp += 256;
+  int8_t* cctA = (int8_t*)sp; sp += NW * 32;
+  int8_t* cesA = (int8_t*)sp; sp += NW * 32;
+  int8_t* sidx = (int8_t*)sp;  // [nC][256] (KNN)
+  for (int i = threadIdx.x; i < H; i += blockDim.x) sT[i] = a.cat_T[i];
+  for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) slut[i] = a.cat_lut[i];
+  for (int i = threadIdx.x; i < ROW_TABLE_ENTRIES * 2; i += blockDim.x) rowtab[i] = a.rowtab[i];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) { scs[i] = a.cslot_of[i]; ses[i] = a.eslot_of[i]; }
+  if (KNN) for (int i = threadIdx.x; i < a.nC * 256; i += blockDim.x) sidx[i] = a.setidx[i];
+  if (a.rdf_in_smem) for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) srdf[i] = 0;
+  if (threadIdx.x == 0) *since_flush = 0ull;
+  __syncthreads();
+
+  const Grid& g = a.g;
+  const bool doR = (a.flags & PP_RDF) != 0;
+  const bool doK = KNN;
+  float4* cpos = cposA + warp * 32;
+  uint32_t* csl = cslA + warp * 32;
+  int8_t* cct = cctA + warp * 32;
+  int8_t* ces = cesA + warp * 32;
+  float* L = lists + (size_t)warp * a.emax * CB * K;   // set p, centre c: L + (p * CB + c) * K
+  const uint32_t lt = (1u << lane) - 1u, lemask = (2u << lane) - 1u;
+  const float m2 = 2.f * g.margin;
+  const float Rp = a.R + g.margin, Rp2 = Rp * Rp;
+  // rows |dy| = k can hold a neighbour while (k - 1) h - 2 margin <= R + margin
+  const int sr_need = (int)floorf((Rp + m2) * g.inv_h) + 1;
+  const int sr = min(ROW_SMAX, sr_need);
+  const int nrows = (2 * sr + 1) * (2 * sr + 1);
+  const int8_t* tab = rowtab + 2 * row_table_offset(sr);
+  if (sr_need > ROW_SMAX && threadIdx.x == 0) atomicOr(a.status, ST_BAD_SLOT);
+  const uint32_t nbx = (uint32_t)((g.nx + a.bx - 1) / a.bx);
+  unsigned long long pairs_lane = 0, centres = 0;
+  constexpr unsigned long long FLUSH = 1ull << 30;
+  __shared__ uint32_t s_tile, s_next;
+  const uint32_t T = a.tile;
+  const uint32_t ntiles = (a.nbricks + T - 1) / T;
+  for (;;) {
+    if (threadIdx.x == 0) { s_tile = atomicAdd(a.work, 1u); s_next = 0; }
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= ntiles) break;
+    const uint32_t b0 = tile * T, blen = min(T, a.nbricks - b0);
+    for (;;) {
+      uint32_t kb = 0;
+      if (lane == 0) kb = atomicAdd(&s_next, 1u);
+      kb = __shfl_sync(FULL, kb, 0);
+      if (kb >= blen) break;
+      const uint32_t b = (a.sample_stride > 1) ? (b0 + kb) * a.sample_stride : b0 + kb;
+      const uint32_t zy = b / nbx;
+      const int xb = (int)(b - zy * nbx) * a.bx;
+      const int y = (int)(zy % (uint32_t)g.ny), z = (int)(zy / (uint32_t)g.ny);
+      const int xe = min(xb + a.bx, g.nx);
+      const uint64_t hrow = ((uint64_t)z * g.ny + y) * g.nx;
+      const uint32_t s1 = a.cell_start[hrow + xe];
+      uint32_t pos = a.cell_start[hrow + xb];
+      while (pos < s1) {
+        // ---- the next batch: up to CB centres of the brick in slot order
+        int mc = 0;
+        while (pos < s1 && mc < CB) {
+          const uint32_t sl = pos + lane;
+          const bool isc = sl < s1 && a.cflag[sl] != 0;
+          const uint32_t cm = __ballot_sync(FULL, isc);
+          const int room = CB - mc, have = __popc(cm);
+          uint32_t takem = cm;
+          if (have > room) {
+            const int lastl = (int)__fns(cm, 0, room);
+            takem = cm & ((2u << lastl) - 1u);
+            pos += (uint32_t)lastl + 1u;
+          } else {
+            pos += 32u;
+          }
+          if ((takem >> lane) & 1u) {
+            const int at = mc + __popc(takem & lt);
+            const float4 cp = a.ions[sl];
+            cpos[at] = cp;
+            csl[at] = sl;
+            const uint32_t ct = a.labels ? (uint32_t)a.labels[sl] : __float_as_uint(cp.w);
+            cct[at] = scs[ct & 255];
+            ces[at] = ses[ct & 255];
+          }
+          mc += min(have, room);
+        }
+        __syncwarp();
+        if (mc == 0) break;
+        if (KNN) {
+          for (int e = lane; e < a.emax * CB * K; e += 32) L[e] = kInf();
+          __syncwarp();
+        }
+        uint32_t inb = 0;
+        // ---- stencil rows of the brick, nearest first
+        for (int r0 = 0; r0 < nrows; r0 += 32) {
+          const int r = r0 + lane;
+          uint32_t st = 0, len = 0;
+          if (r < nrows) {
+            const int dy = tab[2 * r], dz = tab[2 * r + 1];
+            const int yy = y + dy, zz = z + dz;
+            if (yy >= 0 && yy < g.ny && zz >= 0 && zz < g.nz) {
+              const float gy = fmaxf(0.f, (float)(abs(dy) - 1) * g.h - m2);
+              const float gz = fmaxf(0.f, (float)(abs(dz) - 1) * g.h - m2);
+              const float rem = Rp2 - gy * gy - gz * gz;
+              if (rem >= 0.f) {
+                const float half = sqrtf(rem);
+                const int x0 = max(0, (int)floorf(((float)xb * g.h - m2 - half) * g.inv_h));
+                const int x1 = min(g.nx - 1, (int)floorf(((float)xe * g.h + m2 + half) * g.inv_h));
+                const uint64_t cb = ((uint64_t)zz * g.ny + yy) * g.nx;
+                int xs = x0;
+                if (a.sym) {
+                  // cells before the brick in slot order that hold only centres:
+                  // each of their pairs with the brick is taken from their side
+                  const bool own = (zz == z && yy == y);
+                  if (own || zz < z || (zz == z && yy < y)) {
+                    const int xend = own ? min(x1, xb - 1) : x1;
+                    if (xend >= x0 && a.nc_pre[cb + xend + 1] == a.nc_pre[cb + x0]) xs = xend + 1;
+                  }
+                }
+                if (xs <= x1) {
+                  st = a.cell_start[cb + xs];
+                  len = a.cell_start[cb + x1 + 1] - st;
+                }
+              }
+            }
+          }
+          const uint32_t ne = __ballot_sync(FULL, len > 0);
+          const int cnt = __popc(ne);
+          if (cnt == 0) continue;
+          const int src = (lane < cnt) ? (int)__fns(ne, 0, lane + 1) : 0;
+          const uint32_t rst = __shfl_sync(FULL, st, src);
+          uint32_t rlen = __shfl_sync(FULL, len, src);
+          if (lane >= cnt) rlen = 0;
+          uint32_t inc = rlen;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc += t;
+          }
+          const uint32_t exc = inc - rlen;
+          const uint32_t total = __shfl_sync(FULL, inc, 31);
+          int before = 0;
+          for (uint32_t bb = 0; bb < total; bb += 32) {
+            const uint32_t bitv = (lane < cnt && rlen > 0 && exc >= bb && exc < bb + 32) ? (1u << (exc - bb)) : 0u;
+            const uint32_t smask = __reduce_or_sync(FULL, bitv);
+            const int row = before + __popc(smask & lemask) - 1;
+            before += __popc(smask);
+            const int rowc = row < 0 ? 0 : (row > 31 ? 31 : row);
+            const uint32_t rs = __shfl_sync(FULL, rst, rowc);
+            const uint32_t rp = __shfl_sync(FULL, exc, rowc);
+            const uint32_t t = bb + lane;
+            const bool valid = t < total;
+            const uint32_t slot = rs + (t - rp);
+            float4 q = make_float4(kInf(), kInf(), kInf(), 0.f);
+            uint32_t m = 0;
+            bool jc = false;
+            if (valid) {
+              q = __ldg(a.ions + slot);
+              m = a.labels ? (uint32_t)a.labels[slot] : __float_as_uint(q.w);
+              if (a.sym) jc = a.cflag[slot] != 0;
+            }
+            const int esj = ses[m & 255];
+            for (int c = 0; c < mc; ++c) {
+              const float4 cp = cpos[c];
+              const uint32_t isl = csl[c];
+              const float d2 = dist2(cp.x, cp.y, cp.z, q.x, q.y, q.z);
+              const bool inball = valid && (d2 <= a.R2) && (slot != isl) && !(jc && slot < isl);
+              const int cs = cct[c];
+              if (inball) {
+                ++inb;
+                int cat = -1;
+                if (doR && esj >= 0) {
+                  cat = category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+                  const uint32_t idx = ((uint32_t)cs * a.nE + esj) * H + cat;
+                  if (a.rdf_in_smem) atomicAdd(&srdf[idx], 1u);
+                  else atomicAdd(&a.rdf_core[idx], 1ull);
+                }
+                if (jc && slot > isl) {
+                  // the same pair seen from neighbour j, a centre too
+                  ++inb;
+                  const int csj = scs[m & 255], esi = ces[c];
+                  if (doR && esi >= 0 && csj >= 0) {
+                    if (cat < 0) cat = category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+                    const uint32_t idx = ((uint32_t)csj * a.nE + esi) * H + cat;
+                    if (a.rdf_in_smem) atomicAdd(&srdf[idx], 1u);
+                    else atomicAdd(&a.rdf_core[idx], 1ull);
+                  }
+                }
+              }
+              if (KNN && doK) {
+                // sorted lists of the K smallest d^2 per (set, centre), one
+                // insertion at a time while some lane beats its list's k-th
+                const int ps = inball ? (int)sidx[cs * 256 + (m & 255)] : -1;
+                uint32_t mask = __ballot_sync(FULL, ps >= 0 && d2 < L[((ps < 0 ? 0 : ps) * CB + c) * K + K - 1]);
+                while (mask) {
+                  const int srcl = __ffs(mask) - 1;
+                  const float x = __shfl_sync(FULL, d2, srcl);
+                  const int pp = __shfl_sync(FULL, ps, srcl);
+                  float* lp = L + (pp * CB + c) * K;
+                  const float v = lane < K ? lp[lane] : kInf();
+                  const int at = __popc(__ballot_sync(FULL, lane < K && v <= x));
+                  const float up = __shfl_up_sync(FULL, v, 1);
+                  __syncwarp();
+                  if (lane < K && lane >= at) lp[lane] = (lane == at) ? x : up;
+                  __syncwarp();
+                  mask &= ~(1u << srcl);
+                  mask &= __ballot_sync(FULL, ps >= 0 && d2 < L[((ps < 0 ? 0 : ps) * CB + c) * K + K - 1]);
+                }
+              }
+            }
+          }
+        }
+        // ---- the batch's kNN bins
+        if (KNN && doK) {
+          __syncwarp();
+          for (int c = 0; c < mc; ++c) {
+            const int cs = cct[c];
+            const int ntg = a.nsets[cs] * a.nkI;
+            for (int t = lane; t < ntg; t += 32) {
+              const int pp = t / a.nkI, kk = t - pp * a.nkI;
+              const float v = L[(pp * CB + c) * K + a.kvals[kk] - 1];
+              const int cat = (v == kInf()) ? a.cat_miss
+                                            : category_lut(v, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+              const int Sg = a.set_list[cs * 32 + pp];
+              atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
+            }
+          }
+          __syncwarp();
+        }
+        pairs_lane += inb;
+        if (lane == 0) centres += (unsigned long long)mc;
+        if (a.rdf_in_smem && doR) {
+          uint32_t tot = inb;
+          for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+          unsigned long long old = 0;
+          if (lane == 0) old = atomicAdd(since_flush, (unsigned long long)tot);
+          old = __shfl_sync(FULL, old, 0);
+          if (old / FLUSH != (old + tot) / FLUSH) {
+            for (int i = lane; i < a.nC * a.nE * H; i += 32) {
+              const uint32_t v = atomicExch(&srdf[i], 0u);
+              if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+  }
+  for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
+  if (lane == 0) {
+    atomicAdd(&a.counters[0], pairs_lane);
+    atomicAdd(&a.counters[1], centres);
+  }
+  __syncthreads();
+  if (a.rdf_in_smem && doR) {
+    for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) {
+      const uint32_t v = srdf[i];
       if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
     }
   }
@@ -973,7 +1278,7 @@ __global__ void __launch_bounds__(1024, 1) k_apply(ApplyArgs a) {
     const uint32_t tile = item / a.ngroups, grp = item - tile * a.ngroups;
     const int rb = (int)grp * G;
     const W* lab = (const W*)(a.labels + (uint64_t)grp * a.n * G);
-    const W* okw = (const W*)(a.centre_ok + (uint64_t)grp * a.ncentres * G);
+    const W* okw = (const W*)(a.centre_ok + ((uint64_t)grp * a.nc_total + a.cbase) * G);
     const uint32_t c0 = tile * a.tile, c1 = min(c0 + a.tile, a.ncentres);
     // one kNN count: bin (c, set q, order kk, category) of realisation rb + r
     auto knn_add = [&](int c, int q, int kk, int cat, int r) {
@@ -1018,8 +1323,8 @@ __global__ void __launch_bounds__(1024, 1) k_apply(ApplyArgs a) {
         int cat = 0;
         W nw = 0;
         if (valid) {
-          cat = a.pair_cat[e];
-          nw = lab[a.pair_slot[e]];
+          cat = a.pair_cat[e - a.pair_base];
+          nw = lab[a.pair_slot[e - a.pair_base]];
         }
 #pragma unroll
         for (int r = 0; r < G; ++r) {
@@ -1200,8 +1505,8 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
         const int ne = (int)min(32ull, o1 - e0);
         uint32_t my_slot = 0, my_cat = 0;
         if (lane < ne) {
-          my_slot = a.pair_slot[e0 + lane];
-          my_cat = a.pair_cat[e0 + lane];
+          my_slot = a.pair_slot[e0 + lane - a.pair_base];
+          my_cat = a.pair_cat[e0 + lane - a.pair_base];
         }
         for (int j0 = 0; j0 < ne; j0 += 8) {
           uint32_t t8[8];
@@ -1263,22 +1568,27 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
 // knn_core of realisation grp * 32 + r, set set_list[c][q], order kk.
 __global__ void __launch_bounds__(1024, 1) k_knn_bin(KnnArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  uint32_t* hist = (uint32_t*)smem;                  // [nC][H][32]
+  uint32_t* hist = (uint32_t*)smem;                  // [cblk][H][32]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int NT = a.nsmax * a.nkI;
-  const uint32_t nh = (uint32_t)a.nC * a.H * 32;
+  // centre types are histogrammed a block of cblk types at a time when all
+  // nC do not fit shared memory (records are then read once per block)
+  const int cblk = a.cblk, ncb = (a.nC + cblk - 1) / cblk;
+  const uint32_t nh = (uint32_t)cblk * a.H * 32;
   __shared__ uint32_t s_item;
   for (uint32_t i = threadIdx.x; i < nh; i += blockDim.x) hist[i] = 0;
   const uint32_t nranges = (a.cn + a.tile - 1) / a.tile;
-  const uint32_t nitems = nranges * (uint32_t)NT;
+  const uint32_t nitems = nranges * (uint32_t)NT * (uint32_t)ncb;
   for (;;) {
     __syncthreads();
     if (threadIdx.x == 0) s_item = atomicAdd(a.work, 1u);
     __syncthreads();
     const uint32_t item = s_item;
     if (item >= nitems) break;
-    const uint32_t range = item / NT;
-    const int t = (int)(item - range * NT);
+    const uint32_t range = item / (NT * ncb);
+    const uint32_t rest = item - range * NT * ncb;
+    const int t = (int)(rest / ncb);
+    const int c_lo = (int)(rest - (uint32_t)t * ncb) * cblk;
     const uint32_t l0 = range * a.tile, l1 = min(l0 + a.tile, a.cn);
     // 8 centres per step: their loads are in flight together
     for (uint32_t lb = l0 + warp * 8; lb < l1; lb += nwarps * 8) {
@@ -1294,8 +1604,11 @@ __global__ void __launch_bounds__(1024, 1) k_knn_bin(KnnArgs a) {
         }
       }
 #pragma unroll
-      for (int u = 0; u < 8; ++u)
-        if (c8[u] != 0xff && v8[u] != 0xffff) atomicAdd(&hist[(c8[u] * a.H + v8[u]) * 32 + lane], 1u);
+      for (int u = 0; u < 8; ++u) {
+        const int cr = (int)c8[u] - c_lo;
+        if (c8[u] != 0xff && v8[u] != 0xffff && cr >= 0 && cr < cblk)
+          atomicAdd(&hist[((uint32_t)cr * a.H + v8[u]) * 32 + lane], 1u);
+      }
     }
     __syncthreads();
     const int q = t / a.nkI, kk = t - q * a.nkI;
@@ -1305,8 +1618,9 @@ __global__ void __launch_bounds__(1024, 1) k_knn_bin(KnnArgs a) {
         hist[i] = 0;
         const int rr = a.grp * 32 + (int)(i & 31);
         const uint32_t cb = i >> 5;
-        const int c = (int)(cb / a.H), cat = (int)(cb - (uint32_t)c * a.H);
-        if (rr < a.nreal && q < a.nsets[c]) {
+        const int cr = (int)(cb / a.H), cat = (int)(cb - (uint32_t)cr * a.H);
+        const int c = c_lo + cr;
+        if (rr < a.nreal && c < a.nC && q < a.nsets[c]) {
           const int Sg = a.set_list[c * 32 + q];
           atomicAdd(&a.knn_core[((((uint64_t)rr * a.nC + c) * a.nS + Sg) * a.nkI + kk) * a.H + cat],
                     (unsigned long long)v);
@@ -1616,7 +1930,7 @@ static int launch_scan_t(const ScanArgs& a, int sm_count, size_t smem, cudaStrea
 
 int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s) {
   const int nwarps = 8;
-  size_t smem = 16 + ROW_TABLE_ENTRIES * 2 + (size_t)((a.H + 3) & ~3) * 4 + 512;
+  size_t smem = 16 + ROW_TABLE_ENTRIES * 2 + (size_t)((a.H + 3) & ~3) * 4 + (size_t)((a.lut_n + 7) & ~7) * 2 + 512;
   if (kr > 0) smem += (size_t)a.nC * 256 * 4;
   if (kr > 0 && a.disjoint) smem += (size_t)nwarps * a.emax * (kr * 32 + 1) * 4;
   if (a.rdf_in_smem) smem += (size_t)a.nC * a.nE * a.H * 4;
@@ -1639,6 +1953,33 @@ int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_
     if (emax <= 8) return launch_scan_t<4, 8>(a, sm_count, smem, s);
   }
   return -2;
+}
+
+size_t brick_smem(const ScanArgs& a, bool knn) {
+  constexpr int NW = 8;
+  size_t b = 16 + NW * 32 * 16 + NW * 32 * 4 + (size_t)((a.H + 3) & ~3) * 4 + (size_t)((a.lut_n + 7) & ~7) * 2;
+  if (a.rdf_in_smem) b += (size_t)a.nC * a.nE * a.H * 4;
+  if (knn) b += (size_t)NW * a.emax * a.bcap * a.kmax * 4;
+  b += ROW_TABLE_ENTRIES * 2 + 512 + 2 * NW * 32;
+  if (knn) b += (size_t)a.nC * 256;
+  return b;
+}
+
+int launch_brick(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cudaStream_t s) {
+  const bool knn = kr > 0;
+  if (a.mode != 0 || (a.flags & PP_CNTNB) || kr > 1 || (knn && !a.disjoint) || a.bx < 1 || a.bcap < 1 || a.bcap > 32)
+    return -3;
+  const size_t smem = brick_smem(a, knn);
+  if (smem_used) *smem_used = smem;
+  if (smem > 200 * 1024) return -3;
+  auto kern = knn ? k_brick<true> : k_brick<false>;
+  if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return -1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem) != cudaSuccess || per_sm < 1) return -1;
+  counted();
+  kern<<<sm_count * per_sm, 256, smem, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 template <int G, bool KS>
@@ -1715,10 +2056,13 @@ static int knn_walk_warps(const KnnArgs& k) {
   return 0;
 }
 
-int knn32_check(const KnnArgs& k) {
+int knn32_check(KnnArgs& k) {
   if (k.nsmax > 32 || k.kmax > 254 || k.nC > 254) return -2;
   if (!knn_walk_warps(k)) return -2;
-  if ((size_t)k.nC * k.H * 32 * 4 > 200 * 1024) return -2;
+  // centre types per bin histogram block
+  const size_t per_type = (size_t)k.H * 32 * 4;
+  if (per_type > 200 * 1024) return -2;
+  k.cblk = (int)std::min<size_t>((size_t)k.nC, (200 * 1024) / per_type);
   return 0;
 }
 
@@ -1738,7 +2082,8 @@ int launch_knn_walk(const KnnArgs& k, int sm_count, cudaStream_t s) {
 }
 
 int launch_knn_bin(const KnnArgs& k, int sm_count, cudaStream_t s) {
-  const size_t smem = (size_t)k.nC * k.H * 32 * 4;
+  if (k.cblk < 1) return -2;
+  const size_t smem = (size_t)k.cblk * k.H * 32 * 4;
   if (smem > 200 * 1024) return -2;
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(k_knn_bin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

@@ -15,6 +15,11 @@ pytestmark = pytest.mark.gpu
 ALL = N.PP_RDF | N.PP_1NN | N.PP_RIPK | N.PP_MKNN
 
 
+def BRICK(cells, batch):
+    """Tile code of the brick scan: cells per brick, centres per warp batch."""
+    return (cells << 16) | batch
+
+
 def _run_both(ctx, oracle, spec, rmin, rincr, rmax, flags, trg, env, ks, surf=None, perm_labels=None, carve=2.0):
     cid = ctx.upload(spec.xyz, spec.labels)
     ctx.hull(cid, spec.hull, carve)
@@ -218,12 +223,13 @@ def test_results_independent_of_tuning(ctx, oracle):
     ctx.tasks(trg, env)
     ctx.hist(0.0, 0.01, 1.4)
     outs = []
-    for ratio, tile in ((2.0, 1), (3.5, 64), (5.0, 7), (1.0, 1000)):
+    for ratio, tile in ((2.0, 1), (3.5, 64), (5.0, 7), (1.0, 1000), (4.0, BRICK(8, 16)), (2.0, BRICK(1, 1)),
+                        (5.0, BRICK(16, 32)), (3.0, BRICK(3, 5))):
         ctx.tuning(cid, ratio, tile)
         ctx.run(cid, ALL, [6, 2, 1])
         outs.append(ctx.fetch())
     r, t = ctx.autotune(cid, ALL, [6, 2, 1], sample=2000)
-    assert 2.0 <= r <= 5.0 and t in (32, 128, 512)
+    assert 2.0 <= r <= 5.0 and (t in (32, 128, 512) or (t >> 16) in (4, 8, 16))
     ctx.run(cid, ALL, [6, 2, 1])
     outs.append(ctx.fetch())
     for o in outs[1:]:
@@ -250,3 +256,73 @@ def test_symmetric_rdf_pass(ctx, oracle):
                                     perm_labels=None if p is None else (p, labels))
         assert st["pairs"] == ref["pairs"]
         assert np.array_equal(gpu, ref["bins"])
+
+
+@pytest.mark.parametrize("tile", [BRICK(8, 16), BRICK(1, 1), BRICK(16, 32), BRICK(5, 7)])
+@pytest.mark.parametrize("ratio", [2.0, 3.0, 5.0])
+def test_brick_scan(ctx, oracle, tile, ratio):
+    """The brick scan against the oracle: a symmetric RDF/RIPK pass under a
+    label permutation with a non-zero lower radius, and a kNN pass over all
+    species pairs (disjoint environment sets)."""
+    spec = synth.cone_specimen(n=40000, r_apex=8.0, half_angle_deg=10.0, length=16.0, n_clusters=20,
+                               members=40, nspecies=3, seed=53, nseg=64, stack=4.0)
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tuning(cid, ratio, tile)
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    rng = np.random.default_rng(int(ratio * 10) + (tile >> 16))
+    perm = rng.permutation(spec.xyz.shape[0]).astype(np.uint32)
+    lab = spec.labels[perm]
+    trg, env = [[1], [2, 3], [3]], [[1, 2], [1, 2, 3], [1]]
+    ctx.tasks(trg, env)
+    ctx.hist(0.1, 0.02, 1.3)
+    ctx.run(cid, N.PP_RDF | N.PP_RIPK, [], label_perm=perm)
+    gpu, st = ctx.fetch(), ctx.stats()
+    ref = oracle.spatstat(spec.xyz, lab, surf, 0.1, 0.02, 1.3, N.PP_RDF | N.PP_RIPK, trg, env, [])
+    assert st["pairs"] == ref["pairs"] and np.array_equal(gpu, ref["bins"])
+    types = [1, 2, 3]
+    trg = [[a] for a in types for b in types]
+    env = [[b] for a in types for b in types]
+    ctx.tasks(trg, env)
+    ctx.hist(0.0, 0.005, 1.2)
+    ks = [12, 3, 1]
+    ctx.run(cid, N.PP_1NN | N.PP_MKNN, ks)
+    gpu, st = ctx.fetch(), ctx.stats()
+    ref = oracle.spatstat(spec.xyz, spec.labels, surf, 0.0, 0.005, 1.2, N.PP_1NN | N.PP_MKNN, trg, env, ks)
+    assert st["pairs"] == ref["pairs"] and np.array_equal(gpu, ref["bins"])
+    ctx.free(cid)
+
+
+@pytest.mark.parametrize("rincr", [0.02, 0.001])
+def test_batched_chunked_geometry(ctx, oracle, rincr):
+    """Pair lists held a chunk of centres at a time (batched_pair_cap) give the
+    same bins as lists held whole, for the fused and the 32-realisation kNN
+    kernels."""
+    spec = synth.cone_specimen(n=30000, r_apex=8.0, half_angle_deg=10.0, length=14.0, n_clusters=15,
+                               members=40, nspecies=3, seed=61, nseg=64, stack=4.0)
+    types = [1, 2, 3]
+    trg = [[a] for a in types for b in types]
+    env = [[b] for a in types for b in types]
+    ks = [5, 2, 1]
+    flags = N.PP_RDF | N.PP_MKNN
+    sets = np.stack([N.shuffle_labels(spec.labels, 300 + s) for s in range(4)])
+    rois = np.array([[0.0, 0.0, 7.0, 5.0]], dtype=np.float32)
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks(trg, env)
+    ctx.hist(0.0, rincr, 1.2)
+    ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets, rois=rois)
+    whole = [ctx.fetch_batched(r) for r in range(6)]
+    pairs = sum(ctx.batched_stats(r)["pairs"] for r in range(6))
+    try:
+        ctx.set_option("batched_pair_cap", 20000)
+        ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets, rois=rois)
+        for r in range(6):
+            assert np.array_equal(ctx.fetch_batched(r), whole[r]), r
+        assert sum(ctx.batched_stats(r)["pairs"] for r in range(6)) == pairs
+    finally:
+        ctx.set_option("batched_pair_cap", 0)
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    ref = oracle.spatstat(spec.xyz, sets[2], surf, 0.0, rincr, 1.2, flags, trg, env, ks)
+    assert np.array_equal(whole[3], ref["bins"])
+    ctx.free(cid)
