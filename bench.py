@@ -64,6 +64,22 @@ def workload(name):
                            f"L {length:.1f} nm), 6 species, 36 pair tasks; pass 1 RDF R=2.0/0.01, pass 2 kNN "
                            "k=1..10 R=2.0/0.005, hull-distance exclusion",
                "ions": n, "tasks": 36, "R_nm": 2.0}
+    elif name == "tip150m":
+        # configuration 5: apex r 50 nm, 12 deg, L 400 nm, 150M ions, 8 species,
+        # 5000 clusters; RDF and kNN k = 1..20 for all 64 pairs in one pass
+        # (one bin geometry, 2.5 nm / 0.01 nm)
+        n = 150_000_000
+        spec = synth.cone_specimen(n=n, r_apex=50.0, half_angle_deg=12.0, length=400.0, n_clusters=5000,
+                                   sigma=1.5, members=50, cluster_p=(0.7, 0.3),
+                                   iid=(0.02, 0.01, 0.005, 0.005, 0.002), nspecies=8, seed=20261208)
+        types = list(range(1, 9))
+        trg = [[a] for a in types for b in types]
+        env = [[b] for a in types for b in types]
+        runs = [dict(flags=1 | 8, hist=(0.0, 0.01, 2.5), k=list(range(20, 0, -1)))]
+        cfg = {"workload": "tip150m: 150M-ion clustered truncated cone (r_apex 50 nm, 12 deg, L 400 nm), 8 species, "
+                           "5000 clusters, 64 pair tasks; one pass RDF + kNN k=1..20, R=2.5/0.01, hull-distance "
+                           "exclusion",
+               "ions": n, "tasks": 64, "R_nm": 2.5}
     elif name == "cyl1m":
         spec = synth.cylinder_specimen(n=1_000_000, radius=10.0, height=63.66, fractions=(0.90, 0.08, 0.02),
                                        seed=20261204)
@@ -365,8 +381,13 @@ def run_gpu(args):
                                           f"{frac * 100:.3f}% of ions eligible as centres "
                                           f"({p} pairs, {s:.1f} s statistics phase)"}
     if not args.no_batched:
-        ctx.free(cid)
-        line["batched"] = batched_leg(ctx, torch, stream)
+        if args.workload == "tip150m":
+            line["batched"] = batched_leg_large(ctx, cid, spec, trg, env, runs[0], torch, stream,
+                                                per_pass_pairs[0], per_pass_ms[0])
+            ctx.free(cid)
+        else:
+            ctx.free(cid)
+            line["batched"] = batched_leg(ctx, torch, stream)
     if not args.no_served:
         line["served"] = served_leg(ctx)
     ctx.close()
@@ -451,6 +472,37 @@ def batched_leg(ctx, torch, stream):
             "tuning": {"cell_edge_nm": round(1.5 / ratio, 4), "tile": tile},
             "includes": "pair-list geometry, label gathers and layouts, masks, the realisation passes (one CUDA "
                         "graph: persistent RDF/count launch + 32-realisation kNN walk/bin launches), result fetch"}
+
+
+def batched_leg_large(ctx, cid, spec, trg, env, run, torch, stream, plain_pairs, plain_ms):
+    """Configuration 5's batched form: the measured labels plus 32 label
+    shuffles in one batched call on the resident 150M-ion cloud.  Its pair
+    lists (about 10^11 pairs) exceed HBM, so they are built and applied a chunk
+    of centres at a time.  Compared with the plain pass on the same cloud."""
+    from paraprobe_gb300 import native as N
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        sets = list(ex.map(lambda r: N.shuffle_labels(spec.labels, 5000 + r), range(32)))
+    sets_dev = torch.from_numpy(np.stack(sets)).to("cuda")
+    del sets
+    ctx.tasks(trg, env)
+    ctx.hist(*run["hist"])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.run_batched(cid, run["flags"], run["k"], include_original=True, label_sets=sets_dev.data_ptr(), nsets=32,
+                    stream=stream.cuda_stream)
+    nreal = ctx.batched_count()
+    pairs = sum(ctx.batched_stats(r)["pairs"] for r in range(nreal))
+    el = time.perf_counter() - t0
+    apply_ms = ctx.last_kernel_ms()
+    plain = plain_pairs / (statistics.mean(plain_ms) * 1e-3)
+    return {"workload": "configuration 5 batched: 1 measured + 32 shuffled label sets, RDF + kNN k=1..20, "
+                        "R=2.5/0.01, 64 pair tasks, pair lists built and applied in centre chunks",
+            "realisations": nreal, "pairs": int(pairs), "value": pairs / el, "unit": UNIT, "seconds": round(el, 3),
+            "apply_graph_ms": round(apply_ms, 3), "cuda_graph": ctx.batched_graph(),
+            "plain_single_query": plain, "ratio_vs_plain": (pairs / el) / plain,
+            "includes": "pair-list geometry (count pass, per-chunk emit), label gathers and layouts, all "
+                        "realisation passes, result fetch"}
 
 
 # ------------------------------------------------------------- served queries
@@ -580,7 +632,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="tip20m", choices=["tip20m", "tip10m", "cyl1m"])
+    ap.add_argument("--workload", default="tip20m", choices=["tip20m", "tip10m", "cyl1m", "tip150m"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched realisation leg")

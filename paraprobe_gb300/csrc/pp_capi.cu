@@ -159,6 +159,7 @@ struct pp_ctx {
   DevBuf pair_count, pair_off, pair_slot, pair_cat, geo_centres, centre_ok, real_labels, rois_dev;
   DevBuf labels_il, ok_il;  // group-major interleaved copies of real_labels / centre_ok
   DevBuf knn_labels, knn_ok, knn_rec, knn_recc;  // 32-realisation kNN: layouts and records
+  DevBuf knn_rest_labels, knn_rest_ok;           // the realisations after the last full 32
   DevBuf maxlist;           // longest pair list (one uint32)
   uint32_t geo_maxlist = 0;
   uint64_t geo_key_version = ~0ull;
@@ -1585,6 +1586,7 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     b.nsmax = std::max(P.emax, 1);
     b.disjoint = P.disjoint;
     b.setidx = D.setidx;
+    b.count = 1;
     // kNN of 32 realisations per warp (walk + bin) where its records and bins
     // fit; the fused kernel then does RDF and the per-realisation counters
     pp::KnnArgs kq;
@@ -1644,12 +1646,43 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     int ng32 = 0;
     uint32_t chunk = 0;
     const uint64_t NT = (uint64_t)kq.nsmax * kq.nkI;
+    // a few realisations beyond the last full group of 32 take the rank walk
+    // of the fused kernel in a launch of their own (a 32-lane group of them
+    // would leave most lanes idle)
+    pp::ApplyArgs bk;
+    std::memset(&bk, 0, sizeof bk);
+    bool knn_rest = false;
     if (knn32) {
+      const int rest = nreal % 32;
       ng32 = (nreal + 31) / 32;
-      CK(ctx->knn_labels.ensure(std::max<uint64_t>(n, 1) * 32 * ng32));
-      CK(ctx->knn_ok.ensure(std::max<uint64_t>(nc, 1) * 32 * ng32));
-      pp::launch_interleave(RL, nreal, n, 32, ctx->knn_labels.as<uint8_t>(), s);
-      pp::launch_interleave(OK, nreal, nc, 32, ctx->knn_ok.as<uint8_t>(), s);
+      if (rest > 0 && rest <= 8) {
+        bk = b;
+        bk.flags = PP_MKNN;
+        bk.count = 0;
+        bk.rbase = nreal - rest;
+        bk.nreal = rest;
+        if (pp::apply_configure(bk) == 0) {
+          knn_rest = true;
+          ng32 = nreal / 32;
+          bk.ngroups = (rest + bk.group - 1) / bk.group;
+          bk.tile = b.tile;
+          const uint64_t nrk = (uint64_t)bk.ngroups * bk.group;
+          CK(ctx->knn_rest_labels.ensure(std::max<uint64_t>(n, 1) * nrk));
+          CK(ctx->knn_rest_ok.ensure(std::max<uint64_t>(nc, 1) * nrk));
+          pp::launch_interleave(RL + (uint64_t)bk.rbase * n, rest, n, bk.group, ctx->knn_rest_labels.as<uint8_t>(), s);
+          pp::launch_interleave(OK + (uint64_t)bk.rbase * nc, rest, nc, bk.group, ctx->knn_rest_ok.as<uint8_t>(), s);
+          bk.labels = ctx->knn_rest_labels.as<uint8_t>();
+          bk.centre_ok = ctx->knn_rest_ok.as<uint8_t>();
+        }
+      }
+      // the realisations of the 32-lane groups (all, or all but the rest)
+      const uint64_t r32 = std::min<uint64_t>((uint64_t)ng32 * 32, (uint64_t)nreal);
+      CK(ctx->knn_labels.ensure(std::max<uint64_t>(n, 1) * 32 * std::max(ng32, 1)));
+      CK(ctx->knn_ok.ensure(std::max<uint64_t>(nc, 1) * 32 * std::max(ng32, 1)));
+      if (r32) {
+        pp::launch_interleave(RL, r32, n, 32, ctx->knn_labels.as<uint8_t>(), s);
+        pp::launch_interleave(OK, r32, nc, 32, ctx->knn_ok.as<uint8_t>(), s);
+      }
       kq.labels = ctx->knn_labels.as<uint8_t>();
       kq.centre_ok = ctx->knn_ok.as<uint8_t>();
       // records of one launch: at most 3 GiB
@@ -1676,6 +1709,17 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
         bc.pair_base = ch.p0;
         if (cudaMemsetAsync(ctx->work.p, 0, 8, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
         if (pp::launch_apply(bc, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "apply launch failed");
+        if (knn_rest) {
+          pp::ApplyArgs kc = bk;
+          kc.centres = bk.centres + ch.c0;
+          kc.ncentres = ch.c1 - ch.c0;
+          kc.pair_off = bk.pair_off + ch.c0;
+          kc.cbase = ch.c0;
+          kc.pair_base = ch.p0;
+          kc.work = ctx->work.as<uint32_t>() + 3;
+          if (cudaMemsetAsync(kc.work, 0, 4, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
+          if (pp::launch_apply(kc, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "kNN rest launch failed");
+        }
         pp::KnnArgs k = kq;
         k.pair_base = ch.p0;
         for (int g = 0; g < ng32; ++g) {
@@ -1698,6 +1742,7 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
     std::string sig((const char*)&b, sizeof b);
     sig.append((const char*)&kq, sizeof kq);
     sig.append((const char*)&ea_sig, sizeof ea_sig);
+    sig.append((const char*)&bk, sizeof bk);
     sig.append((const char*)chunks.data(), chunks.size() * sizeof(Chunk));
     const uint64_t extra[5] = {(uint64_t)ng32, chunk, nc, (uint64_t)ctx->sm_count, chunked ? 1u : 0u};
     sig.append((const char*)extra, sizeof extra);

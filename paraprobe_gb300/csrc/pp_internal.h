@@ -103,6 +103,8 @@ struct ApplyArgs {
   const uint8_t* labels;         // [ngroups][n][group] type per sorted slot
   const uint8_t* centre_ok;      // [ngroups][nc_total][group] 1 if a centre in that realisation
   uint32_t cbase, nc_total;      // this launch's centres are entries [cbase, cbase + ncentres) of nc_total
+  int rbase;                     // realisation r of this launch is rbase + r of the result
+  int count;                     // 1: add pair and centre counts (one launch per realisation does)
   unsigned long long pair_base;  // pair_slot/pair_cat hold list positions from pair_base on
   uint64_t n;
   int nreal;

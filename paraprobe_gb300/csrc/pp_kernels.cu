@@ -1288,7 +1288,7 @@ __global__ void __launch_bounds__(1024, 1) k_apply(ApplyArgs a) {
         const uint32_t i16 = bin * G + r;
         atomicAdd(&sKnn[i16 >> 1], 1u << ((i16 & 1u) * 16));
       } else {
-        atomicAdd(&a.knn_core[(uint64_t)(rb + r) * knn_real + bin], 1ull);
+        atomicAdd(&a.knn_core[(uint64_t)(a.rbase + rb + r) * knn_real + bin], 1ull);
       }
     };
     for (uint32_t ci = c0 + warp; ci < c1; ci += nwarps) {
@@ -1407,13 +1407,16 @@ __global__ void __launch_bounds__(1024, 1) k_apply(ApplyArgs a) {
     __syncthreads();
     for (int i = threadIdx.x; i < 2 * G; i += blockDim.x) {
       const unsigned long long v = sCnt[i];
-      if (v) { atomicAdd(&a.counters[2 * (uint64_t)rb + i], v); sCnt[i] = 0; }
+      if (v) {
+        if (a.count) atomicAdd(&a.counters[2 * ((uint64_t)a.rbase + rb) + i], v);
+        sCnt[i] = 0;
+      }
     }
     for (int i = threadIdx.x; i < L.nrdf * G; i += blockDim.x) {
       const uint32_t v = sRdf[i];
       if (v) {
         const int r = i % G, bin = i / G;
-        atomicAdd(&a.rdf_core[(uint64_t)(rb + r) * L.nrdf + bin], (unsigned long long)v);
+        atomicAdd(&a.rdf_core[(uint64_t)(a.rbase + rb + r) * L.nrdf + bin], (unsigned long long)v);
         sRdf[i] = 0;
       }
     }
@@ -1428,7 +1431,7 @@ __global__ void __launch_bounds__(1024, 1) k_apply(ApplyArgs a) {
               const uint32_t i16 = 2 * w + h;
               const int r = i16 % G;
               const uint32_t bin = i16 / G;
-              atomicAdd(&a.knn_core[(uint64_t)(rb + r) * knn_real + bin], (unsigned long long)c16);
+              atomicAdd(&a.knn_core[(uint64_t)(a.rbase + rb + r) * knn_real + bin], (unsigned long long)c16);
             }
           }
           sKnn[w] = 0;

@@ -326,3 +326,30 @@ def test_batched_chunked_geometry(ctx, oracle, rincr):
     ref = oracle.spatstat(spec.xyz, sets[2], surf, 0.0, rincr, 1.2, flags, trg, env, ks)
     assert np.array_equal(whole[3], ref["bins"])
     ctx.free(cid)
+
+
+@pytest.mark.parametrize("nsets", [33, 40])
+def test_batched_32_lane_groups_and_rest(ctx, oracle, nsets):
+    """More than 32 realisations: full 32-lane kNN groups, plus either a short
+    rest taken by the rank walk (1 + 33 = 34: rest 2) or a partly filled group
+    (1 + 40 = 41: rest 9); realisations on both sides of the split checked."""
+    spec = synth.cone_specimen(n=20000, r_apex=8.0, half_angle_deg=10.0, length=10.0, n_clusters=10,
+                               members=40, nspecies=3, seed=71, nseg=48, stack=4.0)
+    types = [1, 2, 3]
+    trg = [[a] for a in types for b in types]
+    env = [[b] for a in types for b in types]
+    ks = [4, 1]
+    flags = N.PP_RDF | N.PP_MKNN
+    sets = np.stack([N.shuffle_labels(spec.labels, 1200 + s) for s in range(nsets)])
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks(trg, env)
+    ctx.hist(0.0, 0.02, 1.1)
+    ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets)
+    assert ctx.batched_count() == 1 + nsets
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    for r in (0, 5, 31, 32, 33, nsets):
+        lab = spec.labels if r == 0 else sets[r - 1]
+        ref = oracle.spatstat(spec.xyz, lab, surf, 0.0, 0.02, 1.1, flags, trg, env, ks)
+        assert np.array_equal(ctx.fetch_batched(r), ref["bins"]), r
+    ctx.free(cid)
