@@ -106,6 +106,16 @@ int pp_surfdist_upload(pp_ctx* ctx, int cloud, const float* d2);
 /* The ion2surf values pp_run used last for this cloud (n floats, input order). */
 int pp_surfdist_fetch(pp_ctx* ctx, int cloud, float* d2_out, uint64_t n);
 
+/* NumberOfIonsInside and VolumeInside, the two values heading the RDF reports:
+ * the occupancy grid of vxlizer::rectangular_binning
+ * (src/PARAPROBE_SolverHdl.cpp:5342-5386) with voxel edge 0.5 (bin_width_min +
+ * bin_width_max) (Settings AdvIonPruneBinWidthMin/Max), its Hoshen-Kopelman
+ * vacuum, surface and inside voxels (:5059-5270,
+ * src/PARAPROBE_HoshenKopelman.cpp).  voxels (nullable) receives 6 counts:
+ * vacuum, surface and inside voxels, then nx, ny, nz. */
+int pp_cloud_inside(pp_ctx* ctx, int cloud, float bin_width_min, float bin_width_max, uint64_t* nions_inside,
+                    float* volume_inside, uint64_t* voxels);
+
 /* ion2surf without any device allocation, for callers that cannot call
  * cudaMalloc (a host whose own pool owns the device memory, a loop that may
  * not take the synchronisation cudaFree implies).  No counterpart in the

@@ -61,6 +61,9 @@ def lib():
         L.ppo_neighbors.restype = C.c_int
         L.ppo_category.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float]
         L.ppo_category.restype = C.c_int
+        L.ppo_voxelize.argtypes = [f32p, C.c_uint64, C.c_float, C.c_float, C.POINTER(C.c_uint64),
+                                   C.POINTER(C.c_float), u64p]
+        L.ppo_voxelize.restype = C.c_int
         _lib = L
     return _lib
 
@@ -138,3 +141,16 @@ def neighbors(xyz, centre, R):
 
 def category(rmin, rincr, rmax, x):
     return lib().ppo_category(np.float32(rmin), np.float32(rincr), np.float32(rmax), np.float32(x))
+
+
+def voxelize(xyz, w_min=1.0, w_max=1.0):
+    """NumberOfIonsInside, VolumeInside and voxel counts of the occupancy grid."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float32)
+    nin, vol = C.c_uint64(), C.c_float()
+    bins = np.zeros(6, dtype=np.uint64)
+    rc = lib().ppo_voxelize(xyz.reshape(-1), xyz.shape[0], np.float32(w_min), np.float32(w_max), C.byref(nin),
+                            C.byref(vol), bins)
+    if rc:
+        raise RuntimeError(f"ppo_voxelize failed ({rc})")
+    return dict(nions_inside=nin.value, volume_inside=np.float32(vol.value), vacuum=int(bins[0]),
+                surface=int(bins[1]), inside=int(bins[2]), nx=int(bins[3]), ny=int(bins[4]), nz=int(bins[5]))

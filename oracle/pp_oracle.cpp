@@ -18,6 +18,10 @@
 //   * the ion-to-hull squared distance used to exclude centres near the
 //     specimen surface (src/PARAPROBE_SolverHdl.cpp:312-479,
 //     src/PARAPROBE_Math.cpp:88-184, src/PARAPROBE_AABBTree.cpp:112-124)
+//   * the occupancy grid that gives the RDF header its NumberOfIonsInside and
+//     VolumeInside (src/PARAPROBE_SolverHdl.cpp:5059-5386, 1471-1508; the
+//     outer vacuum is the face-connected cluster of empty voxels holding the
+//     guard corner, which src/PARAPROBE_HoshenKopelman.cpp labels)
 //
 // The restatement is pinned against the reference's own units compiled from
 // the read-only reference tree (oracle/ref/), through golden fixtures under
@@ -31,6 +35,7 @@
 //   CNTNB is returned separately as [ntasks][cntnb_len] counts.
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -555,6 +560,100 @@ int ppo_neighbors(const float* xyz, uint64_t n, uint64_t centre, float R,
 
 // The float category of one distance under histogram::add, exported so tests
 // can check the device's bin-edge table against the CPU rounding.
+// Occupancy grid of the whole cloud (vxlizer::rectangular_binning and the
+// steps it calls, src/PARAPROBE_SolverHdl.cpp:5059-5386, :1471-1508, :1778-1791).
+// bins[0..5] = vacuum, surface, inside voxels, nx, ny, nz.  Returns -1 when the
+// grid has 2^32 voxels or more (the reference stops there too).
+int ppo_voxelize(const float* xyz, uint64_t n, float w_min, float w_max, uint64_t* nions_inside,
+                 float* volume_inside, uint64_t* bins) {
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (uint64_t i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) {
+      const float v = xyz[3 * i + k];
+      if (v <= lo[k]) lo[k] = v;
+      if (v >= hi[k]) hi[k] = v;
+    }
+  const float w = (float)(0.5 * (double)(w_min + w_max));
+  uint64_t nv[3];
+  for (int k = 0; k < 3; ++k) {
+    lo[k] -= w;
+    hi[k] += w;
+    nv[k] = (uint64_t)std::ceil((hi[k] - lo[k]) / w) + 2;
+  }
+  const uint64_t nx = nv[0], ny = nv[1], nz = nv[2], nxy = nx * ny, nxyz = nxy * nz;
+  if (nx >= 0xffffffffull || ny >= 0xffffffffull || nz >= 0xffffffffull || nxyz >= 0xffffffffull) return -1;
+  std::vector<uint32_t> occ(nxyz, 0);
+  std::vector<uint64_t> bin(n);
+  for (uint64_t i = 0; i < n; ++i) {
+    uint64_t c[3];
+    for (int k = 0; k < 3; ++k) {
+      const float t = (xyz[3 * i + k] - lo[k]) / w;
+      const uint64_t sz = (uint64_t)t;
+      c[k] = (sz != nv[k] - 1) ? 1 + sz : nv[k] - 1;
+    }
+    bin[i] = c[0] + c[1] * nx + c[2] * nxy;
+    occ[bin[i]] += 1;
+  }
+  // outer vacuum: the cluster of the corner (0, 0, nz - 1) among the empty
+  // voxels, labelled in raster order with the reference's rules
+  // (src/PARAPROBE_HoshenKopelman.cpp:55-146): a voxel joins the clusters of
+  // its labelled -x, -y, -z neighbours, except that with all three labelled
+  // only -y and -z are merged; voxel 0 carries label 0 and so stays unlabelled
+  std::vector<uint32_t> uf(nxyz);
+  for (uint64_t b = 0; b < nxyz; ++b) uf[b] = (uint32_t)b;
+  auto root = [&](uint32_t a) {
+    while (uf[a] != a) { uf[a] = uf[uf[a]]; a = uf[a]; }
+    return a;
+  };
+  auto unite = [&](uint32_t a, uint32_t b) {
+    a = root(a); b = root(b);
+    if (a != b) uf[a] = b;
+  };
+  auto labelled = [&](uint64_t b) { return b != 0 && occ[b] == 0; };
+  for (uint64_t z = 0; z < nz; ++z)
+    for (uint64_t y = 0; y < ny; ++y)
+      for (uint64_t x = 0; x < nx; ++x) {
+        const uint64_t v = x + y * nx + z * nxy;
+        if (!labelled(v)) continue;
+        const bool L = x > 0 && labelled(v - 1), B = y > 0 && labelled(v - nx), F = z > 0 && labelled(v - nxy);
+        if (L && B && F) { unite(v - nx, v - nxy); unite(v, v - nx); continue; }
+        if (L) unite(v, v - 1);
+        if (B) unite(v, v - nx);
+        if (F) unite(v, v - nxy);
+      }
+  std::vector<char> vac(nxyz, 0);
+  const uint64_t corner = (nz - 1) * nxy;
+  if (labelled(corner)) {
+    const uint32_t rc = root((uint32_t)corner);
+    for (uint64_t b = 0; b < nxyz; ++b) vac[b] = labelled(b) && root((uint32_t)b) == rc;
+  }
+  // surface: non-vacuum Moore neighbours of vacuum voxels off the grid border
+  std::vector<char> srf(nxyz, 0);
+  for (uint64_t z = 1; z + 1 < nz; ++z)
+    for (uint64_t y = 1; y + 1 < ny; ++y)
+      for (uint64_t x = 1; x + 1 < nx; ++x) {
+        if (!vac[x + y * nx + z * nxy]) continue;
+        for (int dz = -1; dz <= 1; ++dz)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+              const uint64_t t = (x + dx) + (y + dy) * nx + (z + dz) * nxy;
+              if ((dx || dy || dz) && !vac[t]) srf[t] = 1;
+            }
+      }
+  uint64_t nv_b = 0, ns_b = 0, ni_b = 0, nin = 0;
+  for (uint64_t b = 0; b < nxyz; ++b) {
+    nv_b += vac[b];
+    ns_b += srf[b];
+    if (!vac[b] && !srf[b]) { ++ni_b; nin += occ[b]; }
+  }
+  float vol = (float)ni_b;
+  vol *= w * w * w;
+  if (nions_inside) *nions_inside = nin;
+  if (volume_inside) *volume_inside = vol;
+  if (bins) { bins[0] = nv_b; bins[1] = ns_b; bins[2] = ni_b; bins[3] = nx; bins[4] = ny; bins[5] = nz; }
+  return 0;
+}
+
 int ppo_category(float rmin, float rincr, float rmax, float x) {
   Hist h; h.init(rmin, rincr, rmax);
   double xx = x;

@@ -14,6 +14,7 @@
 //   ref_spatstat <simid> <settings.xml> <nthreads> <outdir>
 //                [--labels <file of uint8 per ion, original order>]
 //                [--inside <nions_inside> <volume_inside>]
+//                [--voxelize]
 //                [--dump-surf]
 // Writes into <outdir>:
 //   the reference CSV files (report_apriori_descrstat2/3 layout),
@@ -21,11 +22,15 @@
 //   raw_cntnb.u64   uint64 [ntasks][L] neighbour-count histogram, L in stats
 //   stats.txt       centres, discarded, pairs, nbins, ntasks, nk, L
 //   ion2surf.f32    (with --dump-surf) squared hull distance per original ion
+//   voxel.txt       (with --voxelize) the occupancy grid's NumberOfIonsInside and
+//                   VolumeInside, which then also head the RDF reports; the
+//                   Hoshen-Kopelman clustering is the reference's percAnalyzer
 // The process runs everything single-rank; nthreads selects the z-slab count
 // (one KD-tree per slab) exactly as OMP_NUM_THREADS does in the reference.
 
 #include "PARAPROBE_KDTree.h"
 #include "PARAPROBE_DiscreteHistogram.h"
+#include "PARAPROBE_HoshenKopelman.h"
 
 #include <omp.h>
 #include <sys/stat.h>
@@ -193,6 +198,86 @@ void report3(const string& outdir, const string& trg, const string& env, discrhi
 
 }  // namespace
 
+// Occupancy grid of the whole cloud, restating vxlizer::rectangular_binning
+// (src/PARAPROBE_SolverHdl.cpp:5342-5386) and the steps it calls: the tip box
+// (:1778-1791), define_vxlgrid (:5318-5340), threadmemory::binning with
+// rectangular_transfer (:1471-1508), binarization (:5272-5292),
+// identify_vacuum_bins (:5196-5270, the reference's own percAnalyzer),
+// identify_surface_adjacent_bins (:5132-5194), identify_inside_bins
+// (:5115-5130) and characterize_binning (:5059-5112).
+struct VoxelResult {
+  size_t nions_inside = 0, vacuum = 0, surface = 0, inside = 0, nx = 0, ny = 0, nz = 0;
+  apt_real volume_inside = 0.f;
+};
+
+static bool voxelize(const vector<pos>& raw, VoxelResult& out) {
+  aabb3d tip = aabb3d();
+  for (const pos& p : raw) {
+    if (p.x <= tip.xmi) tip.xmi = p.x;
+    if (p.x >= tip.xmx) tip.xmx = p.x;
+    if (p.y <= tip.ymi) tip.ymi = p.y;
+    if (p.y >= tip.ymx) tip.ymx = p.y;
+    if (p.z <= tip.zmi) tip.zmi = p.z;
+    if (p.z >= tip.zmx) tip.zmx = p.z;
+  }
+  tip.scale();
+  const apt_xyz binwidth = 0.5 * (Settings::AdvIonPruneBinWidthMin + Settings::AdvIonPruneBinWidthMax);
+  aabb3d ti = tip;
+  const apt_real guardwidth = static_cast<apt_real>(binwidth);
+  ti.blowup(guardwidth);
+  const size_t nx = static_cast<size_t>(ceil((ti.xmx - ti.xmi) / binwidth)) + 2;
+  const size_t ny = static_cast<size_t>(ceil((ti.ymx - ti.ymi) / binwidth)) + 2;
+  const size_t nz = static_cast<size_t>(ceil((ti.zmx - ti.zmi) / binwidth)) + 2;
+  const size_t nxy = nx * ny, nxyz = nxy * nz;
+  if (nx >= UINT32MX || ny >= UINT32MX || nz >= UINT32MX || nxyz >= UINT32MX) return false;
+  auto transfer = [](apt_xyz p, apt_xyz mi, apt_xyz w, size_t nvxl) {
+    const apt_xyz tmpd = (p - mi) / w;
+    const size_t tmpsz = static_cast<size_t>(tmpd);
+    return (tmpsz != nvxl - 1) ? 1 + tmpsz : nvxl - 1;
+  };
+  vector<size_t> ion2bin(raw.size());
+  for (size_t i = 0; i < raw.size(); ++i) {
+    const size_t x = transfer(raw[i].x, ti.xmi, binwidth, nx);
+    const size_t y = transfer(raw[i].y, ti.ymi, binwidth, ny);
+    const size_t z = transfer(raw[i].z, ti.zmi, binwidth, nz);
+    ion2bin[i] = x + y * nx + z * nxy;
+  }
+  vector<char> vac(nxyz, 0), srf(nxyz, 0), ins(nxyz, 0);
+  bool* IsVacuum = new bool[nxyz];
+  for (size_t b = 0; b < nxyz; ++b) IsVacuum[b] = false;
+  for (size_t b : ion2bin) IsVacuum[b] = true;  // binarization: true = holds ions
+  {
+    percAnalyzer hk;
+    if (!hk.initialize(IsVacuum, (unsigned int)nx, (unsigned int)ny, (unsigned int)nz) || !hk.hoshen_kopelman() ||
+        !hk.compactify() || !hk.determine_clustersize_distr()) { delete[] IsVacuum; return false; }
+    const unsigned int corner = 0 + 0 * (unsigned int)nx + ((unsigned int)nz - 1) * (unsigned int)nxy;
+    if (!hk.rebinarize(corner, (unsigned int)nxyz, IsVacuum)) { delete[] IsVacuum; return false; }
+  }
+  for (size_t b = 0; b < nxyz; ++b) vac[b] = IsVacuum[b] ? 1 : 0;
+  delete[] IsVacuum;
+  for (size_t bz = 1; bz + 1 < nz; ++bz)
+    for (size_t by = 1; by + 1 < ny; ++by)
+      for (size_t bx = 1; bx + 1 < nx; ++bx) {
+        if (!vac[bx + by * nx + bz * nxy]) continue;
+        for (int dz = -1; dz <= 1; ++dz)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+              if (!dx && !dy && !dz) continue;
+              const size_t there = (bx + dx) + (by + dy) * nx + (bz + dz) * nxy;
+              if (!vac[there]) srf[there] = 1;
+            }
+      }
+  for (size_t b = 0; b < nxyz; ++b) ins[b] = (!vac[b] && !srf[b]) ? 1 : 0;
+  out = VoxelResult();
+  for (size_t b : ion2bin) out.nions_inside += ins[b] ? 1 : 0;
+  for (size_t b = 0; b < nxyz; ++b) { out.vacuum += vac[b]; out.surface += srf[b]; out.inside += ins[b]; }
+  apt_real InsideVolume = static_cast<apt_real>(out.inside);
+  InsideVolume *= CUBE(static_cast<apt_xyz>(binwidth));
+  out.volume_inside = InsideVolume;
+  out.nx = nx; out.ny = ny; out.nz = nz;
+  return true;
+}
+
 int main(int argc, char** argv) {
   if (argc < 5) {
     cerr << "usage: ref_spatstat <simid> <settings.xml> <nthreads> <outdir> [--labels f] [--inside n v] [--dump-surf]\n";
@@ -206,9 +291,10 @@ int main(int argc, char** argv) {
   string labels_fn;
   size_t nions_inside = 0;
   double volume_inside = 0.0;
-  bool dump_surf = false;
+  bool dump_surf = false, do_voxel = false;
   for (int a = 5; a < argc; ++a) {
     string s = argv[a];
+    if (s == "--voxelize") { do_voxel = true; continue; }
     if (s == "--labels" && a + 1 < argc) labels_fn = argv[++a];
     else if (s == "--inside" && a + 2 < argc) { nions_inside = stoull(argv[a + 1]); volume_inside = stod(argv[a + 2]); a += 2; }
     else if (s == "--dump-surf") dump_surf = true;
@@ -219,6 +305,17 @@ int main(int argc, char** argv) {
   // ---- ingest + ranging (src/PARAPROBE_SolverHdl.cpp:6797-6930, :7340-7438)
   vector<pos> raw;
   if (!read_pos(Settings::RAWFilenameIn, raw)) { cerr << "cannot read POS\n"; return 4; }
+  if (do_voxel) {
+    VoxelResult v;
+    if (!voxelize(raw, v)) { cerr << "voxelisation failed\n"; return 8; }
+    nions_inside = v.nions_inside;
+    volume_inside = v.volume_inside;
+    ofstream vf((outdir + "/voxel.txt").c_str());
+    vf.precision(18);
+    vf << "nions_inside " << v.nions_inside << "\nvolume_inside " << v.volume_inside << "\nvacuum_bins " << v.vacuum
+       << "\nsurface_bins " << v.surface << "\ninside_bins " << v.inside << "\nnx " << v.nx << "\nny " << v.ny
+       << "\nnz " << v.nz << "\n";
+  }
   PeriodicTable pse;
   if (!pse.read_rangefile2(Settings::RRNGFilenameIn)) { cerr << "cannot read RRNG\n"; return 5; }
   const size_t N = raw.size();

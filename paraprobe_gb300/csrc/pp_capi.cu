@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -930,6 +931,134 @@ int pp_surfdist_upload(pp_ctx* ctx, int cloud, const float* d2) {
   CK(cudaMemcpy(c->user_surf.p, d2, c->n * 4, cudaMemcpyHostToDevice));
   c->has_user_surf = true;
   c->surf_version = ~0ull;
+  return PP_OK;
+}
+
+// NumberOfIonsInside / VolumeInside of the RDF header: the reference's
+// occupancy grid (vxlizer::rectangular_binning and the steps it calls,
+// src/PARAPROBE_SolverHdl.cpp:5059-5386).  The device bins every ion; the
+// host labels the empty voxels in raster order with the Hoshen-Kopelman rules
+// of src/PARAPROBE_HoshenKopelman.cpp:55-146 -- a voxel joins its labelled -x,
+// -y and -z neighbours, except that with all three labelled only -y and -z are
+// merged, and voxel 0 (label 0) stays unlabelled -- takes the cluster of the
+// guard corner (0, 0, nz - 1) as vacuum (:5196-5270), marks the non-vacuum
+// Moore neighbours of vacuum voxels off the border as surface (:5132-5194) and
+// counts the rest as inside (:5059-5130).
+int pp_cloud_inside(pp_ctx* ctx, int cloud, float bin_width_min, float bin_width_max, uint64_t* nions_inside,
+                    float* volume_inside, uint64_t* voxels) {
+  Cloud* cl = ctx ? get_cloud(ctx, cloud) : nullptr;
+  if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
+  if (!(bin_width_min > 0.f) || !(bin_width_max > 0.f) || !std::isfinite(bin_width_min) || !std::isfinite(bin_width_max))
+    return fail(ctx, PP_ERR_INVALID, "bin widths must be finite and positive");
+  CK(cudaSetDevice(ctx->device));
+  const uint64_t n = cl->n;
+  cudaStream_t s = 0;
+  // tip box (src/PARAPROBE_SolverHdl.cpp:1778-1791): min / max of every coordinate
+  CK(ctx->bbox.ensure(8 * sizeof(uint32_t)));
+  const uint32_t init[8] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0, 0, 0, 0, 0};
+  CK(cudaMemcpyAsync(ctx->bbox.p, init, sizeof init, cudaMemcpyHostToDevice, s));
+  pp::launch_bbox(cl->xyz.as<float>(), n, ctx->bbox.as<float>(), s);
+  uint32_t bb[8];
+  CK(cudaMemcpyAsync(bb, ctx->bbox.p, sizeof bb, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (bb[6]) return fail(ctx, PP_ERR_INVALID, "cloud has %u non-finite coordinates", bb[6]);
+  auto o2f = [](uint32_t o) {
+    const uint32_t u = (o & 0x80000000u) ? (o & 0x7fffffffu) : ~o;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+  };
+  // define_vxlgrid (:5318-5340): box grown by one voxel, one more voxel each side
+  const float w = (float)(0.5 * (double)(bin_width_min + bin_width_max));
+  float lo[3];
+  uint64_t nv[3];
+  for (int k = 0; k < 3; ++k) {
+    float a = n ? o2f(bb[k]) : std::numeric_limits<float>::max();
+    float b = n ? o2f(bb[3 + k]) : std::numeric_limits<float>::lowest();
+    a -= w;
+    b += w;
+    lo[k] = a;
+    nv[k] = (uint64_t)std::ceil((b - a) / w) + 2;
+  }
+  const uint64_t nx = nv[0], ny = nv[1], nz = nv[2], nxy = nx * ny, nxyz = nxy * nz;
+  if (nx >= 0xffffffffull || ny >= 0xffffffffull || nz >= 0xffffffffull || nxyz >= 0xffffffffull)
+    return fail(ctx, PP_ERR_UNSUPPORTED, "the occupancy grid needs 2^32 or more voxels (the reference's limit too)");
+  DevBuf occ_dev;
+  CK(occ_dev.ensure(nxyz * 4));
+  CK(cudaMemsetAsync(occ_dev.p, 0, nxyz * 4, s));
+  CK(ctx->res.status.ensure(4));
+  CK(cudaMemsetAsync(ctx->res.status.p, 0, 4, s));
+  const uint32_t nv32[3] = {(uint32_t)nx, (uint32_t)ny, (uint32_t)nz};
+  pp::launch_voxel_count(cl->xyz.as<float>(), n, lo, w, nv32, occ_dev.as<uint32_t>(), ctx->res.status.as<int>(), s);
+  std::vector<uint32_t> occ(nxyz);
+  int st = 0;
+  CK(cudaMemcpyAsync(occ.data(), occ_dev.p, nxyz * 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&st, ctx->res.status.p, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (st) return fail(ctx, PP_ERR_DEVICE, "an ion fell outside the occupancy grid");
+  // Hoshen-Kopelman clusters of the empty voxels (union-find over voxel ids)
+  std::vector<uint32_t> parent(nxyz);
+  for (uint64_t b = 0; b < nxyz; ++b) parent[b] = (uint32_t)b;
+  auto root = [&](uint32_t a) {
+    while (parent[a] != a) {
+      parent[a] = parent[parent[a]];
+      a = parent[a];
+    }
+    return a;
+  };
+  auto join = [&](uint32_t a, uint32_t b) {
+    a = root(a);
+    b = root(b);
+    if (a != b) parent[a] = b;
+  };
+  auto labelled = [&](uint64_t b) { return b != 0 && occ[b] == 0; };
+  for (uint64_t z = 0; z < nz; ++z)
+    for (uint64_t y = 0; y < ny; ++y)
+      for (uint64_t x = 0; x < nx; ++x) {
+        const uint64_t v = x + y * nx + z * nxy;
+        if (!labelled(v)) continue;
+        const bool lx = x > 0 && labelled(v - 1), ly = y > 0 && labelled(v - nx), lz = z > 0 && labelled(v - nxy);
+        if (lx && ly && lz) {
+          join((uint32_t)(v - nx), (uint32_t)(v - nxy));
+          join((uint32_t)v, (uint32_t)(v - nx));
+          continue;
+        }
+        if (lx) join((uint32_t)v, (uint32_t)(v - 1));
+        if (ly) join((uint32_t)v, (uint32_t)(v - nx));
+        if (lz) join((uint32_t)v, (uint32_t)(v - nxy));
+      }
+  std::vector<uint8_t> cls(nxyz, 0);  // 1 vacuum, 2 surface
+  const uint64_t corner = (nz - 1) * nxy;
+  if (labelled(corner)) {
+    const uint32_t rc = root((uint32_t)corner);
+    for (uint64_t b = 0; b < nxyz; ++b)
+      if (labelled(b) && root((uint32_t)b) == rc) cls[b] = 1;
+  }
+  for (uint64_t z = 1; z + 1 < nz; ++z)
+    for (uint64_t y = 1; y + 1 < ny; ++y)
+      for (uint64_t x = 1; x + 1 < nx; ++x) {
+        if (cls[x + y * nx + z * nxy] != 1) continue;
+        for (int dz = -1; dz <= 1; ++dz)
+          for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+              const uint64_t t = (x + dx) + (y + dy) * nx + (z + dz) * nxy;
+              if ((dx || dy || dz) && cls[t] != 1) cls[t] = 2;
+            }
+      }
+  uint64_t nvac = 0, nsrf = 0, nin = 0, ions_in = 0;
+  for (uint64_t b = 0; b < nxyz; ++b) {
+    if (cls[b] == 1) ++nvac;
+    else if (cls[b] == 2) ++nsrf;
+    else { ++nin; ions_in += occ[b]; }
+  }
+  float vol = (float)nin;
+  vol *= w * w * w;
+  if (nions_inside) *nions_inside = ions_in;
+  if (volume_inside) *volume_inside = vol;
+  if (voxels) {
+    voxels[0] = nvac; voxels[1] = nsrf; voxels[2] = nin;
+    voxels[3] = nx; voxels[4] = ny; voxels[5] = nz;
+  }
   return PP_OK;
 }
 

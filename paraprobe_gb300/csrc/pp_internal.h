@@ -157,6 +157,9 @@ void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const 
 void launch_surface_xyz(const float* xyz, uint64_t n, const float* tbox, const float* tri, const uint32_t* tstart,
                         const uint32_t* tlist, Grid tg, float rp, float* out, cudaStream_t s);
 void launch_tri_box(const float* tri, uint64_t ntri, float* box, cudaStream_t s);
+// ions per voxel of the occupancy grid (lo = grid origin, nv = voxels per axis)
+void launch_voxel_count(const float* xyz, uint64_t n, const float* lo, float w, const uint32_t* nv, uint32_t* occ,
+                        int* status, cudaStream_t s);
 // adds the list entries binning into tg makes to *total (caller zeroes it)
 void launch_tri_entries(const float* tbox, uint64_t ntri, Grid tg, float grow, unsigned long long* total,
                         cudaStream_t s);

@@ -308,6 +308,30 @@ __global__ void k_surface(const float4* __restrict__ ions, uint64_t n, const flo
   }
 }
 
+// Occupancy grid behind the RDF header: voxel of every ion as
+// threadmemory::rectangular_transfer computes it (src/PARAPROBE_SolverHdl.cpp:
+// 1471-1508): t = (p - lo) / w in float, voxel 1 + (size_t)t unless that
+// truncation lands on the last voxel.  Counts ions per voxel.
+__global__ void k_voxel_count(const float* __restrict__ xyz, uint64_t n, float lox, float loy, float loz, float w,
+                              uint32_t nx, uint32_t ny, uint32_t nz, uint32_t* __restrict__ occ, int* status) {
+  const float lo[3] = {lox, loy, loz};
+  const uint64_t nv[3] = {nx, ny, nz};
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float t = __fdiv_rn(__fsub_rn(xyz[3 * i + k], lo[k]), w);
+      const uint64_t sz = (uint64_t)t;
+      c[k] = (sz != nv[k] - 1) ? 1 + sz : nv[k] - 1;
+    }
+    if (c[0] >= nx || c[1] >= ny || c[2] >= nz) {  // cannot happen for a box that holds the cloud
+      atomicOr(status, ST_BAD_SLOT);
+      continue;
+    }
+    atomicAdd(&occ[c[0] + c[1] * nx + c[2] * (uint64_t)nx * ny], 1u);
+  }
+}
+
 // Caller-order variant for the entry point without allocations: positions as
 // packed xyz triples and ion2surf written in the same order.  The candidate
 // test and the minimum are those of k_surface, so both give the same bits.
@@ -1894,6 +1918,12 @@ void launch_tri_entries(const float* tbox, uint64_t ntri, Grid tg, float grow, u
                         cudaStream_t s) {
   counted();
   k_tri_entries<<<grid_for(ntri, 256), 256, 0, s>>>(tbox, ntri, tg, grow, total);
+}
+
+void launch_voxel_count(const float* xyz, uint64_t n, const float* lo, float w, const uint32_t* nv, uint32_t* occ,
+                        int* status, cudaStream_t s) {
+  counted();
+  k_voxel_count<<<grid_for(n, 256), 256, 0, s>>>(xyz, n, lo[0], lo[1], lo[2], w, nv[0], nv[1], nv[2], occ, status);
 }
 
 void launch_tri_box(const float* tri, uint64_t ntri, float* box, cudaStream_t s) {

@@ -11,9 +11,10 @@
 // (on the device), attach the VTK hull, parse the tasks, run the statistics
 // through the C ABI, and write the same CSV files.  With
 // SpatStatAdditionalLabelRandomization = 1 a second pass runs with shuffled
-// labels and writes the ".Rndmized" files.  --inside supplies the
-// NumberOfIonsInside / VolumeInside values printed in the RDF header (the
-// reference takes them from its voxeliser).  --labels replays a given label
+// labels and writes the ".Rndmized" files.  The NumberOfIonsInside /
+// VolumeInside values printed in the RDF header come from the reference's
+// occupancy grid (pp_cloud_inside, voxel edge from AdvIonPruneBinWidthMin/Max);
+// --inside supplies them instead.  --labels replays a given label
 // assignment (one byte per ion, file order, e.g. a stored null-model shuffle)
 // and writes ".Rndmized" files.  --plan prints the parsed task plan as JSON
 // and runs nothing.  Every pass also recomputes the distances of a sample of
@@ -104,6 +105,7 @@ int main(int argc, char** argv) {
   int device = 0;
   uint64_t nions_inside = 0;
   double volume_inside = 0.0;
+  bool inside_given = false;
   bool plan_only = false;
   std::string labels_file;
   uint32_t audit_centres = 20000;
@@ -111,7 +113,12 @@ int main(int argc, char** argv) {
     const std::string s = argv[a];
     if (s == "--outdir" && a + 1 < argc) outdir = argv[++a];
     else if (s == "--device" && a + 1 < argc) device = std::atoi(argv[++a]);
-    else if (s == "--inside" && a + 2 < argc) { nions_inside = std::strtoull(argv[a + 1], nullptr, 10); volume_inside = std::strtod(argv[a + 2], nullptr); a += 2; }
+    else if (s == "--inside" && a + 2 < argc) {
+      nions_inside = std::strtoull(argv[a + 1], nullptr, 10);
+      volume_inside = std::strtod(argv[a + 2], nullptr);
+      inside_given = true;
+      a += 2;
+    }
     else if (s == "--plan") plan_only = true;
     else if (s == "--labels" && a + 1 < argc) labels_file = argv[++a];
     else if (s == "--fp64-audit" && a + 1 < argc) audit_centres = (uint32_t)std::strtoul(argv[++a], nullptr, 10);
@@ -201,6 +208,17 @@ int main(int argc, char** argv) {
     const float rp = std::max(S.rmax, S.carving_radius);
     std::vector<float> d2(n, rp * rp);
     if (check(ctx, pp_surfdist_upload(ctx, cloud, d2.data()), "pp_surfdist_upload")) return 7;
+  }
+  if (!inside_given && S.do_rdf) {
+    // the reference's TipBinning (vxlizer::rectangular_binning) supplies these
+    float vol = 0.f;
+    uint64_t vox[6] = {0, 0, 0, 0, 0, 0};
+    if (check(ctx, pp_cloud_inside(ctx, cloud, S.bin_w_min, S.bin_w_max, &nions_inside, &vol, vox), "pp_cloud_inside"))
+      return 7;
+    volume_inside = vol;
+    std::cout << "TipBinning with a nxyz grid " << vox[3] << ";" << vox[4] << ";" << vox[5] << ": " << vox[0]
+              << " vacuum, " << vox[1] << " surface, " << vox[2] << " inside bins, " << nions_inside
+              << " ions inside" << std::endl;
   }
   const int nt = (int)tasks.size();
   std::vector<uint32_t> trg(8 * (size_t)nt, 0), env(8 * (size_t)nt, 0);

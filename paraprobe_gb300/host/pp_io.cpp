@@ -160,6 +160,9 @@ Settings read_settings(const std::string& path) {
   s.spatstat = any;
   int tess = 0;
   if (has("AnalysisVolumeTessellation")) tess = to_ul(val("AnalysisVolumeTessellation")) == 1 ? 1 : 0;
+  if (has("AdvIonPruneBinWidthMin")) s.bin_w_min = to_real(val("AdvIonPruneBinWidthMin"));
+  if (has("AdvIonPruneBinWidthIncr")) s.bin_w_incr = to_real(val("AdvIonPruneBinWidthIncr"));
+  if (has("AdvIonPruneBinWidthMax")) s.bin_w_max = to_real(val("AdvIonPruneBinWidthMax"));
   if (has("DebugComputeDistance")) s.debug_compute_distance = to_ul(val("DebugComputeDistance")) == 1;
   if (s.spatstat) {
     if (has("DescrStatTasksCode")) s.tasks_code = val("DescrStatTasksCode");
@@ -184,6 +187,8 @@ std::string check_settings(const Settings& s) {
     return "ReconstructionAlgorithm is POS but InputFileformat is neither POS nor HDF5!";
   if (s.recon_algo == 3 && s.input_format != 2) return "ReconstructionAlgorithm is EPOS but InputFileformat is not EPOS!";
   if (s.recon_algo == 4 && s.input_format != 2) return "Reconstruction is Bas et al. but InputFileformat is not EPOS!";
+  if (s.bin_w_min > s.bin_w_max || s.bin_w_min > s.bin_w_incr || s.bin_w_max < s.bin_w_incr)
+    return "Invalid choice for AdvIonPruneBinning";
   if (s.spatstat) {
     if (s.rmin < 0.f) return "SpatStatRadiusMin must be positive or zero!";
     if (s.rincr < kEpsilon) return "SpatStatRadiusIncr must be positive!";

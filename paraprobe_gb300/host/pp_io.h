@@ -36,6 +36,9 @@ struct Settings {
   size_t knn_order = 0;          // SpatStatKNNOrder - 1
   bool label_rnd = false;
   float carving_radius = 2.f;    // SurfaceCellsCarvingRadius default
+  // occupancy-grid bin width keys (src/PARAPROBE_Settings.cpp:83-85, 460-465);
+  // the grid behind the RDF header uses 0.5 (min + max)
+  float bin_w_min = 1.f, bin_w_incr = 1.f, bin_w_max = 1.f;
   unsigned int rnd_seed = 0xffffffffu;
 };
 

@@ -27,7 +27,7 @@ EXPORTS = (
     "pp_batched_stats", "pp_neighbors", "pp_shuffle_labels", "pp_device_info", "pp_kernel_launches",
     "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option", "pp_cloud_prepare",
     "pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_stats", "pp_server_destroy",
-    "pp_fp64_audit", "pp_surfdist_noalloc", "pp_batched_graph",
+    "pp_fp64_audit", "pp_surfdist_noalloc", "pp_batched_graph", "pp_cloud_inside",
 )
 
 _lib = None
@@ -89,6 +89,7 @@ def load():
                            C.POINTER(u64), C.POINTER(u64), vp, vp, u64, C.POINTER(u64)], i32),
         "pp_surfdist_noalloc": ([vp, u64, vp, u64, f32, vp, vp, C.c_char_p, C.c_size_t], i32),
         "pp_batched_graph": ([vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)], i32),
+        "pp_cloud_inside": ([vp, i32, f32, f32, C.POINTER(u64), C.POINTER(f32), vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -308,6 +309,15 @@ class Context:
         c, p = C.c_uint64(), C.c_uint64()
         self._ck(self.L.pp_batched_stats(self.h, r, C.byref(c), C.byref(p)), "pp_batched_stats")
         return dict(centres=c.value, pairs=p.value)
+
+    def inside(self, cloud, bin_width_min=1.0, bin_width_max=1.0):
+        """NumberOfIonsInside, VolumeInside and the voxel counts of the occupancy grid."""
+        nin, vol = C.c_uint64(), C.c_float()
+        vox = np.zeros(6, dtype=np.uint64)
+        self._ck(self.L.pp_cloud_inside(self.h, cloud, bin_width_min, bin_width_max, C.byref(nin), C.byref(vol),
+                                        _p(vox)), "pp_cloud_inside")
+        return dict(nions_inside=nin.value, volume_inside=np.float32(vol.value), vacuum=int(vox[0]),
+                    surface=int(vox[1]), inside=int(vox[2]), nx=int(vox[3]), ny=int(vox[4]), nz=int(vox[5]))
 
     def batched_graph(self):
         nodes, caps, launches = C.c_uint64(), C.c_uint64(), C.c_uint64()

@@ -244,7 +244,7 @@ def write_vtk(path: str, tri: np.ndarray) -> None:
 
 def write_settings_xml(path: str, pos: str, rrng: str, vtk: str | None, analyses: str,
                        tasks: str, rmin: str, rincr: str, rmax: str, mknn: str = "",
-                       knn_order: int = 1, label_rnd: int = 0) -> None:
+                       knn_order: int = 1, label_rnd: int = 0, bin_width=None) -> None:
     """XML with the keys the descriptive-statistics path reads; numbers are
     passed as strings so they reach the float parser exactly as written."""
     surf = "4" if vtk else "0"
@@ -270,8 +270,12 @@ def write_settings_xml(path: str, pos: str, rrng: str, vtk: str | None, analyses
         f"\t<SpatStatKNNOrder>{knn_order}</SpatStatKNNOrder>",
         f"\t<SpatStatMKNNCode>{mknn}</SpatStatMKNNCode>",
         f"\t<SpatStatAdditionalLabelRandomization>{label_rnd}</SpatStatAdditionalLabelRandomization>",
-        "</Parameters>", "",
     ]
+    if bin_width is not None:  # (min, incr, max) of the occupancy grid, as strings
+        body += [f"\t<AdvIonPruneBinWidthMin>{bin_width[0]}</AdvIonPruneBinWidthMin>",
+                 f"\t<AdvIonPruneBinWidthIncr>{bin_width[1]}</AdvIonPruneBinWidthIncr>",
+                 f"\t<AdvIonPruneBinWidthMax>{bin_width[2]}</AdvIonPruneBinWidthMax>"]
+    body += ["</Parameters>", ""]
     with open(path, "w") as f:
         f.write("\n".join(body))
 

@@ -8,7 +8,9 @@ PeriodicTable.cpp / Settings.cpp compiled from the read-only reference tree
 by oracle/ref/Makefile, driven by a restatement of the SolverHdl.cpp glue.
 The fixture stores the inputs (float32 arrays), the settings text, and the
 reference's outputs: raw histogram counts, neighbour-count histograms,
-centre/pair statistics, ion-to-hull distances and the CSV files.
+centre/pair statistics, ion-to-hull distances, the occupancy grid's
+NumberOfIonsInside / VolumeInside (which head the RDF files) and the CSV
+files.
 
 Run in the development container (the reference tree must be present):
     make -C oracle/ref REF=/root/reference
@@ -40,7 +42,8 @@ CASES = [
     dict(name="cntnb", geom="cyl", n=12000, radius=4.5, height=14.0, seed=103, analyses="16",
          tasks="Sc-Al,Sc,Zr;Al,Sc-Zr", r=("0.0", "0.02", "1.2"), mknn="", threads=2),
     dict(name="edges", geom="cyl", n=12000, radius=4.5, height=14.0, seed=104, analyses="1234",
-         tasks="Al-Al,Sc,Zr;Sc-Al", r=("0.3", "0.1", "1.3"), mknn="2;40", threads=5),
+         tasks="Al-Al,Sc,Zr;Sc-Al", r=("0.3", "0.1", "1.3"), mknn="2;40", threads=5,
+         bin_width=("0.5", "0.6", "0.7")),
     dict(name="shuffled", geom="cyl", n=15000, radius=5.0, height=14.0, seed=105, analyses="12",
          tasks="Sc-Al,Sc,Zr", r=("0.0", "0.01", "1.0"), mknn="", threads=4, shuffle_seed=9001),
     dict(name="nohull", geom="cyl", n=12000, radius=4.5, height=14.0, seed=106, analyses="24",
@@ -68,12 +71,11 @@ def make(c, outdir):
         hull = c.get("hull", True)
         xml = os.path.join(tmp, "settings.xml")
         synth.write_settings_xml(xml, pos, rrng, vtk if hull else None, c["analyses"], tasks, *c["r"],
-                                 mknn=c["mknn"])
+                                 mknn=c["mknn"], bin_width=c.get("bin_width"))
         out = os.path.join(tmp, "out")
-        nins = int(spec.xyz.shape[0])
-        vol = float(synth.cylinder_volume(c["radius"], c["height"])) if c["geom"] == "cyl" else \
-            float(synth.cone_volume(7.0, 10.0, 16.0))
-        cmd = [REF, "7", xml, str(c["threads"]), out, "--dump-surf", "--inside", str(nins), repr(vol)]
+        # the harness computes NumberOfIonsInside / VolumeInside with the
+        # reference's occupancy grid (its own Hoshen-Kopelman unit)
+        cmd = [REF, "7", xml, str(c["threads"]), out, "--dump-surf", "--voxelize"]
         labels = spec.labels
         if "shuffle_seed" in c:
             from paraprobe_gb300 import native
@@ -85,6 +87,11 @@ def make(c, outdir):
         if r.returncode != 0:
             raise RuntimeError(f"{c['name']}: reference harness failed\n{r.stderr[-2000:]}")
         _, mq = synth.read_pos(pos)
+        voxel = {}
+        for line in open(os.path.join(out, "voxel.txt")):
+            k, v = line.split()
+            voxel[k] = float(v) if k == "volume_inside" else int(v)
+        nins, vol = voxel["nions_inside"], voxel["volume_inside"]
         stats = {}
         task_lines, ks = [], []
         for line in open(os.path.join(out, "stats.txt")):
@@ -102,7 +109,7 @@ def make(c, outdir):
             if f.endswith(".csv"):
                 csvs[f] = open(os.path.join(out, f)).read()
         meta = dict(case=c, tasks_code=tasks, trg=trg, env=env, names=[t[1:3] for t in task_lines], k=ks,
-                    stats=stats, nions_inside=nins, volume_inside=vol,
+                    stats=stats, nions_inside=nins, volume_inside=vol, voxel=voxel,
                     settings_xml=open(xml).read().replace(tmp + "/", ""),
                     rrng=open(rrng).read())
         np.savez_compressed(

@@ -23,7 +23,9 @@ def load(name):
     for d in c["analyses"]:
         flags |= FLAG_OF_DIGIT.get(d, 0)
     rmin, rincr, rmax = (np.float32(float(x)) for x in c["r"])
+    bw = c.get("bin_width") or ("1.0", "1.0", "1.0")
     return dict(xyz=z["xyz"], mq=z["mq"], labels=z["labels"], hull=z["hull"], surf=z["surf"], bins=z["bins"],
                 cntnb=z["cntnb"], meta=meta, csv=json.loads(str(z["csv"])), flags=flags,
                 rmin=rmin, rincr=rincr, rmax=rmax, trg=meta["trg"], env=meta["env"], k=meta["k"],
-                stats=meta["stats"])
+                stats=meta["stats"], voxel=meta["voxel"],
+                bin_width=(np.float32(float(bw[0])), np.float32(float(bw[2]))))

@@ -15,14 +15,18 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CLI = os.path.join(ROOT, "paraprobe_gb300", "_lib", "paraprobe_gpu")
 
 
+@pytest.mark.parametrize("inside", ["given", "computed"])
 @pytest.mark.parametrize("name", G.names())
-def test_cli_csv_identical(ctx, tmp_path, name):
+def test_cli_csv_identical(ctx, tmp_path, name, inside):
+    """With --inside the header values are passed in; without it the CLI
+    computes them with the occupancy grid, as the reference does."""
     c = G.load(name)
     write_case(c, str(tmp_path))
     out = tmp_path / "out"
     out.mkdir()
-    cmd = [CLI, "7", "settings.xml", "--outdir", str(out), "--inside", str(c["meta"]["nions_inside"]),
-           repr(c["meta"]["volume_inside"])]
+    cmd = [CLI, "7", "settings.xml", "--outdir", str(out)]
+    if inside == "given":
+        cmd += ["--inside", str(c["meta"]["nions_inside"]), repr(c["meta"]["volume_inside"])]
     if name == "shuffled":
         np.ascontiguousarray(c["labels"], dtype=np.uint8).tofile(tmp_path / "labels.u8")
         cmd += ["--labels", "labels.u8"]

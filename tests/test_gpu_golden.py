@@ -28,3 +28,15 @@ def test_gpu_matches_reference(ctx, name):
         cn = ctx.fetch_cntnb()
         assert np.array_equal(cn, c["cntnb"].reshape(len(c["trg"]), L))
     ctx.free(cid)
+
+
+@pytest.mark.parametrize("name", G.names())
+def test_gpu_voxelizer_matches_reference(ctx, name):
+    c = G.load(name)
+    cid = ctx.upload(c["xyz"], c["labels"])
+    v = ctx.inside(cid, *c["bin_width"])
+    ref = c["voxel"]
+    assert v["nions_inside"] == ref["nions_inside"] and float(v["volume_inside"]) == ref["volume_inside"]
+    assert (v["vacuum"], v["surface"], v["inside"]) == (ref["vacuum_bins"], ref["surface_bins"], ref["inside_bins"])
+    assert (v["nx"], v["ny"], v["nz"]) == (ref["nx"], ref["ny"], ref["nz"])
+    ctx.free(cid)

@@ -46,3 +46,18 @@ def test_category_edges(oracle):
     assert oracle.nbins(0.3, 0.1, 1.3) == 9
     assert oracle.nbins(0.0, 0.01, 1.3) == 129
     assert oracle.category(0.0, 0.01, 1.0, np.float32(1.0) + np.float32(1e-6)) == 101
+
+
+def _voxel_equal(v, ref):
+    return (v["nions_inside"] == ref["nions_inside"] and float(v["volume_inside"]) == ref["volume_inside"]
+            and v["vacuum"] == ref["vacuum_bins"] and v["surface"] == ref["surface_bins"]
+            and v["inside"] == ref["inside_bins"] and (v["nx"], v["ny"], v["nz"]) == (ref["nx"], ref["ny"], ref["nz"]))
+
+
+@pytest.mark.parametrize("name", G.names())
+def test_oracle_voxelizer_matches_reference(oracle, name):
+    """NumberOfIonsInside / VolumeInside (and the voxel classes behind them)
+    against the reference's occupancy grid and Hoshen-Kopelman unit."""
+    c = G.load(name)
+    v = oracle.voxelize(c["xyz"], *c["bin_width"])
+    assert _voxel_equal(v, c["voxel"]), (v, c["voxel"])
