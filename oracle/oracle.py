@@ -64,6 +64,9 @@ def lib():
         L.ppo_voxelize.argtypes = [f32p, C.c_uint64, C.c_float, C.c_float, C.POINTER(C.c_uint64),
                                    C.POINTER(C.c_float), u64p]
         L.ppo_voxelize.restype = C.c_int
+        L.ppo_npcorr.argtypes = [f32p, u8p, f32p, C.c_uint64, C.c_float, C.c_float, C.c_int, u32p, u32p,
+                                 C.c_uint32, u32p, C.c_uint64, C.POINTER(C.c_uint64)]
+        L.ppo_npcorr.restype = C.c_int
         _lib = L
     return _lib
 
@@ -154,3 +157,20 @@ def voxelize(xyz, w_min=1.0, w_max=1.0):
         raise RuntimeError(f"ppo_voxelize failed ({rc})")
     return dict(nions_inside=nin.value, volume_inside=np.float32(vol.value), vacuum=int(bins[0]),
                 surface=int(bins[1]), inside=int(bins[2]), nx=int(bins[3]), ny=int(bins[4]), nz=int(bins[5]))
+
+
+def npcorr(xyz, labels, ion2surf, rincr, rmax, trg, env, order):
+    """n-point correlation counts: (ntasks, edge, edge, edge) uint32, [z][y][x]."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float32)
+    labels = np.ascontiguousarray(labels, dtype=np.uint8)
+    surf = np.ascontiguousarray(ion2surf, dtype=np.float32)
+    tm, em = type_masks(trg), type_masks(env)
+    half = int(np.ceil(np.float32(rmax) / np.float32(rincr)) + 1)
+    edge = 1 + 2 * half
+    out = np.zeros(len(trg) * edge ** 3, dtype=np.uint32)
+    e = C.c_uint64()
+    rc = lib().ppo_npcorr(xyz.reshape(-1), labels, surf, xyz.shape[0], np.float32(rincr), np.float32(rmax), len(trg),
+                          tm.reshape(-1), em.reshape(-1), order, out, out.size, C.byref(e))
+    if rc:
+        raise RuntimeError(f"ppo_npcorr failed ({rc})")
+    return out.reshape(len(trg), edge, edge, edge)

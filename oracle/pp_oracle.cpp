@@ -654,6 +654,89 @@ int ppo_voxelize(const float* xyz, uint64_t n, float w_min, float w_max, uint64_
   return 0;
 }
 
+// n-point correlations (AnalysisSpatDistrType 5): for every centre (the
+// filter of ppo_spatstat) and every task whose targets hold its type, the
+// (order+1)-th nearest environment neighbour within R -- by (d^2, ion index)
+// -- contributes its difference vector (neighbour minus centre) to the task's
+// cubic histogram, binned as npc3d::add does (src/PARAPROBE_SolverHdl.cpp:
+// 3899-3955, src/PARAPROBE_NPointCorrelations3D.cpp:48-160).  out holds
+// ntasks * edge^3 uint32 counts; *edge_out = edge.  Returns -2 if out_cap is
+// too small.  (The reference takes the element nth_element places at order,
+// so among exact distance ties its pick is arbitrary; here ties go to the
+// lower ion index.)
+int ppo_npcorr(const float* xyz, const uint8_t* label, const float* ion2surf, uint64_t n, float rincr, float rmax,
+               int ntasks, const uint32_t* trg_mask, const uint32_t* env_mask, uint32_t order, uint32_t* out,
+               uint64_t out_cap, uint64_t* edge_out) {
+  const uint64_t half = (uint64_t)(std::ceil(rmax / rincr) + 1.f);
+  const uint64_t edge = 1 + 2 * half, nxy = edge * edge, nxyz = nxy * edge;
+  if (edge_out) *edge_out = edge;
+  if ((uint64_t)ntasks * nxyz > out_cap) return -2;
+  std::fill(out, out + (uint64_t)ntasks * nxyz, 0u);
+  const float R = rmax, RSQR = R * R, inv = 1.f / rincr;
+  std::vector<uint8_t> any_trg(256, 0);
+  for (int t = 0; t < ntasks; ++t)
+    for (uint32_t ty = 0; ty < 256; ++ty) if (bit(trg_mask + 8 * t, ty)) any_trg[ty] = 1;
+  // neighbour search on a uniform grid of edge R
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (uint64_t i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], xyz[3 * i + k]); hi[k] = std::max(hi[k], xyz[3 * i + k]); }
+  int64_t g[3];
+  for (int k = 0; k < 3; ++k) g[k] = std::max<int64_t>(1, (int64_t)((hi[k] - lo[k]) / R) + 1);
+  auto cell_of = [&](uint64_t i, int k) {
+    return std::min<int64_t>(g[k] - 1, std::max<int64_t>(0, (int64_t)((xyz[3 * i + k] - lo[k]) / R)));
+  };
+  std::vector<std::vector<uint64_t>> cells((size_t)(g[0] * g[1] * g[2]));
+  for (uint64_t i = 0; i < n; ++i)
+    cells[(size_t)((cell_of(i, 2) * g[1] + cell_of(i, 1)) * g[0] + cell_of(i, 0))].push_back(i);
+  struct Cand { float d2; uint64_t j; };
+#pragma omp parallel
+  {
+    std::vector<Cand> nb, tmp;
+    std::vector<uint32_t> mine((uint64_t)ntasks * nxyz, 0u);
+#pragma omp for schedule(dynamic, 256)
+    for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+      const uint64_t i = (uint64_t)ii;
+      if (!any_trg[label[i]] || !(ion2surf[i] >= RSQR)) continue;
+      nb.clear();
+      const int64_t c0 = cell_of(i, 0), c1 = cell_of(i, 1), c2 = cell_of(i, 2);
+      for (int64_t z = std::max<int64_t>(0, c2 - 1); z <= std::min<int64_t>(g[2] - 1, c2 + 1); ++z)
+        for (int64_t y = std::max<int64_t>(0, c1 - 1); y <= std::min<int64_t>(g[1] - 1, c1 + 1); ++y)
+          for (int64_t x = std::max<int64_t>(0, c0 - 1); x <= std::min<int64_t>(g[0] - 1, c0 + 1); ++x)
+            for (uint64_t j : cells[(size_t)((z * g[1] + y) * g[0] + x)]) {
+              if (j == i) continue;
+              const float dx = xyz[3 * i] - xyz[3 * j], dy = xyz[3 * i + 1] - xyz[3 * j + 1],
+                          dz = xyz[3 * i + 2] - xyz[3 * j + 2];
+              const float d2 = (dx * dx + dy * dy) + dz * dz;
+              if (d2 <= RSQR) nb.push_back({d2, j});
+            }
+      for (int t = 0; t < ntasks; ++t) {
+        if (!bit(trg_mask + 8 * t, label[i])) continue;
+        tmp.clear();
+        for (const Cand& c : nb) if (bit(env_mask + 8 * t, label[c.j])) tmp.push_back(c);
+        if (tmp.size() <= order) continue;
+        std::nth_element(tmp.begin(), tmp.begin() + order, tmp.end(), [](const Cand& a, const Cand& b) {
+          return a.d2 < b.d2 || (a.d2 == b.d2 && a.j < b.j);
+        });
+        const uint64_t j = tmp[order].j;
+        const float u = xyz[3 * j] - xyz[3 * i], v = xyz[3 * j + 1] - xyz[3 * i + 1], w = xyz[3 * j + 2] - xyz[3 * i + 2];
+        const float d = std::sqrt((u * u + v * v) + w * w);
+        if (!(d <= R)) continue;
+        int64_t b[3];
+        const float comp[3] = {u, v, w};
+        for (int k = 0; k < 3; ++k) {
+          const float there = comp[k] * inv;
+          const int disc = (there >= 0.f) ? (int)((double)there + 0.5) : (int)((double)there - 0.5);
+          b[k] = disc + (int64_t)half;
+        }
+        mine[(uint64_t)t * nxyz + (uint64_t)(b[0] + b[1] * (int64_t)edge + b[2] * (int64_t)nxy)] += 1;
+      }
+    }
+#pragma omp critical
+    for (uint64_t k = 0; k < mine.size(); ++k) out[k] += mine[k];
+  }
+  return 0;
+}
+
 int ppo_category(float rmin, float rincr, float rmax, float x) {
   Hist h; h.init(rmin, rincr, rmax);
   double xx = x;

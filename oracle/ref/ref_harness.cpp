@@ -22,6 +22,8 @@
 //   raw_cntnb.u64   uint64 [ntasks][L] neighbour-count histogram, L in stats
 //   stats.txt       centres, discarded, pairs, nbins, ntasks, nk, L
 //   ion2surf.f32    (with --dump-surf) squared hull distance per original ion
+//   raw_npcorr.u32  (AnalysisSpatDistrType 5) uint32 [ntasks][edge^3] n-point
+//                   correlation counts of the reference's npc3d class
 //   voxel.txt       (with --voxelize) the occupancy grid's NumberOfIonsInside and
 //                   VolumeInside, which then also head the RDF reports; the
 //                   Hoshen-Kopelman clustering is the reference's percAnalyzer
@@ -31,6 +33,7 @@
 #include "PARAPROBE_KDTree.h"
 #include "PARAPROBE_DiscreteHistogram.h"
 #include "PARAPROBE_HoshenKopelman.h"
+#include "PARAPROBE_NPointCorrelations3D.h"
 
 #include <omp.h>
 #include <sys/stat.h>
@@ -441,11 +444,22 @@ int main(int argc, char** argv) {
     if (Settings::SpatStatDoMKNN) for (size_t k = 0; k < kcand.size(); ++k) gM.push_back(histogram(Rs, Ri, Rm));
   }
   const unsigned int MaxTypes = pse.get_maxtypeid();
+  // n-point correlations (src/PARAPROBE_SolverHdl.cpp:3706-3712, 3730-3736)
+  const bool doP = Settings::SpatStatDoNPCorr;
+  if (doP && npc3d(Rm, Ri, 0.f, false).get_support().nxyz > CUBE(MAXIMUM_NPC3D_BIN_RESOLUTION)) {
+    cerr << "Computation of 2-point statistics would require too large buffers, skipping!\n";
+    return 9;
+  }
+  vector<npc3d> gP;
+  if (doP) for (size_t t = 0; t < ntsk; ++t) gP.push_back(npc3d(Rm, Ri, 0.f, true));
+  const size_t KNNOrder = Settings::SpatStatKNNOrder;
   size_t centres = 0, discarded = 0, pairs = 0;
 #pragma omp parallel reduction(+ : centres, discarded, pairs)
   {
     vector<histogram> mR, m1, mK, mM;
     vector<discrhistogram> mC;
+    vector<npc3d> mP;
+    if (doP) for (size_t t = 0; t < ntsk; ++t) mP.push_back(npc3d(Rm, Ri, 0.f, true));
     for (size_t t = 0; t < ntsk; ++t) {
       if (Settings::SpatStatDoRDF) mR.push_back(histogram(Rs, Ri, Rm));
       if (Settings::SpatStatDo1NN) m1.push_back(histogram(Rs, Ri, Rm));
@@ -476,6 +490,40 @@ int main(int argc, char** argv) {
           for (int o = thr - 1; o > -1; --o) reg[o].tree->range_rball_noclear_nosort_external(me, reg[o].ions_kd, RSQR, nb);
         }
         pairs += nb.size();
+        if (doP) {
+          // the KNNOrder-th environment neighbour's difference vector
+          // (src/PARAPROBE_SolverHdl.cpp:3899-3955)
+          vector<p3dm1> nb3;
+          kauri->range_rball_noclear_nosort_p3dm1(i, these, RSQR, nb3);
+          if (!((me.z - R) > reg[thr].zmi && (me.z + R) < reg[thr].zmx)) {
+            for (int o = thr + 1; o < T; ++o)
+              reg[o].tree->range_rball_noclear_nosort_external_p3dm1(me, reg[o].ions_kd, RSQR, nb3);
+            for (int o = thr - 1; o > -1; --o)
+              reg[o].tree->range_rball_noclear_nosort_external_p3dm1(me, reg[o].ions_kd, RSQR, nb3);
+          }
+          for (size_t t = 0; t < ntsk; ++t) {
+            for (auto kt = tasks[t].trgcandidates.begin(); kt != tasks[t].trgcandidates.end(); ++kt) {
+              if (me.m != kt->second) continue;
+              if (nb3.size() > KNNOrder) {
+                vector<npnbor> tmp;
+                for (size_t nbb = 0; nbb < nb3.size(); ++nbb) {
+                  for (auto jt = tasks[t].envcandidates.begin(); jt != tasks[t].envcandidates.end(); ++jt) {
+                    if (nb3[nbb].m != jt->second) continue;
+                    p3dm1 thisnb = nb3[nbb];
+                    d3d diffv = d3d(thisnb.x - me.x, thisnb.y - me.y, thisnb.z - me.z);
+                    apt_xyz dd = sqrt(SQR(diffv.u) + SQR(diffv.v) + SQR(diffv.w));
+                    tmp.push_back(npnbor(diffv, dd));
+                  }
+                }
+                if (tmp.size() > KNNOrder) {
+                  nth_element(tmp.begin(), tmp.begin() + KNNOrder, tmp.end(), SortNPNeighborsForAscDistance);
+                  mP[t].add(tmp[KNNOrder]);
+                }
+              }
+              break;
+            }
+          }
+        }
         // counting sort by type (:3975-3997)
         vector<size_t> s(MaxTypes, 0), e(MaxTypes, 0), c(MaxTypes, 0);
         for (auto& q : nb) c[q.m]++;
@@ -531,6 +579,8 @@ int main(int argc, char** argv) {
         if (Settings::SpatStatDoCountNbors) for (size_t b = 0; b < mC[t].cnts.size(); ++b) gC[t].add(b, mC[t].cnts.at(b));
       }
       for (size_t h = 0; h < mM.size(); ++h) merge(gM[h], mM[h]);
+      for (size_t t = 0; t < mP.size(); ++t)
+        for (size_t v = 0; v < mP[t].cnts.size(); ++v) gP[t].cnts[v] += mP[t].cnts[v];
     }
   }
 
@@ -570,10 +620,16 @@ int main(int argc, char** argv) {
   f = fopen((outdir + "/raw_cntnb.u64").c_str(), "wb");
   if (!cn.empty()) fwrite(cn.data(), 8, cn.size(), f);
   fclose(f);
+  if (doP) {
+    FILE* fp = fopen((outdir + "/raw_npcorr.u32").c_str(), "wb");
+    for (auto& g : gP) fwrite(g.cnts.data(), 4, g.cnts.size(), fp);
+    fclose(fp);
+  }
   unsigned int nbins = histogram(Rs, Ri, Rm).bincount();
   ofstream st((outdir + "/stats.txt").c_str());
   st << "centres " << centres << "\ndiscarded " << discarded << "\npairs " << pairs << "\nnbins " << nbins
-     << "\nntasks " << ntsk << "\nnk " << kcand.size() << "\ncntnb_len " << L << "\nmaxtypeid " << MaxTypes << "\n";
+     << "\nntasks " << ntsk << "\nnk " << kcand.size() << "\ncntnb_len " << L << "\nmaxtypeid " << MaxTypes
+     << "\nnpc_edge " << (doP ? npc3d(Rm, Ri, 0.f, false).get_support().nx : 0) << "\n";
   for (size_t t = 0; t < ntsk; ++t) {
     string a, b; names(t, a, b);
     st << "task " << t << " " << a << " " << b;

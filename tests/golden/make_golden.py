@@ -52,6 +52,8 @@ CASES = [
          tasks="Al-Al,Sc,Zr;Sc-Sc,Zr", r=("0.0", "0.01", "1.3"), mknn="1;33;64;100", threads=3),
     dict(name="rdf_sym", geom="cone", n=20000, seed=108, nspecies=4, analyses="13",
          tasks="Al-Al,Sc;Sc,Zr-Al,Sc,Zr;Si-Al", r=("0.1", "0.02", "1.6"), mknn="", threads=3),
+    dict(name="npcorr", geom="cone", n=15000, seed=109, nspecies=3, analyses="125",
+         tasks="Al-Al,Sc;Sc-Al,Sc,Zr;Zr-Zr", r=("0.0", "0.05", "1.0"), mknn="", threads=3, knn_order=3),
 ]
 
 
@@ -71,7 +73,7 @@ def make(c, outdir):
         hull = c.get("hull", True)
         xml = os.path.join(tmp, "settings.xml")
         synth.write_settings_xml(xml, pos, rrng, vtk if hull else None, c["analyses"], tasks, *c["r"],
-                                 mknn=c["mknn"], bin_width=c.get("bin_width"))
+                                 mknn=c["mknn"], bin_width=c.get("bin_width"), knn_order=c.get("knn_order", 1))
         out = os.path.join(tmp, "out")
         # the harness computes NumberOfIonsInside / VolumeInside with the
         # reference's occupancy grid (its own Hoshen-Kopelman unit)
@@ -118,6 +120,8 @@ def make(c, outdir):
             surf=np.fromfile(os.path.join(out, "ion2surf.f32"), dtype=np.float32),
             bins=np.fromfile(os.path.join(out, "raw_bins.u64"), dtype=np.uint64),
             cntnb=np.fromfile(os.path.join(out, "raw_cntnb.u64"), dtype=np.uint64),
+            npcorr=(np.fromfile(os.path.join(out, "raw_npcorr.u32"), dtype=np.uint32)
+                    if os.path.exists(os.path.join(out, "raw_npcorr.u32")) else np.zeros(0, np.uint32)),
             meta=np.array(json.dumps(meta)), csv=np.array(json.dumps(csvs)))
         return stats
 

@@ -28,4 +28,6 @@ def load(name):
                 cntnb=z["cntnb"], meta=meta, csv=json.loads(str(z["csv"])), flags=flags,
                 rmin=rmin, rincr=rincr, rmax=rmax, trg=meta["trg"], env=meta["env"], k=meta["k"],
                 stats=meta["stats"], voxel=meta["voxel"],
+                npcorr=z["npcorr"] if "npcorr" in z.files else np.zeros(0, np.uint32),
+                npcorr_order=int(c.get("knn_order", 1)) - 1,
                 bin_width=(np.float32(float(bw[0])), np.float32(float(bw[2]))))

@@ -61,3 +61,13 @@ def test_oracle_voxelizer_matches_reference(oracle, name):
     c = G.load(name)
     v = oracle.voxelize(c["xyz"], *c["bin_width"])
     assert _voxel_equal(v, c["voxel"]), (v, c["voxel"])
+
+
+def test_oracle_npcorr_matches_reference(oracle):
+    """n-point correlation counts against the reference's npc3d class driven
+    by its own KD-tree queries and nth_element (fixture "npcorr")."""
+    c = G.load("npcorr")
+    out = oracle.npcorr(c["xyz"], c["labels"], c["surf"], c["rincr"], c["rmax"], c["trg"], c["env"],
+                        c["npcorr_order"])
+    assert c["npcorr"].size == out.size and c["npcorr"].sum() > 0
+    assert np.array_equal(out.reshape(-1), c["npcorr"])
