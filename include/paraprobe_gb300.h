@@ -59,7 +59,7 @@ extern "C" {
 #define PP_1NN 2u
 #define PP_RIPK 4u
 #define PP_MKNN 8u
-#define PP_NPCORR 16u /* not provided: rejected with PP_ERR_UNSUPPORTED */
+#define PP_NPCORR 16u /* n-point correlations (pp_run only; order via option "npcorr_order") */
 #define PP_CNTNB 32u
 
 #define PP_TYPE_WORDS 8 /* 256 ion types */
@@ -180,10 +180,25 @@ int pp_fp64_audit(pp_ctx* ctx, int cloud, uint32_t max_centres, double* max_abs,
                   uint64_t* pairs, uint64_t* bin_disagree, uint64_t* set_disagree,
                   uint64_t* listing_ids, double* listing_d, uint64_t cap, uint64_t* nlisted);
 
-/* Context options (value 0 or 1):
- *   "symmetric"  RDF/RIPK-only passes take each pair of two centres once and
- *                credit both (default 1); 0 scans every centre's full ball.
- * Results are identical either way; the option exists to compare the two. */
+/* n-point correlations of the last pp_run with PP_NPCORR
+ * (src/PARAPROBE_SolverHdl.cpp:3899-3955, src/PARAPROBE_NPointCorrelations3D.cpp):
+ * per task a cubic histogram of edge = 1 + 2 (ceil(rmax / rincr) + 1) voxels
+ * a side, counts[task][z][y][x], of the difference vector (neighbour minus
+ * centre) of each centre's (order+1)-th nearest environment member within
+ * rmax, order = option "npcorr_order" (SpatStatKNNOrder - 1, default 0).
+ * Exact distance ties go to the lower ion id.  Histograms above 503^3 voxels
+ * are refused with PP_ERR_UNSUPPORTED, as the reference refuses them.  With
+ * counts == NULL only *edge is set. */
+int pp_fetch_npcorr(pp_ctx* ctx, uint32_t* counts, uint64_t cap, uint64_t* edge);
+
+/* Context options:
+ *   "symmetric"         RDF/RIPK-only passes take each pair of two centres
+ *                       once and credit both (default 1); 0 scans every
+ *                       centre's full ball.  Results are identical either way.
+ *   "npcorr_order"      SpatStatKNNOrder - 1 for PP_NPCORR (0..31, default 0).
+ *   "batched_pair_cap"  most pairs pp_run_batched holds at once; larger lists
+ *                       are built and applied a chunk of centres at a time
+ *                       (0 = sized from free device memory, the default). */
 int pp_set_option(pp_ctx* ctx, const char* name, int value);
 
 /* Results of the last pp_run (synchronises). cap = capacity in uint64. */

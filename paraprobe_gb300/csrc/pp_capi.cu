@@ -116,6 +116,10 @@ struct RunPlan {
   int cat_miss = 0;
   std::vector<float> catT;
   std::vector<uint16_t> lut;       // category by high bits of d^2 (see build_lut)
+  // n-point correlations: tasks per centre type with their local env set
+  std::vector<int> ntk, tk_task, tk_set;  // [nC], [nC][32], [nC][32]
+  int npc_half = 0, npc_K = 0;
+  uint32_t npc_edge = 0;
   int lut_shift = 0;
   uint32_t lut_base = 0;
   int disjoint = 0;
@@ -130,7 +134,7 @@ struct Result {
   uint32_t nbins = 0;
   int ntasks = 0;
   std::vector<uint32_t> trg, env;  // task masks
-  DevBuf rdf, knn, cnt, counters, status;
+  DevBuf rdf, knn, cnt, counters, status, npc;
   uint64_t ncentres_total = 0, n_ions = 0;
   std::vector<unsigned long long> counters_h;  // per realisation [pairs, centres]
   std::vector<uint64_t> centres_sel;           // per realisation (selected count, plain runs)
@@ -170,6 +174,7 @@ struct pp_ctx {
   uint64_t geo_pairs = 0;
   bool geo_emitted_all = false;  // the pair buffer holds every list (not one chunk's)
   uint64_t pair_cap_opt = 0;     // option "batched_pair_cap": most pairs held at once (0 = by free memory)
+  uint32_t npc_order = 0;        // option "npcorr_order": SpatStatKNNOrder - 1 of the n-point correlations
   DevBuf geo_counters;           // pair counters of the geometry passes
   int geo_H = 0;
   float geo_rmin = 0, geo_rincr = 0;
@@ -492,8 +497,7 @@ int ensure_surface(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s, const float*
 int make_plan(pp_ctx* ctx, uint32_t flags, const uint32_t* k_list, int nk, RunPlan& P) {
   if (!ctx->tasks_ok) return fail(ctx, PP_ERR_STATE, "pp_tasks_set was not called");
   if (!ctx->hist_ok) return fail(ctx, PP_ERR_STATE, "pp_hist_params was not called");
-  if (flags & PP_NPCORR) return fail(ctx, PP_ERR_UNSUPPORTED, "n-point correlations are not provided by this library");
-  if (flags & ~(PP_RDF | PP_1NN | PP_RIPK | PP_MKNN | PP_CNTNB)) return fail(ctx, PP_ERR_INVALID, "unknown flags");
+  if (flags & ~(PP_RDF | PP_1NN | PP_RIPK | PP_MKNN | PP_CNTNB | PP_NPCORR)) return fail(ctx, PP_ERR_INVALID, "unknown flags");
   const Tables& t = ctx->tab;
   if (t.nbins == 0) return fail(ctx, PP_ERR_INVALID, "histogram has no bins (rincr <= 1e-6 or rmax <= rmin)");
   if (t.nbins + 2 > 16384) return fail(ctx, PP_ERR_UNSUPPORTED, "more than 16382 bins");
@@ -550,7 +554,8 @@ int make_plan(pp_ctx* ctx, uint32_t flags, const uint32_t* k_list, int nk, RunPl
       if (!has_type(&ctx->trg[8 * k], P.ctype[c])) continue;
       if (std::find(local.begin(), local.end(), P.task_set[k]) == local.end()) local.push_back(P.task_set[k]);
     }
-    if (P.kr > 0 && local.size() > 32) return fail(ctx, PP_ERR_UNSUPPORTED, "more than 32 environment sets for one centre type");
+    if ((P.kr > 0 || (flags & PP_NPCORR)) && local.size() > 32)
+      return fail(ctx, PP_ERR_UNSUPPORTED, "more than 32 environment sets for one centre type");
     P.nsets[c] = (int)local.size();
     for (size_t p = 0; p < local.size() && p < 32; ++p) {
       P.set_list[c * 32 + p] = local[p];
@@ -570,6 +575,30 @@ int make_plan(pp_ctx* ctx, uint32_t flags, const uint32_t* k_list, int nk, RunPl
       if (__builtin_popcount(b) > 1) P.disjoint = 0;
       if (b) P.setidx[c * 256 + ty] = (int8_t)__builtin_ctz(b);
     }
+  if (flags & PP_NPCORR) {
+    // npc3d geometry (src/PARAPROBE_NPointCorrelations3D.cpp:53-73) and the
+    // size limit of src/PARAPROBE_SolverHdl.cpp:3706-3712
+    const float realhalf = std::ceil(t.rmax / t.rincr) + 1.f;
+    P.npc_half = (int)realhalf;
+    P.npc_edge = 1u + 2u * (uint32_t)P.npc_half;
+    const double nxyz = (double)P.npc_edge * P.npc_edge * P.npc_edge;
+    if (nxyz > 503.0 * 503.0 * 503.0)
+      return fail(ctx, PP_ERR_UNSUPPORTED, "Computation of 2-point statistics would require too large buffers");
+    P.npc_K = (int)ctx->npc_order + 1;
+    P.ntk.assign(std::max(P.nC, 1), 0);
+    P.tk_task.assign((size_t)std::max(P.nC, 1) * 32, -1);
+    P.tk_set.assign((size_t)std::max(P.nC, 1) * 32, -1);
+    for (int c = 0; c < P.nC; ++c)
+      for (int k = 0; k < nt; ++k) {
+        if (!has_type(&ctx->trg[8 * k], P.ctype[c])) continue;
+        if (P.ntk[c] == 32) return fail(ctx, PP_ERR_UNSUPPORTED, "more than 32 n-point correlation tasks per centre type");
+        int q = 0;
+        while (q < P.nsets[c] && P.set_list[c * 32 + q] != P.task_set[k]) ++q;
+        P.tk_task[c * 32 + P.ntk[c]] = k;
+        P.tk_set[c * 32 + P.ntk[c]] = q;
+        ++P.ntk[c];
+      }
+  }
   P.catT = threshold_table(t);
   build_lut(P.catT, t.rmax * t.rmax, 4096, P.lut, P.lut_shift, P.lut_base);
   P.cat_miss = category_of_distance(t, (float)((double)t.rmax + kEpsilon));
@@ -582,6 +611,7 @@ struct DevTables {
   uint16_t* lut;
   int8_t* setidx;
   int8_t* rowtab;
+  int* ntk; int* tk_task; int* tk_set;
 };
 
 int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
@@ -606,6 +636,9 @@ int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
   const int8_t* rows = pp::row_table_host(&nrow);
   const size_t o9 = put(rows, (size_t)nrow * 2);
   const size_t o10 = put(P.lut.data(), P.lut.size() * 2);
+  const size_t o11 = put(P.ntk.data(), P.ntk.size() * 4);
+  const size_t o12 = put(P.tk_task.data(), P.tk_task.size() * 4);
+  const size_t o13 = put(P.tk_set.data(), P.tk_set.size() * 4);
   CK(ctx->tables_dev.ensure(blob.size()));
   CK(cudaMemcpyAsync(ctx->tables_dev.p, blob.data(), blob.size(), cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));  // blob is a host temporary
@@ -615,6 +648,9 @@ int upload_tables(pp_ctx* ctx, const RunPlan& P, DevTables& D, cudaStream_t s) {
   D.setidx = (int8_t*)(b + o8);
   D.rowtab = (int8_t*)(b + o9);
   D.lut = (uint16_t*)(b + o10);
+  D.ntk = (int*)(b + o11);
+  D.tk_task = (int*)(b + o12);
+  D.tk_set = (int*)(b + o13);
   return PP_OK;
 }
 
@@ -761,6 +797,11 @@ int alloc_result(pp_ctx* ctx, const RunPlan& P, int nreal, bool batched, cudaStr
   if (P.flags & PP_CNTNB) {
     CK(R.cnt.ensure(cnt_sz * 8));
     CK(cudaMemsetAsync(R.cnt.p, 0, cnt_sz * 8, s));
+  }
+  if (P.flags & PP_NPCORR) {
+    const size_t npc_sz = std::max<size_t>((size_t)ctx->ntasks * P.npc_edge * P.npc_edge * P.npc_edge, 1);
+    CK(R.npc.ensure(npc_sz * 4));
+    CK(cudaMemsetAsync(R.npc.p, 0, npc_sz * 4, s));
   }
   CK(R.counters.ensure(16 * (size_t)nreal));
   CK(cudaMemsetAsync(R.counters.p, 0, 16 * (size_t)nreal, s));
@@ -1062,6 +1103,22 @@ int pp_cloud_inside(pp_ctx* ctx, int cloud, float bin_width_min, float bin_width
   return PP_OK;
 }
 
+int pp_fetch_npcorr(pp_ctx* ctx, uint32_t* counts, uint64_t cap, uint64_t* edge) {
+  if (!ctx || !ctx->res.valid || ctx->res.batched || !(ctx->res.plan.flags & PP_NPCORR))
+    return fail(ctx, PP_ERR_STATE, "no pass with PP_NPCORR");
+  const uint64_t e = ctx->res.plan.npc_edge;
+  const uint64_t need = (uint64_t)ctx->res.ntasks * e * e * e;
+  if (edge) *edge = e;
+  if (!counts) return PP_OK;
+  if (cap < need) return fail(ctx, PP_ERR_INVALID, "counts need %llu uint32", (unsigned long long)need);
+  CK(cudaStreamSynchronize(ctx->res.stream));
+  int st = 0;
+  CK(cudaMemcpy(&st, ctx->res.status.p, 4, cudaMemcpyDeviceToHost));
+  if (st) return fail(ctx, PP_ERR_DEVICE, "device status %d", st);
+  CK(cudaMemcpy(counts, ctx->res.npc.p, need * 4, cudaMemcpyDeviceToHost));
+  return PP_OK;
+}
+
 int pp_surfdist_fetch(pp_ctx* ctx, int cloud, float* out, uint64_t n) {
   Cloud* c = ctx ? get_cloud(ctx, cloud) : nullptr;
   if (!c || !out || n < c->n) return fail(ctx, PP_ERR_INVALID, "bad argument");
@@ -1206,6 +1263,28 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
       }
     }
     if (rc == -3) rc = pp::launch_scan(a, P.kr, P.emax, ctx->sm_count, &smem, s);
+    if (rc == 0 && (flags & PP_NPCORR)) {
+      pp::NpcArgs np{};
+      np.id_of_slot = cl->id_of_slot.as<uint32_t>();
+      np.K = P.npc_K;
+      np.ntk = D.ntk;
+      np.tk_task = D.tk_task;
+      np.tk_set = D.tk_set;
+      np.half = P.npc_half;
+      np.edge = P.npc_edge;
+      np.inv_w = 1.f / ctx->tab.rincr;
+      np.rmax = ctx->tab.rmax;
+      np.counts = ctx->res.npc.as<uint32_t>();
+      pp::ScanArgs an = a;
+      an.sample_stride = 0;
+      an.sym = 0;  // every centre needs its whole ball, not the pairs it owns
+      rc = pp::launch_npcorr(an, np, ctx->sm_count, s);
+      if (rc) {
+        CK(cudaEventRecord(ctx->ev1, s));
+        ctx->ev_recorded = true;
+        return fail(ctx, PP_ERR_CUDA, "n-point correlation launch failed");
+      }
+    }
     CK(cudaEventRecord(ctx->ev1, s));
     ctx->ev_recorded = true;
     if (rc == -2) return fail(ctx, PP_ERR_UNSUPPORTED, "no kernel variant for k=%d with %d environment sets", P.kmax, P.emax);
@@ -1353,6 +1432,11 @@ int pp_fp64_audit(pp_ctx* ctx, int cloud, uint32_t max_centres, double* max_abs,
 int pp_set_option(pp_ctx* ctx, const char* name, int value) {
   if (!ctx || !name) return PP_ERR_INVALID;
   if (std::strcmp(name, "symmetric") == 0) { ctx->no_sym = (value == 0); return PP_OK; }
+  if (std::strcmp(name, "npcorr_order") == 0) {
+    if (value < 0 || value > 31) return fail(ctx, PP_ERR_INVALID, "npcorr_order must be in [0, 31]");
+    ctx->npc_order = (uint32_t)value;
+    return PP_OK;
+  }
   if (std::strcmp(name, "batched_pair_cap") == 0) {
     if (value < 0) return fail(ctx, PP_ERR_INVALID, "batched_pair_cap must be >= 0");
     ctx->pair_cap_opt = (uint64_t)value;
@@ -1492,7 +1576,7 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
   if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
   if (n_label_sets < 0 || n_rois < 0 || (n_label_sets && !label_sets) || (n_rois && !rois))
     return fail(ctx, PP_ERR_INVALID, "bad realisation arguments");
-  if (flags & PP_CNTNB) return fail(ctx, PP_ERR_UNSUPPORTED, "PP_CNTNB is provided by pp_run only");
+  if (flags & (PP_CNTNB | PP_NPCORR)) return fail(ctx, PP_ERR_UNSUPPORTED, "PP_CNTNB and PP_NPCORR are provided by pp_run only");
   const int nreal = (include_original ? 1 : 0) + n_label_sets + n_rois;
   if (nreal == 0) return fail(ctx, PP_ERR_INVALID, "no realisation requested");
   CK(cudaSetDevice(ctx->device));

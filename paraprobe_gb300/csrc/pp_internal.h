@@ -220,6 +220,22 @@ int knn32_check(KnnArgs& k);
 int launch_knn_walk(const KnnArgs& k, int sm_count, cudaStream_t s);
 int launch_knn_bin(const KnnArgs& k, int sm_count, cudaStream_t s);
 
+// n-point correlations (AnalysisSpatDistrType 5): per centre and task, the
+// K-th nearest environment member's difference vector binned in a cubic grid
+struct NpcArgs {
+  const uint32_t* id_of_slot;       // ties in distance go to the lower ion id
+  int K;                            // SpatStatKNNOrder + 1 (<= 32)
+  const int* ntk;                   // [nC] tasks whose targets hold the centre type
+  const int* tk_task;               // [nC][32] those tasks
+  const int* tk_set;                // [nC][32] their environment set (local index)
+  int half;                         // histogram half edge (voxels)
+  uint32_t edge;                    // 1 + 2 half
+  float inv_w;                      // 1 / SpatStatRadiusIncr (float)
+  float rmax;                       // SpatStatRadiusMax: longer vectors are not binned
+  uint32_t* counts;                 // [ntasks][edge^3]
+};
+int launch_npcorr(const ScanArgs& a, const NpcArgs& p, int sm_count, cudaStream_t s);
+
 constexpr int kApplyThreads = 1024;
 // picks the realisation group and where kNN bins accumulate; -2 = no fit
 int apply_configure(ApplyArgs& a);

@@ -932,6 +932,95 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
   }
 }
 
+// ------------------------------------------------------- n-point correlations
+// One warp per centre (the pass's centre list).  For each environment set of
+// the centre type a shared list keeps the K smallest (d^2, ion id) keys with
+// their slots; afterwards every task whose targets hold the centre type bins
+// the difference vector (neighbour minus centre) of its set's K-th member as
+// npc3d::add does (src/PARAPROBE_NPointCorrelations3D.cpp:146-176): skipped
+// beyond SpatStatRadiusMax, each component times the float reciprocal of the
+// bin width, rounded half away from zero in double, offset by the half edge.
+__global__ void __launch_bounds__(256) k_npcorr(ScanArgs a, NpcArgs p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int K = p.K;
+  unsigned long long* keysA = (unsigned long long*)smem;                 // [nwarps][emax][32]
+  uint32_t* slotsA = (uint32_t*)(keysA + (size_t)nwarps * a.emax * 32);   // [nwarps][emax][32]
+  uint32_t* env = slotsA + (size_t)nwarps * a.emax * 32;                  // [nC][256]
+  int8_t* rowtab = (int8_t*)(env + a.nC * 256);
+  int8_t* scs = rowtab + ROW_TABLE_ENTRIES * 2;                           // 256
+  for (int i = threadIdx.x; i < a.nC * 256; i += blockDim.x) env[i] = a.envbits[i];
+  for (int i = threadIdx.x; i < ROW_TABLE_ENTRIES * 2; i += blockDim.x) rowtab[i] = a.rowtab[i];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) scs[i] = a.cslot_of[i];
+  __syncthreads();
+  unsigned long long* keys = keysA + (size_t)warp * a.emax * 32;
+  uint32_t* slots = slotsA + (size_t)warp * a.emax * 32;
+  const unsigned long long NONE = ~0ull;
+  const uint64_t nxy = (uint64_t)p.edge * p.edge, nxyz = nxy * p.edge;
+  for (uint32_t ci = blockIdx.x * nwarps + warp; ci < a.ncentres; ci += gridDim.x * nwarps) {
+    const uint32_t self = a.centres[ci];
+    const float4 cp = a.ions[self];
+    const uint32_t ct = a.labels ? (uint32_t)a.labels[self] : __float_as_uint(cp.w);
+    const int cs = scs[ct & 255];
+    if (cs < 0 || p.ntk[cs] == 0) continue;
+    const int nset = a.nsets[cs];
+    for (int e = lane; e < nset * 32; e += 32) { keys[e] = NONE; slots[e] = 0; }
+    __syncwarp();
+    for_each_candidate(a, rowtab, cp, self, lane,
+                       [&](bool valid, uint32_t slot, float d2, bool inball, uint32_t m, bool) {
+      (void)valid;
+      const uint32_t eb = inball ? env[cs * 256 + (m & 255)] : 0u;
+      const unsigned long long key =
+          eb ? (((unsigned long long)__float_as_uint(d2) << 32) | p.id_of_slot[slot]) : NONE;
+      for (int q = 0; q < nset; ++q) {
+        uint32_t mask = __ballot_sync(FULL, ((eb >> q) & 1u) && key < keys[q * 32 + K - 1]);
+        while (mask) {
+          const int src = __ffs(mask) - 1;
+          const unsigned long long x = __shfl_sync(FULL, key, src);
+          const uint32_t xs = __shfl_sync(FULL, slot, src);
+          unsigned long long* lk = keys + q * 32;
+          uint32_t* ls = slots + q * 32;
+          const unsigned long long v = lane < K ? lk[lane] : NONE;
+          const uint32_t vs = lane < K ? ls[lane] : 0u;
+          const int at = __popc(__ballot_sync(FULL, lane < K && v <= x));
+          const unsigned long long up = __shfl_up_sync(FULL, v, 1);
+          const uint32_t ups = __shfl_up_sync(FULL, vs, 1);
+          __syncwarp();
+          if (lane < K && lane >= at) {
+            lk[lane] = (lane == at) ? x : up;
+            ls[lane] = (lane == at) ? xs : ups;
+          }
+          __syncwarp();
+          mask &= ~(1u << src);
+          mask &= __ballot_sync(FULL, ((eb >> q) & 1u) && key < keys[q * 32 + K - 1]);
+        }
+      }
+    });
+    __syncwarp();
+    for (int i = lane; i < p.ntk[cs]; i += 32) {
+      const int t = p.tk_task[cs * 32 + i], q = p.tk_set[cs * 32 + i];
+      if (keys[q * 32 + K - 1] == NONE) continue;
+      const float4 nb = a.ions[slots[q * 32 + K - 1]];
+      const float c[3] = {__fsub_rn(nb.x, cp.x), __fsub_rn(nb.y, cp.y), __fsub_rn(nb.z, cp.z)};
+      const float d = sqrtf(__fadd_rn(__fadd_rn(__fmul_rn(c[0], c[0]), __fmul_rn(c[1], c[1])), __fmul_rn(c[2], c[2])));
+      if (!(d <= p.rmax)) continue;
+      int64_t b[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float there = __fmul_rn(c[k], p.inv_w);
+        const int disc = (there >= 0.f) ? (int)__dadd_rn((double)there, 0.5) : (int)__dsub_rn((double)there, 0.5);
+        b[k] = (int64_t)disc + p.half;
+      }
+      if (b[0] < 0 || b[1] < 0 || b[2] < 0 || b[0] >= p.edge || b[1] >= p.edge || b[2] >= p.edge) {
+        atomicOr(a.status, ST_BAD_SLOT);
+        continue;
+      }
+      atomicAdd(&p.counts[(uint64_t)t * nxyz + (uint64_t)b[0] + (uint64_t)b[1] * p.edge + (uint64_t)b[2] * nxy], 1u);
+    }
+    __syncwarp();
+  }
+}
+
 // -------------------------------------------------------- K3' brick scan
 // The same pass as k_scan, organised around bricks: a brick is up to bx
 // consecutive cells of one grid row, and a warp takes the centres of a brick
@@ -1986,6 +2075,21 @@ int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_
     if (emax <= 8) return launch_scan_t<4, 8>(a, sm_count, smem, s);
   }
   return -2;
+}
+
+int launch_npcorr(const ScanArgs& a, const NpcArgs& p, int sm_count, cudaStream_t s) {
+  const int nwarps = 8;
+  const size_t smem = (size_t)nwarps * a.emax * 32 * 12 + (size_t)a.nC * 256 * 4 + ROW_TABLE_ENTRIES * 2 + 256;
+  if (p.K < 1 || p.K > 32 || smem > 200 * 1024) return -2;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_npcorr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return -1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_npcorr, nwarps * 32, smem) != cudaSuccess || per_sm < 1)
+    return -1;
+  counted();
+  k_npcorr<<<sm_count * per_sm, nwarps * 32, smem, s>>>(a, p);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 size_t brick_smem(const ScanArgs& a, bool knn) {

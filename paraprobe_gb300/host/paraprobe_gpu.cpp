@@ -135,7 +135,6 @@ int main(int argc, char** argv) {
   const std::string bad = ppio::check_settings(S);
   if (!bad.empty()) { stopping("Control file settings failed the validity check! " + bad); return 3; }
   if (!S.spatstat) { reporting("No spatial statistics task to do"); return 0; }
-  if (S.do_npcorr) { stopping("n-point correlations (AnalysisSpatDistrType 5) are not provided"); return 4; }
   if (S.input_format != 1) { stopping("only POS input (InputFileformat 1) feeds this path"); return 4; }
   if (S.surface_mode != 0 && S.surface_mode != 4) {
     stopping("only SurfaceReconstructionType 0 (none) or 4 (existing VTK hull) are provided");
@@ -153,7 +152,16 @@ int main(int argc, char** argv) {
     return 3;
   }
   uint32_t flags = (S.do_rdf ? PP_RDF : 0u) | (S.do_1nn ? PP_1NN : 0u) | (S.do_ripk ? PP_RIPK : 0u) |
-                   (S.do_mknn ? PP_MKNN : 0u) | (S.do_cntnb ? PP_CNTNB : 0u);
+                   (S.do_mknn ? PP_MKNN : 0u) | (S.do_cntnb ? PP_CNTNB : 0u) | (S.do_npcorr ? PP_NPCORR : 0u);
+  if (S.do_npcorr) {
+    // the reference skips the whole statistics task when the n-point
+    // histogram would exceed 503^3 voxels (src/PARAPROBE_SolverHdl.cpp:3706-3712)
+    const double edge = 1.0 + 2.0 * (double)(uint64_t)(std::ceil(S.rmax / S.rincr) + 1.f);
+    if (edge * edge * edge > 503.0 * 503.0 * 503.0) {
+      std::cout << "WARNING::Computation of 2-point statistics would require too large buffers, skipping!" << std::endl;
+      return 0;
+    }
+  }
   if (plan_only) {
     std::cout << "{\"flags\": " << flags << ", \"rmin\": " << S.rmin << ", \"rincr\": " << S.rincr
               << ", \"rmax\": " << S.rmax << ", \"k\": [";
@@ -228,6 +236,7 @@ int main(int argc, char** argv) {
   }
   if (check(ctx, pp_tasks_set(ctx, trg.data(), env.data(), nt), "pp_tasks_set")) return 7;
   if (check(ctx, pp_hist_params(ctx, S.rmin, S.rincr, S.rmax), "pp_hist_params")) return 7;
+  if (S.do_npcorr && check(ctx, pp_set_option(ctx, "npcorr_order", (int)S.knn_order), "pp_set_option")) return 7;
   const uint32_t fl_run = flags & ~(uint32_t)((S.do_mknn && ks.empty()) ? PP_MKNN : 0u);
 
   auto pass = [&](const uint32_t* perm, bool randomized) -> int {
@@ -263,6 +272,28 @@ int main(int argc, char** argv) {
         for (size_t k = 0; k < ks.size(); ++k, o += H)
           ppio::write_report(outdir, S.sim_id, ppio::Report::MKNN, "MKNN" + std::to_string(ks[k]), tasks[t].trg_name(),
                              tasks[t].env_name(), hist(o), randomized, nions_inside, volume_inside);
+    if (fl_run & PP_NPCORR) {
+      // the reference writes these histograms to HDF5; here one raw file of
+      // edge^3 uint32 counts ([z][y][x], voxel size SpatStatRadiusIncr) per task
+      uint64_t e = 0;
+      if (check(ctx, pp_fetch_npcorr(ctx, nullptr, 0, &e), "pp_fetch_npcorr")) return 7;
+      const uint64_t per = e * e * e;
+      std::vector<uint32_t> cnt(std::max<uint64_t>(per * nt, 1));
+      if (check(ctx, pp_fetch_npcorr(ctx, cnt.data(), cnt.size(), &e), "pp_fetch_npcorr")) return 7;
+      for (int t = 0; t < nt; ++t) {
+        const std::string fn = outdir + "/PARAPROBE.SimID." + std::to_string(S.sim_id) + ".NPCORR." +
+                               tasks[t].trg_name() + "." + tasks[t].env_name() + "." +
+                               (randomized ? "Rndmized" : "Original") + "." + std::to_string(e) + "x" +
+                               std::to_string(e) + "x" + std::to_string(e) + ".u32";
+        FILE* f = std::fopen(fn.c_str(), "wb");
+        if (!f || std::fwrite(cnt.data() + (size_t)t * per, 4, per, f) != per) {
+          if (f) std::fclose(f);
+          stopping("cannot write " + fn);
+          return 7;
+        }
+        std::fclose(f);
+      }
+    }
     if (fl_run & PP_CNTNB) {
       uint64_t L = 0;
       if (check(ctx, pp_fetch_cntnb(ctx, nullptr, 0, &L), "pp_fetch_cntnb")) return 7;

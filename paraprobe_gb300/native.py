@@ -27,7 +27,7 @@ EXPORTS = (
     "pp_batched_stats", "pp_neighbors", "pp_shuffle_labels", "pp_device_info", "pp_kernel_launches",
     "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option", "pp_cloud_prepare",
     "pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_stats", "pp_server_destroy",
-    "pp_fp64_audit", "pp_surfdist_noalloc", "pp_batched_graph", "pp_cloud_inside",
+    "pp_fp64_audit", "pp_surfdist_noalloc", "pp_batched_graph", "pp_cloud_inside", "pp_fetch_npcorr",
 )
 
 _lib = None
@@ -90,6 +90,7 @@ def load():
         "pp_surfdist_noalloc": ([vp, u64, vp, u64, f32, vp, vp, C.c_char_p, C.c_size_t], i32),
         "pp_batched_graph": ([vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)], i32),
         "pp_cloud_inside": ([vp, i32, f32, f32, C.POINTER(u64), C.POINTER(f32), vp], i32),
+        "pp_fetch_npcorr": ([vp, vp, u64, C.POINTER(u64)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -318,6 +319,16 @@ class Context:
                                         _p(vox)), "pp_cloud_inside")
         return dict(nions_inside=nin.value, volume_inside=np.float32(vol.value), vacuum=int(vox[0]),
                     surface=int(vox[1]), inside=int(vox[2]), nx=int(vox[3]), ny=int(vox[4]), nz=int(vox[5]))
+
+    def fetch_npcorr(self):
+        """n-point correlation counts of the last pass: (ntasks, edge, edge, edge) uint32."""
+        e = C.c_uint64()
+        self._ck(self.L.pp_fetch_npcorr(self.h, None, 0, C.byref(e)), "pp_fetch_npcorr")
+        edge = e.value
+        ntasks = self.ntasks
+        out = np.zeros(max(ntasks * edge ** 3, 1), dtype=np.uint32)
+        self._ck(self.L.pp_fetch_npcorr(self.h, _p(out), out.size, C.byref(e)), "pp_fetch_npcorr")
+        return out[: ntasks * edge ** 3].reshape(ntasks, edge, edge, edge)
 
     def batched_graph(self):
         nodes, caps, launches = C.c_uint64(), C.c_uint64(), C.c_uint64()

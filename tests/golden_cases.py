@@ -8,7 +8,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 
-FLAG_OF_DIGIT = {"1": 1, "2": 2, "3": 4, "4": 8, "6": 32}
+FLAG_OF_DIGIT = {"1": 1, "2": 2, "3": 4, "4": 8, "5": 16, "6": 32}
 
 
 def names():
@@ -31,3 +31,11 @@ def load(name):
                 npcorr=z["npcorr"] if "npcorr" in z.files else np.zeros(0, np.uint32),
                 npcorr_order=int(c.get("knn_order", 1)) - 1,
                 bin_width=(np.float32(float(bw[0])), np.float32(float(bw[2]))))
+
+
+def task_index(c, filename):
+    """Task of a per-task output file, from the task names in its name."""
+    for t, (a, b) in enumerate(c["meta"]["names"]):
+        if f".{a}.{b}." in filename:
+            return t
+    raise KeyError(filename)

@@ -32,8 +32,16 @@ def test_cli_csv_identical(ctx, tmp_path, name, inside):
         cmd += ["--labels", "labels.u8"]
     r = subprocess.run(cmd, cwd=tmp_path, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr + r.stdout
-    produced = sorted(f for f in os.listdir(out) if ".FP64Audit." not in f)
+    produced = sorted(f for f in os.listdir(out) if f.endswith(".csv") and ".FP64Audit." not in f)
     assert produced == sorted(c["csv"].keys())
+    # n-point correlations: one raw uint32 file per task, as the reference's counts
+    raws = sorted(f for f in os.listdir(out) if ".NPCORR." in f)
+    if c["npcorr"].size:
+        got = np.concatenate([np.fromfile(out / f, dtype=np.uint32) for f in
+                              sorted(raws, key=lambda f: [G.task_index(c, f)])])
+        assert len(raws) == len(c["trg"]) and np.array_equal(got, c["npcorr"])
+    else:
+        assert not raws
     for f in produced:
         assert (out / f).read_text() == c["csv"][f], f
     # the FP64 audit beside the reports: small errors, every listed pair on an edge

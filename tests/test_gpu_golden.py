@@ -15,6 +15,7 @@ def test_gpu_matches_reference(ctx, name):
         ctx.hull(cid, c["hull"], 2.0)
     ctx.tasks(c["trg"], c["env"])
     ctx.hist(c["rmin"], c["rincr"], c["rmax"])
+    ctx.set_option("npcorr_order", c["npcorr_order"])
     ctx.run(cid, c["flags"], c["k"])
     out = ctx.fetch()
     st = ctx.stats()
@@ -27,6 +28,9 @@ def test_gpu_matches_reference(ctx, name):
     if L:
         cn = ctx.fetch_cntnb()
         assert np.array_equal(cn, c["cntnb"].reshape(len(c["trg"]), L))
+    if c["npcorr"].size:
+        npc = ctx.fetch_npcorr()
+        assert npc.size == c["npcorr"].size and np.array_equal(npc.reshape(-1), c["npcorr"])
     ctx.free(cid)
 
 

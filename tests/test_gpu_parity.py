@@ -353,3 +353,27 @@ def test_batched_32_lane_groups_and_rest(ctx, oracle, nsets):
         ref = oracle.spatstat(spec.xyz, lab, surf, 0.0, 0.02, 1.1, flags, trg, env, ks)
         assert np.array_equal(ctx.fetch_batched(r), ref["bins"]), r
     ctx.free(cid)
+
+
+@pytest.mark.parametrize("order", [0, 4])
+def test_npcorr_matches_oracle(ctx, oracle, order):
+    """n-point correlations (analysis mode 5) with overlapping environment sets,
+    beside RDF in the same pass."""
+    spec = synth.cone_specimen(n=25000, r_apex=8.0, half_angle_deg=10.0, length=12.0, n_clusters=12,
+                               members=40, nspecies=3, seed=81, nseg=64, stack=4.0)
+    trg, env = [[1], [2, 3], [3]], [[1, 2], [1, 2, 3], [1]]
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks(trg, env)
+    ctx.hist(0.0, 0.04, 1.1)
+    ctx.set_option("npcorr_order", order)
+    ctx.run(cid, N.PP_RDF | N.PP_NPCORR, [])
+    npc = ctx.fetch_npcorr()
+    rdf = ctx.fetch()
+    ctx.set_option("npcorr_order", 0)
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    ref = oracle.npcorr(spec.xyz, spec.labels, surf, 0.04, 1.1, trg, env, order)
+    assert ref.sum() > 0 and np.array_equal(npc, ref)
+    ref_rdf = oracle.spatstat(spec.xyz, spec.labels, surf, 0.0, 0.04, 1.1, N.PP_RDF, trg, env, [])
+    assert np.array_equal(rdf, ref_rdf["bins"])
+    ctx.free(cid)

@@ -43,7 +43,7 @@ def _plan(tmp_path, xml):
 
 def test_analysis_digit_rules(native_lib, tmp_path):
     (tmp_path / "x.rrng").write_text("[Ranges]\nRange1=1 2 Vol:0.1 Al:1 Color:0\nRange2=3 4 Vol:0.1 Sc:1 Color:0\n")
-    cases = {"1": 1, "14": 9, "1234": 15, "12346": None, "104": None, "6": 32, "26": 34}
+    cases = {"1": 1, "14": 9, "1234": 15, "12346": None, "104": None, "6": 32, "26": 34, "5": 16, "125": 19}
     for code, flags in cases.items():
         xml = _xml(tmp_path, analyses=code, tasks="Al-Sc", rmin="0", rincr="0.1", rmax="1", mknn="1;2")
         r = _plan(tmp_path, xml)
