@@ -135,7 +135,11 @@ int main(int argc, char** argv) {
   const std::string bad = ppio::check_settings(S);
   if (!bad.empty()) { stopping("Control file settings failed the validity check! " + bad); return 3; }
   if (!S.spatstat) { reporting("No spatial statistics task to do"); return 0; }
-  if (S.input_format != 1) { stopping("only POS input (InputFileformat 1) feeds this path"); return 4; }
+  if (S.input_format != 1 && !(S.input_format == 2 && S.recon_algo == 3)) {
+    stopping("only POS input (InputFileformat 1) or EPOS input with its own coordinates (InputFileformat 2, "
+             "ReconstructionAlgorithm 3) feeds this path");
+    return 4;
+  }
   if (S.surface_mode != 0 && S.surface_mode != 4) {
     stopping("only SurfaceReconstructionType 0 (none) or 4 (existing VTK hull) are provided");
     return 4;
@@ -183,17 +187,20 @@ int main(int argc, char** argv) {
 
   // ---- inputs
   std::vector<float> xyz, mq;
-  if (!ppio::read_pos(S.raw_file, xyz, mq)) { stopping("File " + S.raw_file + " cannot be read!"); return 5; }
-  const uint64_t n = mq.size();
-  // raw image for device ingest (big-endian records as in the file)
+  // raw image for device ingest: big-endian (x, y, z, m/q) records, as a POS
+  // file holds them (EPOS records are cut to their first 16 bytes)
   std::vector<uint8_t> raw;
-  {
+  if (S.input_format == 2) {
+    if (!ppio::read_epos_as_pos(S.raw_file, raw)) { stopping("File " + S.raw_file + " cannot be read!"); return 5; }
+  } else {
+    if (!ppio::read_pos(S.raw_file, xyz, mq)) { stopping("File " + S.raw_file + " cannot be read!"); return 5; }
     FILE* f = std::fopen(S.raw_file.c_str(), "rb");
-    raw.resize(n * 16);
+    raw.resize(mq.size() * 16);
     const size_t got = f ? std::fread(raw.data(), 1, raw.size(), f) : 0;
     if (f) std::fclose(f);
     if (got != raw.size()) { stopping("I/O failed on " + S.raw_file); return 5; }
   }
+  const uint64_t n = raw.size() / 16;
   std::vector<float> rlo, rhi;
   std::vector<uint8_t> rty;
   rng.flat(rlo, rhi, rty);

@@ -392,6 +392,23 @@ std::vector<Task> parse_tasks(const std::string& code, const Ranging& rng) {
 }
 
 // ---------------------------------------------------------------- readers
+bool read_epos_as_pos(const std::string& path, std::vector<uint8_t>& pos_image) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  std::fseek(f, 0, SEEK_END);
+  const long sz = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  if (sz < 0 || sz % 44) { std::fclose(f); return false; }
+  const size_t n = (size_t)sz / 44;
+  std::vector<uint8_t> raw((size_t)sz);
+  const size_t got = std::fread(raw.data(), 1, raw.size(), f);
+  std::fclose(f);
+  if (got != raw.size()) return false;
+  pos_image.resize(16 * n);
+  for (size_t i = 0; i < n; ++i) std::memcpy(&pos_image[16 * i], &raw[44 * i], 16);
+  return true;
+}
+
 bool read_pos(const std::string& path, std::vector<float>& xyz, std::vector<float>& mq) {
   FILE* f = std::fopen(path.c_str(), "rb");
   if (!f) return false;

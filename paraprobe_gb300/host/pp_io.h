@@ -74,6 +74,14 @@ struct Task {
 std::vector<Task> parse_tasks(const std::string& code, const Ranging& rng);
 
 bool read_pos(const std::string& path, std::vector<float>& xyz, std::vector<float>& mq);
+// An EPOS file (src/PARAPROBE_SolverHdl.cpp:6933-7040, EPOS record of
+// src/PARAPROBE_EPOSEndianness.h:87-140: 44-byte big-endian records of nine
+// floats x, y, z, m/q, tof, Vdc, Vpulse, detx, dety and two int32 pulse
+// fields) as the POS image of its reconstructed positions: per ion the first
+// 16 bytes (x, y, z, m/q), the coordinates ReconstructionAlgorithm 3 takes
+// as they are.  False if the file cannot be read or its size is not a
+// multiple of 44 bytes.
+bool read_epos_as_pos(const std::string& path, std::vector<uint8_t>& pos_image);
 bool read_vtk_hull(const std::string& path, std::vector<float>& tri);
 
 // One histogram as the reference holds it: counts per bin plus the dumps.

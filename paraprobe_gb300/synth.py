@@ -212,6 +212,20 @@ def write_pos(path: str, xyz: np.ndarray, mq: np.ndarray) -> None:
     rec.tofile(path)
 
 
+def write_epos(path: str, xyz: np.ndarray, mq: np.ndarray, seed: int = 11) -> None:
+    """EPOS file: 44-byte big-endian records, nine floats (x, y, z, m/q, tof,
+    Vdc, Vpulse, detx, dety) and two int32 (pulses since last, ions per
+    pulse); the detector fields are seeded filler."""
+    rng = np.random.default_rng(seed)
+    n = xyz.shape[0]
+    rec = np.zeros(n, dtype=[("f", ">f4", 9), ("i", ">i4", 2)])
+    rec["f"][:, :3] = xyz
+    rec["f"][:, 3] = mq
+    rec["f"][:, 4:] = rng.uniform(0.0, 1000.0, (n, 5)).astype(np.float32)
+    rec["i"][:] = rng.integers(0, 4, (n, 2))
+    rec.tofile(path)
+
+
 def read_pos(path: str):
     rec = np.fromfile(path, dtype=">f4").reshape(-1, 4).astype(np.float32)
     return np.ascontiguousarray(rec[:, :3]), np.ascontiguousarray(rec[:, 3])

@@ -54,3 +54,28 @@ def test_cli_csv_identical(ctx, tmp_path, name, inside):
     assert len(rows) == min(int(head["BinDisagreements"]) + int(head["InBallDisagreements"]), 1 << 16)
     for row in rows:
         assert abs(float(row[6])) <= 1e-6 * max(float(row[3]), 1e-3), row
+
+
+@pytest.mark.parametrize("name", ["cyl_basic", "npcorr"])
+def test_cli_epos_input(ctx, tmp_path, name):
+    """The same specimen given as an EPOS file (InputFileformat 2, coordinates
+    taken as they are: ReconstructionAlgorithm 3) gives the same CSV files."""
+    from paraprobe_gb300 import synth
+    c = G.load(name)
+    write_case(c, str(tmp_path))
+    stem = c["meta"]["case"]["name"]
+    synth.write_epos(str(tmp_path / (stem + ".epos")), c["xyz"], c["mq"])
+    xml = (tmp_path / "settings.xml").read_text()
+    xml = xml.replace("<InputFileformat>1<", "<InputFileformat>2<")
+    xml = xml.replace("<ReconstructionAlgorithm>2<", "<ReconstructionAlgorithm>3<")
+    xml = xml.replace(stem + ".pos<", stem + ".epos<")
+    assert "<InputFileformat>2<" in xml and ".epos<" in xml
+    (tmp_path / "settings.xml").write_text(xml)
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([CLI, "7", "settings.xml", "--outdir", str(out)], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr + r.stdout
+    produced = sorted(f for f in os.listdir(out) if f.endswith(".csv") and ".FP64Audit." not in f)
+    assert produced == sorted(c["csv"].keys())
+    for f in produced:
+        assert (out / f).read_text() == c["csv"][f], f
