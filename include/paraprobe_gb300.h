@@ -149,6 +149,19 @@ int pp_hist_params(pp_ctx* ctx, float rmin, float rincr, float rmax);
  * null model of rndlabeler, src/PARAPROBE_SolverHdl.cpp:2809-3003). */
 int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk,
            const uint32_t* label_perm, void* stream);
+/* Descriptive statistics after clustering, for the current histogram
+ * settings and hull (clustertask::flag2exclude_guard and generic_spatstat,
+ * src/PARAPROBE_SolverHdl.cpp:4790-4945).  clustered: n bytes in input order,
+ * nonzero = the ion belongs to a cluster.  Guard zone: every unclustered ion
+ * within R (float d^2 <= R^2) of a clustered ion.  Centres: unclustered,
+ * unguarded ions at least R from the hull; their neighbours: every unclustered
+ * ion within R, of any type.  flags: PP_RDF and PP_RIPK count every
+ * neighbour, PP_1NN the closest (a centre without one adds nothing).  The
+ * result is one task in the pp_fetch layout; the tasks set with pp_tasks_set
+ * stay as they were.  The reference's guard loop flags ions_kdtree.at(cand),
+ * the candidate's position in its result list, instead of the candidate
+ * itself (:4807-4815); this library flags the candidate. */
+int pp_run_aposteriori(pp_ctx* ctx, int cloud, const uint8_t* clustered, uint32_t flags, void* stream);
 /* Project-written autotuner: times the scan on about `sample` centres
  * (0 = 200000) for cell edges R/2 .. R/5, with the per-centre scan at block
  * tiles of 32, 128 and 512 centres and with the brick scan at bricks of 4, 8

@@ -67,6 +67,9 @@ def lib():
         L.ppo_npcorr.argtypes = [f32p, u8p, f32p, C.c_uint64, C.c_float, C.c_float, C.c_int, u32p, u32p,
                                  C.c_uint32, u32p, C.c_uint64, C.POINTER(C.c_uint64)]
         L.ppo_npcorr.restype = C.c_int
+        L.ppo_aposteriori.argtypes = [f32p, u8p, f32p, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_uint32,
+                                      u64p, C.c_uint64, u64p]
+        L.ppo_aposteriori.restype = C.c_int
         _lib = L
     return _lib
 
@@ -174,3 +177,20 @@ def npcorr(xyz, labels, ion2surf, rincr, rmax, trg, env, order):
     if rc:
         raise RuntimeError(f"ppo_npcorr failed ({rc})")
     return out.reshape(len(trg), edge, edge, edge)
+
+
+def aposteriori(xyz, clustered, ion2surf, rmin, rincr, rmax, analyses):
+    """Statistics after clustering: ({"rdf"|"1nn"|"ripk": (H,) uint64}, stats),
+    stats = (centres, guard ions, centres without an unclustered neighbour)."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float32)
+    clus = np.ascontiguousarray(clustered, dtype=np.uint8)
+    surf = np.ascontiguousarray(ion2surf, dtype=np.float32)
+    H = nbins(rmin, rincr, rmax) + 2
+    names = [nm for bit, nm in ((RDF, "rdf"), (NN1, "1nn"), (RIPK, "ripk")) if analyses & bit]
+    out = np.zeros(max(1, len(names)) * H, dtype=np.uint64)
+    st = np.zeros(3, dtype=np.uint64)
+    rc = lib().ppo_aposteriori(xyz.reshape(-1), clus, surf, xyz.shape[0], np.float32(rmin), np.float32(rincr),
+                               np.float32(rmax), analyses, out, out.size, st)
+    if rc:
+        raise RuntimeError(f"ppo_aposteriori failed ({rc})")
+    return {nm: out[i * H:(i + 1) * H].copy() for i, nm in enumerate(names)}, tuple(int(v) for v in st)

@@ -22,6 +22,8 @@
 //     VolumeInside (src/PARAPROBE_SolverHdl.cpp:5059-5386, 1471-1508; the
 //     outer vacuum is the face-connected cluster of empty voxels holding the
 //     guard corner, which src/PARAPROBE_HoshenKopelman.cpp labels)
+//   * the statistics after clustering, centres outside a guard zone about the
+//     clustered ions (src/PARAPROBE_SolverHdl.cpp:4790-4945)
 //
 // The restatement is pinned against the reference's own units compiled from
 // the read-only reference tree (oracle/ref/), through golden fixtures under
@@ -734,6 +736,92 @@ int ppo_npcorr(const float* xyz, const uint8_t* label, const float* ion2surf, ui
 #pragma omp critical
     for (uint64_t k = 0; k < mine.size(); ++k) out[k] += mine[k];
   }
+  return 0;
+}
+
+// Statistics after clustering (src/PARAPROBE_SolverHdl.cpp:4790-4945).
+// clustered[i] != 0 marks a cluster member.  Guard zone: every unclustered ion
+// within R (float d^2 <= R^2) of a clustered ion -- the intended rule; the
+// reference's loop flags ions_kdtree.at(cand), the candidate's position in
+// its result list, instead of the candidate (:4807-4815).  Centres:
+// unclustered, unguarded ions with ion2surf >= R^2; neighbours: unclustered
+// ions of any type.  RDF and RIPK add every neighbour distance, 1NN the
+// smallest one and nothing without one (:4886-4913).  out: [RDF][1NN][RIPK]
+// histograms (each present when asked), H = nbins + 2 uint64 each;
+// stats = {centres, guard ions, centres without a neighbour}.
+int ppo_aposteriori(const float* xyz, const uint8_t* clustered, const float* ion2surf, uint64_t n, float rmin,
+                    float rincr, float rmax, uint32_t analyses, uint64_t* out, uint64_t out_cap, uint64_t* stats) {
+  if (!xyz || !clustered || !ion2surf || !out) return -1;
+  Hist proto; proto.init(rmin, rincr, rmax);
+  const uint64_t H = proto.nbins + 2;
+  const bool doR = analyses & A_RDF, do1 = analyses & A_1NN, doK = analyses & A_RIPK;
+  if (H * ((doR ? 1 : 0) + (do1 ? 1 : 0) + (doK ? 1 : 0)) > out_cap) return -2;
+  const float R = rmax, RSQR = R * R;
+  // uniform grid with cells a little wider than R: the +-1 cell stencil holds
+  // every neighbour within R whatever the rounding of the cell coordinates
+  const float h = R * 1.001f;
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (uint64_t i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], xyz[3 * i + k]); hi[k] = std::max(hi[k], xyz[3 * i + k]); }
+  int64_t g[3];
+  for (int k = 0; k < 3; ++k) g[k] = n ? std::max<int64_t>(1, (int64_t)((hi[k] - lo[k]) / h) + 1) : 1;
+  auto cell_of = [&](uint64_t i, int k) {
+    return std::min<int64_t>(g[k] - 1, std::max<int64_t>(0, (int64_t)((xyz[3 * i + k] - lo[k]) / h)));
+  };
+  std::vector<std::vector<uint64_t>> cells((size_t)(g[0] * g[1] * g[2]));
+  for (uint64_t i = 0; i < n; ++i)
+    cells[(size_t)((cell_of(i, 2) * g[1] + cell_of(i, 1)) * g[0] + cell_of(i, 0))].push_back(i);
+  auto each_nb = [&](uint64_t i, auto&& f) {
+    const int64_t c0 = cell_of(i, 0), c1 = cell_of(i, 1), c2 = cell_of(i, 2);
+    for (int64_t z = std::max<int64_t>(0, c2 - 1); z <= std::min<int64_t>(g[2] - 1, c2 + 1); ++z)
+      for (int64_t y = std::max<int64_t>(0, c1 - 1); y <= std::min<int64_t>(g[1] - 1, c1 + 1); ++y)
+        for (int64_t x = std::max<int64_t>(0, c0 - 1); x <= std::min<int64_t>(g[0] - 1, c0 + 1); ++x)
+          for (uint64_t j : cells[(size_t)((z * g[1] + y) * g[0] + x)]) {
+            if (j == i) continue;
+            const float dx = xyz[3 * i] - xyz[3 * j], dy = xyz[3 * i + 1] - xyz[3 * j + 1],
+                        dz = xyz[3 * i + 2] - xyz[3 * j + 2];
+            const float d2 = (dx * dx + dy * dy) + dz * dz;
+            if (d2 <= RSQR) f(j, d2);
+          }
+  };
+  std::vector<uint8_t> guard(n, 0);
+  for (uint64_t i = 0; i < n; ++i)
+    if (clustered[i]) each_nb(i, [&](uint64_t j, float) { if (!clustered[j]) guard[j] = 1; });
+  uint64_t ncent = 0, nlost = 0, nguard = 0;
+  for (uint64_t i = 0; i < n; ++i) nguard += guard[i];
+  Hist hR = proto, h1 = proto, hK = proto;
+#pragma omp parallel
+  {
+    Hist mR = proto, m1 = proto, mK = proto;
+    uint64_t myc = 0, myl = 0;
+#pragma omp for schedule(dynamic, 256)
+    for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+      const uint64_t i = (uint64_t)ii;
+      if (!(ion2surf[i] >= RSQR) || clustered[i] || guard[i]) continue;
+      ++myc;
+      float closest = FLT_MAX;
+      bool any = false;
+      each_nb(i, [&](uint64_t j, float d2) {
+        if (clustered[j]) return;
+        const float d = std::sqrt(d2);
+        if (doR) mR.add(d);
+        if (doK) mK.add(d);
+        if (d <= closest) { closest = d; any = true; }
+      });
+      if (do1) { if (any) m1.add(closest); else ++myl; }
+    }
+#pragma omp critical
+    {
+      hR.merge(mR); h1.merge(m1); hK.merge(mK);
+      ncent += myc; nlost += myl;
+    }
+  }
+  uint64_t o = 0;
+  auto put = [&](const Hist& hh) { for (uint64_t b = 0; b < H; ++b) out[o++] = (uint64_t)hh.cnt[b]; };
+  if (doR) put(hR);
+  if (do1) put(h1);
+  if (doK) put(hK);
+  if (stats) { stats[0] = ncent; stats[1] = nguard; stats[2] = nlost; }
   return 0;
 }
 

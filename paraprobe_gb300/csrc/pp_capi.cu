@@ -1177,8 +1177,11 @@ int select_centres(pp_ctx* ctx, Cloud& cl, const uint8_t* labels, const float* s
 
 // One pass of compute_generic_spatstat3 on the device.  centre_limit > 0
 // restricts the pass to the first centres (cell order), for tuning.
+// labels_override (sorted-slot order) replaces the cloud's labels; no_miss
+// drops the kNN miss dump (a centre without a neighbour adds nothing).
 int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, int nk, const uint32_t* label_perm,
-              cudaStream_t s, uint32_t centre_limit) {
+              cudaStream_t s, uint32_t centre_limit, const uint8_t* labels_override = nullptr,
+              bool no_miss = false) {
   RunPlan P;
   int rc = make_plan(ctx, flags, k_list, nk, P);
   if (rc) return rc;
@@ -1201,6 +1204,7 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
                               ctx->labels_run.as<uint8_t>(), s);
     labels = ctx->labels_run.as<uint8_t>();
   }
+  if (labels_override) labels = labels_override;
   uint32_t ncent = 0;
   if ((rc = select_centres(ctx, *cl, labels, surf, D.cslot, R, &ncent, s))) return rc;
   // a tuning sample: every stride-th centre (or brick) over the whole cloud
@@ -1218,6 +1222,7 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   a.labels = labels;
   a.centres = ctx->centres.as<uint32_t>();
   a.ncentres = ncent;
+  if (no_miss) a.cat_miss = -1;
   a.flags = flags & (PP_RDF | PP_RIPK | PP_CNTNB);
   if (flags & PP_RIPK) a.flags |= PP_RDF;
   a.rdf_core = ctx->res.rdf.as<unsigned long long>();
@@ -1309,6 +1314,79 @@ int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int n
   if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
   CK(cudaSetDevice(ctx->device));
   return run_plain(ctx, cl, flags, k_list, nk, label_perm, (cudaStream_t)stream, 0);
+}
+
+// Statistics after clustering (clustertask::flag2exclude_guard and
+// generic_spatstat, src/PARAPROBE_SolverHdl.cpp:4790-4945).  The device labels
+// of this pass are 1 (neither clustered nor guard: centre and environment),
+// 2 (guard: environment only) and 3 (clustered: neither); one internal task
+// takes label 1 as targets and labels 1 and 2 as environment, so the plain
+// pass computes exactly the reference's per-centre loop.  The caller's tasks
+// are put back afterwards.
+int pp_run_aposteriori(pp_ctx* ctx, int cloud, const uint8_t* clustered, uint32_t flags, void* stream) {
+  if (!ctx) return PP_ERR_INVALID;
+  Cloud* cl = get_cloud(ctx, cloud);
+  if (!cl || !clustered) return fail(ctx, PP_ERR_INVALID, "bad argument");
+  if (!flags || (flags & ~(uint32_t)(PP_RDF | PP_1NN | PP_RIPK)))
+    return fail(ctx, PP_ERR_INVALID, "flags: a combination of PP_RDF, PP_1NN and PP_RIPK");
+  if (!ctx->hist_ok) return fail(ctx, PP_ERR_STATE, "pp_hist_params was not called");
+  CK(cudaSetDevice(ctx->device));
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint64_t n = cl->n;
+  const std::vector<uint32_t> keep_trg = ctx->trg, keep_env = ctx->env;
+  const int keep_nt = ctx->ntasks;
+  const bool keep_ok = ctx->tasks_ok;
+  ctx->trg.assign(8, 0u);
+  ctx->env.assign(8, 0u);
+  ctx->trg[0] = 1u << 1;
+  ctx->env[0] = (1u << 1) | (1u << 2);
+  ctx->ntasks = 1;
+  ctx->tasks_ok = true;
+  int rc = PP_OK;
+  do {
+    RunPlan P;
+    if ((rc = make_plan(ctx, flags, nullptr, 0, P))) break;
+    if ((rc = ensure_grid(ctx, *cl, ctx->tab.rmax, s))) break;
+    DevTables D{};
+    if ((rc = upload_tables(ctx, P, D, s))) break;
+    // [clustered flags by slot | guard flags, then labels | status word]
+    const uint64_t stat_off = (2 * n + 15) & ~uint64_t(15);
+    if (ctx->gather_src.ensure(std::max<uint64_t>(n, 1)) != cudaSuccess ||
+        ctx->perm_dev.ensure(stat_off + 16) != cudaSuccess) {
+      rc = fail(ctx, PP_ERR_NOMEM, "device allocation failed");
+      break;
+    }
+    uint8_t* clus = ctx->perm_dev.as<uint8_t>();
+    uint8_t* lab = clus + n;
+    int* gstat = reinterpret_cast<int*>(clus + stat_off);
+    if (cudaMemcpyAsync(ctx->gather_src.p, clustered, n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemsetAsync(lab, 0, n, s) != cudaSuccess || cudaMemsetAsync(gstat, 0, 4, s) != cudaSuccess) {
+      rc = fail(ctx, PP_ERR_CUDA, "copy of the cluster flags failed");
+      break;
+    }
+    pp::launch_gather_labels(ctx->gather_src.as<uint8_t>(), cl->id_of_slot.as<uint32_t>(), n, clus, 1, s);
+    pp::ScanArgs a{};
+    fill_scan_common(a, *cl, P, D, ctx->tab);
+    a.status = gstat;
+    pp::launch_guard(a, clus, lab, n, ctx->sm_count, s);
+    int st = 0;
+    if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&st, gstat, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      rc = fail(ctx, PP_ERR_CUDA, "guard zone pass failed");
+      break;
+    }
+    if (st) {
+      rc = fail(ctx, PP_ERR_DEVICE, "guard zone pass: device status %d", st);
+      break;
+    }
+    rc = run_plain(ctx, cl, flags, nullptr, 0, nullptr, s, 0, lab, true);
+  } while (false);
+  ctx->trg = keep_trg;
+  ctx->env = keep_env;
+  ctx->ntasks = keep_nt;
+  ctx->tasks_ok = keep_ok;
+  ctx->geo_cloud = -1;
+  return rc;
 }
 
 // Times the scan on the first `sample` centres for each candidate cell ratio

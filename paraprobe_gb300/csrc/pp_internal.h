@@ -235,6 +235,10 @@ struct NpcArgs {
   uint32_t* counts;                 // [ntasks][edge^3]
 };
 int launch_npcorr(const ScanArgs& a, const NpcArgs& p, int sm_count, cudaStream_t s);
+// guard zone of the clustered slots (clus != 0), then, in the same array, the
+// labels of the statistics after clustering: 1 free, 2 guard, 3 clustered
+void launch_guard(const ScanArgs& a, const uint8_t* clus, uint8_t* guard_then_labels, uint64_t n, int sm_count,
+                  cudaStream_t s);
 
 constexpr int kApplyThreads = 1024;
 // picks the realisation group and where kNN bins accumulate; -2 = no fit

@@ -820,7 +820,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
             auto emit = [&](int p, int kk, float v) {
               const int Sg = a.set_list[cs * 32 + p];
               const int cat = (v == kInf()) ? a.cat_miss : category_lut(v, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H);
-              atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
+              if (cat >= 0) atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
             };
             if constexpr (SL) {
               for (int p = 0; p < nset; ++p)
@@ -930,6 +930,34 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
       if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
     }
   }
+}
+
+// ------------------------------------------------- statistics after clustering
+// Guard zone about the clusters (clustertask::flag2exclude_guard,
+// src/PARAPROBE_SolverHdl.cpp:4790-4817): every ion that is not clustered and
+// lies within R (float d^2 <= R^2) of a clustered ion.  One warp per slot;
+// warps of unclustered slots move on at once.
+__global__ void __launch_bounds__(256) k_guard(ScanArgs a, const uint8_t* __restrict__ clus, uint8_t* guard,
+                                               uint64_t n) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t self = gw; self < n; self += nw) {
+    if (!clus[self]) continue;
+    const float4 cp = a.ions[self];
+    for_each_candidate(a, a.rowtab, cp, (uint32_t)self, lane,
+                       [&](bool, uint32_t slot, float, bool inball, uint32_t, bool) {
+                         if (inball && !clus[slot]) guard[slot] = 1;
+                       });
+  }
+}
+
+// labels of the statistics after clustering, in place over the guard flags:
+// 1 = neither clustered nor guard (centres and environment), 2 = guard
+// (environment only), 3 = clustered (neither)
+__global__ void k_cluster_labels(const uint8_t* __restrict__ clus, uint64_t n, uint8_t* guard_then_label) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    guard_then_label[i] = clus[i] ? 3 : (guard_then_label[i] ? 2 : 1);
 }
 
 // ------------------------------------------------------- n-point correlations
@@ -1270,7 +1298,7 @@ __global__ void __launch_bounds__(256) k_brick(ScanArgs a) {
               const int cat = (v == kInf()) ? a.cat_miss
                                             : category_lut(v, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
               const int Sg = a.set_list[cs * 32 + pp];
-              atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
+              if (cat >= 0) atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
             }
           }
           __syncwarp();
@@ -2075,6 +2103,14 @@ int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_
     if (emax <= 8) return launch_scan_t<4, 8>(a, sm_count, smem, s);
   }
   return -2;
+}
+
+void launch_guard(const ScanArgs& a, const uint8_t* clus, uint8_t* guard_then_labels, uint64_t n, int sm_count,
+                  cudaStream_t s) {
+  counted();
+  k_guard<<<sm_count * 8, 256, 0, s>>>(a, clus, guard_then_labels, n);
+  counted();
+  k_cluster_labels<<<grid_for(n, 256), 256, 0, s>>>(clus, n, guard_then_labels);
 }
 
 int launch_npcorr(const ScanArgs& a, const NpcArgs& p, int sm_count, cudaStream_t s) {

@@ -28,6 +28,7 @@ EXPORTS = (
     "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option", "pp_cloud_prepare",
     "pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_stats", "pp_server_destroy",
     "pp_fp64_audit", "pp_surfdist_noalloc", "pp_batched_graph", "pp_cloud_inside", "pp_fetch_npcorr",
+    "pp_run_aposteriori",
 )
 
 _lib = None
@@ -91,6 +92,7 @@ def load():
         "pp_batched_graph": ([vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)], i32),
         "pp_cloud_inside": ([vp, i32, f32, f32, C.POINTER(u64), C.POINTER(f32), vp], i32),
         "pp_fetch_npcorr": ([vp, vp, u64, C.POINTER(u64)], i32),
+        "pp_run_aposteriori": ([vp, i32, vp, u32, vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -319,6 +321,12 @@ class Context:
                                         _p(vox)), "pp_cloud_inside")
         return dict(nions_inside=nin.value, volume_inside=np.float32(vol.value), vacuum=int(vox[0]),
                     surface=int(vox[1]), inside=int(vox[2]), nx=int(vox[3]), ny=int(vox[4]), nz=int(vox[5]))
+
+    def run_aposteriori(self, cloud, clustered, flags, stream=0):
+        """Statistics after clustering; clustered: per ion in input order, nonzero = in a cluster.
+        The result (one task) is read with fetch()."""
+        cf = np.ascontiguousarray(clustered, dtype=np.uint8)
+        self._ck(self.L.pp_run_aposteriori(self.h, cloud, _p(cf), flags, C.c_void_p(stream)), "pp_run_aposteriori")
 
     def fetch_npcorr(self):
         """n-point correlation counts of the last pass: (ntasks, edge, edge, edge) uint32."""
