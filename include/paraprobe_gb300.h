@@ -63,6 +63,7 @@ extern "C" {
 #define PP_CNTNB 32u
 
 #define PP_TYPE_WORDS 8 /* 256 ion types */
+#define PP_TILE_LANES 0x100u /* tile code (b << 16) | PP_TILE_LANES: see pp_cloud_tuning */
 
 typedef struct pp_ctx pp_ctx;
 
@@ -176,8 +177,12 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
  * item; (b << 16) | c with b in 1..64 and c in 1..32 = the brick scan, a warp
  * taking up to c centres of b consecutive cells of a grid row together (used
  * for passes without CNTNB whose kNN, if any, has k <= 32 and disjoint
- * environment sets; other passes use the per-centre scan).  Results do not
- * depend on the tuning. */
+ * environment sets; other passes use the per-centre scan);
+ * ((bx | by << 8 | bz << 12) << 16) | PP_TILE_LANES with bx in 1..64 and by,
+ * bz in 0..15 (0 = 1) = blocks of bx x by x bz cells for the centre-per-lane
+ * scan that RDF / RIPK passes without CNTNB take (one centre per lane, the
+ * block's stencil ions staged in shared memory; default 4 x 2 x 2), leaving
+ * the other code as it was.  Results do not depend on the tuning. */
 int pp_cloud_tuning(pp_ctx* ctx, int cloud, float cell_ratio, uint32_t tile);
 
 /* FP64 audit of the current tasks and histogram settings on up to
@@ -208,6 +213,9 @@ int pp_fetch_npcorr(pp_ctx* ctx, uint32_t* counts, uint64_t cap, uint64_t* edge)
  *   "symmetric"         RDF/RIPK-only passes take each pair of two centres
  *                       once and credit both (default 1); 0 scans every
  *                       centre's full ball.  Results are identical either way.
+ *   "lanes"             RDF/RIPK-only passes take the centre-per-lane brick
+ *                       scan (default 1); 0 = the per-centre or brick scan.
+ *                       Results are identical either way.
  *   "npcorr_order"      SpatStatKNNOrder - 1 for PP_NPCORR (0..31, default 0).
  *   "batched_pair_cap"  most pairs pp_run_batched holds at once; larger lists
  *                       are built and applied a chunk of centres at a time

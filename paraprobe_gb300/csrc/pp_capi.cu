@@ -32,6 +32,8 @@ using pp::Grid;
 namespace {
 
 constexpr double kEpsilon = 1.0e-6;  // src/PARAPROBE_Numerics.h:44
+// cell block of the centre-per-lane scan
+constexpr uint32_t kLanesDefaultBx = 4, kLanesDefaultBy = 2, kLanesDefaultBz = 2;
 
 struct DevBuf {
   void* p = nullptr;
@@ -79,6 +81,9 @@ struct Cloud {
   // brick scan: (cells per brick << 16) | centres per warp batch; 0 = the
   // per-centre scan with `tile` centres per block work item
   uint32_t brick = 0;
+  // RDF / RIPK passes: cell block (x, y, z) of the centre-per-lane scan
+  // (0 = the defaults below)
+  uint32_t lanes_bx = 0, lanes_by = 0, lanes_bz = 0;
   Hull hull;
   DevBuf user_surf;             // input order, when given
   bool has_user_surf = false;
@@ -180,6 +185,7 @@ struct pp_ctx {
   float geo_rmin = 0, geo_rincr = 0;
   uint64_t grid_counter = 1;
   bool no_sym = false;  // testing hook: force the one-sided scan
+  bool no_lanes = false;  // option "lanes" = 0: RDF passes take the per-centre or brick scan
   pp_ctx* parent = nullptr;     // serving workers share the parent's clouds
   bool readonly_clouds = false; // ... and never rebuild them
   DevBuf surf_own;              // ion2surf for an R' the cloud does not cache
@@ -1253,7 +1259,23 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
     CK(cudaEventRecord(ctx->ev0, s));
     rc = -3;
     const Grid& g = cl->g;
-    if (cl->brick && (int)std::floor((R + 3.f * g.margin) * g.inv_h) + 1 <= 7) {
+    const bool rows_fit = (int)std::floor((R + 3.f * g.margin) * g.inv_h) + 1 <= 7;
+    if (rows_fit && !ctx->no_lanes && P.kr == 0 && !(flags & (PP_CNTNB | PP_NPCORR)) && (a.flags & PP_RDF)) {
+      a.bx = (int)(cl->lanes_bx ? cl->lanes_bx : kLanesDefaultBx);
+      a.by = (int)(cl->lanes_by ? cl->lanes_by : kLanesDefaultBy);
+      a.bz = (int)(cl->lanes_bz ? cl->lanes_bz : kLanesDefaultBz);
+      const uint64_t nb_x = ((uint64_t)g.nx + a.bx - 1) / a.bx, nb_y = ((uint64_t)g.ny + a.by - 1) / a.by;
+      uint64_t nb = nb_x * nb_y * (((uint64_t)g.nz + a.bz - 1) / a.bz);
+      if (stride > 1) nb = std::max<uint64_t>(1, nb / stride);
+      if (nb < (1ull << 32)) {
+        a.nbricks = (uint32_t)nb;
+        const uint32_t keep = a.tile;
+        a.tile = 4;  // bricks per warp work item
+        rc = pp::launch_lanes(a, P.kr, ctx->sm_count, &smem, s);
+        a.tile = keep;
+      }
+    }
+    if (rc == -3 && cl->brick && rows_fit) {
       a.bx = (int)(cl->brick >> 16);
       a.bcap = (int)(cl->brick & 0xffffu);
       const uint64_t nbx = ((uint64_t)g.nx + a.bx - 1) / a.bx;
@@ -1510,6 +1532,7 @@ int pp_fp64_audit(pp_ctx* ctx, int cloud, uint32_t max_centres, double* max_abs,
 int pp_set_option(pp_ctx* ctx, const char* name, int value) {
   if (!ctx || !name) return PP_ERR_INVALID;
   if (std::strcmp(name, "symmetric") == 0) { ctx->no_sym = (value == 0); return PP_OK; }
+  if (std::strcmp(name, "lanes") == 0) { ctx->no_lanes = (value == 0); return PP_OK; }
   if (std::strcmp(name, "npcorr_order") == 0) {
     if (value < 0 || value > 31) return fail(ctx, PP_ERR_INVALID, "npcorr_order must be in [0, 31]");
     ctx->npc_order = (uint32_t)value;
@@ -1527,7 +1550,14 @@ int pp_cloud_tuning(pp_ctx* ctx, int cloud, float cell_ratio, uint32_t tile) {
   Cloud* cl = ctx ? get_cloud(ctx, cloud) : nullptr;
   if (!cl || !(cell_ratio >= 1.0f && cell_ratio <= 8.0f) || tile == 0)
     return fail(ctx, PP_ERR_INVALID, "cell_ratio in [1, 8] and a tile code required");
-  if (tile >= 65536u) {
+  if (tile >= 65536u && (tile & 0xffffu) == PP_TILE_LANES) {
+    const uint32_t bx = (tile >> 16) & 0xffu, by = (tile >> 24) & 0xfu, bz = tile >> 28;
+    if (bx < 1 || bx > 64)
+      return fail(ctx, PP_ERR_INVALID, "centre-per-lane code: (bx | by << 8 | bz << 12) << 16, bx in [1, 64]");
+    cl->lanes_bx = bx;
+    cl->lanes_by = by ? by : 1;
+    cl->lanes_bz = bz ? bz : 1;
+  } else if (tile >= 65536u) {
     const uint32_t bx = tile >> 16, cap = tile & 0xffffu;
     if (bx < 1 || bx > 64 || cap < 1 || cap > 32)
       return fail(ctx, PP_ERR_INVALID, "brick code: cells per brick in [1, 64] << 16 | batch in [1, 32]");
@@ -2265,6 +2295,7 @@ int pp_server_create(pp_ctx* ctx, int slots, uint64_t budget_bytes, pp_server** 
     w->parent = ctx;
     w->readonly_clouds = true;
     w->no_sym = ctx->no_sym;
+    w->no_lanes = ctx->no_lanes;
     S->workers.push_back(w);
     S->streams.push_back(st);
   }

@@ -48,8 +48,10 @@ struct ScanArgs {
   const uint16_t* cat_lut;
   int lut_n, lut_shift;
   uint32_t lut_base;
-  // brick scan: cells per brick, centres per warp batch, bricks to process
+  // brick scan: cells per brick, centres per warp batch, bricks to process;
+  // the centre-per-lane scan takes blocks of bx x by x bz cells
   int bx, bcap;
+  int by, bz;
   uint32_t nbricks;
   // tuning samples: centre ci (brick b) of the pass is entry ci * stride
   // (b * stride) of the full list; 0 or 1 = every entry
@@ -182,6 +184,8 @@ int launch_tri_bins(const float* tbox, uint64_t ntri, Grid tg, float grow, uint3
 int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s);
 // the brick variant of k_scan; -3 when it does not apply to these arguments
 int launch_brick(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cudaStream_t s);
+// centre-per-lane brick scan of RDF / RIPK passes (k_lanes); -3 = not applicable
+int launch_lanes(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cudaStream_t s);
 int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s);
 // Batched kNN in two phases, 32 realisations per warp (one per lane).
 // Walk: per (centre, realisation) the category of the k-th member of every

@@ -1337,6 +1337,320 @@ __global__ void __launch_bounds__(256) k_brick(ScanArgs a) {
   }
 }
 
+// Ion range [st, st + len) of row r of the stencil of the cell block
+// [xb, xe) x [yb, ye) x [zb, ze): rows are (yy, zz) with yy in [yb - sr,
+// ye - 1 + sr] and zz in [zb - sr, ze - 1 + sr], r = (zz - zb + sr) * nry +
+// (yy - yb + sr), each trimmed in x to the block's reach; len = 0 when the row
+// cannot hold a neighbour of a point of the block.  In symmetric mode the
+// leading cells that precede the block's first cell in slot order and hold
+// only centres are dropped: their pairs with the block are taken from their
+// side (every ion of such a cell has a lower slot than every block centre).
+__device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nrows, int nry, int sr, int xb, int xe,
+                                                int yb, int ye, int zb, int ze, bool sym, uint32_t& st,
+                                                uint32_t& len) {
+  const Grid& g = a.g;
+  st = 0;
+  len = 0;
+  if (r >= nrows) return;
+  const int rz = r / nry, ry = r - rz * nry;
+  const int yy = yb - sr + ry, zz = zb - sr + rz;
+  if (yy < 0 || yy >= g.ny || zz < 0 || zz >= g.nz) return;
+  const float m2 = 2.f * g.margin;
+  const float Rp = a.R + g.margin, Rp2 = Rp * Rp;
+  const int cy = yy < yb ? yb - yy : (yy >= ye ? yy - (ye - 1) : 0);
+  const int cz = zz < zb ? zb - zz : (zz >= ze ? zz - (ze - 1) : 0);
+  const float gy = fmaxf(0.f, (float)(cy - 1) * g.h - m2);
+  const float gz = fmaxf(0.f, (float)(cz - 1) * g.h - m2);
+  const float rem = Rp2 - gy * gy - gz * gz;
+  if (rem < 0.f) return;
+  const float half = sqrtf(rem);
+  const int x0 = max(0, (int)floorf(((float)xb * g.h - m2 - half) * g.inv_h));
+  const int x1 = min(g.nx - 1, (int)floorf(((float)xe * g.h + m2 + half) * g.inv_h));
+  const uint64_t cb = ((uint64_t)zz * g.ny + yy) * g.nx;
+  int xs = x0;
+  if (sym) {
+    const bool own = (zz == zb && yy == yb);
+    if (own || zz < zb || (zz == zb && yy < yb)) {
+      const int xend = own ? min(x1, xb - 1) : x1;
+      if (xend >= x0 && a.nc_pre[cb + xend + 1] == a.nc_pre[cb + x0]) xs = xend + 1;
+    }
+  }
+  if (xs <= x1) {
+    st = a.cell_start[cb + xs];
+    len = a.cell_start[cb + x1 + 1] - st;
+  }
+}
+
+// ----------------------------------------------- K3'' centre-per-lane blocks
+// RDF / RIPK pass with one centre per lane.  A warp takes up to 32 centres of
+// a block of bx x by x bz cells (rows of the block in slot order) and streams
+// the block's stencil rows through a per-warp staging buffer, 32 ions at a
+// time; every lane then tests the 32 staged ions against its own centre and
+// keeps a 32-bit mask of the ions it takes.  A test is one broadcast shared
+// load, the exact d^2 and a predicated bit set -- no branch and no store; the
+// row mapping, the record load and the type lookups are paid once per staged
+// ion, not once per (centre, ion).  A compact block (cells of R/4 or so, a few
+// cells a side) keeps the staged region close to the union of the centres'
+// balls.  After each staged batch every lane walks its mask, recomputes d^2 of
+// the taken ions and bins them, so the bin lookup and the histogram atomics
+// run for in-ball pairs only.  Pair set, d^2 expression, bins and the
+// symmetric rule (a pair of two centres is taken by the lower slot and
+// credited to both) are those of k_scan; in symmetric mode a staged ion
+// carries key = its slot when it is a centre and 0xffffffff otherwise, and a
+// lane takes it when key > its own slot.  Warps fetch blocks `tile` at a time
+// from the global work counter, without block barriers.
+constexpr int kLanesWarps = 16;  // warps per block of k_lanes
+
+template <bool SYM>
+__global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
+  constexpr int NW = kLanesWarps;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int H = a.H;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned char* sp = smem;
+  unsigned long long* since_flush = (unsigned long long*)sp; sp += 16;
+  float4* candA = (float4*)sp; sp += NW * 32 * 16;
+  float4* cposA = (float4*)sp; sp += NW * 32 * 16;
+  uint32_t* ccodeA = (uint32_t*)sp; sp += NW * 32 * 4;
+  uint32_t* cinfoA = (uint32_t*)sp; sp += NW * 32 * 4;
+  uint16_t* plistA = (uint16_t*)sp; sp += NW * 1024 * 2;
+  float* sT = (float*)sp; sp += ((H + 3) & ~3) * 4;
+  uint32_t* srdf = (uint32_t*)sp; sp += (a.rdf_in_smem ? (size_t)a.nC * a.nE * H * 4 : 0);
+  uint16_t* slut = (uint16_t*)sp; sp += ((a.lut_n + 7) & ~7) * 2;
+  int8_t* scs = (int8_t*)sp; sp += 256;
+  int8_t* ses = (int8_t*)sp;
+  for (int i = threadIdx.x; i < H; i += blockDim.x) sT[i] = a.cat_T[i];
+  for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) slut[i] = a.cat_lut[i];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) { scs[i] = a.cslot_of[i]; ses[i] = a.eslot_of[i]; }
+  if (a.rdf_in_smem) for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) srdf[i] = 0;
+  if (threadIdx.x == 0) *since_flush = 0ull;
+  __syncthreads();
+
+  const Grid& g = a.g;
+  float4* cand = candA + warp * 32;
+  float4* cpos = cposA + warp * 32;     // centre of lane c
+  uint32_t* ccode = ccodeA + warp * 32;
+  uint32_t* cinfo = cinfoA + warp * 32; // lane c: centre slot * nE | (env slot + 1) << 16
+  uint16_t* plist = plistA + warp * 1024;  // the staged batch's pairs, (lane << 5) | staged index
+  const uint32_t lemask = (2u << lane) - 1u;
+  const float Rp = a.R + g.margin;
+  // rows up to sr cells away (in y or z) from the block can hold a neighbour
+  const int sr = (int)floorf((Rp + 2.f * g.margin) * g.inv_h) + 1;
+  const int BX = max(a.bx, 1), BY = max(a.by, 1), BZ = max(a.bz, 1);
+  const int nry = BY + 2 * sr, nrows = nry * (BZ + 2 * sr);
+  const uint32_t nbx = (uint32_t)((g.nx + BX - 1) / BX), nby = (uint32_t)((g.ny + BY - 1) / BY);
+  const float R2 = a.R2;
+  unsigned long long pairs_lane = 0, centres = 0;
+  constexpr unsigned long long FLUSH = 1ull << 30;
+  const uint32_t WT = max(a.tile, 1u);
+  for (;;) {
+    uint32_t w0 = 0;
+    if (lane == 0) w0 = atomicAdd(a.work, WT);
+    w0 = __shfl_sync(FULL, w0, 0);
+    if (w0 >= a.nbricks) break;
+    const uint32_t wend = min(w0 + WT, a.nbricks);
+    for (uint32_t wb = w0; wb < wend; ++wb) {
+      const uint32_t b = (a.sample_stride > 1) ? wb * a.sample_stride : wb;
+      const uint32_t bz_i = b / (nbx * nby), rest = b - bz_i * (nbx * nby);
+      const uint32_t by_i = rest / nbx, bx_i = rest - by_i * nbx;
+      const int xb = (int)bx_i * BX, yb = (int)by_i * BY, zb = (int)bz_i * BZ;
+      const int xe = min(xb + BX, g.nx), ye = min(yb + BY, g.ny), ze = min(zb + BZ, g.nz);
+      const int nseg = (ye - yb) * (ze - zb);
+      // centres: the block's row segments [cell_start(row, xb), cell_start(row, xe)) in slot order
+      int seg = 0;
+      uint32_t pos = 0, s1 = 0;
+      {
+        const uint64_t hrow = ((uint64_t)zb * g.ny + yb) * g.nx;
+        pos = a.cell_start[hrow + xb];
+        s1 = a.cell_start[hrow + xe];
+      }
+      for (;;) {
+        // ---- the next batch: lane l takes the l-th next centre of the block
+        int mc = 0;
+        uint32_t self = 0xffffffffu;
+        while (mc < 32) {
+          if (pos >= s1) {
+            if (++seg >= nseg) break;
+            const int sy = yb + seg % (ye - yb), sz = zb + seg / (ye - yb);
+            const uint64_t hrow = ((uint64_t)sz * g.ny + sy) * g.nx;
+            pos = a.cell_start[hrow + xb];
+            s1 = a.cell_start[hrow + xe];
+            continue;
+          }
+          const uint32_t sl = pos + lane;
+          const uint32_t cm = __ballot_sync(FULL, sl < s1 && a.cflag[sl] != 0);
+          const int room = 32 - mc, have = __popc(cm);
+          const uint32_t base = pos;
+          uint32_t takem = cm;
+          if (have > room) {
+            const int lastl = (int)__fns(cm, 0, room);
+            takem = cm & ((2u << lastl) - 1u);
+            pos += (uint32_t)lastl + 1u;
+          } else {
+            pos += 32u;
+          }
+          const int ntake = __popc(takem);
+          const int want = lane - mc;
+          if (want >= 0 && want < ntake) self = base + (uint32_t)__fns(takem, 0, want + 1);
+          mc += ntake;
+        }
+        if (mc == 0) break;
+        float4 cp = make_float4(kInf(), kInf(), kInf(), 0.f);
+        int cs = -1, es = -1;
+        if (self != 0xffffffffu) {
+          cp = a.ions[self];
+          const uint32_t ct = a.labels ? (uint32_t)a.labels[self] : __float_as_uint(cp.w);
+          cs = scs[ct & 255];
+          es = ses[ct & 255];
+          if (cs < 0) {  // selection guarantees a slot; record and drop the centre otherwise
+            atomicOr(a.status, ST_TYPE_RANGE);
+            cp = make_float4(kInf(), kInf(), kInf(), 0.f);
+            self = 0xffffffffu;
+          }
+        }
+        cpos[lane] = cp;
+        cinfo[lane] = (uint32_t)(cs < 0 ? 0 : cs) * (uint32_t)a.nE | ((uint32_t)(es + 1) << 16);
+        const uint32_t live = __ballot_sync(FULL, self != 0xffffffffu);
+        uint32_t inb = 0;
+        // ---- stencil rows of the block
+        for (int r0 = 0; r0 < nrows && live; r0 += 32) {
+          uint32_t st, len;
+          block_row_range(a, r0 + lane, nrows, nry, sr, xb, xe, yb, ye, zb, ze, SYM, st, len);
+          const uint32_t ne = __ballot_sync(FULL, len > 0);
+          const int cnt_rows = __popc(ne);
+          if (cnt_rows == 0) continue;
+          const int src = (lane < cnt_rows) ? (int)__fns(ne, 0, lane + 1) : 0;
+          const uint32_t rst = __shfl_sync(FULL, st, src);
+          uint32_t rlen = __shfl_sync(FULL, len, src);
+          if (lane >= cnt_rows) rlen = 0;
+          uint32_t inc = rlen;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc += t;
+          }
+          const uint32_t exc = inc - rlen;
+          const uint32_t total = __shfl_sync(FULL, inc, 31);
+          int before = 0;
+          for (uint32_t bb = 0; bb < total; bb += 32) {
+            // stage 32 ions: position, key, and (env slot + 1) | (centre slot + 1) << 8 | is-centre << 16;
+            // past the end an ion at infinity, which no lane takes
+            const uint32_t bitv = (lane < cnt_rows && rlen > 0 && exc >= bb && exc < bb + 32) ? (1u << (exc - bb)) : 0u;
+            const uint32_t smask = __reduce_or_sync(FULL, bitv);
+            const int row = before + __popc(smask & lemask) - 1;
+            before += __popc(smask);
+            const int rowc = row < 0 ? 0 : (row > 31 ? 31 : row);
+            const uint32_t rs = __shfl_sync(FULL, rst, rowc);
+            const uint32_t rp = __shfl_sync(FULL, exc, rowc);
+            const uint32_t t = bb + lane;
+            float4 q = make_float4(kInf(), kInf(), kInf(), 0.f);
+            uint32_t key = 0u, code = 0u;
+            if (t < total) {
+              const uint32_t slot = rs + (t - rp);
+              q = __ldg(a.ions + slot);
+              const uint32_t m = a.labels ? (uint32_t)a.labels[slot] : __float_as_uint(q.w);
+              const bool jc = SYM && a.cflag[slot] != 0;
+              key = SYM ? (jc ? slot : 0xffffffffu) : slot;
+              code = (uint32_t)(ses[m & 255] + 1) | (jc ? ((uint32_t)(scs[m & 255] + 1) << 8) | 0x10000u : 0u);
+            }
+            cand[lane] = make_float4(q.x, q.y, q.z, __uint_as_float(key));
+            ccode[lane] = code;
+            __syncwarp();
+            // ---- every lane tests the 32 staged ions against its centre
+            uint32_t tm = 0;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const float4 c = cand[j];
+              const float d2 = dist2(cp.x, cp.y, cp.z, c.x, c.y, c.z);
+              const uint32_t k = __float_as_uint(c.w);
+              const bool take = (d2 <= R2) && (SYM ? (k > self) : (k != self));
+              tm |= take ? (1u << j) : 0u;
+            }
+            // ---- bin the taken pairs: each lane lists its pairs at its offset in
+            // the batch's pair list, then the lanes take the list 64 at a time
+            const uint32_t np = __popc(tm);
+            uint32_t ex = np;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const uint32_t t = __shfl_up_sync(FULL, ex, o);
+              if (lane >= o) ex += t;
+            }
+            const uint32_t E = __shfl_sync(FULL, ex, 31);
+            inb += np;
+            for (uint32_t at = ex - np; tm; ++at) {
+              const int j = __ffs(tm) - 1;
+              tm &= tm - 1u;
+              plist[at] = (uint16_t)((lane << 5) | j);
+            }
+            __syncwarp();
+            auto bin_pair = [&](uint32_t e) {
+              const int c = (int)(e >> 5), j = (int)(e & 31u);
+              const float4 p = cpos[c];
+              const float4 q = cand[j];
+              const float d2 = dist2(p.x, p.y, p.z, q.x, q.y, q.z);
+              const uint32_t cj = ccode[j], ci = cinfo[c];
+              const int cat = category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+              const int esj = (int)(cj & 255u) - 1;
+              if (esj >= 0) {
+                const uint32_t idx = ((ci & 0xffffu) + (uint32_t)esj) * (uint32_t)H + (uint32_t)cat;
+                if (a.rdf_in_smem) atomicAdd(&srdf[idx], 1u);
+                else atomicAdd(&a.rdf_core[idx], 1ull);
+              }
+              if (SYM && (cj & 0x10000u)) {
+                // the same pair seen from the staged ion, a centre too
+                ++inb;
+                const int csj = (int)((cj >> 8) & 255u) - 1;
+                const int esc = (int)(ci >> 16) - 1;
+                if (esc >= 0 && csj >= 0) {
+                  const uint32_t idx = ((uint32_t)csj * a.nE + (uint32_t)esc) * (uint32_t)H + (uint32_t)cat;
+                  if (a.rdf_in_smem) atomicAdd(&srdf[idx], 1u);
+                  else atomicAdd(&a.rdf_core[idx], 1ull);
+                }
+              }
+            };
+            for (uint32_t k = lane; k < E; k += 64) {
+              const uint32_t e0 = plist[k];
+              const bool two = k + 32 < E;
+              const uint32_t e1 = two ? plist[k + 32] : 0u;
+              bin_pair(e0);
+              if (two) bin_pair(e1);
+            }
+            __syncwarp();
+          }
+        }
+        pairs_lane += inb;
+        if (lane == 0) centres += (unsigned long long)__popc(live);
+        if (a.rdf_in_smem) {
+          uint32_t tot = inb;
+          for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+          unsigned long long old = 0;
+          if (lane == 0) old = atomicAdd(since_flush, (unsigned long long)tot);
+          old = __shfl_sync(FULL, old, 0);
+          if (old / FLUSH != (old + tot) / FLUSH) {
+            for (int i = lane; i < a.nC * a.nE * H; i += 32) {
+              const uint32_t v = atomicExch(&srdf[i], 0u);
+              if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
+  }
+  for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
+  if (lane == 0) {
+    atomicAdd(&a.counters[0], pairs_lane);
+    atomicAdd(&a.counters[1], centres);
+  }
+  __syncthreads();
+  if (a.rdf_in_smem) {
+    for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) {
+      const uint32_t v = srdf[i];
+      if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
+    }
+  }
+}
+
 // --------------------------------------------------------------- K5 batched
 // One work item = (tile of geometry centres, group of G realisations).  Labels
 // and centre masks are stored group-major, G realisations interleaved per slot
@@ -2152,6 +2466,33 @@ int launch_brick(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cud
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem) != cudaSuccess || per_sm < 1) return -1;
   counted();
   kern<<<sm_count * per_sm, 256, smem, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+size_t lanes_smem(const ScanArgs& a) {
+  constexpr int NW = kLanesWarps;
+  size_t b = 16 + 2 * NW * 32 * 16 + 2 * NW * 32 * 4 + NW * 1024 * 2 + (size_t)((a.H + 3) & ~3) * 4;
+  if (a.rdf_in_smem) b += (size_t)a.nC * a.nE * a.H * 4;
+  b += (size_t)((a.lut_n + 7) & ~7) * 2 + 512;
+  return b;
+}
+
+int launch_lanes(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cudaStream_t s) {
+  if (a.mode != 0 || kr > 0 || (a.flags & PP_CNTNB) || !(a.flags & PP_RDF) || a.bx < 1 || a.by < 1 || a.bz < 1 ||
+      a.nC > 254 || a.nE > 254)
+    return -3;
+  const size_t smem = lanes_smem(a);
+  if (smem_used) *smem_used = smem;
+  if (smem > 200 * 1024) return -3;
+  auto kern = a.sym ? k_lanes<true> : k_lanes<false>;
+  if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return -1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kLanesWarps * 32, smem) != cudaSuccess ||
+      per_sm < 1)
+    return -1;
+  counted();
+  kern<<<sm_count * per_sm, kLanesWarps * 32, smem, s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

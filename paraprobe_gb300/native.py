@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libparaprobe_gb300.so")
 PP_RDF, PP_1NN, PP_RIPK, PP_MKNN, PP_NPCORR, PP_CNTNB = 1, 2, 4, 8, 16, 32
 PP_OK, PP_ERR_INVALID, PP_ERR_CUDA, PP_ERR_NOMEM, PP_ERR_UNSUPPORTED = 0, -1, -2, -3, -4
 PP_ERR_STATE, PP_ERR_OVERFLOW, PP_ERR_DEVICE, PP_ERR_IO = -5, -6, -7, -8
+PP_TILE_LANES = 0x100  # tile code (cells << 16) | PP_TILE_LANES: centre-per-lane scan of RDF/RIPK passes
 
 # every symbol include/paraprobe_gb300.h declares
 EXPORTS = (

@@ -276,8 +276,12 @@ def test_brick_scan(ctx, oracle, tile, ratio):
     trg, env = [[1], [2, 3], [3]], [[1, 2], [1, 2, 3], [1]]
     ctx.tasks(trg, env)
     ctx.hist(0.1, 0.02, 1.3)
-    ctx.run(cid, N.PP_RDF | N.PP_RIPK, [], label_perm=perm)
-    gpu, st = ctx.fetch(), ctx.stats()
+    ctx.set_option("lanes", 0)  # the RDF pass through the brick scan, not the centre-per-lane scan
+    try:
+        ctx.run(cid, N.PP_RDF | N.PP_RIPK, [], label_perm=perm)
+        gpu, st = ctx.fetch(), ctx.stats()
+    finally:
+        ctx.set_option("lanes", 1)
     ref = oracle.spatstat(spec.xyz, lab, surf, 0.1, 0.02, 1.3, N.PP_RDF | N.PP_RIPK, trg, env, [])
     assert st["pairs"] == ref["pairs"] and np.array_equal(gpu, ref["bins"])
     types = [1, 2, 3]
@@ -377,3 +381,56 @@ def test_npcorr_matches_oracle(ctx, oracle, order):
     ref_rdf = oracle.spatstat(spec.xyz, spec.labels, surf, 0.0, 0.04, 1.1, N.PP_RDF, trg, env, [])
     assert np.array_equal(rdf, ref_rdf["bins"])
     ctx.free(cid)
+
+
+def LANES(bx, by=1, bz=1):
+    """Tile code of the centre-per-lane scan: a block of bx x by x bz cells."""
+    return ((bx | by << 8 | bz << 12) << 16) | N.PP_TILE_LANES
+
+
+@pytest.mark.parametrize("block", [(1, 1, 1), (2, 1, 1), (4, 2, 2), (3, 3, 2), (8, 1, 3)])
+@pytest.mark.parametrize("ratio", [2.0, 3.5, 5.0])
+@pytest.mark.parametrize("symmetric", [1, 0])
+def test_lanes_scan(ctx, oracle, block, ratio, symmetric):
+    """The centre-per-lane block scan of RDF/RIPK passes against the oracle and
+    against the per-centre scan: overlapping target and environment sets, a
+    label permutation, a non-zero lower radius, the symmetric and the
+    one-sided pair rule."""
+    spec = synth.cone_specimen(n=50000, r_apex=8.0, half_angle_deg=10.0, length=18.0, n_clusters=25,
+                               members=40, nspecies=4, seed=61, nseg=64, stack=4.0)
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tuning(cid, ratio, LANES(*block))
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    perm = np.random.default_rng(sum(block) * 7 + int(ratio)).permutation(spec.xyz.shape[0]).astype(np.uint32)
+    trg, env = [[1], [2, 3], [4], [1, 2, 3, 4]], [[1, 2], [1, 2, 3], [1], [4]]
+    ctx.tasks(trg, env)
+    ctx.hist(0.1, 0.02, 1.4)
+    flags = N.PP_RDF | N.PP_RIPK
+    ctx.set_option("symmetric", symmetric)
+    try:
+        ctx.run(cid, flags, [], label_perm=perm)
+        lanes, st = ctx.fetch(), ctx.stats()
+        ctx.set_option("lanes", 0)
+        ctx.run(cid, flags, [], label_perm=perm)
+        scan, st2 = ctx.fetch(), ctx.stats()
+    finally:
+        ctx.set_option("lanes", 1)
+        ctx.set_option("symmetric", 1)
+    ctx.free(cid)
+    ref = oracle.spatstat(spec.xyz, spec.labels[perm], surf, 0.1, 0.02, 1.4, flags, trg, env, [])
+    assert st["pairs"] == ref["pairs"] == st2["pairs"] and st["centres"] == ref["centres"]
+    assert np.array_equal(lanes, ref["bins"]) and np.array_equal(scan, ref["bins"])
+
+
+def test_lanes_scan_rdf_bins_in_global_memory(ctx, oracle):
+    """Many tasks: the RDF cores do not fit shared memory and the
+    centre-per-lane scan adds to the global uint64 bins directly."""
+    spec = synth.cone_specimen(n=30000, r_apex=8.0, half_angle_deg=10.0, length=12.0, n_clusters=10,
+                               members=30, nspecies=8, seed=67, nseg=64, stack=4.0)
+    types = list(range(1, 9))
+    trg = [[a] for a in types for b in types]
+    env = [[b] for a in types for b in types]
+    gpu, st, ref, _ = _run_both(ctx, oracle, spec, 0.0, 0.002, 1.2, N.PP_RDF, trg, env, [])
+    assert st["pairs"] == ref["pairs"]
+    assert np.array_equal(gpu, ref["bins"])
