@@ -114,17 +114,17 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def traffic_bytes(workload_name):
-    """DRAM bytes per scan launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "k_scan_dram_traffic.md")
+def traffic_bytes(workload_name, kernel):
+    """DRAM bytes (read + write) per launch of `kernel` on the workload, from
+    the committed ncu summary profiles/dram_traffic.md, if it lists them."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        parts = line.strip().strip("|").split("|")
-        parts = [x.strip() for x in parts]
-        if len(parts) >= 3 and parts[0] == workload_name:
+        parts = [x.strip().strip("`") for x in line.strip().strip("|").split("|")]
+        if len(parts) >= 3 and parts[0] == workload_name and parts[1] == kernel:
             try:
-                return [float(x) for x in parts[1:3]]  # per pass
+                return float(parts[2])
             except ValueError:
                 continue
     return None
@@ -259,16 +259,19 @@ def run_gpu(args):
     ctx.hist(*heavy["hist"])
     ratio, tile = ctx.autotune(cid, heavy["flags"], heavy["k"], sample=200000)
 
+    pass_kernel = ["" for _ in runs]
+
     def step():
         pairs = 0
         kms = []
-        for r in runs:
+        for i, r in enumerate(runs):
             ctx.tasks(trg, env)
             ctx.hist(*r["hist"])
             ctx.run(cid, r["flags"], r["k"], stream=sh)
             ctx.fetch()
             pairs += ctx.stats()["pairs"]
             kms.append(ctx.last_kernel_ms())
+            pass_kernel[i] = ctx.last_kernel()
         return pairs, kms
 
     for _ in range(args.warmup):
@@ -352,16 +355,23 @@ def run_gpu(args):
            "d2h_bytes_per_step": int(d2h), "steps": e_steps,
            "includes": "upload + device grid build + hull distance + all passes + result fetch"}
 
-    # ---- roofline of the dominant kernel (k_scan), measured live
+    # ---- roofline of the dominant kernel (the pass with the longest launch),
+    # measured live with CUDA events around each launch on its stream
     peak, kind = peaks()
-    scan_s = sum(sum(m) for m in per_pass_ms) / 1e3
-    alg_bytes = sum(BYTES_PER_PAIR * per_pass_pairs[i] * len(per_pass_ms[i]) for i in range(len(runs)))
-    achieved = alg_bytes / scan_s / 1e9
-    tb = traffic_bytes(args.workload)
-    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(achieved / peak, 4), "peak_kind": kind,
-            "traffic": (None if tb is None else int(sum(tb) / len(tb))),
-            "kernel": "k_scan", "kernel_ms_per_pass": [round(statistics.mean(m), 3) for m in per_pass_ms],
+    per_pass = []
+    for i in range(len(runs)):
+        ms = statistics.mean(per_pass_ms[i])
+        ach = BYTES_PER_PAIR * per_pass_pairs[i] / (ms / 1e3) / 1e9
+        per_pass.append({"kernel": pass_kernel[i], "ms": round(ms, 3), "pairs": int(per_pass_pairs[i]),
+                         "achieved": round(ach, 1), "frac": round(ach / peak, 4),
+                         "traffic": traffic_bytes(args.workload, pass_kernel[i])})
+    dom = max(range(len(runs)), key=lambda i: per_pass[i]["ms"])
+    all_s = sum(p["ms"] for p in per_pass) / 1e3
+    all_ach = BYTES_PER_PAIR * sum(per_pass_pairs) / all_s / 1e9
+    roof = {"bound": "hbm", "achieved": per_pass[dom]["achieved"], "peak": peak, "unit": "GB/s",
+            "frac": per_pass[dom]["frac"], "peak_kind": kind, "traffic": per_pass[dom]["traffic"],
+            "kernel": per_pass[dom]["kernel"], "per_pass": per_pass,
+            "all_passes": {"achieved": round(all_ach, 1), "frac": round(all_ach / peak, 4)},
             "algorithmic_bytes_per_pair": BYTES_PER_PAIR}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -163,13 +163,15 @@ int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int n
  * the candidate's position in its result list, instead of the candidate
  * itself (:4807-4815); this library flags the candidate. */
 int pp_run_aposteriori(pp_ctx* ctx, int cloud, const uint8_t* clustered, uint32_t flags, void* stream);
-/* Project-written autotuner: times the scan on about `sample` centres
- * (0 = 200000) for cell edges R/2 .. R/5, with the per-centre scan at block
- * tiles of 32, 128 and 512 centres and with the brick scan at bricks of 4, 8
- * and 16 cells, keeps the fastest for this cloud and rebuilds its cell grid.
- * best_tile comes back in the pp_cloud_tuning encoding.  Uses the current
- * tasks and histogram settings; results of the trial runs are discarded.  Has
- * no counterpart in the reference (its KD-tree has no tuning). */
+/* Project-written autotuner: times the pass on about `sample` centres
+ * (0 = 200000) for cell edges R/2 .. R/5 -- for passes the centre-per-lane
+ * scan takes, at two cell-block shapes per edge; for other passes with the
+ * per-centre scan at block tiles of 32, 128 and 512 centres and with the
+ * brick scan at bricks of 4, 8 and 16 cells -- keeps the fastest for this
+ * cloud and rebuilds its cell grid.  best_tile comes back in the
+ * pp_cloud_tuning encoding.  Uses the current tasks and histogram settings;
+ * results of the trial runs are discarded.  Has no counterpart in the
+ * reference (its KD-tree has no tuning). */
 int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk,
                 uint32_t sample, float* best_ratio, uint32_t* best_tile);
 /* Set the tuning of a cloud directly: cell edge R / cell_ratio, and a tile
@@ -272,6 +274,11 @@ int pp_kernel_launches(uint64_t* count);
  * realisation pass of pp_run_batched), measured with CUDA events recorded
  * around that launch on the run's stream.  Synchronises. */
 int pp_last_kernel_ms(pp_ctx* ctx, float* ms);
+/* Name of the stencil kernel the last pp_run took: "k_scan" (per-centre
+ * scan), "k_brick" (brick scan), "k_lanes" (centre-per-lane scan of RDF /
+ * RIPK passes) or "k_lanes_knn" (centre-per-lane scan of kNN passes); a static
+ * string.  No counterpart in the reference. */
+int pp_last_kernel(pp_ctx* ctx, const char** name);
 
 /* Prepare a cloud for queries with r_lo <= rmax <= r_hi (r_hi <= 6 r_lo):
  * builds its cell grid with edge r_lo, the hull lists for R' up to

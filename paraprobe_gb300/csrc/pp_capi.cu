@@ -32,8 +32,6 @@ using pp::Grid;
 namespace {
 
 constexpr double kEpsilon = 1.0e-6;  // src/PARAPROBE_Numerics.h:44
-// cell block of the centre-per-lane scan
-constexpr uint32_t kLanesDefaultBx = 4, kLanesDefaultBy = 2, kLanesDefaultBz = 2;
 
 struct DevBuf {
   void* p = nullptr;
@@ -76,7 +74,7 @@ struct Cloud {
   DevBuf ions, cell_start, slot_of_id, id_of_slot, label_sorted;
   // hull / ion2surf
   // tuning (pp_autotune): cell edge = R / cell_ratio, centres per block tile
-  float cell_ratio = 3.0f;
+  float cell_ratio = 4.0f;
   uint32_t tile = 128;
   // brick scan: (cells per brick << 16) | centres per warp batch; 0 = the
   // per-centre scan with `tile` centres per block work item
@@ -84,6 +82,7 @@ struct Cloud {
   // RDF / RIPK passes: cell block (x, y, z) of the centre-per-lane scan
   // (0 = the defaults below)
   uint32_t lanes_bx = 0, lanes_by = 0, lanes_bz = 0;
+  uint64_t occupied = 0;  // non-empty cells of the grid
   Hull hull;
   DevBuf user_surf;             // input order, when given
   bool has_user_surf = false;
@@ -186,6 +185,8 @@ struct pp_ctx {
   uint64_t grid_counter = 1;
   bool no_sym = false;  // testing hook: force the one-sided scan
   bool no_lanes = false;  // option "lanes" = 0: RDF passes take the per-centre or brick scan
+  DevBuf brows;           // stencil rows of a cell block, nearest first (centre-per-lane scan)
+  int brows_key[3] = {-1, -1, -1};
   pp_ctx* parent = nullptr;     // serving workers share the parent's clouds
   bool readonly_clouds = false; // ... and never rebuild them
   DevBuf surf_own;              // ion2surf for an R' the cloud does not cache
@@ -197,6 +198,7 @@ struct pp_ctx {
   std::string apply_sig;
   uint64_t graph_nodes = 0, graph_captures = 0, graph_launches = 0;
   bool ev_recorded = false;
+  int last_kind = 0;  // kernel of the last plain pass: 0 per-centre scan, 1 brick, 2/3 centre-per-lane RDF/kNN
 };
 
 namespace {
@@ -371,10 +373,30 @@ int build_grid(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
                      ctx->tmp_rank.as<uint32_t>(), cl.cell_start.as<uint32_t>(), cl.ions.as<float4>(),
                      cl.slot_of_id.as<uint32_t>(), cl.id_of_slot.as<uint32_t>(), cl.label_sorted.as<uint8_t>(), s);
   CK(cudaGetLastError());
+  // non-empty cells: the default cell block of the centre-per-lane scans
+  unsigned long long occ = 0;
+  CK(ctx->work.ensure(16));
+  CK(cudaMemsetAsync(ctx->work.p, 0, 8, s));
+  pp::launch_count_occupied(cl.cell_start.as<uint32_t>(), g.ncells, ctx->work.as<unsigned long long>(),
+                            ctx->sm_count, s);
+  CK(cudaMemcpyAsync(&occ, ctx->work.p, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  cl.occupied = occ;
   cl.g = g;
   cl.grid_ok = true;
   cl.grid_version = ctx->grid_counter++;
   return PP_OK;
+}
+
+// Default cell block of the centre-per-lane scans: about 28 ions (a warp's
+// worth of centres) at the cloud's mean occupancy of non-empty cells, twice as
+// long in x as in y and z.
+void default_block(const Cloud& cl, int* bx, int* by, int* bz) {
+  const double per_cell = cl.occupied ? (double)cl.n / (double)cl.occupied : 1.0;
+  const double cells = std::max(1.0, 28.0 / std::max(per_cell, 1e-3));
+  const int side = (int)std::lround(std::cbrt(cells / 2.0));
+  *by = *bz = std::min(15, std::max(1, side));
+  *bx = (int)std::min(64L, std::max(1L, std::lround(cells / ((double)*by * *bz))));
 }
 
 // A grid serves every radius with R / h in [1, 6] (stencils of 3..13 cells a
@@ -1161,6 +1183,39 @@ int pp_hist_params(pp_ctx* ctx, float rmin, float rincr, float rmax) {
 
 namespace {
 
+// Stencil rows of a by x bz block of grid rows with sr rows on each side, as
+// (ry, rz) offsets from (yb - sr, zb - sr), ordered by the squared gap (in
+// cells) between the row and the block, then by rz and ry; cached per shape.
+int ensure_block_rows(pp_ctx* ctx, int by, int bz, int sr, cudaStream_t s, const int16_t** out) {
+  if (ctx->brows_key[0] != by || ctx->brows_key[1] != bz || ctx->brows_key[2] != sr) {
+    const int ny = by + 2 * sr, nz = bz + 2 * sr;
+    if (ny > 30000 || nz > 30000) return fail(ctx, PP_ERR_UNSUPPORTED, "cell block too large");
+    auto gap = [sr](int r, int b) { return r < sr ? sr - r : (r >= sr + b ? r - (sr + b - 1) : 0); };
+    std::vector<std::pair<int, int>> order;
+    order.reserve((size_t)ny * nz);
+    for (int rz = 0; rz < nz; ++rz)
+      for (int ry = 0; ry < ny; ++ry) {
+        const int gy = gap(ry, by), gz = gap(rz, bz);
+        order.push_back({gy * gy + gz * gz, rz * ny + ry});
+      }
+    std::stable_sort(order.begin(), order.end(),
+                     [](const std::pair<int, int>& x, const std::pair<int, int>& y) { return x.first < y.first; });
+    std::vector<int16_t> tab(order.size() * 2);
+    for (size_t i = 0; i < order.size(); ++i) {
+      tab[2 * i] = (int16_t)(order[i].second % ny);
+      tab[2 * i + 1] = (int16_t)(order[i].second / ny);
+    }
+    CK(ctx->brows.ensure(tab.size() * 2));
+    CK(cudaMemcpyAsync(ctx->brows.p, tab.data(), tab.size() * 2, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    ctx->brows_key[0] = by;
+    ctx->brows_key[1] = bz;
+    ctx->brows_key[2] = sr;
+  }
+  *out = ctx->brows.as<int16_t>();
+  return PP_OK;
+}
+
 // Select the centres of a plain run into ctx->centres (cell order); returns
 // their number.  Synchronises the stream once to learn the count.
 int select_centres(pp_ctx* ctx, Cloud& cl, const uint8_t* labels, const float* surf, const int8_t* cslot, float R,
@@ -1256,14 +1311,24 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   ctx->ev_recorded = false;
   if (ncent > 0) {
     size_t smem = 0;
-    CK(cudaEventRecord(ctx->ev0, s));
-    rc = -3;
     const Grid& g = cl->g;
     const bool rows_fit = (int)std::floor((R + 3.f * g.margin) * g.inv_h) + 1 <= 7;
+    // centre-per-lane scans: cell block and its stencil rows
+    if (cl->lanes_bx) {
+      a.bx = (int)cl->lanes_bx;
+      a.by = (int)std::max<uint32_t>(cl->lanes_by, 1);
+      a.bz = (int)std::max<uint32_t>(cl->lanes_bz, 1);
+    } else {
+      default_block(*cl, &a.bx, &a.by, &a.bz);
+    }
+    a.bsr = (int)std::floor(((R + g.margin) + 2.f * g.margin) * g.inv_h) + 1;
+    a.brows = nullptr;
+    if (rows_fit && !ctx->no_lanes && !(flags & (PP_CNTNB | PP_NPCORR)) &&
+        (rc = ensure_block_rows(ctx, a.by, a.bz, a.bsr, s, &a.brows)) != PP_OK)
+      return rc;
+    CK(cudaEventRecord(ctx->ev0, s));
+    rc = -3;
     if (rows_fit && !ctx->no_lanes && P.kr == 0 && !(flags & (PP_CNTNB | PP_NPCORR)) && (a.flags & PP_RDF)) {
-      a.bx = (int)(cl->lanes_bx ? cl->lanes_bx : kLanesDefaultBx);
-      a.by = (int)(cl->lanes_by ? cl->lanes_by : kLanesDefaultBy);
-      a.bz = (int)(cl->lanes_bz ? cl->lanes_bz : kLanesDefaultBz);
       const uint64_t nb_x = ((uint64_t)g.nx + a.bx - 1) / a.bx, nb_y = ((uint64_t)g.ny + a.by - 1) / a.by;
       uint64_t nb = nb_x * nb_y * (((uint64_t)g.nz + a.bz - 1) / a.bz);
       if (stride > 1) nb = std::max<uint64_t>(1, nb / stride);
@@ -1272,6 +1337,23 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
         const uint32_t keep = a.tile;
         a.tile = 4;  // bricks per warp work item
         rc = pp::launch_lanes(a, P.kr, ctx->sm_count, &smem, s);
+        if (rc == 0) ctx->last_kind = 2;
+        a.tile = keep;
+      }
+    }
+    // kNN-only passes (with RDF in the same pass every in-ball pair would be
+    // walked per lane; the per-centre scan does that pass better)
+    if (rc == -3 && rows_fit && !ctx->no_lanes && P.kr > 0 && !(a.flags & PP_RDF) &&
+        !(flags & (PP_CNTNB | PP_NPCORR))) {
+      const uint64_t nb_x = ((uint64_t)g.nx + a.bx - 1) / a.bx, nb_y = ((uint64_t)g.ny + a.by - 1) / a.by;
+      uint64_t nb = nb_x * nb_y * (((uint64_t)g.nz + a.bz - 1) / a.bz);
+      if (stride > 1) nb = std::max<uint64_t>(1, nb / stride);
+      if (nb < (1ull << 32)) {
+        a.nbricks = (uint32_t)nb;
+        const uint32_t keep = a.tile;
+        a.tile = 4;  // blocks per warp work item
+        rc = pp::launch_lanes_knn(a, P.disjoint != 0, ctx->sm_count, &smem, s);
+        if (rc == 0) ctx->last_kind = 3;
         a.tile = keep;
       }
     }
@@ -1286,10 +1368,14 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
         const uint32_t keep = a.tile;
         a.tile = 16;
         rc = pp::launch_brick(a, P.kr, ctx->sm_count, &smem, s);
+        if (rc == 0) ctx->last_kind = 1;
         a.tile = keep;
       }
     }
-    if (rc == -3) rc = pp::launch_scan(a, P.kr, P.emax, ctx->sm_count, &smem, s);
+    if (rc == -3) {
+      rc = pp::launch_scan(a, P.kr, P.emax, ctx->sm_count, &smem, s);
+      ctx->last_kind = 0;
+    }
     if (rc == 0 && (flags & PP_NPCORR)) {
       pp::NpcArgs np{};
       np.id_of_slot = cl->id_of_slot.as<uint32_t>();
@@ -1421,34 +1507,66 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
   if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
   CK(cudaSetDevice(ctx->device));
   if (sample == 0) sample = 200000;
-  const float ratios[] = {2.0f, 3.0f, 4.0f, 5.0f};
-  // per-centre tiles, then brick codes (cells per brick << 16 | batch)
-  const uint32_t tiles[] = {32, 128, 512, (4u << 16) | 16u, (8u << 16) | 16u, (8u << 16) | 32u, (16u << 16) | 32u};
-  float bestr = cl->cell_ratio, bestms = 1e30f;
-  uint32_t bestt = cl->brick ? cl->brick : cl->tile;
   const float R = ctx->tab.rmax;
-  for (float r : ratios) {
-    cl->cell_ratio = r;
-    int rc = build_grid(ctx, *cl, R, 0);
-    if (rc) return rc;
-    for (uint32_t t : tiles) {
-      if (t >= 65536u) cl->brick = t;
-      else { cl->tile = t; cl->brick = 0; }
-      float ms = 0.f;
-      for (int rep = 0; rep < 2; ++rep) {  // first repetition warms caches and lazy state
-        rc = run_plain(ctx, cl, flags, k_list, nk, nullptr, 0, sample);
-        if (rc) return rc;
-        rc = pp_last_kernel_ms(ctx, &ms);
-        if (rc) return rc;
-      }
-      if (ms < bestms) { bestms = ms; bestr = r; bestt = t; }
+  const float ratios[] = {2.0f, 3.0f, 4.0f, 5.0f};
+  auto lanes_code = [](uint32_t bx, uint32_t by, uint32_t bz) {
+    return ((bx | by << 8 | bz << 12) << 16) | PP_TILE_LANES;
+  };
+  // passes the centre-per-lane scan takes: cell blocks of about 2 x 1 x 1 R/2
+  // (a few tens of centres at atom-probe densities) for each cell edge
+  const uint32_t lanes_tiles[4][2] = {{lanes_code(2, 1, 1), lanes_code(2, 2, 1)},
+                                      {lanes_code(3, 2, 2), lanes_code(2, 2, 2)},
+                                      {lanes_code(4, 2, 2), lanes_code(4, 3, 3)},
+                                      {lanes_code(5, 3, 3), lanes_code(4, 4, 4)}};
+  // other passes: per-centre tiles, then brick codes (cells per brick << 16 | batch)
+  const uint32_t scan_tiles[] = {32, 128, 512, (4u << 16) | 16u, (8u << 16) | 16u, (8u << 16) | 32u,
+                                 (16u << 16) | 32u};
+  const float keep_ratio = cl->cell_ratio;
+  const uint32_t keep[5] = {cl->tile, cl->brick, cl->lanes_bx, cl->lanes_by, cl->lanes_bz};
+  auto apply = [&](uint32_t t) {
+    if (t >= 65536u && (t & 0xffffu) == PP_TILE_LANES) {
+      cl->lanes_bx = (t >> 16) & 0xffu;
+      cl->lanes_by = (t >> 24) & 0xfu;
+      cl->lanes_bz = t >> 28;
+    } else if (t >= 65536u) {
+      cl->brick = t;
+    } else {
+      cl->tile = t;
+      cl->brick = 0;
     }
+  };
+  float bestr = keep_ratio, bestms = 1e30f;
+  uint32_t bestt = 0;
+  int rc = PP_OK;
+  for (int ri = 0; ri < 4 && rc == PP_OK; ++ri) {
+    cl->cell_ratio = ratios[ri];
+    if ((rc = build_grid(ctx, *cl, R, 0))) break;
+    // which kernel does this pass take at this cell edge?
+    cl->lanes_bx = cl->lanes_by = cl->lanes_bz = 0;
+    if ((rc = run_plain(ctx, cl, flags, k_list, nk, nullptr, 0, sample))) break;
+    const bool lanes = ctx->last_kind >= 2;
+    const uint32_t* tiles = lanes ? lanes_tiles[ri] : scan_tiles;
+    const int ntiles = lanes ? 2 : (int)(sizeof scan_tiles / sizeof scan_tiles[0]);
+    for (int ti = 0; ti < ntiles && rc == PP_OK; ++ti) {
+      apply(tiles[ti]);
+      float ms = 0.f;
+      for (int rep = 0; rep < 2 && rc == PP_OK; ++rep) {  // first repetition warms caches and lazy state
+        if ((rc = run_plain(ctx, cl, flags, k_list, nk, nullptr, 0, sample))) break;
+        rc = pp_last_kernel_ms(ctx, &ms);
+      }
+      if (rc == PP_OK && ms < bestms) { bestms = ms; bestr = ratios[ri]; bestt = tiles[ti]; }
+    }
+    if (lanes) { cl->lanes_bx = keep[2]; cl->lanes_by = keep[3]; cl->lanes_bz = keep[4]; }
+    else { cl->tile = keep[0]; cl->brick = keep[1]; }
+  }
+  if (rc != PP_OK) {
+    cl->cell_ratio = keep_ratio;
+    build_grid(ctx, *cl, R, 0);
+    return rc;
   }
   cl->cell_ratio = bestr;
-  if (bestt >= 65536u) cl->brick = bestt;
-  else { cl->tile = bestt; cl->brick = 0; }
-  int rc = build_grid(ctx, *cl, R, 0);
-  if (rc) return rc;
+  if (bestt) apply(bestt);
+  if ((rc = build_grid(ctx, *cl, R, 0))) return rc;
   ctx->res.valid = false;
   if (best_ratio) *best_ratio = bestr;
   if (best_tile) *best_tile = bestt;
@@ -2113,6 +2231,13 @@ int pp_last_kernel_ms(pp_ctx* ctx, float* ms) {
   if (!ctx->ev_recorded) { *ms = 0.f; return PP_OK; }
   CK(cudaEventSynchronize(ctx->ev1));
   CK(cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+  return PP_OK;
+}
+
+int pp_last_kernel(pp_ctx* ctx, const char** name) {
+  if (!ctx || !name) return PP_ERR_INVALID;
+  static const char* names[] = {"k_scan", "k_brick", "k_lanes", "k_lanes_knn"};
+  *name = names[ctx->last_kind < 0 || ctx->last_kind > 3 ? 0 : ctx->last_kind];
   return PP_OK;
 }
 

@@ -53,6 +53,10 @@ struct ScanArgs {
   int bx, bcap;
   int by, bz;
   uint32_t nbricks;
+  // centre-per-lane scan: stencil rows of a block, (ry, rz) offsets from
+  // (yb - bsr, zb - bsr), nearest to the block first; bsr rows each side
+  const int16_t* brows;
+  int bsr;
   // tuning samples: centre ci (brick b) of the pass is entry ci * stride
   // (b * stride) of the full list; 0 or 1 = every entry
   uint32_t sample_stride;
@@ -186,6 +190,13 @@ int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_
 int launch_brick(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cudaStream_t s);
 // centre-per-lane brick scan of RDF / RIPK passes (k_lanes); -3 = not applicable
 int launch_lanes(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cudaStream_t s);
+// *out += the number of non-empty cells (cell_start has ncells + 1 entries)
+void launch_count_occupied(const uint32_t* cell_start, uint64_t ncells, unsigned long long* out, int sm_count,
+                           cudaStream_t s);
+// centre-per-lane block scan of kNN-only passes (k_lanes_knn); disjoint_sets:
+// every type in at most one environment set of each centre type
+// (ScanArgs::setidx valid); -3 = not applicable
+int launch_lanes_knn(const ScanArgs& a, bool disjoint_sets, int sm_count, size_t* smem_used, cudaStream_t s);
 int launch_apply(const ApplyArgs& a, int sm_count, cudaStream_t s);
 // Batched kNN in two phases, 32 realisations per warp (one per lane).
 // Walk: per (centre, realisation) the category of the k-th member of every

@@ -1339,20 +1339,20 @@ __global__ void __launch_bounds__(256) k_brick(ScanArgs a) {
 
 // Ion range [st, st + len) of row r of the stencil of the cell block
 // [xb, xe) x [yb, ye) x [zb, ze): rows are (yy, zz) with yy in [yb - sr,
-// ye - 1 + sr] and zz in [zb - sr, ze - 1 + sr], r = (zz - zb + sr) * nry +
-// (yy - yb + sr), each trimmed in x to the block's reach; len = 0 when the row
-// cannot hold a neighbour of a point of the block.  In symmetric mode the
+// ye - 1 + sr] and zz in [zb - sr, ze - 1 + sr], row r at (yb - sr + ry,
+// zb - sr + rz) for (ry, rz) = a.brows[r] (nearest to the block first), each
+// trimmed in x to the block's reach; len = 0 when the row cannot hold a
+// neighbour of a point of the block.  In symmetric mode the
 // leading cells that precede the block's first cell in slot order and hold
 // only centres are dropped: their pairs with the block are taken from their
 // side (every ion of such a cell has a lower slot than every block centre).
-__device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nrows, int nry, int sr, int xb, int xe,
-                                                int yb, int ye, int zb, int ze, bool sym, uint32_t& st,
-                                                uint32_t& len) {
+__device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nrows, int sr, int xb, int xe, int yb,
+                                                int ye, int zb, int ze, bool sym, uint32_t& st, uint32_t& len) {
   const Grid& g = a.g;
   st = 0;
   len = 0;
   if (r >= nrows) return;
-  const int rz = r / nry, ry = r - rz * nry;
+  const int ry = a.brows[2 * r], rz = a.brows[2 * r + 1];
   const int yy = yb - sr + ry, zz = zb - sr + rz;
   if (yy < 0 || yy >= g.ny || zz < 0 || zz >= g.nz) return;
   const float m2 = 2.f * g.margin;
@@ -1382,66 +1382,45 @@ __device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nr
 }
 
 // ----------------------------------------------- K3'' centre-per-lane blocks
-// RDF / RIPK pass with one centre per lane.  A warp takes up to 32 centres of
-// a block of bx x by x bz cells (rows of the block in slot order) and streams
-// the block's stencil rows through a per-warp staging buffer, 32 ions at a
-// time; every lane then tests the 32 staged ions against its own centre and
-// keeps a 32-bit mask of the ions it takes.  A test is one broadcast shared
-// load, the exact d^2 and a predicated bit set -- no branch and no store; the
-// row mapping, the record load and the type lookups are paid once per staged
-// ion, not once per (centre, ion).  A compact block (cells of R/4 or so, a few
+// Passes with one centre per lane.  A warp takes up to 32 centres of a block
+// of bx x by x bz cells (rows of the block in slot order) and streams the
+// block's stencil rows through a per-warp staging buffer, 32 ions at a time;
+// every lane then tests the 32 staged ions against its own centre and keeps a
+// 32-bit mask of the ions it takes.  A test is one broadcast shared load, the
+// exact d^2 and a predicated bit set -- no branch and no store; the row
+// mapping, the record load and the type lookups are paid once per staged ion,
+// not once per (centre, ion).  A compact block (cells of R/4 or so, a few
 // cells a side) keeps the staged region close to the union of the centres'
-// balls.  After each staged batch every lane walks its mask, recomputes d^2 of
-// the taken ions and bins them, so the bin lookup and the histogram atomics
-// run for in-ball pairs only.  Pair set, d^2 expression, bins and the
-// symmetric rule (a pair of two centres is taken by the lower slot and
-// credited to both) are those of k_scan; in symmetric mode a staged ion
-// carries key = its slot when it is a centre and 0xffffffff otherwise, and a
-// lane takes it when key > its own slot.  Warps fetch blocks `tile` at a time
+// balls.  The pair set and d^2 expression are those of k_scan; what is done
+// with the taken pairs is up to the pass (k_lanes: RDF / RIPK bins,
+// k_lanes_knn: kNN lists).  Warps fetch blocks `tile` at a time
 // from the global work counter, without block barriers.
-constexpr int kLanesWarps = 16;  // warps per block of k_lanes
-
-template <bool SYM>
-__global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
-  constexpr int NW = kLanesWarps;
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int H = a.H;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned char* sp = smem;
-  unsigned long long* since_flush = (unsigned long long*)sp; sp += 16;
-  float4* candA = (float4*)sp; sp += NW * 32 * 16;
-  float4* cposA = (float4*)sp; sp += NW * 32 * 16;
-  uint32_t* ccodeA = (uint32_t*)sp; sp += NW * 32 * 4;
-  uint32_t* cinfoA = (uint32_t*)sp; sp += NW * 32 * 4;
-  uint16_t* plistA = (uint16_t*)sp; sp += NW * 1024 * 2;
-  float* sT = (float*)sp; sp += ((H + 3) & ~3) * 4;
-  uint32_t* srdf = (uint32_t*)sp; sp += (a.rdf_in_smem ? (size_t)a.nC * a.nE * H * 4 : 0);
-  uint16_t* slut = (uint16_t*)sp; sp += ((a.lut_n + 7) & ~7) * 2;
-  int8_t* scs = (int8_t*)sp; sp += 256;
-  int8_t* ses = (int8_t*)sp;
-  for (int i = threadIdx.x; i < H; i += blockDim.x) sT[i] = a.cat_T[i];
-  for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) slut[i] = a.cat_lut[i];
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) { scs[i] = a.cslot_of[i]; ses[i] = a.eslot_of[i]; }
-  if (a.rdf_in_smem) for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) srdf[i] = 0;
-  if (threadIdx.x == 0) *since_flush = 0ull;
-  __syncthreads();
-
+//
+// lanes_walk calls, warp-uniformly,
+//   stage(slot, q, key, code)  per staged ion (its lane): key and code to stage
+//   start(self)                a new batch; self = this lane's centre slot or
+//                              0xffffffff; returns the lane's centre position
+//                              (at infinity for no centre)
+//   accept(j, d2)              per test of an in-ball staged ion j (inlined
+//                              into the test loop; a constant true costs nothing)
+//   taken(tm, nin)             after each staged batch: tm = the lane's mask,
+//                              nin = its in-ball ions (counted when COUNT)
+//   finish(live)               after the batch's last staged ions
+// In symmetric mode (SYM) a lane takes a staged ion when key > its own slot,
+// otherwise when key != its own slot; stage() sets key accordingly.
+template <bool SYM, bool COUNT, class Stage, class Start, class Accept, class Taken, class Finish>
+__device__ __forceinline__ void lanes_walk(const ScanArgs& a, float4* cand, uint32_t* ccode, Stage stage,
+                                           Start start, Accept accept, Taken taken, Finish finish) {
   const Grid& g = a.g;
-  float4* cand = candA + warp * 32;
-  float4* cpos = cposA + warp * 32;     // centre of lane c
-  uint32_t* ccode = ccodeA + warp * 32;
-  uint32_t* cinfo = cinfoA + warp * 32; // lane c: centre slot * nE | (env slot + 1) << 16
-  uint16_t* plist = plistA + warp * 1024;  // the staged batch's pairs, (lane << 5) | staged index
+  const int lane = threadIdx.x & 31;
   const uint32_t lemask = (2u << lane) - 1u;
-  const float Rp = a.R + g.margin;
   // rows up to sr cells away (in y or z) from the block can hold a neighbour
-  const int sr = (int)floorf((Rp + 2.f * g.margin) * g.inv_h) + 1;
+  // (sr = floor((R + 3 margin) / h) + 1, computed by the host with the row table)
+  const int sr = a.bsr;
   const int BX = max(a.bx, 1), BY = max(a.by, 1), BZ = max(a.bz, 1);
   const int nry = BY + 2 * sr, nrows = nry * (BZ + 2 * sr);
   const uint32_t nbx = (uint32_t)((g.nx + BX - 1) / BX), nby = (uint32_t)((g.ny + BY - 1) / BY);
   const float R2 = a.R2;
-  unsigned long long pairs_lane = 0, centres = 0;
-  constexpr unsigned long long FLUSH = 1ull << 30;
   const uint32_t WT = max(a.tile, 1u);
   for (;;) {
     uint32_t w0 = 0;
@@ -1495,27 +1474,13 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
           mc += ntake;
         }
         if (mc == 0) break;
-        float4 cp = make_float4(kInf(), kInf(), kInf(), 0.f);
-        int cs = -1, es = -1;
-        if (self != 0xffffffffu) {
-          cp = a.ions[self];
-          const uint32_t ct = a.labels ? (uint32_t)a.labels[self] : __float_as_uint(cp.w);
-          cs = scs[ct & 255];
-          es = ses[ct & 255];
-          if (cs < 0) {  // selection guarantees a slot; record and drop the centre otherwise
-            atomicOr(a.status, ST_TYPE_RANGE);
-            cp = make_float4(kInf(), kInf(), kInf(), 0.f);
-            self = 0xffffffffu;
-          }
-        }
-        cpos[lane] = cp;
-        cinfo[lane] = (uint32_t)(cs < 0 ? 0 : cs) * (uint32_t)a.nE | ((uint32_t)(es + 1) << 16);
-        const uint32_t live = __ballot_sync(FULL, self != 0xffffffffu);
-        uint32_t inb = 0;
+        const float4 cp = start(self);
+        const uint32_t live = __ballot_sync(FULL, cp.x != kInf());
+        if (live) self = (cp.x != kInf()) ? self : 0xffffffffu;
         // ---- stencil rows of the block
         for (int r0 = 0; r0 < nrows && live; r0 += 32) {
           uint32_t st, len;
-          block_row_range(a, r0 + lane, nrows, nry, sr, xb, xe, yb, ye, zb, ze, SYM, st, len);
+          block_row_range(a, r0 + lane, nrows, sr, xb, xe, yb, ye, zb, ze, SYM, st, len);
           const uint32_t ne = __ballot_sync(FULL, len > 0);
           const int cnt_rows = __popc(ne);
           if (cnt_rows == 0) continue;
@@ -1533,8 +1498,7 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
           const uint32_t total = __shfl_sync(FULL, inc, 31);
           int before = 0;
           for (uint32_t bb = 0; bb < total; bb += 32) {
-            // stage 32 ions: position, key, and (env slot + 1) | (centre slot + 1) << 8 | is-centre << 16;
-            // past the end an ion at infinity, which no lane takes
+            // stage 32 ions; past the end an ion at infinity, which no lane takes
             const uint32_t bitv = (lane < cnt_rows && rlen > 0 && exc >= bb && exc < bb + 32) ? (1u << (exc - bb)) : 0u;
             const uint32_t smask = __reduce_or_sync(FULL, bitv);
             const int row = before + __popc(smask & lemask) - 1;
@@ -1548,95 +1512,171 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
             if (t < total) {
               const uint32_t slot = rs + (t - rp);
               q = __ldg(a.ions + slot);
-              const uint32_t m = a.labels ? (uint32_t)a.labels[slot] : __float_as_uint(q.w);
-              const bool jc = SYM && a.cflag[slot] != 0;
-              key = SYM ? (jc ? slot : 0xffffffffu) : slot;
-              code = (uint32_t)(ses[m & 255] + 1) | (jc ? ((uint32_t)(scs[m & 255] + 1) << 8) | 0x10000u : 0u);
+              stage(slot, q, key, code);
             }
             cand[lane] = make_float4(q.x, q.y, q.z, __uint_as_float(key));
             ccode[lane] = code;
             __syncwarp();
             // ---- every lane tests the 32 staged ions against its centre
-            uint32_t tm = 0;
+            uint32_t tm = 0, nin = 0;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               const float4 c = cand[j];
               const float d2 = dist2(cp.x, cp.y, cp.z, c.x, c.y, c.z);
               const uint32_t k = __float_as_uint(c.w);
-              const bool take = (d2 <= R2) && (SYM ? (k > self) : (k != self));
-              tm |= take ? (1u << j) : 0u;
+              const bool inball = (d2 <= R2) && (SYM ? (k > self) : (k != self));
+              if (COUNT) nin += inball ? 1u : 0u;
+              tm |= (inball && accept(j, d2)) ? (1u << j) : 0u;
             }
-            // ---- bin the taken pairs: each lane lists its pairs at its offset in
-            // the batch's pair list, then the lanes take the list 64 at a time
-            const uint32_t np = __popc(tm);
-            uint32_t ex = np;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-              const uint32_t t = __shfl_up_sync(FULL, ex, o);
-              if (lane >= o) ex += t;
-            }
-            const uint32_t E = __shfl_sync(FULL, ex, 31);
-            inb += np;
-            for (uint32_t at = ex - np; tm; ++at) {
-              const int j = __ffs(tm) - 1;
-              tm &= tm - 1u;
-              plist[at] = (uint16_t)((lane << 5) | j);
-            }
-            __syncwarp();
-            auto bin_pair = [&](uint32_t e) {
-              const int c = (int)(e >> 5), j = (int)(e & 31u);
-              const float4 p = cpos[c];
-              const float4 q = cand[j];
-              const float d2 = dist2(p.x, p.y, p.z, q.x, q.y, q.z);
-              const uint32_t cj = ccode[j], ci = cinfo[c];
-              const int cat = category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
-              const int esj = (int)(cj & 255u) - 1;
-              if (esj >= 0) {
-                const uint32_t idx = ((ci & 0xffffu) + (uint32_t)esj) * (uint32_t)H + (uint32_t)cat;
-                if (a.rdf_in_smem) atomicAdd(&srdf[idx], 1u);
-                else atomicAdd(&a.rdf_core[idx], 1ull);
-              }
-              if (SYM && (cj & 0x10000u)) {
-                // the same pair seen from the staged ion, a centre too
-                ++inb;
-                const int csj = (int)((cj >> 8) & 255u) - 1;
-                const int esc = (int)(ci >> 16) - 1;
-                if (esc >= 0 && csj >= 0) {
-                  const uint32_t idx = ((uint32_t)csj * a.nE + (uint32_t)esc) * (uint32_t)H + (uint32_t)cat;
-                  if (a.rdf_in_smem) atomicAdd(&srdf[idx], 1u);
-                  else atomicAdd(&a.rdf_core[idx], 1ull);
-                }
-              }
-            };
-            for (uint32_t k = lane; k < E; k += 64) {
-              const uint32_t e0 = plist[k];
-              const bool two = k + 32 < E;
-              const uint32_t e1 = two ? plist[k + 32] : 0u;
-              bin_pair(e0);
-              if (two) bin_pair(e1);
-            }
+            taken(tm, nin);
             __syncwarp();
           }
         }
-        pairs_lane += inb;
-        if (lane == 0) centres += (unsigned long long)__popc(live);
-        if (a.rdf_in_smem) {
-          uint32_t tot = inb;
-          for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
-          unsigned long long old = 0;
-          if (lane == 0) old = atomicAdd(since_flush, (unsigned long long)tot);
-          old = __shfl_sync(FULL, old, 0);
-          if (old / FLUSH != (old + tot) / FLUSH) {
-            for (int i = lane; i < a.nC * a.nE * H; i += 32) {
-              const uint32_t v = atomicExch(&srdf[i], 0u);
-              if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
-            }
-          }
-        }
+        finish(live);
         __syncwarp();
       }
     }
   }
+}
+
+// RDF / RIPK pass.  After each staged batch every lane lists its taken pairs
+// at its offset in the batch's pair list and the lanes take the list 64 at a
+// time: d^2 is recomputed, binned and added to the (shared) RDF bins, so the
+// bin lookup and the histogram atomics run for in-ball pairs only.  In
+// symmetric mode a staged ion carries key = its slot when it is a centre and
+// 0xffffffff otherwise, and a pair of two centres is taken by the lower slot
+// and credited to both.
+constexpr int kLanesWarps = 16;  // warps per block of k_lanes
+
+template <bool SYM>
+__global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
+  constexpr int NW = kLanesWarps;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int H = a.H;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned char* sp = smem;
+  unsigned long long* since_flush = (unsigned long long*)sp; sp += 16;
+  float4* candA = (float4*)sp; sp += NW * 32 * 16;
+  float4* cposA = (float4*)sp; sp += NW * 32 * 16;
+  uint32_t* ccodeA = (uint32_t*)sp; sp += NW * 32 * 4;
+  uint32_t* cinfoA = (uint32_t*)sp; sp += NW * 32 * 4;
+  uint16_t* plistA = (uint16_t*)sp; sp += NW * 1024 * 2;
+  float* sT = (float*)sp; sp += ((H + 3) & ~3) * 4;
+  uint32_t* srdf = (uint32_t*)sp; sp += (a.rdf_in_smem ? (size_t)a.nC * a.nE * H * 4 : 0);
+  uint16_t* slut = (uint16_t*)sp; sp += ((a.lut_n + 7) & ~7) * 2;
+  int8_t* scs = (int8_t*)sp; sp += 256;
+  int8_t* ses = (int8_t*)sp;
+  for (int i = threadIdx.x; i < H; i += blockDim.x) sT[i] = a.cat_T[i];
+  for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) slut[i] = a.cat_lut[i];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) { scs[i] = a.cslot_of[i]; ses[i] = a.eslot_of[i]; }
+  if (a.rdf_in_smem) for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) srdf[i] = 0;
+  if (threadIdx.x == 0) *since_flush = 0ull;
+  __syncthreads();
+
+  float4* cand = candA + warp * 32;
+  float4* cpos = cposA + warp * 32;        // centre of lane c
+  uint32_t* ccode = ccodeA + warp * 32;
+  uint32_t* cinfo = cinfoA + warp * 32;    // lane c: centre slot * nE | (env slot + 1) << 16
+  uint16_t* plist = plistA + warp * 1024;  // the staged batch's pairs, (lane << 5) | staged index
+  unsigned long long pairs_lane = 0, centres = 0;
+  constexpr unsigned long long FLUSH = 1ull << 30;
+  uint32_t inb = 0;
+
+  auto stage = [&](uint32_t slot, const float4& q, uint32_t& key, uint32_t& code) {
+    // (env slot + 1) | (centre slot + 1) << 8 | is-centre << 16
+    const uint32_t m = a.labels ? (uint32_t)a.labels[slot] : __float_as_uint(q.w);
+    const bool jc = SYM && a.cflag[slot] != 0;
+    key = SYM ? (jc ? slot : 0xffffffffu) : slot;
+    code = (uint32_t)(ses[m & 255] + 1) | (jc ? ((uint32_t)(scs[m & 255] + 1) << 8) | 0x10000u : 0u);
+  };
+  auto start = [&](uint32_t self) {
+    float4 cp = make_float4(kInf(), kInf(), kInf(), 0.f);
+    int cs = -1, es = -1;
+    if (self != 0xffffffffu) {
+      cp = a.ions[self];
+      const uint32_t ct = a.labels ? (uint32_t)a.labels[self] : __float_as_uint(cp.w);
+      cs = scs[ct & 255];
+      es = ses[ct & 255];
+      if (cs < 0) {  // selection guarantees a slot; record and drop the centre otherwise
+        atomicOr(a.status, ST_TYPE_RANGE);
+        cp = make_float4(kInf(), kInf(), kInf(), 0.f);
+      }
+    }
+    cpos[lane] = cp;
+    cinfo[lane] = (uint32_t)(cs < 0 ? 0 : cs) * (uint32_t)a.nE | ((uint32_t)(es + 1) << 16);
+    inb = 0;
+    return cp;
+  };
+  auto bin_pair = [&](uint32_t e) {
+    const int c = (int)(e >> 5), j = (int)(e & 31u);
+    const float4 p = cpos[c];
+    const float4 q = cand[j];
+    const float d2 = dist2(p.x, p.y, p.z, q.x, q.y, q.z);
+    const uint32_t cj = ccode[j], ci = cinfo[c];
+    const int cat = category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+    const int esj = (int)(cj & 255u) - 1;
+    if (esj >= 0) {
+      const uint32_t idx = ((ci & 0xffffu) + (uint32_t)esj) * (uint32_t)H + (uint32_t)cat;
+      if (a.rdf_in_smem) atomicAdd(&srdf[idx], 1u);
+      else atomicAdd(&a.rdf_core[idx], 1ull);
+    }
+    if (SYM && (cj & 0x10000u)) {
+      // the same pair seen from the staged ion, a centre too
+      ++inb;
+      const int csj = (int)((cj >> 8) & 255u) - 1;
+      const int esc = (int)(ci >> 16) - 1;
+      if (esc >= 0 && csj >= 0) {
+        const uint32_t idx = ((uint32_t)csj * a.nE + (uint32_t)esc) * (uint32_t)H + (uint32_t)cat;
+        if (a.rdf_in_smem) atomicAdd(&srdf[idx], 1u);
+        else atomicAdd(&a.rdf_core[idx], 1ull);
+      }
+    }
+  };
+  auto taken = [&](uint32_t tm, uint32_t) {
+    const uint32_t np = __popc(tm);
+    uint32_t ex = np;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(FULL, ex, o);
+      if (lane >= o) ex += t;
+    }
+    const uint32_t E = __shfl_sync(FULL, ex, 31);
+    inb += np;
+    for (uint32_t at = ex - np; tm; ++at) {
+      const int j = __ffs(tm) - 1;
+      tm &= tm - 1u;
+      plist[at] = (uint16_t)((lane << 5) | j);
+    }
+    __syncwarp();
+    for (uint32_t k = lane; k < E; k += 64) {
+      const uint32_t e0 = plist[k];
+      const bool two = k + 32 < E;
+      const uint32_t e1 = two ? plist[k + 32] : 0u;
+      bin_pair(e0);
+      if (two) bin_pair(e1);
+    }
+  };
+  auto finish = [&](uint32_t live) {
+    pairs_lane += inb;
+    if (lane == 0) centres += (unsigned long long)__popc(live);
+    if (a.rdf_in_smem) {
+      // keep every shared bin below 2^32 (see k_scan)
+      uint32_t tot = inb;
+      for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+      unsigned long long old = 0;
+      if (lane == 0) old = atomicAdd(since_flush, (unsigned long long)tot);
+      old = __shfl_sync(FULL, old, 0);
+      if (old / FLUSH != (old + tot) / FLUSH) {
+        for (int i = lane; i < a.nC * a.nE * H; i += 32) {
+          const uint32_t v = atomicExch(&srdf[i], 0u);
+          if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
+        }
+      }
+    }
+  };
+  auto accept = [](int, float) { return true; };
+  lanes_walk<SYM, false>(a, cand, ccode, stage, start, accept, taken, finish);
+
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
   if (lane == 0) {
     atomicAdd(&a.counters[0], pairs_lane);
@@ -1648,6 +1688,135 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
       const uint32_t v = srdf[i];
       if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
     }
+  }
+}
+
+// kNN pass (no RDF in the same pass), every type in at most one environment
+// set of each centre type.  Each lane keeps, in shared memory, the K smallest
+// d^2 of its centre per environment set (set p, rank r of lane l at
+// [(p * K + r) * 32 + l]: the lanes never share a bank).  Stencil rows come
+// nearest to the block first, so the lists fill with near ions and their K-th
+// values tighten early.  A staged ion carries its environment set for every
+// centre slot (4 bits each, nC <= 8), and a lane takes it only when its d^2
+// beats the lane's K-th value of that set -- after the first rows few pairs
+// are taken.  Taken ions go into the sorted lists.  At the end of the batch
+// the k-th values are binned (a missing neighbour at R + EPSILON), as k_scan
+// does.
+constexpr int kLanesKnnWarps = 8;
+
+// KB > 0: K <= KB, and an insertion loads the whole list at once (KB
+// independent shared loads) instead of walking it; KB = 0: any K.
+template <int KB>
+__global__ void __launch_bounds__(kLanesKnnWarps * 32, 2) k_lanes_knn(ScanArgs a) {
+  constexpr int NW = kLanesKnnWarps;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int H = a.H, K = a.kmax, EM = a.emax;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned char* sp = smem;
+  float4* candA = (float4*)sp; sp += NW * 32 * 16;
+  uint32_t* ccodeA = (uint32_t*)sp; sp += NW * 32 * 4;
+  float* listA = (float*)sp; sp += (size_t)NW * EM * K * 32 * 4;
+  float* sT = (float*)sp; sp += ((H + 3) & ~3) * 4;
+  uint16_t* slut = (uint16_t*)sp; sp += ((a.lut_n + 7) & ~7) * 2;
+  int8_t* scs = (int8_t*)sp; sp += 256;
+  int8_t* sidx = (int8_t*)sp;  // [nC][256]
+  for (int i = threadIdx.x; i < H; i += blockDim.x) sT[i] = a.cat_T[i];
+  for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) slut[i] = a.cat_lut[i];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) scs[i] = a.cslot_of[i];
+  for (int i = threadIdx.x; i < a.nC * 256; i += blockDim.x) sidx[i] = a.setidx[i];
+  __syncthreads();
+
+  float4* cand = candA + warp * 32;
+  uint32_t* ccode = ccodeA + warp * 32;
+  float* L = listA + (size_t)warp * EM * K * 32 + lane;  // set p, rank r at L[(p * K + r) * 32]
+  unsigned long long pairs_lane = 0, centres = 0;
+  uint32_t inb = 0;
+  float4 cp;
+  int cs = -1, nset = 0;
+  const int last = (K - 1) * 32;
+
+  auto stage = [&](uint32_t slot, const float4& q, uint32_t& key, uint32_t& code) {
+    key = slot;
+    const uint32_t m = (a.labels ? (uint32_t)a.labels[slot] : __float_as_uint(q.w)) & 255u;
+    code = 0;
+    for (int c = 0; c < a.nC; ++c) code |= (uint32_t)(sidx[c * 256 + m] & 15) << (4 * c);
+  };
+  auto start = [&](uint32_t self) {
+    cp = make_float4(kInf(), kInf(), kInf(), 0.f);
+    cs = -1;
+    if (self != 0xffffffffu) {
+      cp = a.ions[self];
+      const uint32_t ct = a.labels ? (uint32_t)a.labels[self] : __float_as_uint(cp.w);
+      cs = scs[ct & 255];
+      if (cs < 0) {  // selection guarantees a slot; record and drop the centre otherwise
+        atomicOr(a.status, ST_TYPE_RANGE);
+        cp = make_float4(kInf(), kInf(), kInf(), 0.f);
+      }
+    }
+    nset = cs >= 0 ? a.nsets[cs] : 0;
+    for (int e = 0; e < nset * K; ++e) L[e * 32] = kInf();
+    inb = 0;
+    return cp;
+  };
+  auto accept = [&](int j, float d2) {
+    // set of the staged ion for this lane's centre type (15 = none), then its K-th value
+    const uint32_t p = (ccode[j] >> (4 * (cs < 0 ? 0 : cs))) & 15u;
+    return p != 15u && d2 < L[p * K * 32 + last];
+  };
+  auto insert = [&](int p, float d2) {
+    float* Lp = L + p * K * 32;
+    if (!(d2 < Lp[last])) return;
+    if constexpr (KB > 0) {
+      float v[KB];
+      int pos = 0;
+#pragma unroll
+      for (int r = 0; r < KB; ++r) {
+        v[r] = (r < K) ? Lp[r * 32] : kInf();
+        pos += (r < K && v[r] <= d2) ? 1 : 0;
+      }
+#pragma unroll
+      for (int r = 0; r < KB; ++r)
+        if (r < K && r >= pos) Lp[r * 32] = (r == pos) ? d2 : v[r > 0 ? r - 1 : 0];
+    } else {
+      int r = K - 1;
+      while (r > 0) {
+        const float v = Lp[(r - 1) * 32];
+        if (!(v > d2)) break;
+        Lp[r * 32] = v;
+        --r;
+      }
+      Lp[r * 32] = d2;
+    }
+  };
+  auto taken = [&](uint32_t tm, uint32_t nin) {
+    inb += nin;
+    while (tm) {
+      const int j = __ffs(tm) - 1;
+      tm &= tm - 1u;
+      const float4 q = cand[j];
+      const float d2 = dist2(cp.x, cp.y, cp.z, q.x, q.y, q.z);
+      insert((int)((ccode[j] >> (4 * cs)) & 15u), d2);
+    }
+  };
+  auto finish = [&](uint32_t live) {
+    if (lane == 0) centres += (unsigned long long)__popc(live);
+    pairs_lane += inb;
+    // the k-th smallest d^2 of each set -> its bin (or the miss bin)
+    for (int p = 0; p < nset; ++p) {
+      const int Sg = a.set_list[cs * 32 + p];
+      for (int kk = 0; kk < a.nkI; ++kk) {
+        const float v = L[(p * K + a.kvals[kk] - 1) * 32];
+        const int cat = (v == kInf()) ? a.cat_miss : category_lut(v, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+        if (cat >= 0) atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
+      }
+    }
+  };
+  lanes_walk<false, true>(a, cand, ccode, stage, start, accept, taken, finish);
+
+  for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
+  if (lane == 0) {
+    atomicAdd(&a.counters[0], pairs_lane);
+    atomicAdd(&a.counters[1], centres);
   }
 }
 
@@ -2299,6 +2468,21 @@ void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const 
   k_surface<<<grid_for(n, 256), 256, 0, s>>>(ions, n, tri_box, tri, tcs, tct, tg, rprime, surf);
 }
 
+// number of cells holding at least one ion
+__global__ void k_count_occupied(const uint32_t* __restrict__ cell_start, uint64_t ncells, unsigned long long* out) {
+  unsigned long long c = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < ncells; i += (uint64_t)gridDim.x * blockDim.x)
+    c += cell_start[i + 1] > cell_start[i] ? 1ull : 0ull;
+  for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(FULL, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+void launch_count_occupied(const uint32_t* cell_start, uint64_t ncells, unsigned long long* out, int sm_count,
+                           cudaStream_t s) {
+  counted();
+  k_count_occupied<<<sm_count * 4, 256, 0, s>>>(cell_start, ncells, out);
+}
+
 void launch_nc_prefix(const uint32_t* cell_start, uint64_t ncells, const uint8_t* cflag, uint32_t* out,
                       uint32_t* scan_tmp, uint64_t scan_tmp_elems, cudaStream_t s) {
   counted();
@@ -2479,7 +2663,7 @@ size_t lanes_smem(const ScanArgs& a) {
 
 int launch_lanes(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cudaStream_t s) {
   if (a.mode != 0 || kr > 0 || (a.flags & PP_CNTNB) || !(a.flags & PP_RDF) || a.bx < 1 || a.by < 1 || a.bz < 1 ||
-      a.nC > 254 || a.nE > 254)
+      a.nC > 254 || a.nE > 254 || !a.brows)
     return -3;
   const size_t smem = lanes_smem(a);
   if (smem_used) *smem_used = smem;
@@ -2493,6 +2677,31 @@ int launch_lanes(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cud
     return -1;
   counted();
   kern<<<sm_count * per_sm, kLanesWarps * 32, smem, s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+size_t lanes_knn_smem(const ScanArgs& a) {
+  constexpr int NW = kLanesKnnWarps;
+  return NW * 32 * 16 + NW * 32 * 4 + (size_t)NW * (a.emax > 1 ? a.emax : 1) * a.kmax * 32 * 4 +
+         (size_t)((a.H + 3) & ~3) * 4 + (size_t)((a.lut_n + 7) & ~7) * 2 + 256 + (size_t)a.nC * 256;
+}
+
+int launch_lanes_knn(const ScanArgs& a, bool disjoint_sets, int sm_count, size_t* smem_used, cudaStream_t s) {
+  if (a.mode != 0 || (a.flags & (PP_CNTNB | PP_RDF)) || !disjoint_sets || a.kmax < 1 || a.kmax > 64 || a.bx < 1 ||
+      a.by < 1 || a.bz < 1 || !a.brows || a.nC > 8 || a.emax > 15)  // sets packed 4 bits per centre slot
+    return -3;
+  const size_t smem = lanes_knn_smem(a);
+  if (smem_used) *smem_used = smem;
+  if (smem > 110 * 1024) return -3;  // two blocks of 8 warps per SM, or the per-centre scan
+  auto kern = a.kmax <= 8 ? k_lanes_knn<8> : a.kmax <= 16 ? k_lanes_knn<16> : k_lanes_knn<0>;
+  if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return -1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kLanesKnnWarps * 32, smem) != cudaSuccess ||
+      per_sm < 1)
+    return -1;
+  counted();
+  kern<<<sm_count * per_sm, kLanesKnnWarps * 32, smem, s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -29,7 +29,7 @@ EXPORTS = (
     "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option", "pp_cloud_prepare",
     "pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_stats", "pp_server_destroy",
     "pp_fp64_audit", "pp_surfdist_noalloc", "pp_batched_graph", "pp_cloud_inside", "pp_fetch_npcorr",
-    "pp_run_aposteriori",
+    "pp_run_aposteriori", "pp_last_kernel",
 )
 
 _lib = None
@@ -94,6 +94,7 @@ def load():
         "pp_cloud_inside": ([vp, i32, f32, f32, C.POINTER(u64), C.POINTER(f32), vp], i32),
         "pp_fetch_npcorr": ([vp, vp, u64, C.POINTER(u64)], i32),
         "pp_run_aposteriori": ([vp, i32, vp, u32, vp], i32),
+        "pp_last_kernel": ([vp, C.POINTER(C.c_char_p)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -157,6 +158,12 @@ class Context:
         if rc:
             msg = self.L.pp_last_error(self.h).decode(errors="replace")
             raise PPError(rc, f"{what}: {self.L.pp_strerror(rc).decode()}: {msg}")
+
+    def last_kernel(self) -> str:
+        """Name of the stencil kernel the last run took."""
+        nm = C.c_char_p()
+        self._ck(self.L.pp_last_kernel(self.h, C.byref(nm)), "pp_last_kernel")
+        return nm.value.decode()
 
     def last_kernel_ms(self) -> float:
         ms = C.c_float()

@@ -229,7 +229,8 @@ def test_results_independent_of_tuning(ctx, oracle):
         ctx.run(cid, ALL, [6, 2, 1])
         outs.append(ctx.fetch())
     r, t = ctx.autotune(cid, ALL, [6, 2, 1], sample=2000)
-    assert 2.0 <= r <= 5.0 and (t in (32, 128, 512) or (t >> 16) in (4, 8, 16))
+    lanes = t >= 65536 and (t & 0xffff) == N.PP_TILE_LANES
+    assert 2.0 <= r <= 5.0 and (t in (32, 128, 512) or (t >> 16) in (4, 8, 16) or lanes)
     ctx.run(cid, ALL, [6, 2, 1])
     outs.append(ctx.fetch())
     for o in outs[1:]:
@@ -276,22 +277,22 @@ def test_brick_scan(ctx, oracle, tile, ratio):
     trg, env = [[1], [2, 3], [3]], [[1, 2], [1, 2, 3], [1]]
     ctx.tasks(trg, env)
     ctx.hist(0.1, 0.02, 1.3)
-    ctx.set_option("lanes", 0)  # the RDF pass through the brick scan, not the centre-per-lane scan
+    ctx.set_option("lanes", 0)  # both passes through the brick scan, not the centre-per-lane scan
     try:
         ctx.run(cid, N.PP_RDF | N.PP_RIPK, [], label_perm=perm)
         gpu, st = ctx.fetch(), ctx.stats()
+        ref = oracle.spatstat(spec.xyz, lab, surf, 0.1, 0.02, 1.3, N.PP_RDF | N.PP_RIPK, trg, env, [])
+        assert st["pairs"] == ref["pairs"] and np.array_equal(gpu, ref["bins"])
+        types = [1, 2, 3]
+        trg = [[a] for a in types for b in types]
+        env = [[b] for a in types for b in types]
+        ctx.tasks(trg, env)
+        ctx.hist(0.0, 0.005, 1.2)
+        ks = [12, 3, 1]
+        ctx.run(cid, N.PP_1NN | N.PP_MKNN, ks)
+        gpu, st = ctx.fetch(), ctx.stats()
     finally:
         ctx.set_option("lanes", 1)
-    ref = oracle.spatstat(spec.xyz, lab, surf, 0.1, 0.02, 1.3, N.PP_RDF | N.PP_RIPK, trg, env, [])
-    assert st["pairs"] == ref["pairs"] and np.array_equal(gpu, ref["bins"])
-    types = [1, 2, 3]
-    trg = [[a] for a in types for b in types]
-    env = [[b] for a in types for b in types]
-    ctx.tasks(trg, env)
-    ctx.hist(0.0, 0.005, 1.2)
-    ks = [12, 3, 1]
-    ctx.run(cid, N.PP_1NN | N.PP_MKNN, ks)
-    gpu, st = ctx.fetch(), ctx.stats()
     ref = oracle.spatstat(spec.xyz, spec.labels, surf, 0.0, 0.005, 1.2, N.PP_1NN | N.PP_MKNN, trg, env, ks)
     assert st["pairs"] == ref["pairs"] and np.array_equal(gpu, ref["bins"])
     ctx.free(cid)
@@ -411,6 +412,7 @@ def test_lanes_scan(ctx, oracle, block, ratio, symmetric):
     try:
         ctx.run(cid, flags, [], label_perm=perm)
         lanes, st = ctx.fetch(), ctx.stats()
+        kernel = ctx.last_kernel()
         ctx.set_option("lanes", 0)
         ctx.run(cid, flags, [], label_perm=perm)
         scan, st2 = ctx.fetch(), ctx.stats()
@@ -419,6 +421,7 @@ def test_lanes_scan(ctx, oracle, block, ratio, symmetric):
         ctx.set_option("symmetric", 1)
     ctx.free(cid)
     ref = oracle.spatstat(spec.xyz, spec.labels[perm], surf, 0.1, 0.02, 1.4, flags, trg, env, [])
+    assert kernel == "k_lanes"
     assert st["pairs"] == ref["pairs"] == st2["pairs"] and st["centres"] == ref["centres"]
     assert np.array_equal(lanes, ref["bins"]) and np.array_equal(scan, ref["bins"])
 
@@ -434,3 +437,49 @@ def test_lanes_scan_rdf_bins_in_global_memory(ctx, oracle):
     gpu, st, ref, _ = _run_both(ctx, oracle, spec, 0.0, 0.002, 1.2, N.PP_RDF, trg, env, [])
     assert st["pairs"] == ref["pairs"]
     assert np.array_equal(gpu, ref["bins"])
+
+
+@pytest.mark.parametrize("block", [(1, 1, 1), (4, 2, 2), (3, 3, 2)])
+@pytest.mark.parametrize("ratio", [2.0, 4.0])
+@pytest.mark.parametrize("with_rdf", [False, True])
+def test_lanes_knn_scan(ctx, oracle, block, ratio, with_rdf):
+    """The centre-per-lane block scan of kNN passes (disjoint environment sets,
+    k up to 12, 1NN, the miss bin) against the oracle and the per-centre scan,
+    under a label permutation; with RDF in the same pass the per-centre scan
+    takes it."""
+    spec = synth.cone_specimen(n=50000, r_apex=8.0, half_angle_deg=10.0, length=18.0, n_clusters=25,
+                               members=40, nspecies=4, seed=71, nseg=64, stack=4.0)
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tuning(cid, ratio, LANES(*block))
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    perm = np.random.default_rng(sum(block) + int(ratio)).permutation(spec.xyz.shape[0]).astype(np.uint32)
+    trg = [[1], [1], [2, 3], [4], [1, 2, 3, 4]]
+    env = [[1, 2], [3], [1, 2, 3], [4], [4]]
+    ks = [12, 5, 1]
+    flags = N.PP_1NN | N.PP_MKNN | (N.PP_RDF if with_rdf else 0)
+    ctx.tasks(trg, env)
+    ctx.hist(0.0, 0.01, 1.3)
+    try:
+        ctx.run(cid, flags, ks, label_perm=perm)
+        lanes, st = ctx.fetch(), ctx.stats()
+        kernel = ctx.last_kernel()
+        ctx.set_option("lanes", 0)
+        ctx.run(cid, flags, ks, label_perm=perm)
+        scan = ctx.fetch()
+    finally:
+        ctx.set_option("lanes", 1)
+    ctx.free(cid)
+    ref = oracle.spatstat(spec.xyz, spec.labels[perm], surf, 0.0, 0.01, 1.3, flags, trg, env, ks)
+    assert st["pairs"] == ref["pairs"] and st["centres"] == ref["centres"]
+    assert np.array_equal(lanes, ref["bins"]) and np.array_equal(scan, ref["bins"])
+    assert kernel == ("k_scan" if with_rdf else "k_lanes_knn")
+
+
+def test_lanes_knn_overlapping_sets_fall_back(ctx, oracle):
+    """Overlapping environment sets of one centre type take the per-centre scan."""
+    spec = synth.cone_specimen(n=30000, r_apex=8.0, half_angle_deg=10.0, length=12.0, n_clusters=10,
+                               members=30, nspecies=3, seed=73, nseg=64, stack=4.0)
+    trg, env = [[1], [1]], [[1, 2], [2, 3]]
+    gpu, st, ref, _ = _run_both(ctx, oracle, spec, 0.0, 0.01, 1.2, N.PP_MKNN, trg, env, [6, 1])
+    assert st["pairs"] == ref["pairs"] and np.array_equal(gpu, ref["bins"])
