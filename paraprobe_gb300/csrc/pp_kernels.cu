@@ -1707,7 +1707,7 @@ constexpr int kLanesKnnWarps = 8;
 // KB > 0: K <= KB, and an insertion loads the whole list at once (KB
 // independent shared loads) instead of walking it; KB = 0: any K.
 template <int KB>
-__global__ void __launch_bounds__(kLanesKnnWarps * 32, 2) k_lanes_knn(ScanArgs a) {
+__global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a) {
   constexpr int NW = kLanesKnnWarps;
   extern __shared__ __align__(16) unsigned char smem[];
   const int H = a.H, K = a.kmax, EM = a.emax;
@@ -2692,7 +2692,7 @@ int launch_lanes_knn(const ScanArgs& a, bool disjoint_sets, int sm_count, size_t
     return -3;
   const size_t smem = lanes_knn_smem(a);
   if (smem_used) *smem_used = smem;
-  if (smem > 110 * 1024) return -3;  // two blocks of 8 warps per SM, or the per-centre scan
+  if (smem > 110 * 1024) return -3;  // at least two blocks of 8 warps per SM, or the per-centre scan
   auto kern = a.kmax <= 8 ? k_lanes_knn<8> : a.kmax <= 16 ? k_lanes_knn<16> : k_lanes_knn<0>;
   if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return -1;
