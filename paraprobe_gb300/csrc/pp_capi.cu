@@ -388,12 +388,12 @@ int build_grid(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
   return PP_OK;
 }
 
-// Default cell block of the centre-per-lane scans: about 28 ions (a warp's
-// worth of centres) at the cloud's mean occupancy of non-empty cells, twice as
-// long in x as in y and z.
+// Default cell block of the centre-per-lane scans: about 24 ions (a warp's
+// worth of centres once the ions near the hull are excluded) at the cloud's
+// mean occupancy of non-empty cells, twice as long in x as in y and z.
 void default_block(const Cloud& cl, int* bx, int* by, int* bz) {
   const double per_cell = cl.occupied ? (double)cl.n / (double)cl.occupied : 1.0;
-  const double cells = std::max(1.0, 28.0 / std::max(per_cell, 1e-3));
+  const double cells = std::max(1.0, 24.0 / std::max(per_cell, 1e-3));
   const int side = (int)std::lround(std::cbrt(cells / 2.0));
   *by = *bz = std::min(15, std::max(1, side));
   *bx = (int)std::min(64L, std::max(1L, std::lround(cells / ((double)*by * *bz))));

@@ -2693,7 +2693,10 @@ int launch_lanes_knn(const ScanArgs& a, bool disjoint_sets, int sm_count, size_t
   const size_t smem = lanes_knn_smem(a);
   if (smem_used) *smem_used = smem;
   if (smem > 110 * 1024) return -3;  // at least two blocks of 8 warps per SM, or the per-centre scan
-  auto kern = a.kmax <= 8 ? k_lanes_knn<8> : a.kmax <= 16 ? k_lanes_knn<16> : k_lanes_knn<0>;
+  auto kern = a.kmax <= 8    ? k_lanes_knn<8>
+              : a.kmax <= 10 ? k_lanes_knn<10>
+              : a.kmax <= 16 ? k_lanes_knn<16>
+                             : k_lanes_knn<0>;
   if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return -1;
   int per_sm = 0;
