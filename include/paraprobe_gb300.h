@@ -277,7 +277,11 @@ int pp_last_kernel_ms(pp_ctx* ctx, float* ms);
 /* Name of the stencil kernel the last pp_run took: "k_scan" (per-centre
  * scan), "k_brick" (brick scan), "k_lanes" (centre-per-lane scan of RDF /
  * RIPK passes) or "k_lanes_knn" (centre-per-lane scan of kNN passes); a static
- * string.  No counterpart in the reference. */
+ * string.  The centre-per-lane scans take passes of dense centres (at least
+ * 0.35 per non-empty cell, or a block shape set with pp_cloud_tuning) without
+ * CNTNB or NPCORR, kNN only with disjoint environment sets; a pass with both
+ * RDF / RIPK and kNN takes the per-centre scan.  No counterpart in the
+ * reference. */
 int pp_last_kernel(pp_ctx* ctx, const char** name);
 
 /* Prepare a cloud for queries with r_lo <= rmax <= r_hi (r_hi <= 6 r_lo):

@@ -388,15 +388,20 @@ int build_grid(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
   return PP_OK;
 }
 
-// Default cell block of the centre-per-lane scans: about 24 ions (a warp's
-// worth of centres once the ions near the hull are excluded) at the cloud's
-// mean occupancy of non-empty cells, twice as long in x as in y and z.
-void default_block(const Cloud& cl, int* bx, int* by, int* bz) {
-  const double per_cell = cl.occupied ? (double)cl.n / (double)cl.occupied : 1.0;
-  const double cells = std::max(1.0, 24.0 / std::max(per_cell, 1e-3));
+// Default cell block of the centre-per-lane scans: about 24 centres (a warp's
+// worth) at the mean number of centres per non-empty cell, twice as long in x
+// as in y and z.  Returns false when centres are too sparse for a block to
+// fill a warp without streaming far more ions than the centres' balls hold
+// (fewer than 0.35 centres per non-empty cell); such passes take the
+// per-centre scan.
+bool default_block(const Cloud& cl, uint64_t ncent, int* bx, int* by, int* bz) {
+  const double per_cell = cl.occupied ? (double)ncent / (double)cl.occupied : 0.0;
+  if (per_cell < 0.35) return false;
+  const double cells = std::max(1.0, 24.0 / per_cell);
   const int side = (int)std::lround(std::cbrt(cells / 2.0));
   *by = *bz = std::min(15, std::max(1, side));
   *bx = (int)std::min(64L, std::max(1L, std::lround(cells / ((double)*by * *bz))));
+  return true;
 }
 
 // A grid serves every radius with R / h in [1, 6] (stencils of 3..13 cells a
@@ -1314,21 +1319,24 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
     const Grid& g = cl->g;
     const bool rows_fit = (int)std::floor((R + 3.f * g.margin) * g.inv_h) + 1 <= 7;
     // centre-per-lane scans: cell block and its stencil rows
-    if (cl->lanes_bx) {
+    bool lanes = rows_fit && !ctx->no_lanes && !(flags & (PP_CNTNB | PP_NPCORR)) &&
+                 !(P.kr > 0 && (a.flags & PP_RDF));
+    if (lanes && cl->lanes_bx) {
       a.bx = (int)cl->lanes_bx;
       a.by = (int)std::max<uint32_t>(cl->lanes_by, 1);
       a.bz = (int)std::max<uint32_t>(cl->lanes_bz, 1);
-    } else {
-      default_block(*cl, &a.bx, &a.by, &a.bz);
+    } else if (lanes) {
+      lanes = default_block(*cl, (uint64_t)ncent * std::max<uint32_t>(stride, 1), &a.bx, &a.by, &a.bz);
     }
     a.bsr = (int)std::floor(((R + g.margin) + 2.f * g.margin) * g.inv_h) + 1;
     a.brows = nullptr;
-    if (rows_fit && !ctx->no_lanes && !(flags & (PP_CNTNB | PP_NPCORR)) &&
-        (rc = ensure_block_rows(ctx, a.by, a.bz, a.bsr, s, &a.brows)) != PP_OK)
-      return rc;
+    if (lanes && (rc = ensure_block_rows(ctx, a.by, a.bz, a.bsr, s, &a.brows)) != PP_OK) return rc;
     CK(cudaEventRecord(ctx->ev0, s));
     rc = -3;
-    if (rows_fit && !ctx->no_lanes && P.kr == 0 && !(flags & (PP_CNTNB | PP_NPCORR)) && (a.flags & PP_RDF)) {
+    // passes with RDF / RIPK and kNN together take the per-centre scan: it
+    // serves both from one candidate stream, which measured as fast as or
+    // faster than the two centre-per-lane scans one after the other
+    if (rc == -3 && a.brows && P.kr == 0 && (a.flags & PP_RDF)) {
       const uint64_t nb_x = ((uint64_t)g.nx + a.bx - 1) / a.bx, nb_y = ((uint64_t)g.ny + a.by - 1) / a.by;
       uint64_t nb = nb_x * nb_y * (((uint64_t)g.nz + a.bz - 1) / a.bz);
       if (stride > 1) nb = std::max<uint64_t>(1, nb / stride);
@@ -1343,8 +1351,7 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
     }
     // kNN-only passes (with RDF in the same pass every in-ball pair would be
     // walked per lane; the per-centre scan does that pass better)
-    if (rc == -3 && rows_fit && !ctx->no_lanes && P.kr > 0 && !(a.flags & PP_RDF) &&
-        !(flags & (PP_CNTNB | PP_NPCORR))) {
+    if (rc == -3 && a.brows && P.kr > 0 && !(a.flags & PP_RDF)) {
       const uint64_t nb_x = ((uint64_t)g.nx + a.bx - 1) / a.bx, nb_y = ((uint64_t)g.ny + a.by - 1) / a.by;
       uint64_t nb = nb_x * nb_y * (((uint64_t)g.nz + a.bz - 1) / a.bz);
       if (stride > 1) nb = std::max<uint64_t>(1, nb / stride);

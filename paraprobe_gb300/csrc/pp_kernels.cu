@@ -21,6 +21,9 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "pp_internal.h"
 #include "pp_host.h"
@@ -29,6 +32,25 @@
 namespace pp {
 
 #define FULL 0xffffffffu
+
+// Raises a kernel's dynamic shared-memory limit on the current device to at
+// least `smem` bytes.  The limit only ever grows (per device and kernel, under
+// a lock): serving threads launch the same kernels concurrently with
+// different sizes, and lowering the limit between another thread's set-up and
+// its launch would make that launch fail.
+static bool allow_dynamic_smem(const void* fn, size_t smem) {
+  if (smem <= 48 * 1024) return true;
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> granted;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& g = granted[{dev, fn}];
+  if (smem <= g) return true;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return false;
+  g = smem;
+  return true;
+}
 
 __device__ __forceinline__ float kInf() { return __int_as_float(0x7f800000); }
 
@@ -2368,7 +2390,7 @@ void launch_audit(const ScanArgs& a, double start, double scale, double end, dou
                   cudaStream_t s) {
   AuditArgs x{start, scale, end, R64, nbins, stride, out, list_slots, list_d, cap};
   const size_t smem = ((ROW_TABLE_ENTRIES * 2 + 15) & ~15) + (size_t)a.H * 4;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(k_audit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  allow_dynamic_smem((const void*)k_audit, smem);
   counted();
   k_audit<<<sm_count * 4, 256, smem, s>>>(a, x);
 }
@@ -2566,7 +2588,7 @@ template <int KR, int EMAX>
 static int launch_scan_t(const ScanArgs& a, int sm_count, size_t smem, cudaStream_t s) {
   auto kern = k_scan<KR, EMAX>;
   if (smem > 48 * 1024) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    if (!allow_dynamic_smem((const void*)kern, smem)) return -1;
   }
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem) != cudaSuccess || per_sm < 1) return -1;
@@ -2616,7 +2638,7 @@ int launch_npcorr(const ScanArgs& a, const NpcArgs& p, int sm_count, cudaStream_
   const size_t smem = (size_t)nwarps * a.emax * 32 * 12 + (size_t)a.nC * 256 * 4 + ROW_TABLE_ENTRIES * 2 + 256;
   if (p.K < 1 || p.K > 32 || smem > 200 * 1024) return -2;
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(k_npcorr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      !allow_dynamic_smem((const void*)k_npcorr, smem))
     return -1;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_npcorr, nwarps * 32, smem) != cudaSuccess || per_sm < 1)
@@ -2644,7 +2666,7 @@ int launch_brick(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cud
   if (smem_used) *smem_used = smem;
   if (smem > 200 * 1024) return -3;
   auto kern = knn ? k_brick<true> : k_brick<false>;
-  if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!allow_dynamic_smem((const void*)kern, smem))
     return -1;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem) != cudaSuccess || per_sm < 1) return -1;
@@ -2669,7 +2691,7 @@ int launch_lanes(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cud
   if (smem_used) *smem_used = smem;
   if (smem > 200 * 1024) return -3;
   auto kern = a.sym ? k_lanes<true> : k_lanes<false>;
-  if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!allow_dynamic_smem((const void*)kern, smem))
     return -1;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kLanesWarps * 32, smem) != cudaSuccess ||
@@ -2697,7 +2719,7 @@ int launch_lanes_knn(const ScanArgs& a, bool disjoint_sets, int sm_count, size_t
               : a.kmax <= 10 ? k_lanes_knn<10>
               : a.kmax <= 16 ? k_lanes_knn<16>
                              : k_lanes_knn<0>;
-  if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!allow_dynamic_smem((const void*)kern, smem))
     return -1;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kLanesKnnWarps * 32, smem) != cudaSuccess ||
@@ -2712,7 +2734,7 @@ template <int G, bool KS>
 static int launch_apply_t(const ApplyArgs& a, int sm_count, size_t smem, cudaStream_t s) {
   auto kern = k_apply<G, KS>;
   if (smem > 48 * 1024) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    if (!allow_dynamic_smem((const void*)kern, smem)) return -1;
   }
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kApplyThreads, smem) != cudaSuccess || per_sm < 1)
@@ -2797,7 +2819,7 @@ int launch_knn_walk(const KnnArgs& k, int sm_count, cudaStream_t s) {
   if (!w) return -2;
   const size_t smem = knn_walk_bytes(k, w);
   auto kern = k.disjoint ? k_knn_walk<true> : k_knn_walk<false>;
-  if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (!allow_dynamic_smem((const void*)kern, smem))
     return -1;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, w * 32, smem) != cudaSuccess || per_sm < 1)
@@ -2812,7 +2834,7 @@ int launch_knn_bin(const KnnArgs& k, int sm_count, cudaStream_t s) {
   const size_t smem = (size_t)k.cblk * k.H * 32 * 4;
   if (smem > 200 * 1024) return -2;
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(k_knn_bin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      !allow_dynamic_smem((const void*)k_knn_bin, smem))
     return -1;
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_knn_bin, 1024, smem) != cudaSuccess || per_sm < 1)

@@ -446,7 +446,7 @@ def test_lanes_knn_scan(ctx, oracle, block, ratio, with_rdf):
     """The centre-per-lane block scan of kNN passes (disjoint environment sets,
     k up to 12, 1NN, the miss bin) against the oracle and the per-centre scan,
     under a label permutation; with RDF in the same pass the per-centre scan
-    takes it."""
+    takes the pass."""
     spec = synth.cone_specimen(n=50000, r_apex=8.0, half_angle_deg=10.0, length=18.0, n_clusters=25,
                                members=40, nspecies=4, seed=71, nseg=64, stack=4.0)
     cid = ctx.upload(spec.xyz, spec.labels)
@@ -476,10 +476,13 @@ def test_lanes_knn_scan(ctx, oracle, block, ratio, with_rdf):
     assert kernel == ("k_scan" if with_rdf else "k_lanes_knn")
 
 
-def test_lanes_knn_overlapping_sets_fall_back(ctx, oracle):
+@pytest.mark.parametrize("flags", [N.PP_MKNN, N.PP_MKNN | N.PP_RDF | N.PP_1NN])
+def test_lanes_knn_overlapping_sets_fall_back(ctx, oracle, flags):
     """Overlapping environment sets of one centre type take the per-centre scan."""
     spec = synth.cone_specimen(n=30000, r_apex=8.0, half_angle_deg=10.0, length=12.0, n_clusters=10,
                                members=30, nspecies=3, seed=73, nseg=64, stack=4.0)
     trg, env = [[1], [1]], [[1, 2], [2, 3]]
-    gpu, st, ref, _ = _run_both(ctx, oracle, spec, 0.0, 0.01, 1.2, N.PP_MKNN, trg, env, [6, 1])
-    assert st["pairs"] == ref["pairs"] and np.array_equal(gpu, ref["bins"])
+    gpu, st, ref, _ = _run_both(ctx, oracle, spec, 0.0, 0.01, 1.2, flags, trg, env, [6, 1])
+    assert ctx.last_kernel() == "k_scan"
+    assert st["pairs"] == ref["pairs"] and st["centres"] == ref["centres"]
+    assert np.array_equal(gpu, ref["bins"])
