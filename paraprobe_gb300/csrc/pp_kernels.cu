@@ -1423,14 +1423,17 @@ __device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nr
 //   start(self)                a new batch; self = this lane's centre slot or
 //                              0xffffffff; returns the lane's centre position
 //                              (at infinity for no centre)
-//   accept(j, d2)              per test of an in-ball staged ion j (inlined
-//                              into the test loop; a constant true costs nothing)
+//   accept(j, d2, w)           per test of an in-ball staged ion j whose staged
+//                              key is w (inlined into the test loop; a constant
+//                              true costs nothing)
 //   taken(tm, nin)             after each staged batch: tm = the lane's mask,
 //                              nin = its in-ball ions (counted when COUNT)
 //   finish(live)               after the batch's last staged ions
 // In symmetric mode (SYM) a lane takes a staged ion when key > its own slot,
-// otherwise when key != its own slot; stage() sets key accordingly.
-template <bool SYM, bool COUNT, class Stage, class Start, class Accept, class Taken, class Finish>
+// otherwise (KEYED) when key != its own slot; stage() sets key accordingly.
+// Without KEYED the key is free for accept() and the centre itself (d^2 = 0)
+// passes the in-ball test: the pass excludes it.
+template <bool SYM, bool COUNT, bool KEYED, class Stage, class Start, class Accept, class Taken, class Finish>
 __device__ __forceinline__ void lanes_walk(const ScanArgs& a, float4* cand, uint32_t* ccode, Stage stage,
                                            Start start, Accept accept, Taken taken, Finish finish) {
   const Grid& g = a.g;
@@ -1546,9 +1549,9 @@ __device__ __forceinline__ void lanes_walk(const ScanArgs& a, float4* cand, uint
               const float4 c = cand[j];
               const float d2 = dist2(cp.x, cp.y, cp.z, c.x, c.y, c.z);
               const uint32_t k = __float_as_uint(c.w);
-              const bool inball = (d2 <= R2) && (SYM ? (k > self) : (k != self));
+              const bool inball = (d2 <= R2) && (!KEYED || (SYM ? (k > self) : (k != self)));
               if (COUNT) nin += inball ? 1u : 0u;
-              tm |= (inball && accept(j, d2)) ? (1u << j) : 0u;
+              tm |= (inball && accept(j, d2, k)) ? (1u << j) : 0u;
             }
             taken(tm, nin);
             __syncwarp();
@@ -1696,8 +1699,8 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
       }
     }
   };
-  auto accept = [](int, float) { return true; };
-  lanes_walk<SYM, false>(a, cand, ccode, stage, start, accept, taken, finish);
+  auto accept = [](int, float, uint32_t) { return true; };
+  lanes_walk<SYM, false, true>(a, cand, ccode, stage, start, accept, taken, finish);
 
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
   if (lane == 0) {
@@ -1755,13 +1758,16 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
   uint32_t inb = 0;
   float4 cp;
   int cs = -1, nset = 0;
+  uint32_t me = 0xffffffffu;  // this lane's centre slot
   const int last = (K - 1) * 32;
 
+  // the staged key carries the ion's environment set for every centre slot
+  // (read by the test loop with the position), the code its slot
   auto stage = [&](uint32_t slot, const float4& q, uint32_t& key, uint32_t& code) {
-    key = slot;
     const uint32_t m = (a.labels ? (uint32_t)a.labels[slot] : __float_as_uint(q.w)) & 255u;
-    code = 0;
-    for (int c = 0; c < a.nC; ++c) code |= (uint32_t)(sidx[c * 256 + m] & 15) << (4 * c);
+    key = 0;
+    for (int c = 0; c < a.nC; ++c) key |= (uint32_t)(sidx[c * 256 + m] & 15) << (4 * c);
+    code = slot;
   };
   auto start = [&](uint32_t self) {
     cp = make_float4(kInf(), kInf(), kInf(), 0.f);
@@ -1777,12 +1783,13 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     }
     nset = cs >= 0 ? a.nsets[cs] : 0;
     for (int e = 0; e < nset * K; ++e) L[e * 32] = kInf();
+    me = cp.x != kInf() ? self : 0xffffffffu;
     inb = 0;
     return cp;
   };
-  auto accept = [&](int j, float d2) {
+  auto accept = [&](int, float d2, uint32_t w) {
     // set of the staged ion for this lane's centre type (15 = none), then its K-th value
-    const uint32_t p = (ccode[j] >> (4 * (cs < 0 ? 0 : cs))) & 15u;
+    const uint32_t p = (w >> (4 * (cs < 0 ? 0 : cs))) & 15u;
     return p != 15u && d2 < L[p * K * 32 + last];
   };
   auto insert = [&](int p, float d2) {
@@ -1815,14 +1822,16 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     while (tm) {
       const int j = __ffs(tm) - 1;
       tm &= tm - 1u;
+      if (ccode[j] == me) continue;  // the centre itself
       const float4 q = cand[j];
       const float d2 = dist2(cp.x, cp.y, cp.z, q.x, q.y, q.z);
-      insert((int)((ccode[j] >> (4 * cs)) & 15u), d2);
+      insert((int)((__float_as_uint(q.w) >> (4 * cs)) & 15u), d2);
     }
   };
   auto finish = [&](uint32_t live) {
     if (lane == 0) centres += (unsigned long long)__popc(live);
-    pairs_lane += inb;
+    // every live centre met itself once in the in-ball count (d^2 = 0)
+    pairs_lane += inb - (me != 0xffffffffu ? 1u : 0u);
     // the k-th smallest d^2 of each set -> its bin (or the miss bin)
     for (int p = 0; p < nset; ++p) {
       const int Sg = a.set_list[cs * 32 + p];
@@ -1833,7 +1842,7 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
       }
     }
   };
-  lanes_walk<false, true>(a, cand, ccode, stage, start, accept, taken, finish);
+  lanes_walk<false, true, false>(a, cand, ccode, stage, start, accept, taken, finish);
 
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
   if (lane == 0) {
