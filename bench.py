@@ -260,6 +260,7 @@ def run_gpu(args):
     ratio, tile = ctx.autotune(cid, heavy["flags"], heavy["k"], sample=200000)
 
     pass_kernel = ["" for _ in runs]
+    pass_tests = [0 for _ in runs]
 
     def step():
         pairs = 0
@@ -307,6 +308,7 @@ def run_gpu(args):
         ctx.run(cid, r["flags"], r["k"], stream=sh)
         ctx.fetch()
         per_pass_pairs[i] = ctx.stats()["pairs"]
+        pass_tests[i] = ctx.run_tests()
         au = ctx.fp64_audit(cid, max_centres=20000, cap=1 << 16)
         audits.append({"bins": f"{r['hist'][1]} nm", "pairs": au["pairs"],
                        "max_abs_err_nm": au["max_abs_err"], "max_rel_err": au["max_rel_err"],
@@ -363,6 +365,7 @@ def run_gpu(args):
         ms = statistics.mean(per_pass_ms[i])
         ach = BYTES_PER_PAIR * per_pass_pairs[i] / (ms / 1e3) / 1e9
         per_pass.append({"kernel": pass_kernel[i], "ms": round(ms, 3), "pairs": int(per_pass_pairs[i]),
+                         "tests_per_pair": round(pass_tests[i] / max(per_pass_pairs[i], 1), 3),
                          "achieved": round(ach, 1), "frac": round(ach / peak, 4),
                          "traffic": traffic_bytes(args.workload, pass_kernel[i])})
     dom = max(range(len(runs)), key=lambda i: per_pass[i]["ms"])

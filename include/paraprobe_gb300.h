@@ -283,6 +283,11 @@ int pp_last_kernel_ms(pp_ctx* ctx, float* ms);
  * RDF / RIPK and kNN takes the per-centre scan.  No counterpart in the
  * reference. */
 int pp_last_kernel(pp_ctx* ctx, const char** name);
+/* Candidate distance tests (centre, candidate) the last pp_run evaluated --
+ * an implementation figure beside the in-ball pairs of pp_run_stats (their
+ * ratio is the tests per pair the cell grid and the kernel cost).  Synchronises.
+ * No counterpart in the reference. */
+int pp_run_tests(pp_ctx* ctx, uint64_t* tests);
 
 /* Prepare a cloud for queries with r_lo <= rmax <= r_hi (r_hi <= 6 r_lo):
  * builds its cell grid with edge r_lo, the hull lists for R' up to

@@ -138,7 +138,7 @@ struct Result {
   uint32_t nbins = 0;
   int ntasks = 0;
   std::vector<uint32_t> trg, env;  // task masks
-  DevBuf rdf, knn, cnt, counters, status, npc;
+  DevBuf rdf, knn, cnt, counters, status, npc, tests;
   uint64_t ncentres_total = 0, n_ions = 0;
   std::vector<unsigned long long> counters_h;  // per realisation [pairs, centres]
   std::vector<uint64_t> centres_sel;           // per realisation (selected count, plain runs)
@@ -1296,6 +1296,9 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   a.cnt_core = ctx->res.cnt.as<unsigned long long>();
   a.cmax = P.cmax;
   a.counters = ctx->res.counters.as<unsigned long long>();
+  CK(ctx->res.tests.ensure(8));
+  CK(cudaMemsetAsync(ctx->res.tests.p, 0, 8, s));
+  a.tests = ctx->res.tests.as<unsigned long long>();
   a.work = ctx->work.as<uint32_t>();
   a.status = ctx->res.status.as<int>();
   a.mode = 0;
@@ -2238,6 +2241,16 @@ int pp_last_kernel_ms(pp_ctx* ctx, float* ms) {
   if (!ctx->ev_recorded) { *ms = 0.f; return PP_OK; }
   CK(cudaEventSynchronize(ctx->ev1));
   CK(cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+  return PP_OK;
+}
+
+int pp_run_tests(pp_ctx* ctx, uint64_t* tests) {
+  if (!ctx || !tests) return PP_ERR_INVALID;
+  if (!ctx->res.valid || ctx->res.batched) return fail(ctx, PP_ERR_STATE, "no plain run");
+  CK(cudaStreamSynchronize(ctx->res.stream));
+  unsigned long long t = 0;
+  CK(cudaMemcpy(&t, ctx->res.tests.p, 8, cudaMemcpyDeviceToHost));
+  *tests = t;
   return PP_OK;
 }
 

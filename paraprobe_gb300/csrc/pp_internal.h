@@ -78,6 +78,7 @@ struct ScanArgs {
   unsigned long long* cnt_core;  // [nC][nE][cmax + 1]
   int cmax;
   unsigned long long* counters;  // [0] pairs [1] centres
+  unsigned long long* tests;     // candidate distance tests of a plain pass (nullable)
   uint32_t* work;                // dynamic work counter
   int* status;
   int rdf_in_smem;

@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
   const bool doC = (a.flags & PP_CNTNB) && a.mode == 0;
   const bool doK = KR > 0 && a.mode == 0;
   const int krow = (a.kmax - 1) >> 5, klane = (a.kmax - 1) & 31;
-  unsigned long long pairs_lane = 0, centres = 0;
+  unsigned long long pairs_lane = 0, centres = 0, tests_lane = 0;
   constexpr unsigned long long FLUSH = 1ull << 30;
   __shared__ uint32_t s_tile, s_next;
   const uint32_t T = a.tile;
@@ -765,7 +765,8 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
         }
         for_each_candidate(a, S.rowtab, cp, self, lane,
                            [&](bool valid, uint32_t slot, float d2, bool inball, uint32_t m, bool jside) {
-          (void)valid; (void)slot;
+          (void)slot;
+          tests_lane += valid ? 1u : 0u;
           if (inball) {
             ++inb;
             const int es = S.es[m & 255];
@@ -941,9 +942,11 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
     __syncthreads();
   }
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
+  for (int o = 16; o; o >>= 1) tests_lane += __shfl_xor_sync(FULL, tests_lane, o);
   if (lane == 0) {
     atomicAdd(&a.counters[0], pairs_lane);
     atomicAdd(&a.counters[1], centres);
+    if (a.tests && a.mode == 0) atomicAdd(a.tests, tests_lane);
   }
   __syncthreads();
   if (a.rdf_in_smem && doR) {
@@ -1131,7 +1134,7 @@ __global__ void __launch_bounds__(256) k_brick(ScanArgs a) {
   const int8_t* tab = rowtab + 2 * row_table_offset(sr);
   if (sr_need > ROW_SMAX && threadIdx.x == 0) atomicOr(a.status, ST_BAD_SLOT);
   const uint32_t nbx = (uint32_t)((g.nx + a.bx - 1) / a.bx);
-  unsigned long long pairs_lane = 0, centres = 0;
+  unsigned long long pairs_lane = 0, centres = 0, tests_lane = 0;
   constexpr unsigned long long FLUSH = 1ull << 30;
   __shared__ uint32_t s_tile, s_next;
   const uint32_t T = a.tile;
@@ -1258,6 +1261,7 @@ __global__ void __launch_bounds__(256) k_brick(ScanArgs a) {
               if (a.sym) jc = a.cflag[slot] != 0;
             }
             const int esj = ses[m & 255];
+            tests_lane += valid ? (unsigned long long)mc : 0ull;
             for (int c = 0; c < mc; ++c) {
               const float4 cp = cpos[c];
               const uint32_t isl = csl[c];
@@ -1346,9 +1350,11 @@ __global__ void __launch_bounds__(256) k_brick(ScanArgs a) {
     __syncthreads();
   }
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
+  for (int o = 16; o; o >>= 1) tests_lane += __shfl_xor_sync(FULL, tests_lane, o);
   if (lane == 0) {
     atomicAdd(&a.counters[0], pairs_lane);
     atomicAdd(&a.counters[1], centres);
+    if (a.tests) atomicAdd(a.tests, tests_lane);
   }
   __syncthreads();
   if (a.rdf_in_smem && doR) {
@@ -1434,7 +1440,7 @@ __device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nr
 // Without KEYED the key is free for accept() and the centre itself (d^2 = 0)
 // passes the in-ball test: the pass excludes it.
 template <bool SYM, bool COUNT, bool KEYED, class Stage, class Start, class Accept, class Taken, class Finish>
-__device__ __forceinline__ void lanes_walk(const ScanArgs& a, float4* cand, uint32_t* ccode, Stage stage,
+__device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, float4* cand, uint32_t* ccode, Stage stage,
                                            Start start, Accept accept, Taken taken, Finish finish) {
   const Grid& g = a.g;
   const int lane = threadIdx.x & 31;
@@ -1447,6 +1453,7 @@ __device__ __forceinline__ void lanes_walk(const ScanArgs& a, float4* cand, uint
   const uint32_t nbx = (uint32_t)((g.nx + BX - 1) / BX), nby = (uint32_t)((g.ny + BY - 1) / BY);
   const float R2 = a.R2;
   const uint32_t WT = max(a.tile, 1u);
+  unsigned long long tests = 0;  // (centre, staged ion) distance tests, warp-uniform
   for (;;) {
     uint32_t w0 = 0;
     if (lane == 0) w0 = atomicAdd(a.work, WT);
@@ -1523,6 +1530,7 @@ __device__ __forceinline__ void lanes_walk(const ScanArgs& a, float4* cand, uint
           const uint32_t total = __shfl_sync(FULL, inc, 31);
           int before = 0;
           for (uint32_t bb = 0; bb < total; bb += 32) {
+            tests += (unsigned long long)__popc(live) * min(32u, total - bb);
             // stage 32 ions; past the end an ion at infinity, which no lane takes
             const uint32_t bitv = (lane < cnt_rows && rlen > 0 && exc >= bb && exc < bb + 32) ? (1u << (exc - bb)) : 0u;
             const uint32_t smask = __reduce_or_sync(FULL, bitv);
@@ -1562,6 +1570,7 @@ __device__ __forceinline__ void lanes_walk(const ScanArgs& a, float4* cand, uint
       }
     }
   }
+  return tests;
 }
 
 // RDF / RIPK pass.  After each staged batch every lane lists its taken pairs
@@ -1700,7 +1709,8 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
     }
   };
   auto accept = [](int, float, uint32_t) { return true; };
-  lanes_walk<SYM, false, true>(a, cand, ccode, stage, start, accept, taken, finish);
+  const unsigned long long tests = lanes_walk<SYM, false, true>(a, cand, ccode, stage, start, accept, taken, finish);
+  if (lane == 0 && a.tests) atomicAdd(a.tests, tests);
 
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
   if (lane == 0) {
@@ -1842,7 +1852,8 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
       }
     }
   };
-  lanes_walk<false, true, false>(a, cand, ccode, stage, start, accept, taken, finish);
+  const unsigned long long tests = lanes_walk<false, true, false>(a, cand, ccode, stage, start, accept, taken, finish);
+  if (lane == 0 && a.tests) atomicAdd(a.tests, tests);
 
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
   if (lane == 0) {

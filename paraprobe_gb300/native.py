@@ -29,7 +29,7 @@ EXPORTS = (
     "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option", "pp_cloud_prepare",
     "pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_stats", "pp_server_destroy",
     "pp_fp64_audit", "pp_surfdist_noalloc", "pp_batched_graph", "pp_cloud_inside", "pp_fetch_npcorr",
-    "pp_run_aposteriori", "pp_last_kernel",
+    "pp_run_aposteriori", "pp_last_kernel", "pp_run_tests",
 )
 
 _lib = None
@@ -95,6 +95,7 @@ def load():
         "pp_fetch_npcorr": ([vp, vp, u64, C.POINTER(u64)], i32),
         "pp_run_aposteriori": ([vp, i32, vp, u32, vp], i32),
         "pp_last_kernel": ([vp, C.POINTER(C.c_char_p)], i32),
+        "pp_run_tests": ([vp, C.POINTER(u64)], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -158,6 +159,12 @@ class Context:
         if rc:
             msg = self.L.pp_last_error(self.h).decode(errors="replace")
             raise PPError(rc, f"{what}: {self.L.pp_strerror(rc).decode()}: {msg}")
+
+    def run_tests(self) -> int:
+        """Candidate distance tests of the last run."""
+        t = C.c_uint64()
+        self._ck(self.L.pp_run_tests(self.h, C.byref(t)), "pp_run_tests")
+        return t.value
 
     def last_kernel(self) -> str:
         """Name of the stencil kernel the last run took."""

@@ -412,10 +412,11 @@ def test_lanes_scan(ctx, oracle, block, ratio, symmetric):
     try:
         ctx.run(cid, flags, [], label_perm=perm)
         lanes, st = ctx.fetch(), ctx.stats()
-        kernel = ctx.last_kernel()
+        kernel, tests_lanes = ctx.last_kernel(), ctx.run_tests()
         ctx.set_option("lanes", 0)
         ctx.run(cid, flags, [], label_perm=perm)
         scan, st2 = ctx.fetch(), ctx.stats()
+        tests_scan = ctx.run_tests()
     finally:
         ctx.set_option("lanes", 1)
         ctx.set_option("symmetric", 1)
@@ -423,6 +424,7 @@ def test_lanes_scan(ctx, oracle, block, ratio, symmetric):
     ref = oracle.spatstat(spec.xyz, spec.labels[perm], surf, 0.1, 0.02, 1.4, flags, trg, env, [])
     assert kernel == "k_lanes"
     assert st["pairs"] == ref["pairs"] == st2["pairs"] and st["centres"] == ref["centres"]
+    assert tests_lanes >= st["pairs"] // (2 if symmetric else 1) and tests_scan >= st["pairs"] // 2
     assert np.array_equal(lanes, ref["bins"]) and np.array_equal(scan, ref["bins"])
 
 
