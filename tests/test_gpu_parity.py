@@ -488,3 +488,38 @@ def test_lanes_knn_overlapping_sets_fall_back(ctx, oracle, flags):
     assert ctx.last_kernel() == "k_scan"
     assert st["pairs"] == ref["pairs"] and st["centres"] == ref["centres"]
     assert np.array_equal(gpu, ref["bins"])
+
+
+@pytest.mark.parametrize("block", [(1, 1, 1), (8, 8, 8), (64, 15, 15)])
+def test_lanes_small_and_sparse_clouds(ctx, oracle, block):
+    """Centre-per-lane scans on clouds smaller than one cell block, with
+    isolated ions (kNN misses) and coincident positions, through explicit block
+    shapes: RDF (symmetric and one-sided) and kNN against the oracle."""
+    rng = np.random.default_rng(sum(block))
+    a = (rng.random((150, 3)) * 2.0).astype(np.float32)           # a dense 2 nm cube
+    b = (rng.random((40, 3)) * 2.0 + 9.0).astype(np.float32)      # a far, sparse corner
+    c = np.repeat(a[:5], 2, axis=0)                               # coincident pairs
+    xyz = np.concatenate([a, b, c]).astype(np.float32)
+    labels = (rng.integers(1, 4, size=xyz.shape[0])).astype(np.uint8)
+    n = xyz.shape[0]
+    surf = np.full(n, 100.0, dtype=np.float32)
+    cid = ctx.upload(xyz, labels)
+    ctx.surfdist(cid, surf)
+    ctx.tuning(cid, 5.0, LANES(*block))
+    types = [1, 2, 3]
+    trg = [[t] for t in types for _ in types]
+    env = [[u] for _ in types for u in types]
+    ctx.tasks(trg, env)
+    try:
+        for flags, ks, sym in ((N.PP_RDF | N.PP_RIPK, [], 1), (N.PP_RDF, [], 0), (N.PP_1NN | N.PP_MKNN, [4, 2], 1)):
+            ctx.set_option("symmetric", sym)
+            ctx.hist(0.0, 0.02, 1.0)
+            ctx.run(cid, flags, ks)
+            got, st = ctx.fetch(), ctx.stats()
+            assert ctx.last_kernel() in ("k_lanes", "k_lanes_knn")
+            ref = oracle.spatstat(xyz, labels, surf, 0.0, 0.02, 1.0, flags, trg, env, ks)
+            assert st["pairs"] == ref["pairs"] and st["centres"] == ref["centres"]
+            assert np.array_equal(got, ref["bins"])
+    finally:
+        ctx.set_option("symmetric", 1)
+        ctx.free(cid)
