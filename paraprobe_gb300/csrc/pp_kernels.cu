@@ -1982,15 +1982,35 @@ __global__ void __launch_bounds__(1024, 1) k_apply(ApplyArgs a) {
         for (int r = 0; r < G; ++r)
           if (cs[r] >= 0) { atomicAdd(&sCnt[2 * r], o1 - o0); atomicAdd(&sCnt[2 * r + 1], 1ull); }
       }
+      // entries are loaded two steps ahead (category and slot) and one step
+      // ahead (the neighbour's labels), so the dependent loads of a step are
+      // in flight while the step before it is binned
+      int cat_n = 0, cat_nn = 0;
+      uint32_t slot_nn = 0;
+      W nw_n = 0;
+      {
+        const unsigned long long e0 = o0 + lane, e1 = o0 + 32 + lane;
+        if (e0 < o1) {
+          cat_n = a.pair_cat[e0 - a.pair_base];
+          nw_n = lab[a.pair_slot[e0 - a.pair_base]];
+        }
+        if (e1 < o1) {
+          cat_nn = a.pair_cat[e1 - a.pair_base];
+          slot_nn = a.pair_slot[e1 - a.pair_base];
+        }
+      }
       for (unsigned long long k0 = o0; k0 < o1; k0 += 32) {
         if (!L.nrdf && !kn) break;
         const unsigned long long e = k0 + lane;
         const bool valid = e < o1;
-        int cat = 0;
-        W nw = 0;
-        if (valid) {
-          cat = a.pair_cat[e - a.pair_base];
-          nw = lab[a.pair_slot[e - a.pair_base]];
+        const int cat = cat_n;
+        const W nw = nw_n;
+        // advance the pipeline: labels of the next step, entries of the one after
+        cat_n = cat_nn;
+        nw_n = (e + 32 < o1) ? lab[slot_nn] : (W)0;
+        if (e + 64 < o1) {
+          cat_nn = a.pair_cat[e + 64 - a.pair_base];
+          slot_nn = a.pair_slot[e + 64 - a.pair_base];
         }
 #pragma unroll
         for (int r = 0; r < G; ++r) {
@@ -2167,15 +2187,20 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
       for (int q = 0; q < a.nsmax; ++q) cnt[q * 32] = 0;
       const int row = (c >= 0 ? c : a.nC) * 256;
       const unsigned long long o0 = a.pair_off[ci], o1 = a.pair_off[ci + 1];
-      // 32 entries per coalesced load, then neighbour labels 8 at a time
-      // (independent loads in flight), counted in list order
+      // 32 entries per coalesced load (one step ahead), then neighbour labels
+      // 8 at a time (independent loads in flight), counted in list order
+      uint32_t nx_slot = 0, nx_cat = 0;
+      if (o0 + lane < o1) {
+        nx_slot = a.pair_slot[o0 + lane - a.pair_base];
+        nx_cat = a.pair_cat[o0 + lane - a.pair_base];
+      }
       for (unsigned long long e0 = o0; e0 < o1; e0 += 32) {
         if (!__any_sync(FULL, unsat > 0)) break;
         const int ne = (int)min(32ull, o1 - e0);
-        uint32_t my_slot = 0, my_cat = 0;
-        if (lane < ne) {
-          my_slot = a.pair_slot[e0 + lane - a.pair_base];
-          my_cat = a.pair_cat[e0 + lane - a.pair_base];
+        const uint32_t my_slot = nx_slot, my_cat = nx_cat;
+        if (e0 + 32 + lane < o1) {
+          nx_slot = a.pair_slot[e0 + 32 + lane - a.pair_base];
+          nx_cat = a.pair_cat[e0 + 32 + lane - a.pair_base];
         }
         for (int j0 = 0; j0 < ne; j0 += 8) {
           uint32_t t8[8];
