@@ -44,3 +44,47 @@ def test_gpu_voxelizer_matches_reference(ctx, name):
     assert (v["vacuum"], v["surface"], v["inside"]) == (ref["vacuum_bins"], ref["surface_bins"], ref["inside_bins"])
     assert (v["nx"], v["ny"], v["nz"]) == (ref["nx"], ref["ny"], ref["nz"])
     ctx.free(cid)
+
+
+def _groups(flags, ntasks, nk, H):
+    """(flag, offset, length) of each histogram group in the pp_fetch layout."""
+    out, o = [], 0
+    for f, n in ((1, ntasks), (2, ntasks), (4, ntasks), (8, ntasks * nk)):
+        if flags & f:
+            out.append((f, o, n * H))
+            o += n * H
+    return out
+
+
+@pytest.mark.parametrize("name", G.names())
+def test_gpu_lanes_match_reference(ctx, name):
+    """The centre-per-lane scans on the reference fixtures, forced by a cell
+    block shape: the fixture's RDF/RIPK analyses as one pass and its 1NN/kNN
+    analyses as another, each against the matching groups of the reference's
+    bins (passes the centre-per-lane kernels cannot take run the per-centre
+    scan and must match all the same)."""
+    c = G.load(name)
+    flags = c["flags"] & (1 | 2 | 4 | 8)
+    ntasks, nk = len(c["trg"]), len(c["k"]) if c["flags"] & 8 else 0
+    H = c["stats"]["nbins"] + 2
+    ref = {f: c["bins"][o:o + n] for f, o, n in _groups(c["flags"], ntasks, nk, H)}
+    cid = ctx.upload(c["xyz"], c["labels"])
+    if c["hull"].shape[0]:
+        ctx.hull(cid, c["hull"], 2.0)
+    ctx.tuning(cid, 4.0, ((4 | 2 << 8 | 2 << 12) << 16) | 0x100)
+    ctx.tasks(c["trg"], c["env"])
+    ctx.hist(c["rmin"], c["rincr"], c["rmax"])
+    kernels = []
+    for part in (flags & (1 | 4), flags & (2 | 8)):
+        if not part:
+            continue
+        ks = c["k"] if part & 8 else []
+        ctx.run(cid, part, ks)
+        out, st = ctx.fetch(), ctx.stats()
+        kernels.append(ctx.last_kernel())
+        assert st["pairs"] == c["stats"]["pairs"] and st["centres"] == c["stats"]["centres"]
+        want = np.concatenate([ref[f] for f, _, _ in _groups(part, ntasks, len(ks), H)])
+        assert np.array_equal(out, want), (name, part, kernels[-1])
+    ctx.free(cid)
+    assert kernels
+    print(f"{name}: {kernels}")
