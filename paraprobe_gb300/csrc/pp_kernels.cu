@@ -2149,8 +2149,7 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
   int* sNs = (int*)(smem + (size_t)nrow * (DISJ ? 1 : 4));     // [nC]
   int8_t* sC = (int8_t*)(sNs + a.nC);                          // 256
   int8_t* sK = sC + 256;                                       // 256
-  uint16_t* sRes = (uint16_t*)(sK + 256);                      // [nwarps][NT][32]
-  uint8_t* sCnt = (uint8_t*)(sRes + (size_t)nwarps * NT * 32); // [nwarps][nsmax][32]
+  uint8_t* sCnt = (uint8_t*)(sK + 256);                        // [nwarps][nsmax][32]
   __shared__ uint32_t s_item;
   for (int i = threadIdx.x; i < nrow; i += blockDim.x) {
     const bool last = i >= a.nC * 256;
@@ -2163,7 +2162,6 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
   for (int i = threadIdx.x; i < a.nkI; i += blockDim.x)
     if (a.kvals[i] >= 1 && a.kvals[i] <= 255) sK[a.kvals[i]] = (int8_t)i;
   __syncthreads();
-  uint16_t* res = sRes + (size_t)warp * NT * 32 + lane;
   uint8_t* cnt = sCnt + warp * a.nsmax * 32 + lane;
   const uint8_t* lab = a.labels + (uint64_t)a.grp * a.n * 32 + lane;
   const uint8_t* okp = a.centre_ok + (uint64_t)a.grp * a.ncentres * 32 + lane;
@@ -2187,6 +2185,9 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
       for (int q = 0; q < a.nsmax; ++q) cnt[q * 32] = 0;
       const int row = (c >= 0 ? c : a.nC) * 256;
       const unsigned long long o0 = a.pair_off[ci], o1 = a.pair_off[ci + 1];
+      // records of this centre: one 64-byte row per (set, order) slot,
+      // realisations along the row; a slot is written when its member is met
+      uint16_t* out = a.rec + (uint64_t)li * NT * 32 + lane;
       // 32 entries per coalesced load (one step ahead), then neighbour labels
       // 8 at a time (independent loads in flight), counted in list order
       uint32_t nx_slot = 0, nx_cat = 0;
@@ -2219,7 +2220,7 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
                 const int m = cnt[q * 32];
                 if (m < kmax) {
                   const int kk = sK[m + 1];
-                  if (kk >= 0) res[(q * nkI + kk) * 32] = (uint16_t)cat;
+                  if (kk >= 0) out[(q * nkI + kk) * 32] = (uint16_t)cat;
                   cnt[q * 32] = (uint8_t)(m + 1);
                   unsat -= (m + 1 == kmax);
                 }
@@ -2232,7 +2233,7 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
                 const int m = cnt[q * 32];
                 if (m < kmax) {
                   const int kk = sK[m + 1];
-                  if (kk >= 0) res[(q * nkI + kk) * 32] = (uint16_t)cat;
+                  if (kk >= 0) out[(q * nkI + kk) * 32] = (uint16_t)cat;
                   cnt[q * 32] = (uint8_t)(m + 1);
                   unsat -= (m + 1 == kmax);
                 }
@@ -2241,14 +2242,12 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
           }
         }
       }
-      // records: one 64-byte row per slot, realisations along the row
-      uint16_t* out = a.rec + (uint64_t)li * NT * 32 + lane;
+      // the slots not met: misses of the sets, no slot beyond them
       for (int q = 0; q < a.nsmax; ++q) {
         const int got = cnt[q * 32];
         for (int kk = 0; kk < nkI; ++kk) {
-          uint16_t v = 0xffff;
-          if (q < nset) v = got >= a.kvals[kk] ? res[(q * nkI + kk) * 32] : (uint16_t)a.cat_miss;
-          out[(q * nkI + kk) * 32] = v;
+          if (q < nset && got >= a.kvals[kk]) continue;
+          out[(q * nkI + kk) * 32] = q < nset ? (uint16_t)a.cat_miss : (uint16_t)0xffff;
         }
       }
       a.rec_c[(uint64_t)li * 32 + lane] = c >= 0 ? (uint8_t)c : (uint8_t)0xff;
@@ -2840,7 +2839,7 @@ void launch_max_u32(const uint32_t* v, uint64_t n, uint32_t* out, cudaStream_t s
 
 static size_t knn_walk_bytes(const KnnArgs& k, int nwarps) {
   return (size_t)(k.nC + 1) * 256 * (k.disjoint ? 1 : 4) + (size_t)k.nC * 4 + 512 +
-         (size_t)nwarps * k.nsmax * k.nkI * 64 + (size_t)nwarps * k.nsmax * 32;
+         (size_t)nwarps * k.nsmax * 32;
 }
 
 static int knn_walk_warps(const KnnArgs& k) {
