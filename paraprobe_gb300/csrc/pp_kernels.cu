@@ -59,6 +59,44 @@ __device__ __forceinline__ float dist2(float ax, float ay, float az, float bx, f
   return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
+// Two floats in one 64-bit register pair, for the packed f32x2 arithmetic of
+// sm_100+ (one instruction, two IEEE round-to-nearest results).
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// dist2 of one centre (its coordinates duplicated in each pair: cxx = (cx, cx)
+// ...) against two ions whose x, y and z come as pairs: differences and
+// squares packed, the two sums scalar, in dist2's order.  Bit-identical to
+// dist2 on the GPU (checked on 2M random pairs); with the sums packed as well
+// (add.rn.f32x2) 40% of the results differed from dist2 by an ulp or two, so
+// they are not.
+__device__ __forceinline__ void dist2_x2(unsigned long long cxx, unsigned long long cyy, unsigned long long czz,
+                                         unsigned long long xx, unsigned long long yy, unsigned long long zz,
+                                         float& d0, float& d1) {
+  const unsigned long long dx = f2_sub(cxx, xx), dy = f2_sub(cyy, yy), dz = f2_sub(czz, zz);
+  float x0, x1, y0, y1, z0, z1;
+  f2_unpack(f2_mul(dx, dx), x0, x1);
+  f2_unpack(f2_mul(dy, dy), y0, y1);
+  f2_unpack(f2_mul(dz, dz), z0, z1);
+  d0 = __fadd_rn(__fadd_rn(x0, y0), z0);
+  d1 = __fadd_rn(__fadd_rn(x1, y1), z1);
+}
+
 // ------------------------------------------------------------------ K0 / bbox
 __device__ __forceinline__ uint32_t f2o(float f) {
   const uint32_t u = __float_as_uint(f);
@@ -1414,8 +1452,12 @@ __device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nr
 // of bx x by x bz cells (rows of the block in slot order) and streams the
 // block's stencil rows through a per-warp staging buffer, 32 ions at a time;
 // every lane then tests the 32 staged ions against its own centre and keeps a
-// 32-bit mask of the ions it takes.  A test is one broadcast shared load, the
-// exact d^2 and a predicated bit set -- no branch and no store; the row
+// 32-bit mask of the ions it takes.  A test is half a broadcast shared load,
+// the exact d^2 and a predicated bit set -- no branch and no store.  The
+// staged ions are stored in pairs, (x0, x1, y0, y1) (z0, z1, w0, w1), so that
+// one 128-bit load gives the coordinates of two ions as register pairs and
+// the packed f32x2 instructions take their differences and squares two at a
+// time (dist2_x2; staged_ion() reads one ion back); the row
 // mapping, the record load and the type lookups are paid once per staged ion,
 // not once per (centre, ion).  A compact block (cells of R/4 or so, a few
 // cells a side) keeps the staged region close to the union of the centres'
@@ -1439,6 +1481,11 @@ __device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nr
 // otherwise (KEYED) when key != its own slot; stage() sets key accordingly.
 // Without KEYED the key is free for accept() and the centre itself (d^2 = 0)
 // passes the in-ball test: the pass excludes it.
+__device__ __forceinline__ float4 staged_ion(const float4* cand, int j) {
+  const float* f = (const float*)cand + (j >> 1) * 8 + (j & 1);
+  return make_float4(f[0], f[2], f[4], f[6]);
+}
+
 template <bool SYM, bool COUNT, bool KEYED, class Stage, class Start, class Accept, class Taken, class Finish>
 __device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, float4* cand, uint32_t* ccode, Stage stage,
                                            Start start, Accept accept, Taken taken, Finish finish) {
@@ -1509,6 +1556,7 @@ __device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, floa
         const float4 cp = start(self);
         const uint32_t live = __ballot_sync(FULL, cp.x != kInf());
         if (live) self = (cp.x != kInf()) ? self : 0xffffffffu;
+        const unsigned long long cxx = f2_pack(cp.x, cp.x), cyy = f2_pack(cp.y, cp.y), czz = f2_pack(cp.z, cp.z);
         // ---- stencil rows of the block
         for (int r0 = 0; r0 < nrows && live; r0 += 32) {
           uint32_t st, len;
@@ -1547,19 +1595,28 @@ __device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, floa
               q = __ldg(a.ions + slot);
               stage(slot, q, key, code);
             }
-            cand[lane] = make_float4(q.x, q.y, q.z, __uint_as_float(key));
+            {
+              float* f = (float*)cand + (lane >> 1) * 8 + (lane & 1);
+              f[0] = q.x;
+              f[2] = q.y;
+              f[4] = q.z;
+              f[6] = __uint_as_float(key);
+            }
             ccode[lane] = code;
             __syncwarp();
-            // ---- every lane tests the 32 staged ions against its centre
+            // ---- every lane tests the 32 staged ions against its centre, two at a time
             uint32_t tm = 0, nin = 0;
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-              const float4 c = cand[j];
-              const float d2 = dist2(cp.x, cp.y, cp.z, c.x, c.y, c.z);
-              const uint32_t k = __float_as_uint(c.w);
-              const bool inball = (d2 <= R2) && (!KEYED || (SYM ? (k > self) : (k != self)));
-              if (COUNT) nin += inball ? 1u : 0u;
-              tm |= (inball && accept(j, d2, k)) ? (1u << j) : 0u;
+            for (int j = 0; j < 32; j += 2) {
+              const float4 c0 = cand[j], c1 = cand[j + 1];
+              float d0, d1;
+              dist2_x2(cxx, cyy, czz, f2_pack(c0.x, c0.y), f2_pack(c0.z, c0.w), f2_pack(c1.x, c1.y), d0, d1);
+              const uint32_t k0 = __float_as_uint(c1.z), k1 = __float_as_uint(c1.w);
+              const bool in0 = (d0 <= R2) && (!KEYED || (SYM ? (k0 > self) : (k0 != self)));
+              const bool in1 = (d1 <= R2) && (!KEYED || (SYM ? (k1 > self) : (k1 != self)));
+              if (COUNT) nin += (in0 ? 1u : 0u) + (in1 ? 1u : 0u);
+              tm |= (in0 && accept(j, d0, k0)) ? (1u << j) : 0u;
+              tm |= (in1 && accept(j + 1, d1, k1)) ? (2u << j) : 0u;
             }
             taken(tm, nin);
             __syncwarp();
@@ -1644,7 +1701,7 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
   auto bin_pair = [&](uint32_t e) {
     const int c = (int)(e >> 5), j = (int)(e & 31u);
     const float4 p = cpos[c];
-    const float4 q = cand[j];
+    const float4 q = staged_ion(cand, j);
     const float d2 = dist2(p.x, p.y, p.z, q.x, q.y, q.z);
     const uint32_t cj = ccode[j], ci = cinfo[c];
     const int cat = category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
@@ -1833,7 +1890,7 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
       const int j = __ffs(tm) - 1;
       tm &= tm - 1u;
       if (ccode[j] == me) continue;  // the centre itself
-      const float4 q = cand[j];
+      const float4 q = staged_ion(cand, j);
       const float d2 = dist2(cp.x, cp.y, cp.z, q.x, q.y, q.z);
       insert((int)((__float_as_uint(q.w) >> (4 * cs)) & 15u), d2);
     }
