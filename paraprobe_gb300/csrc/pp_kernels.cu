@@ -1474,8 +1474,9 @@ __device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nr
 //   accept(j, d2, w)           per test of an in-ball staged ion j whose staged
 //                              key is w (inlined into the test loop; a constant
 //                              true costs nothing)
-//   taken(tm, nin)             after each staged batch: tm = the lane's mask,
-//                              nin = its in-ball ions (counted when COUNT)
+//   taken(tm, nin, cxx, cyy, czz)  after each staged batch: tm = the lane's
+//                              mask, nin = its in-ball ions (counted when
+//                              COUNT), the centre's coordinates as f32x2 pairs
 //   finish(live)               after the batch's last staged ions
 // In symmetric mode (SYM) a lane takes a staged ion when key > its own slot,
 // otherwise (KEYED) when key != its own slot; stage() sets key accordingly.
@@ -1618,7 +1619,7 @@ __device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, floa
               tm |= (in0 && accept(j, d0, k0)) ? (1u << j) : 0u;
               tm |= (in1 && accept(j + 1, d1, k1)) ? (2u << j) : 0u;
             }
-            taken(tm, nin);
+            taken(tm, nin, cxx, cyy, czz);
             __syncwarp();
           }
         }
@@ -1723,7 +1724,7 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
       }
     }
   };
-  auto taken = [&](uint32_t tm, uint32_t) {
+  auto taken = [&](uint32_t tm, uint32_t, unsigned long long, unsigned long long, unsigned long long) {
     const uint32_t np = __popc(tm);
     uint32_t ex = np;
 #pragma unroll
@@ -1811,11 +1812,15 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
   float* sT = (float*)sp; sp += ((H + 3) & ~3) * 4;
   uint16_t* slut = (uint16_t*)sp; sp += ((a.lut_n + 7) & ~7) * 2;
   int8_t* scs = (int8_t*)sp; sp += 256;
-  int8_t* sidx = (int8_t*)sp;  // [nC][256]
+  uint32_t* skey = (uint32_t*)sp;  // [256] per type: its environment set for every centre slot, 4 bits each
   for (int i = threadIdx.x; i < H; i += blockDim.x) sT[i] = a.cat_T[i];
   for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) slut[i] = a.cat_lut[i];
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) scs[i] = a.cslot_of[i];
-  for (int i = threadIdx.x; i < a.nC * 256; i += blockDim.x) sidx[i] = a.setidx[i];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    scs[i] = a.cslot_of[i];
+    uint32_t key = 0;
+    for (int c = 0; c < a.nC; ++c) key |= (uint32_t)(a.setidx[c * 256 + i] & 15) << (4 * c);
+    skey[i] = key;
+  }
   __syncthreads();
 
   float4* cand = candA + warp * 32;
@@ -1823,21 +1828,19 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
   float* L = listA + (size_t)warp * EM * K * 32 + lane;  // set p, rank r at L[(p * K + r) * 32]
   unsigned long long pairs_lane = 0, centres = 0;
   uint32_t inb = 0;
-  float4 cp;
-  int cs = -1, nset = 0;
-  uint32_t me = 0xffffffffu;  // this lane's centre slot
+  int cs = -1, nset = 0, sh = 0;  // centre slot, its sets, 4 * slot (its nibble in a staged key)
+  uint32_t me = 0xffffffffu;      // this lane's centre slot
   const int last = (K - 1) * 32;
 
   // the staged key carries the ion's environment set for every centre slot
   // (read by the test loop with the position), the code its slot
   auto stage = [&](uint32_t slot, const float4& q, uint32_t& key, uint32_t& code) {
     const uint32_t m = (a.labels ? (uint32_t)a.labels[slot] : __float_as_uint(q.w)) & 255u;
-    key = 0;
-    for (int c = 0; c < a.nC; ++c) key |= (uint32_t)(sidx[c * 256 + m] & 15) << (4 * c);
+    key = skey[m];
     code = slot;
   };
   auto start = [&](uint32_t self) {
-    cp = make_float4(kInf(), kInf(), kInf(), 0.f);
+    float4 cp = make_float4(kInf(), kInf(), kInf(), 0.f);
     cs = -1;
     if (self != 0xffffffffu) {
       cp = a.ions[self];
@@ -1849,6 +1852,7 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
       }
     }
     nset = cs >= 0 ? a.nsets[cs] : 0;
+    sh = 4 * (cs < 0 ? 0 : cs);
     for (int e = 0; e < nset * K; ++e) L[e * 32] = kInf();
     me = cp.x != kInf() ? self : 0xffffffffu;
     inb = 0;
@@ -1856,23 +1860,24 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
   };
   auto accept = [&](int, float d2, uint32_t w) {
     // set of the staged ion for this lane's centre type (15 = none), then its K-th value
-    const uint32_t p = (w >> (4 * (cs < 0 ? 0 : cs))) & 15u;
+    const uint32_t p = (w >> sh) & 15u;
     return p != 15u && d2 < L[p * K * 32 + last];
   };
   auto insert = [&](int p, float d2) {
     float* Lp = L + p * K * 32;
     if (!(d2 < Lp[last])) return;
     if constexpr (KB > 0) {
-      float v[KB];
-      int pos = 0;
+      // the sorted list with d2 in and its largest value out, as a min/max
+      // network: new[r] = min(v[r], max(v[r - 1], d2)), new[0] = min(v[0], d2)
+      float prev = d2;
 #pragma unroll
       for (int r = 0; r < KB; ++r) {
-        v[r] = (r < K) ? Lp[r * 32] : kInf();
-        pos += (r < K && v[r] <= d2) ? 1 : 0;
+        if (r < K) {
+          const float v = Lp[r * 32];
+          Lp[r * 32] = fminf(v, prev);
+          prev = fmaxf(v, d2);
+        }
       }
-#pragma unroll
-      for (int r = 0; r < KB; ++r)
-        if (r < K && r >= pos) Lp[r * 32] = (r == pos) ? d2 : v[r > 0 ? r - 1 : 0];
     } else {
       int r = K - 1;
       while (r > 0) {
@@ -1884,15 +1889,19 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
       Lp[r * 32] = d2;
     }
   };
-  auto taken = [&](uint32_t tm, uint32_t nin) {
+  auto taken = [&](uint32_t tm, uint32_t nin, unsigned long long cxx, unsigned long long cyy, unsigned long long czz) {
     inb += nin;
+    float cx, cy, cz, dup;
+    f2_unpack(cxx, cx, dup);
+    f2_unpack(cyy, cy, dup);
+    f2_unpack(czz, cz, dup);
     while (tm) {
       const int j = __ffs(tm) - 1;
       tm &= tm - 1u;
       if (ccode[j] == me) continue;  // the centre itself
       const float4 q = staged_ion(cand, j);
-      const float d2 = dist2(cp.x, cp.y, cp.z, q.x, q.y, q.z);
-      insert((int)((__float_as_uint(q.w) >> (4 * cs)) & 15u), d2);
+      const float d2 = dist2(cx, cy, cz, q.x, q.y, q.z);
+      insert((int)((__float_as_uint(q.w) >> sh) & 15u), d2);
     }
   };
   auto finish = [&](uint32_t live) {
@@ -2806,7 +2815,7 @@ int launch_lanes(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cud
 size_t lanes_knn_smem(const ScanArgs& a) {
   constexpr int NW = kLanesKnnWarps;
   return NW * 32 * 16 + NW * 32 * 4 + (size_t)NW * (a.emax > 1 ? a.emax : 1) * a.kmax * 32 * 4 +
-         (size_t)((a.H + 3) & ~3) * 4 + (size_t)((a.lut_n + 7) & ~7) * 2 + 256 + (size_t)a.nC * 256;
+         (size_t)((a.H + 3) & ~3) * 4 + (size_t)((a.lut_n + 7) & ~7) * 2 + 256 + 256 * 4;
 }
 
 int launch_lanes_knn(const ScanArgs& a, bool disjoint_sets, int sm_count, size_t* smem_used, cudaStream_t s) {
