@@ -1481,13 +1481,15 @@ __device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nr
 // In symmetric mode (SYM) a lane takes a staged ion when key > its own slot,
 // otherwise (KEYED) when key != its own slot; stage() sets key accordingly.
 // Without KEYED the key is free for accept() and the centre itself (d^2 = 0)
-// passes the in-ball test: the pass excludes it.
+// passes the in-ball test: the pass excludes it.  With GATED, accept() alone
+// decides whether an ion is taken: it must then imply the in-ball test.
 __device__ __forceinline__ float4 staged_ion(const float4* cand, int j) {
   const float* f = (const float*)cand + (j >> 1) * 8 + (j & 1);
   return make_float4(f[0], f[2], f[4], f[6]);
 }
 
-template <bool SYM, bool COUNT, bool KEYED, class Stage, class Start, class Accept, class Taken, class Finish>
+template <bool SYM, bool COUNT, bool KEYED, bool GATED, class Stage, class Start, class Accept, class Taken,
+          class Finish>
 __device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, float4* cand, uint32_t* ccode, Stage stage,
                                            Start start, Accept accept, Taken taken, Finish finish) {
   const Grid& g = a.g;
@@ -1616,8 +1618,8 @@ __device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, floa
               const bool in0 = (d0 <= R2) && (!KEYED || (SYM ? (k0 > self) : (k0 != self)));
               const bool in1 = (d1 <= R2) && (!KEYED || (SYM ? (k1 > self) : (k1 != self)));
               if (COUNT) nin += (in0 ? 1u : 0u) + (in1 ? 1u : 0u);
-              tm |= (in0 && accept(j, d0, k0)) ? (1u << j) : 0u;
-              tm |= (in1 && accept(j + 1, d1, k1)) ? (2u << j) : 0u;
+              tm |= ((GATED || in0) && accept(j, d0, k0)) ? (1u << j) : 0u;
+              tm |= ((GATED || in1) && accept(j + 1, d1, k1)) ? (2u << j) : 0u;
             }
             taken(tm, nin, cxx, cyy, czz);
             __syncwarp();
@@ -1767,7 +1769,7 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
     }
   };
   auto accept = [](int, float, uint32_t) { return true; };
-  const unsigned long long tests = lanes_walk<SYM, false, true>(a, cand, ccode, stage, start, accept, taken, finish);
+  const unsigned long long tests = lanes_walk<SYM, false, true, false>(a, cand, ccode, stage, start, accept, taken, finish);
   if (lane == 0 && a.tests) atomicAdd(a.tests, tests);
 
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
@@ -1786,8 +1788,12 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
 
 // kNN pass (no RDF in the same pass), every type in at most one environment
 // set of each centre type.  Each lane keeps, in shared memory, the K smallest
-// d^2 of its centre per environment set (set p, rank r of lane l at
-// [(p * K + r) * 32 + l]: the lanes never share a bank).  Stencil rows come
+// d^2 of its centre per environment set, largest first (set p, rank r of lane
+// l at [(p * K + K - 1 - r) * 32 + l]: the lanes never share a bank, and the
+// K-th value of set p is row p * K).  The lists start at the float just above
+// R^2, so beating a list's K-th value implies the in-ball test; one more row
+// after the last set holds -inf for the ions in no set of the centre type,
+// which therefore never pass (no separate test for them).  Stencil rows come
 // nearest to the block first, so the lists fill with near ions and their K-th
 // values tighten early.  A staged ion carries its environment set for every
 // centre slot (4 bits each, nC <= 8), and a lane takes it only when its d^2
@@ -1808,29 +1814,33 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
   unsigned char* sp = smem;
   float4* candA = (float4*)sp; sp += NW * 32 * 16;
   uint32_t* ccodeA = (uint32_t*)sp; sp += NW * 32 * 4;
-  float* listA = (float*)sp; sp += (size_t)NW * EM * K * 32 * 4;
+  float* listA = (float*)sp; sp += (size_t)NW * (EM * K + 1) * 32 * 4;
   float* sT = (float*)sp; sp += ((H + 3) & ~3) * 4;
   uint16_t* slut = (uint16_t*)sp; sp += ((a.lut_n + 7) & ~7) * 2;
   int8_t* scs = (int8_t*)sp; sp += 256;
-  uint32_t* skey = (uint32_t*)sp;  // [256] per type: its environment set for every centre slot, 4 bits each
+  uint32_t* skey = (uint32_t*)sp;  // [256] per type: its environment set (EM: none) for every centre slot, 4 bits each
   for (int i = threadIdx.x; i < H; i += blockDim.x) sT[i] = a.cat_T[i];
   for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) slut[i] = a.cat_lut[i];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) {
     scs[i] = a.cslot_of[i];
     uint32_t key = 0;
-    for (int c = 0; c < a.nC; ++c) key |= (uint32_t)(a.setidx[c * 256 + i] & 15) << (4 * c);
+    for (int c = 0; c < a.nC; ++c) {
+      const int si = a.setidx[c * 256 + i];
+      key |= (uint32_t)(si < 0 ? EM : si) << (4 * c);
+    }
     skey[i] = key;
   }
   __syncthreads();
 
   float4* cand = candA + warp * 32;
   uint32_t* ccode = ccodeA + warp * 32;
-  float* L = listA + (size_t)warp * EM * K * 32 + lane;  // set p, rank r at L[(p * K + r) * 32]
+  float* L = listA + (size_t)warp * (EM * K + 1) * 32 + lane;  // set p, rank r at L[(p * K + K - 1 - r) * 32]
+  L[EM * K * 32] = -kInf();                                     // the row of "no set": nothing beats it
+  const float RUP = (a.R2 >= 0.f && a.R2 < kInf()) ? __uint_as_float(__float_as_uint(a.R2) + 1u) : kInf();
   unsigned long long pairs_lane = 0, centres = 0;
   uint32_t inb = 0;
   int cs = -1, nset = 0, sh = 0;  // centre slot, its sets, 4 * slot (its nibble in a staged key)
   uint32_t me = 0xffffffffu;      // this lane's centre slot
-  const int last = (K - 1) * 32;
 
   // the staged key carries the ion's environment set for every centre slot
   // (read by the test loop with the position), the code its slot
@@ -1853,40 +1863,37 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     }
     nset = cs >= 0 ? a.nsets[cs] : 0;
     sh = 4 * (cs < 0 ? 0 : cs);
-    for (int e = 0; e < nset * K; ++e) L[e * 32] = kInf();
+    for (int e = 0; e < nset * K; ++e) L[e * 32] = RUP;
     me = cp.x != kInf() ? self : 0xffffffffu;
     inb = 0;
     return cp;
   };
   auto accept = [&](int, float d2, uint32_t w) {
-    // set of the staged ion for this lane's centre type (15 = none), then its K-th value
-    const uint32_t p = (w >> sh) & 15u;
-    return p != 15u && d2 < L[p * K * 32 + last];
+    // set of the staged ion for this lane's centre type (EM = none), then its K-th value
+    return d2 < L[((w >> sh) & 15u) * K * 32];
   };
   auto insert = [&](int p, float d2) {
-    float* Lp = L + p * K * 32;
-    if (!(d2 < Lp[last])) return;
+    float* Lp = L + p * K * 32;  // row s holds rank K - 1 - s
+    if (!(d2 < Lp[0])) return;
     if constexpr (KB > 0) {
       // the sorted list with d2 in and its largest value out, as a min/max
-      // network: new[r] = min(v[r], max(v[r - 1], d2)), new[0] = min(v[0], d2)
-      float prev = d2;
+      // network over ranks: new[r] = min(v[r], max(v[r - 1], d2)), new[0] =
+      // min(v[0], d2); rank r - 1 is the next row
+      float v[KB];
 #pragma unroll
-      for (int r = 0; r < KB; ++r) {
-        if (r < K) {
-          const float v = Lp[r * 32];
-          Lp[r * 32] = fminf(v, prev);
-          prev = fmaxf(v, d2);
-        }
-      }
+      for (int s = 0; s < KB; ++s) v[s] = (s < K) ? Lp[s * 32] : -kInf();
+#pragma unroll
+      for (int s = 0; s < KB; ++s)
+        if (s < K) Lp[s * 32] = fminf(v[s], fmaxf(s + 1 < KB ? v[s + 1 < KB ? s + 1 : s] : -kInf(), d2));
     } else {
       int r = K - 1;
       while (r > 0) {
-        const float v = Lp[(r - 1) * 32];
+        const float v = Lp[(K - r) * 32];  // rank r - 1
         if (!(v > d2)) break;
-        Lp[r * 32] = v;
+        Lp[(K - 1 - r) * 32] = v;
         --r;
       }
-      Lp[r * 32] = d2;
+      Lp[(K - 1 - r) * 32] = d2;
     }
   };
   auto taken = [&](uint32_t tm, uint32_t nin, unsigned long long cxx, unsigned long long cyy, unsigned long long czz) {
@@ -1912,13 +1919,13 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     for (int p = 0; p < nset; ++p) {
       const int Sg = a.set_list[cs * 32 + p];
       for (int kk = 0; kk < a.nkI; ++kk) {
-        const float v = L[(p * K + a.kvals[kk] - 1) * 32];
-        const int cat = (v == kInf()) ? a.cat_miss : category_lut(v, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+        const float v = L[(p * K + K - a.kvals[kk]) * 32];
+        const int cat = (v == RUP) ? a.cat_miss : category_lut(v, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
         if (cat >= 0) atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
       }
     }
   };
-  const unsigned long long tests = lanes_walk<false, true, false>(a, cand, ccode, stage, start, accept, taken, finish);
+  const unsigned long long tests = lanes_walk<false, true, false, true>(a, cand, ccode, stage, start, accept, taken, finish);
   if (lane == 0 && a.tests) atomicAdd(a.tests, tests);
 
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
@@ -2814,7 +2821,7 @@ int launch_lanes(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cud
 
 size_t lanes_knn_smem(const ScanArgs& a) {
   constexpr int NW = kLanesKnnWarps;
-  return NW * 32 * 16 + NW * 32 * 4 + (size_t)NW * (a.emax > 1 ? a.emax : 1) * a.kmax * 32 * 4 +
+  return NW * 32 * 16 + NW * 32 * 4 + (size_t)NW * ((a.emax > 1 ? a.emax : 1) * a.kmax + 1) * 32 * 4 +
          (size_t)((a.H + 3) & ~3) * 4 + (size_t)((a.lut_n + 7) & ~7) * 2 + 256 + 256 * 4;
 }
 
