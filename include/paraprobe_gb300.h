@@ -165,9 +165,12 @@ int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int n
 int pp_run_aposteriori(pp_ctx* ctx, int cloud, const uint8_t* clustered, uint32_t flags, void* stream);
 /* Project-written autotuner: times the pass on about `sample` centres
  * (0 = 200000) for cell edges R/2 .. R/5 -- for passes the centre-per-lane
- * scan takes, at two cell-block shapes per edge; for other passes with the
- * per-centre scan at block tiles of 32, 128 and 512 centres and with the
- * brick scan at bricks of 4, 8 and 16 cells -- keeps the fastest for this
+ * scan takes, at the default cell block of that edge (about a warp of
+ * centres) and two fixed shapes; for other passes with the per-centre scan at
+ * block tiles of 32, 128 and 512 centres and with the brick scan at bricks of
+ * 4, 8 and 16 cells, and for passes with RDF / RIPK and kNN together (no
+ * CNTNB or NPCORR) of dense centres also as two centre-per-lane passes at
+ * those cell blocks -- keeps the fastest for this
  * cloud and rebuilds its cell grid.  best_tile comes back in the
  * pp_cloud_tuning encoding.  Uses the current tasks and histogram settings;
  * results of the trial runs are discarded.  Has no counterpart in the
@@ -184,7 +187,12 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
  * bz in 0..15 (0 = 1) = blocks of bx x by x bz cells for the centre-per-lane
  * scan that RDF / RIPK passes without CNTNB take (one centre per lane, the
  * block's stencil ions staged in shared memory; default 4 x 2 x 2), leaving
- * the other code as it was.  Results do not depend on the tuning. */
+ * the other code as it was.  With a cell block set this way, a pass with
+ * RDF / RIPK and kNN together (no CNTNB or NPCORR) runs as two passes: the
+ * RDF / RIPK part on the centre-per-lane scan, then the kNN part on the
+ * centre-per-lane kNN scan (the per-centre scan for overlapping environment
+ * sets or lists too large for shared memory).  Results do not depend on the
+ * tuning. */
 int pp_cloud_tuning(pp_ctx* ctx, int cloud, float cell_ratio, uint32_t tile);
 
 /* FP64 audit of the current tasks and histogram settings on up to
@@ -277,10 +285,12 @@ int pp_last_kernel_ms(pp_ctx* ctx, float* ms);
 /* Name of the stencil kernel the last pp_run took: "k_scan" (per-centre
  * scan), "k_brick" (brick scan), "k_lanes" (centre-per-lane scan of RDF /
  * RIPK passes) or "k_lanes_knn" (centre-per-lane scan of kNN passes); a static
- * string.  The centre-per-lane scans take passes of dense centres (at least
- * 0.35 per non-empty cell, or a block shape set with pp_cloud_tuning) without
- * CNTNB or NPCORR, kNN only with disjoint environment sets; a pass with both
- * RDF / RIPK and kNN takes the per-centre scan.  No counterpart in the
+ * string; "k_lanes+k_lanes_knn" or "k_lanes+k_scan" for a pass with RDF /
+ * RIPK and kNN run as two passes (see pp_cloud_tuning).  The centre-per-lane
+ * scans take passes of dense centres (at least 0.35 per non-empty cell, or a
+ * block shape set with pp_cloud_tuning) without CNTNB or NPCORR, kNN only with
+ * disjoint environment sets; a pass with both RDF / RIPK and kNN takes the
+ * per-centre scan unless a block shape is set.  No counterpart in the
  * reference. */
 int pp_last_kernel(pp_ctx* ctx, const char** name);
 /* Candidate distance tests (centre, candidate) the last pp_run evaluated --

@@ -198,7 +198,9 @@ struct pp_ctx {
   std::string apply_sig;
   uint64_t graph_nodes = 0, graph_captures = 0, graph_launches = 0;
   bool ev_recorded = false;
-  int last_kind = 0;  // kernel of the last plain pass: 0 per-centre scan, 1 brick, 2/3 centre-per-lane RDF/kNN
+  int last_kind = 0;  // kernel of the last plain pass: 0 per-centre scan, 1 brick, 2/3 centre-per-lane RDF/kNN,
+                      // 4/5 centre-per-lane RDF then centre-per-lane kNN / per-centre kNN
+  uint64_t last_centres_all = 0;  // centres of the last plain pass before any tuning sample
 };
 
 namespace {
@@ -1273,6 +1275,7 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   if (labels_override) labels = labels_override;
   uint32_t ncent = 0;
   if ((rc = select_centres(ctx, *cl, labels, surf, D.cslot, R, &ncent, s))) return rc;
+  ctx->last_centres_all = ncent;
   // a tuning sample: every stride-th centre (or brick) over the whole cloud
   uint32_t stride = 1;
   if (centre_limit && ncent > centre_limit) {
@@ -1281,8 +1284,10 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   }
   ctx->res.ncentres_total = ncent;
   ctx->res.n_ions = n;
-  CK(ctx->work.ensure(16));
-  CK(cudaMemsetAsync(ctx->work.p, 0, 16, s));
+  // work counters of up to two launches, then pair / centre counters for a
+  // second launch that must not count them again
+  CK(ctx->work.ensure(32));
+  CK(cudaMemsetAsync(ctx->work.p, 0, 32, s));
   pp::ScanArgs a{};
   fill_scan_common(a, *cl, P, D, ctx->tab);
   a.labels = labels;
@@ -1304,9 +1309,13 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   a.mode = 0;
   a.sample_stride = stride;
   a.rdf_in_smem = ((a.flags & PP_RDF) && (size_t)P.nC * P.nE * P.H * 4 <= 96 * 1024) ? 1 : 0;
+  // RDF / RIPK and kNN in one pass on a cloud tuned to a centre-per-lane cell
+  // block: two centre-per-lane passes, RDF / RIPK then kNN
+  const bool split = P.kr > 0 && (a.flags & PP_RDF) && cl->lanes_bx && !ctx->no_lanes &&
+                     !(flags & (PP_CNTNB | PP_NPCORR));
   // RDF / RIPK alone: each pair of two centres is computed once and credited
   // to both (the counts are the same as the per-centre ball scan's)
-  a.sym = (P.kr == 0 && !(flags & PP_CNTNB) && (a.flags & PP_RDF) && !ctx->no_sym) ? 1 : 0;
+  a.sym = ((P.kr == 0 || split) && !(flags & PP_CNTNB) && (a.flags & PP_RDF) && !ctx->no_sym) ? 1 : 0;
   a.cflag = ctx->cflag.as<uint8_t>();
   if (a.sym) {
     CK(ctx->nc_pre.ensure((cl->g.ncells + 1) * 4));
@@ -1323,7 +1332,7 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
     const bool rows_fit = (int)std::floor((R + 3.f * g.margin) * g.inv_h) + 1 <= 7;
     // centre-per-lane scans: cell block and its stencil rows
     bool lanes = rows_fit && !ctx->no_lanes && !(flags & (PP_CNTNB | PP_NPCORR)) &&
-                 !(P.kr > 0 && (a.flags & PP_RDF));
+                 (split || !(P.kr > 0 && (a.flags & PP_RDF)));
     if (lanes && cl->lanes_bx) {
       a.bx = (int)cl->lanes_bx;
       a.by = (int)std::max<uint32_t>(cl->lanes_by, 1);
@@ -1336,9 +1345,41 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
     if (lanes && (rc = ensure_block_rows(ctx, a.by, a.bz, a.bsr, s, &a.brows)) != PP_OK) return rc;
     CK(cudaEventRecord(ctx->ev0, s));
     rc = -3;
-    // passes with RDF / RIPK and kNN together take the per-centre scan: it
-    // serves both from one candidate stream, which measured as fast as or
-    // faster than the two centre-per-lane scans one after the other
+    // passes with RDF / RIPK and kNN together take the per-centre scan, which
+    // serves both from one candidate stream, unless the cloud is tuned to a
+    // cell block (the autotuner times both): then the RDF / RIPK part and the
+    // kNN part run as two centre-per-lane passes, the second on a fresh work
+    // counter and with its pair and centre counts dropped (the first counted
+    // them)
+    if (rc == -3 && a.brows && split) {
+      const uint64_t nb_x = ((uint64_t)g.nx + a.bx - 1) / a.bx, nb_y = ((uint64_t)g.ny + a.by - 1) / a.by;
+      uint64_t nb = nb_x * nb_y * (((uint64_t)g.nz + a.bz - 1) / a.bz);
+      if (stride > 1) nb = std::max<uint64_t>(1, nb / stride);
+      if (nb < (1ull << 32)) {
+        pp::ScanArgs ar = a;
+        ar.nbricks = (uint32_t)nb;
+        ar.tile = 4;
+        rc = pp::launch_lanes(ar, 0, ctx->sm_count, &smem, s);
+        if (rc == 0) {
+          pp::ScanArgs ak = a;
+          ak.flags &= ~(uint32_t)(PP_RDF | PP_RIPK);
+          ak.sym = 0;
+          ak.work = a.work + 1;
+          ak.counters = (unsigned long long*)(ctx->work.as<unsigned char>() + 16);
+          ak.nbricks = (uint32_t)nb;
+          ak.tile = 4;
+          rc = pp::launch_lanes_knn(ak, P.disjoint != 0, ctx->sm_count, &smem, s);
+          ctx->last_kind = 4;
+          if (rc == -3) {  // overlapping sets, or lists too large for shared memory
+            ak.tile = a.tile;
+            rc = pp::launch_scan(ak, P.kr, P.emax, ctx->sm_count, &smem, s);
+            ctx->last_kind = 5;
+          }
+          if (rc == -3) rc = -1;  // the RDF part already ran
+        }
+      }
+    }
+    if (P.kr > 0) a.sym = 0;  // the per-centre scans need every centre's whole ball
     if (rc == -3 && a.brows && P.kr == 0 && (a.flags & PP_RDF)) {
       const uint64_t nb_x = ((uint64_t)g.nx + a.bx - 1) / a.bx, nb_y = ((uint64_t)g.ny + a.by - 1) / a.by;
       uint64_t nb = nb_x * nb_y * (((uint64_t)g.nz + a.bz - 1) / a.bz);
@@ -1540,11 +1581,17 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
       cl->lanes_bz = t >> 28;
     } else if (t >= 65536u) {
       cl->brick = t;
+      cl->lanes_bx = cl->lanes_by = cl->lanes_bz = 0;
     } else {
       cl->tile = t;
       cl->brick = 0;
+      cl->lanes_bx = cl->lanes_by = cl->lanes_bz = 0;
     }
   };
+  // RDF / RIPK with kNN in one pass: the per-centre scan's tiles and the two
+  // centre-per-lane passes a cell block gives
+  const bool combined = (flags & (PP_RDF | PP_RIPK)) && (flags & (PP_1NN | PP_MKNN)) &&
+                        !(flags & (PP_CNTNB | PP_NPCORR)) && !ctx->no_lanes;
   float bestr = keep_ratio, bestms = 1e30f;
   uint32_t bestt = 0;
   int rc = PP_OK;
@@ -1555,8 +1602,23 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
     cl->lanes_bx = cl->lanes_by = cl->lanes_bz = 0;
     if ((rc = run_plain(ctx, cl, flags, k_list, nk, nullptr, 0, sample))) break;
     const bool lanes = ctx->last_kind >= 2;
-    const uint32_t* tiles = lanes ? lanes_tiles[ri] : scan_tiles;
-    const int ntiles = lanes ? 2 : (int)(sizeof scan_tiles / sizeof scan_tiles[0]);
+    // two fixed cell-block shapes; for RDF / RIPK with kNN also the default
+    // block at this cell edge (about a warp of centres), as the fixed shapes
+    // are sized for R = 2 nm at atom-probe densities.  (Offered to single
+    // passes too, the default block won on the tuning sample but lost on the
+    // whole 20M-ion tip, so they keep the two shapes.)
+    int dbx = 0, dby = 0, dbz = 0;
+    const bool dense = combined && default_block(*cl, ctx->last_centres_all, &dbx, &dby, &dbz);
+    uint32_t tiles[sizeof scan_tiles / sizeof scan_tiles[0] + 3];
+    int ntiles = 0;
+    if (!lanes)
+      for (uint32_t t : scan_tiles) tiles[ntiles++] = t;
+    if (lanes || dense) {
+      const uint32_t dcode = (!lanes && dense) ? lanes_code((uint32_t)dbx, (uint32_t)dby, (uint32_t)dbz) : 0u;
+      if (dcode && dcode != lanes_tiles[ri][0] && dcode != lanes_tiles[ri][1]) tiles[ntiles++] = dcode;
+      tiles[ntiles++] = lanes_tiles[ri][0];
+      tiles[ntiles++] = lanes_tiles[ri][1];
+    }
     for (int ti = 0; ti < ntiles && rc == PP_OK; ++ti) {
       apply(tiles[ti]);
       float ms = 0.f;
@@ -1566,8 +1628,11 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
       }
       if (rc == PP_OK && ms < bestms) { bestms = ms; bestr = ratios[ri]; bestt = tiles[ti]; }
     }
-    if (lanes) { cl->lanes_bx = keep[2]; cl->lanes_by = keep[3]; cl->lanes_bz = keep[4]; }
-    else { cl->tile = keep[0]; cl->brick = keep[1]; }
+    cl->tile = keep[0];
+    cl->brick = keep[1];
+    cl->lanes_bx = keep[2];
+    cl->lanes_by = keep[3];
+    cl->lanes_bz = keep[4];
   }
   if (rc != PP_OK) {
     cl->cell_ratio = keep_ratio;
@@ -2256,8 +2321,9 @@ int pp_run_tests(pp_ctx* ctx, uint64_t* tests) {
 
 int pp_last_kernel(pp_ctx* ctx, const char** name) {
   if (!ctx || !name) return PP_ERR_INVALID;
-  static const char* names[] = {"k_scan", "k_brick", "k_lanes", "k_lanes_knn"};
-  *name = names[ctx->last_kind < 0 || ctx->last_kind > 3 ? 0 : ctx->last_kind];
+  static const char* names[] = {"k_scan", "k_brick", "k_lanes", "k_lanes_knn", "k_lanes+k_lanes_knn",
+                                "k_lanes+k_scan"};
+  *name = names[ctx->last_kind < 0 || ctx->last_kind > 5 ? 0 : ctx->last_kind];
   return PP_OK;
 }
 

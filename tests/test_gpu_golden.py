@@ -85,6 +85,17 @@ def test_gpu_lanes_match_reference(ctx, name):
         assert st["pairs"] == c["stats"]["pairs"] and st["centres"] == c["stats"]["centres"]
         want = np.concatenate([ref[f] for f, _, _ in _groups(part, ntasks, len(ks), H)])
         assert np.array_equal(out, want), (name, part, kernels[-1])
+    if flags & (1 | 4) and flags & (2 | 8):
+        # both in one pass: the RDF/RIPK and the kNN centre-per-lane passes
+        # (or the per-centre scan for kNN with overlapping sets) one after the other
+        ks = c["k"] if flags & 8 else []
+        ctx.run(cid, flags, ks)
+        out, st = ctx.fetch(), ctx.stats()
+        kernels.append(ctx.last_kernel())
+        assert kernels[-1].startswith("k_lanes+")
+        assert st["pairs"] == c["stats"]["pairs"] and st["centres"] == c["stats"]["centres"]
+        want = np.concatenate([ref[f] for f, _, _ in _groups(flags, ntasks, len(ks), H)])
+        assert np.array_equal(out, want), (name, flags, kernels[-1])
     ctx.free(cid)
     assert kernels
     print(f"{name}: {kernels}")

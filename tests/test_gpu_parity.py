@@ -360,6 +360,33 @@ def test_batched_32_lane_groups_and_rest(ctx, oracle, nsets):
     ctx.free(cid)
 
 
+@pytest.mark.parametrize("nspecies,ks", [(10, [12, 3, 1]), (6, [20, 9, 2, 1]), (8, [5, 4, 3, 2, 1])])
+def test_batched_walk_set_counts(ctx, oracle, nspecies, ks):
+    """The 32-realisation kNN walk with one environment set per species for
+    every centre type (six, eight or ten sets), k up to 20, realisations of the
+    first 32-lane group and of the second."""
+    spec = synth.cone_specimen(n=20000, r_apex=8.0, half_angle_deg=10.0, length=10.0, n_clusters=10,
+                               members=40, nspecies=nspecies, seed=83 + nspecies, nseg=48, stack=4.0,
+                               iid=(0.04, 0.03, 0.02))
+    types = list(range(1, nspecies + 1))
+    trg = [[a] for a in types[:3] for b in types]
+    env = [[b] for a in types[:3] for b in types]
+    flags = N.PP_1NN | N.PP_MKNN
+    sets = np.stack([N.shuffle_labels(spec.labels, 1300 + s) for s in range(33)])
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks(trg, env)
+    ctx.hist(0.0, 0.01, 1.2)
+    ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets)
+    assert ctx.batched_count() == 34
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    for r in (0, 1, 31, 32, 33):
+        lab = spec.labels if r == 0 else sets[r - 1]
+        ref = oracle.spatstat(spec.xyz, lab, surf, 0.0, 0.01, 1.2, flags, trg, env, ks)
+        assert np.array_equal(ctx.fetch_batched(r), ref["bins"]), r
+    ctx.free(cid)
+
+
 @pytest.mark.parametrize("order", [0, 4])
 def test_npcorr_matches_oracle(ctx, oracle, order):
     """n-point correlations (analysis mode 5) with overlapping environment sets,
@@ -447,8 +474,9 @@ def test_lanes_scan_rdf_bins_in_global_memory(ctx, oracle):
 def test_lanes_knn_scan(ctx, oracle, block, ratio, with_rdf):
     """The centre-per-lane block scan of kNN passes (disjoint environment sets,
     k up to 12, 1NN, the miss bin) against the oracle and the per-centre scan,
-    under a label permutation; with RDF in the same pass the per-centre scan
-    takes the pass."""
+    under a label permutation; with RDF in the same pass on a cloud tuned to a
+    cell block, the RDF and the kNN centre-per-lane passes run one after the
+    other and the pairs are counted once."""
     spec = synth.cone_specimen(n=50000, r_apex=8.0, half_angle_deg=10.0, length=18.0, n_clusters=25,
                                members=40, nspecies=4, seed=71, nseg=64, stack=4.0)
     cid = ctx.upload(spec.xyz, spec.labels)
@@ -475,7 +503,40 @@ def test_lanes_knn_scan(ctx, oracle, block, ratio, with_rdf):
     ref = oracle.spatstat(spec.xyz, spec.labels[perm], surf, 0.0, 0.01, 1.3, flags, trg, env, ks)
     assert st["pairs"] == ref["pairs"] and st["centres"] == ref["centres"]
     assert np.array_equal(lanes, ref["bins"]) and np.array_equal(scan, ref["bins"])
-    assert kernel == ("k_scan" if with_rdf else "k_lanes_knn")
+    assert kernel == ("k_lanes+k_lanes_knn" if with_rdf else "k_lanes_knn")
+
+
+@pytest.mark.parametrize("symmetric", [1, 0])
+def test_combined_pass_split_with_overlapping_sets(ctx, oracle, symmetric):
+    """RDF/RIPK with kNN on a cloud tuned to a cell block, overlapping
+    environment sets: the RDF part takes the centre-per-lane scan, the kNN part
+    the per-centre scan; untuned, the whole pass takes the per-centre scan."""
+    spec = synth.cone_specimen(n=40000, r_apex=8.0, half_angle_deg=10.0, length=14.0, n_clusters=12,
+                               members=30, nspecies=3, seed=79, nseg=64, stack=4.0)
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    trg, env = [[1], [1], [2, 3]], [[1, 2], [2, 3], [1, 2, 3]]
+    ks = [7, 3, 1]
+    flags = N.PP_RDF | N.PP_RIPK | N.PP_1NN | N.PP_MKNN
+    ctx.tasks(trg, env)
+    ctx.hist(0.05, 0.01, 1.25)
+    ref = oracle.spatstat(spec.xyz, spec.labels, surf, 0.05, 0.01, 1.25, flags, trg, env, ks)
+    ctx.set_option("symmetric", symmetric)
+    try:
+        ctx.run(cid, flags, ks)
+        got, st = ctx.fetch(), ctx.stats()
+        assert ctx.last_kernel() == "k_scan"
+        assert st["pairs"] == ref["pairs"] and np.array_equal(got, ref["bins"])
+        ctx.tuning(cid, 4.0, LANES(4, 2, 2))
+        ctx.run(cid, flags, ks)
+        got, st = ctx.fetch(), ctx.stats()
+        assert ctx.last_kernel() == "k_lanes+k_scan"
+        assert st["pairs"] == ref["pairs"] and st["centres"] == ref["centres"]
+        assert np.array_equal(got, ref["bins"])
+    finally:
+        ctx.set_option("symmetric", 1)
+        ctx.free(cid)
 
 
 @pytest.mark.parametrize("flags", [N.PP_MKNN, N.PP_MKNN | N.PP_RDF | N.PP_1NN])
@@ -511,12 +572,13 @@ def test_lanes_small_and_sparse_clouds(ctx, oracle, block):
     env = [[u] for _ in types for u in types]
     ctx.tasks(trg, env)
     try:
-        for flags, ks, sym in ((N.PP_RDF | N.PP_RIPK, [], 1), (N.PP_RDF, [], 0), (N.PP_1NN | N.PP_MKNN, [4, 2], 1)):
+        for flags, ks, sym in ((N.PP_RDF | N.PP_RIPK, [], 1), (N.PP_RDF, [], 0), (N.PP_1NN | N.PP_MKNN, [4, 2], 1),
+                               (N.PP_RDF | N.PP_MKNN, [3, 1], 1)):
             ctx.set_option("symmetric", sym)
             ctx.hist(0.0, 0.02, 1.0)
             ctx.run(cid, flags, ks)
             got, st = ctx.fetch(), ctx.stats()
-            assert ctx.last_kernel() in ("k_lanes", "k_lanes_knn")
+            assert ctx.last_kernel() in ("k_lanes", "k_lanes_knn", "k_lanes+k_lanes_knn")
             ref = oracle.spatstat(xyz, labels, surf, 0.0, 0.02, 1.0, flags, trg, env, ks)
             assert st["pairs"] == ref["pairs"] and st["centres"] == ref["centres"]
             assert np.array_equal(got, ref["bins"])
