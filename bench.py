@@ -1,12 +1,12 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 spatial-statistics path: neighbour pairs/s.
 
-Default workload ("tip20m", the plain-method tip configuration): 20,000,000
+Default workload ("tip20m", the plain method on an atom-probe tip): 20,000,000
 ions in a truncated cone (apex radius 30 nm, half-angle 10 deg, length 200 nm;
 density follows from N and the geometry, 13.42 nm^-3), Poisson matrix plus
 2,000 Gaussian solute clusters (sigma 1.5 nm, 50 members, species 1/2 at
 70/30 %), three iid minority species -- six species in all.  One step is the
-two passes the reference needs for that configuration (it has one bin width
+two passes the reference needs for that workload (it has one bin width
 per run): all 36 pairwise RDFs to R = 2.0 nm in 0.01 nm bins, then kNN
 k = 1..10 for all 36 pairs in 0.005 nm bins, both with centres excluded within
 R of the triangulated cone surface.  A neighbour pair is one in-ball
@@ -65,7 +65,7 @@ def workload(name):
                            "k=1..10 R=2.0/0.005, hull-distance exclusion",
                "ions": n, "tasks": 36, "R_nm": 2.0}
     elif name == "tip150m":
-        # configuration 5: apex r 50 nm, 12 deg, L 400 nm, 150M ions, 8 species,
+        # the 150M-ion tip: apex r 50 nm, 12 deg, L 400 nm, 8 species,
         # 5000 clusters; RDF and kNN k = 1..20 for all 64 pairs in one pass
         # (one bin geometry, 2.5 nm / 0.01 nm)
         n = 150_000_000
@@ -94,7 +94,7 @@ def workload(name):
 
 
 def tip_cloud(n, seed):
-    """A clustered cone "as in configuration 2": same apex, angle, density
+    """A clustered cone like the tip20m one: same apex, angle, density
     (13.42 nm^-3) and cluster density, length shortened to hold n ions."""
     from paraprobe_gb300 import synth
     rho = 20_000_000 / synth.cone_volume(30.0, 10.0, 200.0)
@@ -412,7 +412,7 @@ def run_gpu(args):
 
 # ---------------------------------------------------- batched (null model + ROIs)
 def batched_leg(ctx, torch, stream):
-    """Configuration 3: a 5M-ion clustered tip, 256 label shuffles (own seeds)
+    """Batched realisations: a 5M-ion clustered tip, 256 label shuffles (own seeds)
     and 64 spherical ROIs (radius log-uniform 5-40 nm, centres uniform in the
     tip) plus the measured labels, RDF to R = 1.5 nm and kNN k = 1..8 in
     0.01 nm bins for all 36 pair tasks -- every realisation in one persistent
@@ -475,7 +475,7 @@ def batched_leg(ctx, torch, stream):
     apply_ms = ctx.last_kernel_ms()
     graph = ctx.batched_graph()
     ctx.free(cid)
-    return {"workload": "5M-ion clustered tip (as configuration 2), 36 pair tasks, RDF + kNN k=1..8, "
+    return {"workload": "5M-ion clustered tip (as tip20m), 36 pair tasks, RDF + kNN k=1..8, "
                         "R=1.5 nm, 0.01 nm bins; 1 measured + 256 shuffled label sets + 64 ROIs",
             "realisations": nreal, "pairs": int(pairs), "value": pairs / cold, "unit": UNIT,
             "seconds": round(cold, 4), "apply_graph_ms": round(apply_ms, 3),
@@ -488,7 +488,7 @@ def batched_leg(ctx, torch, stream):
 
 
 def batched_leg_large(ctx, cid, spec, trg, env, run, torch, stream, plain_pairs, plain_ms):
-    """Configuration 5's batched form: the measured labels plus 32 label
+    """The 150M-ion tip batched: the measured labels plus 32 label
     shuffles in one batched call on the resident 150M-ion cloud.  Its pair
     lists (about 10^11 pairs) exceed HBM, so they are built and applied a chunk
     of centres at a time.  Compared with the plain pass on the same cloud."""
@@ -509,7 +509,7 @@ def batched_leg_large(ctx, cid, spec, trg, env, run, torch, stream, plain_pairs,
     el = time.perf_counter() - t0
     apply_ms = ctx.last_kernel_ms()
     plain = plain_pairs / (statistics.mean(plain_ms) * 1e-3)
-    return {"workload": "configuration 5 batched: 1 measured + 32 shuffled label sets, RDF + kNN k=1..20, "
+    return {"workload": "tip150m batched: 1 measured + 32 shuffled label sets, RDF + kNN k=1..20, "
                         "R=2.5/0.01, 64 pair tasks, pair lists built and applied in centre chunks",
             "realisations": nreal, "pairs": int(pairs), "value": pairs / el, "unit": UNIT, "seconds": round(el, 3),
             "apply_graph_ms": round(apply_ms, 3), "cuda_graph": ctx.batched_graph(),
@@ -520,8 +520,8 @@ def batched_leg_large(ctx, cid, spec, trg, env, run, torch, stream, plain_pairs,
 
 # ------------------------------------------------------------- served queries
 def served_leg(ctx, nq=240, rate=200.0):
-    """Configuration 4: six resident clouds (0.1M .. 50M ions, as
-    configuration 2); queries arrive as a Poisson stream at `rate`/s, each with
+    """Serving: six resident clouds (0.1M .. 50M ions, tips like
+    tip20m); queries arrive as a Poisson stream at `rate`/s, each with
     a random cloud, R ~ U[0.5, 3.0] nm, k ~ U[1, 20] and a random species pair
     (RDF + kNN, 0.01 nm bins).  Continuous batching on 4 worker streams,
     admission by HBM footprint; compared with the same queries run one at a
