@@ -2241,7 +2241,7 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
             k.grp = g;
             k.c0 = c0;
             k.cn = std::min(chunk, ch.c1 - c0);
-            k.tile = 64;
+            k.tile = 4;  // centres per warp work item
             if (cudaMemsetAsync(k.work, 0, 4, st) != cudaSuccess) return fail(ctx, PP_ERR_CUDA, "memset failed");
             if (pp::launch_knn_walk(k, ctx->sm_count, st)) return fail(ctx, PP_ERR_CUDA, "kNN walk launch failed");
             const uint32_t nranges = (uint32_t)std::max<uint64_t>(1, (8ull * ctx->sm_count + NT - 1) / NT);

@@ -2212,7 +2212,7 @@ __global__ void __launch_bounds__(1024, 1) k_apply(ApplyArgs a) {
 template <bool DISJ>
 __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int NT = a.nsmax * a.nkI;
   // set table per centre type, plus a last row that matches nothing (lanes
   // that are no centre in their realisation walk it without effect):
@@ -2223,7 +2223,6 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
   int8_t* sC = (int8_t*)(sNs + a.nC);                          // 256
   int8_t* sK = sC + 256;                                       // 256
   uint8_t* sCnt = (uint8_t*)(sK + 256);                        // [nwarps][nsmax][32]
-  __shared__ uint32_t s_item;
   for (int i = threadIdx.x; i < nrow; i += blockDim.x) {
     const bool last = i >= a.nC * 256;
     if (DISJ) ((int8_t*)sTab)[i] = last ? (int8_t)-1 : a.setidx[i];
@@ -2241,14 +2240,15 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
   const bool real = a.grp * 32 + lane < a.nreal;
   const int kmax = a.kmax, nkI = a.nkI;
   const uint32_t ntiles = (a.cn + a.tile - 1) / a.tile;
+  // each warp fetches its own tile of centres (no block barrier: list
+  // lengths differ from centre to centre)
   for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(a.work, 1u);
-    __syncthreads();
-    const uint32_t item = s_item;
-    __syncthreads();
+    uint32_t item = 0;
+    if (lane == 0) item = atomicAdd(a.work, 1u);
+    item = __shfl_sync(FULL, item, 0);
     if (item >= ntiles) break;
     const uint32_t l0 = item * a.tile, l1 = min(l0 + a.tile, a.cn);
-    for (uint32_t li = l0 + warp; li < l1; li += nwarps) {
+    for (uint32_t li = l0; li < l1; ++li) {
       const uint32_t ci = a.c0 + li;
       const uint32_t self = a.centres[ci];
       const bool ok = real && okp[(uint64_t)ci * 32] != 0;
