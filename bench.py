@@ -207,32 +207,96 @@ def reduce_max(pg, x):
 
 
 # ------------------------------------------------------------ CPU (oracle)
-def cpu_measure(spec, trg, env, runs, target_s, threads):
-    """Oracle port on a bounded sample: a random subset of centre candidates
-    (centre mask), same cloud, tasks and passes.  Returns pairs/s of the
-    statistics phase (DescrStatsThreadparallelCompute) and a description."""
+# One sample rule for every CPU figure (the GPU arm's cpu_baseline leg and the
+# reference arm): the ions whose key (uniform on [0, 1), numpy seed 7) is
+# below the workload's fraction may be centres; the whole cloud stays the
+# environment.  The same mask drives the GPU parity check of the GPU arm.
+CPU_SAMPLE = {"tip20m": 0.02, "tip10m": 0.04, "cyl1m": 1.0, "tip150m": 0.002}
+
+
+def sample_mask(n, frac):
+    if frac >= 1.0:
+        return None
+    return (np.random.default_rng(7).random(n) < frac).astype(np.uint8)
+
+
+def cpu_leg(name, steps, warmup, threads):
+    """The oracle port (the reference's algorithm: z-slabs, per-slab KD-trees,
+    per-centre statistics; OpenMP on `threads` host threads) on the workload's
+    centre sample.  Times the three phases the reference reports separately:
+    Ion2SurfThreadparallelDistancing (hull distance of every ion, once),
+    ThreadparallelKDTreeConstruct (decomposition and KD-trees, once per pass)
+    and DescrStatsThreadparallelCompute (the statistics over the sampled
+    centres).  Returns (record, bins of each pass)."""
     from oracle import oracle as O
-    surf = O.surface_distance(spec.xyz, spec.hull, max(2.0, runs[0]["hist"][2]), nthreads=threads)
+    spec, trg, env, runs, cfg = workload(name)
     n = spec.xyz.shape[0]
-    rng = np.random.default_rng(7)
-    keys = rng.random(n)
+    frac = CPU_SAMPLE[name]
+    mask = sample_mask(n, frac)
+    rp = max(2.0, max(r["hist"][2] for r in runs))
+    t0 = time.perf_counter()
+    surf = O.surface_distance(spec.xyz, spec.hull, rp, nthreads=threads)
+    surf_s = time.perf_counter() - t0
 
-    def one(frac):
-        mask = (keys < frac).astype(np.uint8)
-        pairs = 0
-        secs = 0.0
-        for r in runs:
-            out = O.spatstat(spec.xyz, spec.labels, surf, *r["hist"], r["flags"], trg, env, r["k"],
-                             centre_mask=mask, nthreads=threads)
-            pairs += out["pairs"]
-            secs += out["compute_s"]
-        return pairs, secs
+    def step():
+        return [O.spatstat(spec.xyz, spec.labels, surf, *r["hist"], r["flags"], trg, env, r["k"],
+                           centre_mask=mask, nthreads=threads) for r in runs]
 
-    p0, s0 = one(min(1.0, 2e5 / n))
-    rate = p0 / max(s0, 1e-6)
-    frac = min(1.0, max(1e-4, (min(1.0, 2e5 / n)) * target_s / max(s0, 1e-3)))
-    p1, s1 = one(frac)
-    return p1 / max(s1, 1e-9), frac, p1, s1, rate
+    for _ in range(warmup):
+        step()
+    pairs, comp_s, build_s, outs = 0, 0.0, 0.0, []
+    for _ in range(steps):
+        outs = step()
+        pairs += sum(o["pairs"] for o in outs)
+        comp_s += sum(o["compute_s"] for o in outs)
+        build_s += sum(o["build_s"] for o in outs)
+    per_step_pairs = pairs // max(steps, 1)
+    stat_s = comp_s / max(steps, 1)
+    build_step_s = build_s / max(steps, 1)
+    # one whole step of the reference (every centre, every pass: each pass is
+    # a separate reference run with its own hull distancing and KD-trees)
+    full_stat_s = stat_s / frac
+    full_s = len(runs) * surf_s + build_step_s + full_stat_s
+    rec = {"value": pairs / max(comp_s, 1e-9), "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"oracle port (z-slab KD-trees + OpenMP, restating the reference) over "
+                     f"{frac * 100:g}% of the ions as candidate centres (numpy seed 7 keys), whole cloud as "
+                     f"environment; {steps} timed step(s) after {warmup} warm-up; value = statistics phase",
+           "sample_fraction": frac, "pairs_per_step": int(per_step_pairs),
+           "phases": {"surface_distancing_s": round(surf_s, 4),
+                      "surface_distancing_ions_per_s": n / max(surf_s, 1e-9),
+                      "kdtree_build_s_per_step": round(build_step_s, 4),
+                      "kdtree_build_ions_per_s": n * len(runs) / max(build_step_s, 1e-9),
+                      "statistics_s_per_step": round(stat_s, 4),
+                      "statistics_pairs_per_s": per_step_pairs / max(stat_s, 1e-9)},
+           "full_step_estimate": {"seconds": round(full_s, 3),
+                                  "pairs": int(per_step_pairs / frac),
+                                  "pairs_per_s": per_step_pairs / frac / full_s,
+                                  "rule": "passes x hull distancing + KD-tree builds + statistics / sample "
+                                          "fraction"}}
+    return rec, [o["bins"] for o in outs]
+
+
+def cpu_leg_subprocess(name, steps, warmup):
+    """cpu_leg in a fresh interpreter (no CUDA context, no torch), so that the
+    GPU arm's CPU figure is taken exactly as the reference arm's."""
+    fd, path = tempfile.mkstemp(suffix=".npz")
+    os.close(fd)
+    try:
+        subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-leg", "--workload", name,
+                        "--steps", str(steps), "--warmup", str(warmup), "--cpu-out", path],
+                       check=True, stdout=subprocess.DEVNULL)
+        z = np.load(path, allow_pickle=False)
+        rec = json.loads(str(z["record"]))
+        bins = [z[f"bins{i}"] for i in range(int(z["npass"]))]
+        return rec, bins
+    finally:
+        os.unlink(path)
+
+
+def cpu_leg_main(args):
+    threads = os.cpu_count() or 1
+    rec, bins = cpu_leg(args.workload, args.steps, args.warmup, threads)
+    np.savez(args.cpu_out, record=json.dumps(rec), npass=len(bins), **{f"bins{i}": b for i, b in enumerate(bins)})
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -346,7 +410,7 @@ def run_gpu(args):
     t0 = time.perf_counter()
     e_pairs = 0
     d2h = 0
-    e_steps = max(1, min(args.steps, 3))
+    e_steps = max(3, min(args.steps, 10))
     for _ in range(e_steps):
         p, d2h = e2e_step()
         e_pairs += p
@@ -387,12 +451,27 @@ def run_gpu(args):
             "roofline": roof, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
             "fp64_audit": audits}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        rate, frac, p, s, _ = cpu_measure(spec, trg, env, runs, args.cpu_seconds, threads)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"oracle port (KD-tree + OpenMP, restating the reference), "
-                                          f"{frac * 100:.3f}% of ions eligible as centres "
-                                          f"({p} pairs, {s:.1f} s statistics phase)"}
+        # the oracle on the workload's centre sample (a fresh process), then
+        # the GPU pass on the same sample: the bins must be identical
+        rec, cpu_bins = cpu_leg_subprocess(args.workload, steps=2, warmup=1)
+        line["cpu_baseline"] = rec
+        mask = sample_mask(n, CPU_SAMPLE[args.workload])
+        checks = []
+        for i, r in enumerate(runs):
+            ctx.tasks(trg, env)
+            ctx.hist(*r["hist"])
+            ctx.run(cid, r["flags"], r["k"], stream=sh, centre_mask=mask)
+            g = ctx.fetch()
+            st = ctx.stats()
+            same = g.shape == cpu_bins[i].shape and bool(np.array_equal(g, cpu_bins[i]))
+            checks.append({"pass": i + 1, "kernel": ctx.last_kernel(), "centres": st["centres"],
+                           "pairs": st["pairs"], "bins": int(g.size), "bins_identical": same,
+                           "bins_differing": int(np.count_nonzero(g != cpu_bins[i])) if g.shape == cpu_bins[i].shape
+                           else int(g.size)})
+        line["parity"] = {"against": "oracle port on the cpu_baseline sample (same centre mask, same cloud)",
+                          "sample_fraction": CPU_SAMPLE[args.workload],
+                          "centres": sum(c["centres"] for c in checks), "pairs": sum(c["pairs"] for c in checks),
+                          "bins_identical": all(c["bins_identical"] for c in checks), "passes": checks}
     if not args.no_batched:
         if args.workload == "tip150m":
             line["batched"] = batched_leg_large(ctx, cid, spec, trg, env, runs[0], torch, stream,
@@ -594,44 +673,24 @@ def served_leg(ctx, nq=240, rate=200.0):
 
 # ------------------------------------------------------------ reference arm
 def run_reference(args):
+    """The reference's CPU algorithm (the oracle port; the reference's own
+    units do not build on the Arm host) on all host cores, each step the
+    workload's centre sample, with the same sample rule as the GPU arm's
+    cpu_baseline leg."""
     world, rank, local, pg = dist_setup()
     if rank != 0:
         if pg is not None:
             pg.barrier()
             pg.destroy_process_group()
         return
-    spec, trg, env, runs, cfg = workload(args.workload)
-    from oracle import oracle as O
+    _, _, _, runs, cfg = workload(args.workload)
     threads = os.cpu_count() or 1
-    surf = O.surface_distance(spec.xyz, spec.hull, max(2.0, runs[0]["hist"][2]), nthreads=threads)
-    n = spec.xyz.shape[0]
-    keys = np.random.default_rng(7).random(n)
-    frac = min(1.0, 4e5 / n) if args.workload.startswith("tip") else min(1.0, 2e5 / n)
-    mask = (keys < frac).astype(np.uint8)
-
-    def step():
-        pairs, secs = 0, 0.0
-        for r in runs:
-            out = O.spatstat(spec.xyz, spec.labels, surf, *r["hist"], r["flags"], trg, env, r["k"],
-                             centre_mask=mask, nthreads=threads)
-            pairs += out["pairs"]
-            secs += out["compute_s"]
-        return pairs, secs
-
-    for _ in range(args.warmup):
-        step()
-    tp, ts = 0, 0.0
-    for _ in range(args.steps):
-        p, s = step()
-        tp += p
-        ts += s
-    value = tp / ts
+    rec, _ = cpu_leg(args.workload, args.steps, args.warmup, threads)
+    value = rec["value"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ts / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": dict(cfg, passes=len(runs)),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"oracle port on {frac * 100:.2f}% of ions eligible as centres per step"},
+            "warmup": args.warmup, "ms_per_step": rec["phases"]["statistics_s_per_step"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference", "config": dict(cfg, passes=len(runs)), "cpu_baseline": rec,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     if pg is not None:
@@ -646,11 +705,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="tip20m", choices=["tip20m", "tip10m", "cyl1m", "tip150m"])
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-leg", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-out", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched realisation leg")
     ap.add_argument("--no-served", action="store_true", help="skip the serving leg")
     args = ap.parse_args()
+    if args.cpu_leg:
+        cpu_leg_main(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -150,6 +150,15 @@ int pp_hist_params(pp_ctx* ctx, float rmin, float rincr, float rmax);
  * null model of rndlabeler, src/PARAPROBE_SolverHdl.cpp:2809-3003). */
 int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk,
            const uint32_t* label_perm, void* stream);
+/* pp_run with the centres restricted further: centre_mask holds n bytes in
+ * input order (host memory), and only ions whose byte is nonzero may be
+ * centres, on top of the reference's filter (type is a target, ion2surf >=
+ * R^2, src/PARAPROBE_SolverHdl.cpp:3847-3859).  Neighbours stay every ion.
+ * Used to sample centres (the results equal the reference's per-centre loop
+ * run over those centres only) and for caller-defined regions.  The
+ * reference has no such mask; its per-centre loop is the same. */
+int pp_run_masked(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk,
+                  const uint32_t* label_perm, const uint8_t* centre_mask, void* stream);
 /* Descriptive statistics after clustering, for the current histogram
  * settings and hull (clustertask::flag2exclude_guard and generic_spatstat,
  * src/PARAPROBE_SolverHdl.cpp:4790-4945).  clustered: n bytes in input order,

@@ -164,6 +164,7 @@ struct pp_ctx {
   DevBuf tmp_cell_of, tmp_rank, scan_tmp, bbox, centres, centre_count, work, tables_dev, sel_flags, sel_tmp;
   DevBuf tri_fill, cflag, rowtab, nc_pre;
   DevBuf labels_run, perm_dev, gather_src;
+  DevBuf mask_in;  // caller's centre mask: [n] input order, then [n] sorted-slot order
   // batched geometry cache
   DevBuf pair_count, pair_off, pair_slot, pair_cat, geo_centres, centre_ok, real_labels, rois_dev;
   DevBuf labels_il, ok_il;  // group-major interleaved copies of real_labels / centre_ok
@@ -1226,7 +1227,7 @@ int ensure_block_rows(pp_ctx* ctx, int by, int bz, int sr, cudaStream_t s, const
 // Select the centres of a plain run into ctx->centres (cell order); returns
 // their number.  Synchronises the stream once to learn the count.
 int select_centres(pp_ctx* ctx, Cloud& cl, const uint8_t* labels, const float* surf, const int8_t* cslot, float R,
-                   uint32_t* ncent, cudaStream_t s) {
+                   uint32_t* ncent, cudaStream_t s, const uint8_t* extra_slot_mask = nullptr) {
   const uint64_t n = cl.n;
   CK(ctx->centres.ensure(std::max<uint64_t>(n, 1) * 4));
   CK(ctx->centre_count.ensure(8));
@@ -1235,7 +1236,7 @@ int select_centres(pp_ctx* ctx, Cloud& cl, const uint8_t* labels, const float* s
   CK(ctx->sel_tmp.ensure(tmp_elems * 4 * 2));
   CK(ctx->cflag.ensure(std::max<uint64_t>(n, 1)));
   pp::launch_select_centres(labels ? labels : cl.label_sorted.as<uint8_t>(), surf, n, R * R, cslot,
-                            nullptr, ctx->sel_flags.as<uint32_t>(), ctx->sel_tmp.as<uint32_t>(), tmp_elems * 2,
+                            extra_slot_mask, ctx->sel_flags.as<uint32_t>(), ctx->sel_tmp.as<uint32_t>(), tmp_elems * 2,
                             ctx->centres.as<uint32_t>(), ctx->centre_count.as<uint32_t>(), ctx->cflag.as<uint8_t>(), s);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(ncent, ctx->centre_count.p, 4, cudaMemcpyDeviceToHost, s));
@@ -1247,9 +1248,11 @@ int select_centres(pp_ctx* ctx, Cloud& cl, const uint8_t* labels, const float* s
 // restricts the pass to the first centres (cell order), for tuning.
 // labels_override (sorted-slot order) replaces the cloud's labels; no_miss
 // drops the kNN miss dump (a centre without a neighbour adds nothing).
+// centre_mask (host, input order, nullable): only ions with a nonzero byte
+// may be centres, on top of the type and hull-distance filter.
 int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, int nk, const uint32_t* label_perm,
               cudaStream_t s, uint32_t centre_limit, const uint8_t* labels_override = nullptr,
-              bool no_miss = false) {
+              bool no_miss = false, const uint8_t* centre_mask = nullptr) {
   RunPlan P;
   int rc = make_plan(ctx, flags, k_list, nk, P);
   if (rc) return rc;
@@ -1273,8 +1276,18 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
     labels = ctx->labels_run.as<uint8_t>();
   }
   if (labels_override) labels = labels_override;
+  // caller's centre mask: input order -> sorted-slot order
+  const uint8_t* mask_slot = nullptr;
+  if (centre_mask) {
+    CK(ctx->mask_in.ensure(std::max<uint64_t>(n, 1) * 2));
+    uint8_t* m_in = ctx->mask_in.as<uint8_t>();
+    CK(cudaMemcpyAsync(m_in, centre_mask, n, cudaMemcpyHostToDevice, s));
+    pp::launch_gather_labels(m_in, cl->id_of_slot.as<uint32_t>(), n, m_in + n, 1, s);
+    CK(cudaGetLastError());
+    mask_slot = m_in + n;
+  }
   uint32_t ncent = 0;
-  if ((rc = select_centres(ctx, *cl, labels, surf, D.cslot, R, &ncent, s))) return rc;
+  if ((rc = select_centres(ctx, *cl, labels, surf, D.cslot, R, &ncent, s, mask_slot))) return rc;
   ctx->last_centres_all = ncent;
   // a tuning sample: every stride-th centre (or brick) over the whole cloud
   uint32_t stride = 1;
@@ -1473,6 +1486,16 @@ int pp_run(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int n
   if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
   CK(cudaSetDevice(ctx->device));
   return run_plain(ctx, cl, flags, k_list, nk, label_perm, (cudaStream_t)stream, 0);
+}
+
+int pp_run_masked(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, int nk, const uint32_t* label_perm,
+                  const uint8_t* centre_mask, void* stream) {
+  if (!ctx) return PP_ERR_INVALID;
+  Cloud* cl = get_cloud(ctx, cloud);
+  if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
+  if (!centre_mask) return fail(ctx, PP_ERR_INVALID, "centre_mask is NULL (use pp_run)");
+  CK(cudaSetDevice(ctx->device));
+  return run_plain(ctx, cl, flags, k_list, nk, label_perm, (cudaStream_t)stream, 0, nullptr, false, centre_mask);
 }
 
 // Statistics after clustering (clustertask::flag2exclude_guard and

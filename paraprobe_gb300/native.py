@@ -29,7 +29,7 @@ EXPORTS = (
     "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option", "pp_cloud_prepare",
     "pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_stats", "pp_server_destroy",
     "pp_fp64_audit", "pp_surfdist_noalloc", "pp_batched_graph", "pp_cloud_inside", "pp_fetch_npcorr",
-    "pp_run_aposteriori", "pp_last_kernel", "pp_run_tests",
+    "pp_run_aposteriori", "pp_last_kernel", "pp_run_tests", "pp_run_masked",
 )
 
 _lib = None
@@ -65,6 +65,7 @@ def load():
         "pp_tasks_set": ([vp, vp, vp, i32], i32),
         "pp_hist_params": ([vp, f32, f32, f32], i32),
         "pp_run": ([vp, i32, u32, vp, i32, vp, vp], i32),
+        "pp_run_masked": ([vp, i32, u32, vp, i32, vp, vp, vp], i32),
         "pp_fetch": ([vp, vp, C.c_size_t], i32),
         "pp_fetch_cntnb": ([vp, vp, C.c_size_t, C.POINTER(u64)], i32),
         "pp_result_size": ([vp, C.POINTER(u64), C.POINTER(u64)], i32),
@@ -240,11 +241,17 @@ class Context:
     def hist(self, rmin, rincr, rmax):
         self._ck(self.L.pp_hist_params(self.h, rmin, rincr, rmax), "pp_hist_params")
 
-    def run(self, cloud, flags, k_list=(), label_perm=None, stream=0):
+    def run(self, cloud, flags, k_list=(), label_perm=None, stream=0, centre_mask=None):
+        """One pass; centre_mask (n bytes, input order) restricts the centres further."""
         ks = np.ascontiguousarray(np.asarray(k_list, dtype=np.uint32))
         perm = None if label_perm is None else np.ascontiguousarray(label_perm, dtype=np.uint32)
-        self._ck(self.L.pp_run(self.h, cloud, flags, _p(ks) if ks.size else None, ks.size, _p(perm),
-                               C.c_void_p(stream)), "pp_run")
+        if centre_mask is None:
+            self._ck(self.L.pp_run(self.h, cloud, flags, _p(ks) if ks.size else None, ks.size, _p(perm),
+                                   C.c_void_p(stream)), "pp_run")
+        else:
+            cm = np.ascontiguousarray(centre_mask, dtype=np.uint8)
+            self._ck(self.L.pp_run_masked(self.h, cloud, flags, _p(ks) if ks.size else None, ks.size, _p(perm),
+                                          _p(cm), C.c_void_p(stream)), "pp_run_masked")
 
     def autotune(self, cloud, flags, k_list=(), sample=0):
         ks = np.ascontiguousarray(np.asarray(k_list, dtype=np.uint32))

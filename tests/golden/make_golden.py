@@ -12,8 +12,9 @@ centre/pair statistics, ion-to-hull distances, the occupancy grid's
 NumberOfIonsInside / VolumeInside (which head the RDF files) and the CSV
 files.
 
-Run in the development container (the reference tree must be present):
-    make -C oracle/ref REF=/root/reference
+Run where the reference tree is present (its location in
+PARAPROBE_REFERENCE_TREE, or the default oracle/ref/Makefile names):
+    make -C oracle/ref
     python tests/golden/make_golden.py
 """
 from __future__ import annotations
