@@ -124,13 +124,17 @@ int pp_cloud_inside(pp_ctx* ctx, int cloud, float bin_width_min, float bin_width
  * n packed (x, y, z) floats, tri ntri triangles of 9 floats, d2_out receives n
  * floats in input order -- the same values pp_hull_upload + pp_run +
  * pp_surfdist_fetch give for R' = max(rmax, carve radius).  The triangle
- * boxes, grid and lists live in one static 64 MiB array per device, held from
- * module load until exit; hulls above 2,000,000 triangles are rejected with
- * PP_ERR_UNSUPPORTED, hulls whose lists still do not fit with PP_ERR_OVERFLOW.
- * The first call on a device looks the array up (cudaGetSymbolAddress) and
- * should come before any stream capture.  Calls share the array: calls whose
- * GPU work overlaps (different streams, unordered threads) race.  A message
- * goes to err (err_cap bytes) when it is not NULL.  stream may be NULL. */
+ * boxes, grid and lists live in one static 64 MiB array per device, held until
+ * exit; hulls above 2,000,000 triangles are rejected with PP_ERR_UNSUPPORTED,
+ * hulls whose lists still do not fit with PP_ERR_OVERFLOW.  The first call on
+ * a device looks the array up (cudaGetSymbolAddress); with the runtime's lazy
+ * module loading (the default) that is when the 64 MiB are taken, so a caller
+ * whose own pool takes the whole device first makes one call with n = 0 (set-up
+ * only, no other argument is read but rp) on each device, before the pool
+ * takes it and before any stream capture.  The address is cached per device:
+ * not usable across cudaDeviceReset.  Calls share the array: calls whose GPU
+ * work overlaps (different streams, unordered threads) race.  A message goes
+ * to err (err_cap bytes) when it is not NULL.  stream may be NULL. */
 int pp_surfdist_noalloc(const float* xyz, uint64_t n, const float* tri, uint64_t ntri, float rp,
                         float* d2_out, void* stream, char* err, size_t err_cap);
 
@@ -170,7 +174,14 @@ int pp_run_masked(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list
  * result is one task in the pp_fetch layout; the tasks set with pp_tasks_set
  * stay as they were.  The reference's guard loop flags ions_kdtree.at(cand),
  * the candidate's position in its result list, instead of the candidate
- * itself (:4807-4815); this library flags the candidate. */
+ * itself (:4807-4815); by default this library flags the candidate.  With
+ * option "aposteriori_guard" = 1 it runs the loop as the reference does
+ * instead, positions being the cloud's input order (upload the ions in the
+ * order of the clustering task's KD-tree, ions_kdtree, :4737-4787): for each
+ * position i in order whose ion is clustered -- flagged, or relabelled by an
+ * earlier step -- the ions at positions 0 .. |ball(i)| - 1 take i's clustered
+ * type (flag_as_guarded returns a clustered type unchanged, :4576-4582), so
+ * they leave the statistics as centres and as neighbours. */
 int pp_run_aposteriori(pp_ctx* ctx, int cloud, const uint8_t* clustered, uint32_t flags, void* stream);
 /* Project-written autotuner: times the pass on about `sample` centres
  * (0 = 200000) for cell edges R/2 .. R/5 -- for passes the centre-per-lane
@@ -236,6 +247,9 @@ int pp_fetch_npcorr(pp_ctx* ctx, uint32_t* counts, uint64_t cap, uint64_t* edge)
  *                       scan (default 1); 0 = the per-centre or brick scan.
  *                       Results are identical either way.
  *   "npcorr_order"      SpatStatKNNOrder - 1 for PP_NPCORR (0..31, default 0).
+ *   "aposteriori_guard" pp_run_aposteriori's guard zone: 0 = every
+ *                       unclustered ion within R of a clustered ion (default),
+ *                       1 = the reference's guard loop as written (see there).
  *   "batched_pair_cap"  most pairs pp_run_batched holds at once; larger lists
  *                       are built and applied a chunk of centres at a time
  *                       (0 = sized from free device memory, the default). */

@@ -68,7 +68,7 @@ def lib():
                                  C.c_uint32, u32p, C.c_uint64, C.POINTER(C.c_uint64)]
         L.ppo_npcorr.restype = C.c_int
         L.ppo_aposteriori.argtypes = [f32p, u8p, f32p, C.c_uint64, C.c_float, C.c_float, C.c_float, C.c_uint32,
-                                      u64p, C.c_uint64, u64p]
+                                      C.c_int, u64p, C.c_uint64, u64p]
         L.ppo_aposteriori.restype = C.c_int
         _lib = L
     return _lib
@@ -179,9 +179,11 @@ def npcorr(xyz, labels, ion2surf, rincr, rmax, trg, env, order):
     return out.reshape(len(trg), edge, edge, edge)
 
 
-def aposteriori(xyz, clustered, ion2surf, rmin, rincr, rmax, analyses):
+def aposteriori(xyz, clustered, ion2surf, rmin, rincr, rmax, analyses, guard_mode=0):
     """Statistics after clustering: ({"rdf"|"1nn"|"ripk": (H,) uint64}, stats),
-    stats = (centres, guard ions, centres without an unclustered neighbour)."""
+    stats = (centres, guard ions, centres without an unclustered neighbour).
+    guard_mode 0: every unclustered ion within R of a clustered one is guard;
+    1: the reference's guard loop as written (positions = input order)."""
     xyz = np.ascontiguousarray(xyz, dtype=np.float32)
     clus = np.ascontiguousarray(clustered, dtype=np.uint8)
     surf = np.ascontiguousarray(ion2surf, dtype=np.float32)
@@ -190,7 +192,7 @@ def aposteriori(xyz, clustered, ion2surf, rmin, rincr, rmax, analyses):
     out = np.zeros(max(1, len(names)) * H, dtype=np.uint64)
     st = np.zeros(3, dtype=np.uint64)
     rc = lib().ppo_aposteriori(xyz.reshape(-1), clus, surf, xyz.shape[0], np.float32(rmin), np.float32(rincr),
-                               np.float32(rmax), analyses, out, out.size, st)
+                               np.float32(rmax), analyses, guard_mode, out, out.size, st)
     if rc:
         raise RuntimeError(f"ppo_aposteriori failed ({rc})")
     return {nm: out[i * H:(i + 1) * H].copy() for i, nm in enumerate(names)}, tuple(int(v) for v in st)

@@ -749,8 +749,18 @@ int ppo_npcorr(const float* xyz, const uint8_t* label, const float* ion2surf, ui
 // smallest one and nothing without one (:4886-4913).  out: [RDF][1NN][RIPK]
 // histograms (each present when asked), H = nbins + 2 uint64 each;
 // stats = {centres, guard ions, centres without a neighbour}.
+//
+// guard_mode 1 restates the guard loop as the reference runs it
+// (:4804-4820): positions are the input order (the reference's ions_kdtree
+// order); for every position i, in order, whose ion is clustered -- flagged,
+// or relabelled by an earlier step -- the loop reads ions_kdtree.at(cand) for
+// cand = 0 .. |ball(i)| - 1 and gives every unclustered one i's clustered type
+// (flag_as_guarded leaves a clustered type as it is, :4576-4582).  Those ions
+// are clustered from then on: excluded as centres and as neighbours; the guard
+// count is the number of relabellings.
 int ppo_aposteriori(const float* xyz, const uint8_t* clustered, const float* ion2surf, uint64_t n, float rmin,
-                    float rincr, float rmax, uint32_t analyses, uint64_t* out, uint64_t out_cap, uint64_t* stats) {
+                    float rincr, float rmax, uint32_t analyses, int guard_mode, uint64_t* out, uint64_t out_cap,
+                    uint64_t* stats) {
   if (!xyz || !clustered || !ion2surf || !out) return -1;
   Hist proto; proto.init(rmin, rincr, rmax);
   const uint64_t H = proto.nbins + 2;
@@ -785,10 +795,25 @@ int ppo_aposteriori(const float* xyz, const uint8_t* clustered, const float* ion
           }
   };
   std::vector<uint8_t> guard(n, 0);
-  for (uint64_t i = 0; i < n; ++i)
-    if (clustered[i]) each_nb(i, [&](uint64_t j, float) { if (!clustered[j]) guard[j] = 1; });
+  std::vector<uint8_t> excl(clustered, clustered + n);  // clustered types
   uint64_t ncent = 0, nlost = 0, nguard = 0;
-  for (uint64_t i = 0; i < n; ++i) nguard += guard[i];
+  if (guard_mode == 1) {
+    for (uint64_t i = 0; i < n; ++i) {
+      if (!excl[i]) continue;
+      uint64_t candidates = 0;
+      each_nb(i, [&](uint64_t, float) { ++candidates; });
+      for (uint64_t cand = 0; cand < candidates; ++cand) {
+        if (excl[cand]) continue;
+        excl[cand] = 1;
+        ++nguard;
+      }
+    }
+  } else {
+    for (uint64_t i = 0; i < n; ++i)
+      if (clustered[i]) each_nb(i, [&](uint64_t j, float) { if (!clustered[j]) guard[j] = 1; });
+    for (uint64_t i = 0; i < n; ++i) nguard += guard[i];
+  }
+  const uint8_t* clus = excl.data();
   Hist hR = proto, h1 = proto, hK = proto;
 #pragma omp parallel
   {
@@ -797,12 +822,12 @@ int ppo_aposteriori(const float* xyz, const uint8_t* clustered, const float* ion
 #pragma omp for schedule(dynamic, 256)
     for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
       const uint64_t i = (uint64_t)ii;
-      if (!(ion2surf[i] >= RSQR) || clustered[i] || guard[i]) continue;
+      if (!(ion2surf[i] >= RSQR) || clus[i] || guard[i]) continue;
       ++myc;
       float closest = FLT_MAX;
       bool any = false;
       each_nb(i, [&](uint64_t j, float d2) {
-        if (clustered[j]) return;
+        if (clus[j]) return;
         const float d = std::sqrt(d2);
         if (doR) mR.add(d);
         if (doK) mK.add(d);

@@ -16,6 +16,7 @@
 //                [--inside <nions_inside> <volume_inside>]
 //                [--voxelize]
 //                [--dump-surf]
+//                [--aposteriori <flags file: uint8 per ion, nonzero = clustered> <rdf|1nn|ripk>]
 // Writes into <outdir>:
 //   the reference CSV files (report_apriori_descrstat2/3 layout),
 //   raw_bins.u64    uint64 counts, layout of pp_fetch (RDF,1NN,RIPK,MKNN groups)
@@ -24,6 +25,12 @@
 //   ion2surf.f32    (with --dump-surf) squared hull distance per original ion
 //   raw_npcorr.u32  (AnalysisSpatDistrType 5) uint32 [ntasks][edge^3] n-point
 //                   correlation counts of the reference's npc3d class
+//   raw_apost.u64   (with --aposteriori, one thread) the histogram of the
+//                   statistics after clustering, H = nbins + 2 counts
+//   tree_order.u64  (with --aposteriori) the order of the clustering task's
+//                   global KD-tree: position p holds original ion tree_order[p]
+//   apost_stats.txt (with --aposteriori) guarded ions, centres, centres
+//                   without a neighbour
 //   voxel.txt       (with --voxelize) the occupancy grid's NumberOfIonsInside and
 //                   VolumeInside, which then also head the RDF reports; the
 //                   Hoshen-Kopelman clustering is the reference's percAnalyzer
@@ -52,6 +59,23 @@ void stopping(const int rank, const string what) { cerr << "ERROR::" << rank << 
 void stopping(const string what) { cerr << "ERROR::" << what << endl; }
 
 namespace {
+
+// Type flags of the statistics after clustering (src/PARAPROBE_HPDBScan.cpp:1105-1111,
+// src/PARAPROBE_SolverHdl.cpp:4576-4621), free functions of files that do not
+// compile here, restated.
+unsigned int flag_as_clustered(const unsigned int typid, const unsigned int maxtypid) {
+  return typid <= maxtypid ? typid + ION_IN_CLUSTER : typid;
+}
+unsigned int flag_as_guarded(const unsigned int typid, const unsigned int maxtypid) {
+  return typid <= maxtypid ? typid + ION_AT_CLUSTER : typid;
+}
+bool is_clustered(const unsigned int typid, const unsigned int maxtypid) {
+  if (typid <= maxtypid + ION_IN_CLUSTER) return typid > maxtypid;
+  return false;
+}
+bool is_guardzone(const unsigned int typid, const unsigned int maxtypid) {
+  return typid > maxtypid + ION_IN_CLUSTER;
+}
 
 struct Region {
   apt_real zmi, zmx;
@@ -295,12 +319,14 @@ int main(int argc, char** argv) {
   size_t nions_inside = 0;
   double volume_inside = 0.0;
   bool dump_surf = false, do_voxel = false;
+  string apost_fn, apost_what;
   for (int a = 5; a < argc; ++a) {
     string s = argv[a];
     if (s == "--voxelize") { do_voxel = true; continue; }
     if (s == "--labels" && a + 1 < argc) labels_fn = argv[++a];
     else if (s == "--inside" && a + 2 < argc) { nions_inside = stoull(argv[a + 1]); volume_inside = stod(argv[a + 2]); a += 2; }
     else if (s == "--dump-surf") dump_surf = true;
+    else if (s == "--aposteriori" && a + 2 < argc) { apost_fn = argv[a + 1]; apost_what = argv[a + 2]; a += 2; }
   }
   omp_set_num_threads(T);
   mkdir(outdir.c_str(), 0755);
@@ -395,6 +421,94 @@ int main(int argc, char** argv) {
     FILE* f = fopen((outdir + "/ion2surf.f32").c_str(), "wb");
     fwrite(s.data(), 4, N, f);
     fclose(f);
+  }
+
+  if (!apost_fn.empty()) {
+    if (T != 1) { cerr << "--aposteriori needs one thread (one region in input order)\n"; return 10; }
+    // ---- statistics after clustering.  The cloud stands for the clustering
+    // task's filtered ions (ions_filtered, :4665-4685) with the clustered ones
+    // flagged by HPDBSCAN::summarize2 (flag_as_clustered).
+    vector<uint8_t> cf(N);
+    FILE* ff = fopen(apost_fn.c_str(), "rb");
+    if (!ff || fread(cf.data(), 1, N, ff) != N) { cerr << "bad cluster flags file\n"; return 11; }
+    fclose(ff);
+    const unsigned int mxtypid = pse.get_maxtypeid();
+    vector<p3dm1> ions_filtered = reg[0].ions;
+    vector<apt_xyz> ion2surf_filtered = reg[0].surf;
+    for (size_t i = 0; i < N; ++i)
+      if (cf[i]) ions_filtered[i].m = flag_as_clustered(ions_filtered[i].m, mxtypid);
+    // clustertask::build_kdtree (:4737-4787): the task's global KD-tree, the
+    // ions repacked into its order
+    vector<p3d> ioninput;
+    for (auto& p : ions_filtered) ioninput.push_back(p3d(p.x, p.y, p.z));
+    vector<size_t> permutations;
+    kd_tree* globaltree = new kd_tree;
+    globaltree->build(ioninput, permutations);
+    vector<p3dm1> ions_kdtree;
+    vector<apt_xyz> ion2surf_kdtree;
+    globaltree->pack_p3dm1_d(permutations, ions_filtered, ion2surf_filtered, ions_kdtree, ion2surf_kdtree);
+    if (!globaltree->verify(ions_kdtree)) { cerr << "KD-tree verify failed\n"; return 12; }
+    // clustertask::flag2exclude_guard (:4790-4831), as written: the loop
+    // reads and relabels ions_kdtree.at(cand), the candidate's position in
+    // the result list, and gives it the clustered ion's (clustered) type
+    apt_real Guard = Settings::SpatStatRadiusMax;
+    apt_real SQRGuard = SQR(Guard);
+    size_t guarded = 0;
+    for (size_t i = 0; i < ions_kdtree.size(); ++i) {
+      if (is_clustered(ions_kdtree.at(i).m, mxtypid) == true) {
+        vector<size_t> candidates;
+        globaltree->range_rball_noclear_nosort_indices(i, ions_kdtree, SQRGuard, candidates);
+        for (size_t cand = 0; cand < candidates.size(); ++cand) {
+          if (is_clustered(ions_kdtree.at(cand).m, mxtypid) == true) continue;
+          ions_kdtree.at(cand).m = flag_as_guarded(ions_kdtree.at(i).m, mxtypid);
+          ++guarded;
+        }
+      }
+    }
+    // clustertask::generic_spatstat (:4833-4945) for one analysis
+    histogram globalres = histogram(Settings::SpatStatRadiusMin, Settings::SpatStatRadiusIncr, Settings::SpatStatRadiusMax);
+    const apt_xyz R = Settings::SpatStatRadiusMax;
+    const apt_xyz RSQR = SQR(R);
+    size_t centres = 0, lost = 0;
+    for (size_t i = 0; i < ions_kdtree.size(); ++i) {
+      p3dm1 me = ions_kdtree.at(i);
+      if (ion2surf_kdtree.at(i) >= RSQR && is_clustered(me.m, mxtypid) == false &&
+          is_guardzone(me.m, mxtypid) == false) {
+        vector<nbor> neighbors;
+        globaltree->range_rball_noclear_nosort(i, ions_kdtree, RSQR, neighbors);
+        ++centres;
+        if (apost_what == "rdf" || apost_what == "ripk") {
+          for (size_t nbb = 0; nbb < neighbors.size(); ++nbb)
+            if (is_clustered(neighbors.at(nbb).m, mxtypid) == false) globalres.add(neighbors.at(nbb).d);
+        } else if (apost_what == "1nn") {
+          apt_real closest = F32MX;
+          size_t nborid = numeric_limits<size_t>::max();
+          for (size_t nbb = 0; nbb < neighbors.size(); ++nbb) {
+            if (is_clustered(neighbors.at(nbb).m, mxtypid) == true) continue;
+            if (neighbors.at(nbb).d > closest) continue;
+            closest = neighbors.at(nbb).d;
+            nborid = nbb;
+          }
+          if (nborid != numeric_limits<size_t>::max()) globalres.add(closest);
+          else ++lost;
+        }
+      }
+    }
+    vector<uint64_t> hb;
+    hb.push_back((uint64_t)globalres.cnts_lowest);
+    for (size_t b = 0; b < globalres.bincount(); ++b) hb.push_back((uint64_t)globalres.cnts[b]);
+    hb.push_back((uint64_t)globalres.cnts_highest);
+    FILE* fo = fopen((outdir + "/raw_apost.u64").c_str(), "wb");
+    fwrite(hb.data(), 8, hb.size(), fo);
+    fclose(fo);
+    vector<uint64_t> order(permutations.begin(), permutations.end());
+    fo = fopen((outdir + "/tree_order.u64").c_str(), "wb");
+    fwrite(order.data(), 8, order.size(), fo);
+    fclose(fo);
+    ofstream st((outdir + "/apost_stats.txt").c_str());
+    st << "guarded " << guarded << "\ncentres " << centres << "\nlost " << lost << "\n";
+    delete globaltree;
+    return 0;
   }
 
   // ---- per-slab KD-trees (src/PARAPROBE_SolverHdl.cpp:1593-1663)

@@ -165,6 +165,11 @@ struct pp_ctx {
   DevBuf tri_fill, cflag, rowtab, nc_pre;
   DevBuf labels_run, perm_dev, gather_src;
   DevBuf mask_in;  // caller's centre mask: [n] input order, then [n] sorted-slot order
+  // statistics after clustering: option "aposteriori_guard" = 1 runs the
+  // reference's guard loop as written (see pp_run_aposteriori)
+  bool apost_ref = false;
+  DevBuf apost_cnt;               // neighbours within R per ion (input order)
+  uint64_t apost_relabelled = 0;  // ions the last such run relabelled
   // batched geometry cache
   DevBuf pair_count, pair_off, pair_slot, pair_cat, geo_centres, centre_ok, real_labels, rois_dev;
   DevBuf labels_il, ok_il;  // group-major interleaved copies of real_labels / centre_ok
@@ -1546,10 +1551,63 @@ int pp_run_aposteriori(pp_ctx* ctx, int cloud, const uint8_t* clustered, uint32_
       rc = fail(ctx, PP_ERR_CUDA, "copy of the cluster flags failed");
       break;
     }
-    pp::launch_gather_labels(ctx->gather_src.as<uint8_t>(), cl->id_of_slot.as<uint32_t>(), n, clus, 1, s);
     pp::ScanArgs a{};
     fill_scan_common(a, *cl, P, D, ctx->tab);
     a.status = gstat;
+    if (ctx->apost_ref) {
+      // The guard loop as the reference runs it (src/PARAPROBE_SolverHdl.cpp:4804-4820):
+      // for every position i of ions_kdtree in order whose ion is clustered,
+      // it relabels the ions at positions 0 .. |ball(i)| - 1 -- the loop
+      // reads ions_kdtree.at(cand), cand being the index into the result
+      // list -- with i's clustered type (flag_as_guarded returns a clustered
+      // type unchanged, :4576-4582), so they are clustered from then on and
+      // later steps take them as clustered ions too.  Positions are the
+      // cloud's input order.  The relabelled ions form the prefix [0, G) of
+      // positions, G the largest ball of a clustered position met while the
+      // prefix is extended; they leave the statistics as centres and as
+      // neighbours (:4879, :4890, :4898).
+      if (ctx->apost_cnt.ensure(std::max<uint64_t>(n, 1) * 4) != cudaSuccess) {
+        rc = fail(ctx, PP_ERR_NOMEM, "device allocation failed");
+        break;
+      }
+      pp::launch_ball_count(a, cl->id_of_slot.as<uint32_t>(), n, ctx->apost_cnt.as<uint32_t>(), ctx->sm_count, s);
+      std::vector<uint32_t> ball(n);
+      int st = 0;
+      if (cudaGetLastError() != cudaSuccess ||
+          cudaMemcpyAsync(ball.data(), ctx->apost_cnt.p, n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaMemcpyAsync(&st, gstat, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess) {
+        rc = fail(ctx, PP_ERR_CUDA, "neighbour count pass failed");
+        break;
+      }
+      if (st) {
+        rc = fail(ctx, PP_ERR_DEVICE, "neighbour count pass: device status %d", st);
+        break;
+      }
+      uint64_t G = 0;
+      for (uint64_t i = 0; i < n; ++i)
+        if (clustered[i] || i < G) G = std::max<uint64_t>(G, ball[i]);
+      std::vector<uint8_t> lab_in(n);
+      uint64_t relabelled = 0;
+      for (uint64_t i = 0; i < n; ++i) {
+        const bool out = clustered[i] || i < G;
+        lab_in[i] = out ? 3 : 1;
+        relabelled += (!clustered[i] && i < G) ? 1 : 0;
+      }
+      ctx->apost_relabelled = relabelled;
+      if (cudaMemcpyAsync(ctx->gather_src.p, lab_in.data(), n, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+        rc = fail(ctx, PP_ERR_CUDA, "copy of the labels failed");
+        break;
+      }
+      pp::launch_gather_labels(ctx->gather_src.as<uint8_t>(), cl->id_of_slot.as<uint32_t>(), n, lab, 1, s);
+      if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+        rc = fail(ctx, PP_ERR_CUDA, "label gather failed");
+        break;
+      }
+      rc = run_plain(ctx, cl, flags, nullptr, 0, nullptr, s, 0, lab, true);
+      break;
+    }
+    pp::launch_gather_labels(ctx->gather_src.as<uint8_t>(), cl->id_of_slot.as<uint32_t>(), n, clus, 1, s);
     pp::launch_guard(a, clus, lab, n, ctx->sm_count, s);
     int st = 0;
     if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&st, gstat, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -1752,6 +1810,11 @@ int pp_set_option(pp_ctx* ctx, const char* name, int value) {
   if (std::strcmp(name, "npcorr_order") == 0) {
     if (value < 0 || value > 31) return fail(ctx, PP_ERR_INVALID, "npcorr_order must be in [0, 31]");
     ctx->npc_order = (uint32_t)value;
+    return PP_OK;
+  }
+  if (std::strcmp(name, "aposteriori_guard") == 0) {
+    if (value < 0 || value > 1) return fail(ctx, PP_ERR_INVALID, "aposteriori_guard must be 0 or 1");
+    ctx->apost_ref = value == 1;
     return PP_OK;
   }
   if (std::strcmp(name, "batched_pair_cap") == 0) {

@@ -256,6 +256,10 @@ int launch_npcorr(const ScanArgs& a, const NpcArgs& p, int sm_count, cudaStream_
 void launch_guard(const ScanArgs& a, const uint8_t* clus, uint8_t* guard_then_labels, uint64_t n, int sm_count,
                   cudaStream_t s);
 
+// neighbours within R of every slot (j != i), written by input index
+void launch_ball_count(const ScanArgs& a, const uint32_t* id_of_slot, uint64_t n, uint32_t* count_by_id, int sm_count,
+                       cudaStream_t s);
+
 constexpr int kApplyThreads = 1024;
 // picks the realisation group and where kNN bins accumulate; -2 = no fit
 int apply_configure(ApplyArgs& a);

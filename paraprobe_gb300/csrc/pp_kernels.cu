@@ -1015,6 +1015,24 @@ __global__ void __launch_bounds__(256) k_guard(ScanArgs a, const uint8_t* __rest
   }
 }
 
+// Neighbours within R of every ion (j != i, float d^2 <= R^2), stored by input
+// index: the length of the result list the reference's guard loop takes for a
+// clustered ion (src/PARAPROBE_SolverHdl.cpp:4808-4811).  One warp per slot.
+__global__ void __launch_bounds__(256) k_ball_count(ScanArgs a, const uint32_t* __restrict__ id_of_slot, uint64_t n,
+                                                    uint32_t* __restrict__ count_by_id) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t gw = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t self = gw; self < n; self += nw) {
+    const float4 cp = a.ions[self];
+    uint32_t c = 0;
+    for_each_candidate(a, a.rowtab, cp, (uint32_t)self, lane,
+                       [&](bool, uint32_t, float, bool inball, uint32_t, bool) { c += inball ? 1u : 0u; });
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(FULL, c, o);
+    if (lane == 0) count_by_id[id_of_slot[self]] = c;
+  }
+}
+
 // labels of the statistics after clustering, in place over the guard flags:
 // 1 = neither clustered nor guard (centres and environment), 2 = guard
 // (environment only), 3 = clustered (neither)
@@ -2740,6 +2758,12 @@ int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_
     if (emax <= 8) return launch_scan_t<4, 8>(a, sm_count, smem, s);
   }
   return -2;
+}
+
+void launch_ball_count(const ScanArgs& a, const uint32_t* id_of_slot, uint64_t n, uint32_t* count_by_id, int sm_count,
+                       cudaStream_t s) {
+  counted();
+  k_ball_count<<<sm_count * 8, 256, 0, s>>>(a, id_of_slot, n, count_by_id);
 }
 
 void launch_guard(const ScanArgs& a, const uint8_t* clus, uint8_t* guard_then_labels, uint64_t n, int sm_count,

@@ -8,8 +8,15 @@
 // device buffers for the inputs and the output; every other buffer the pass
 // needs -- the triangle boxes, the triangle grid, its per-cell lists and the
 // prefix-scan partials -- lives in one file-scope __device__ array of fixed
-// size.  Each GPU that loads this library holds that array (64 MiB) from
-// module load until the process exits.
+// size.  Each GPU on which this file's module is loaded holds that array
+// (64 MiB) until the process exits.  The CUDA runtime loads modules lazily by
+// default (CUDA_MODULE_LOADING=LAZY), and this module holds no kernel, so the
+// array is given device memory at the first call on a device, when the call
+// looks its address up.  A caller whose pool takes the whole device makes one
+// call with n = 0 on each device before that (it only does the set-up).  The
+// address is cached per device for the life of the process: after
+// cudaDeviceReset, or once the primary context is destroyed and created
+// again, the cached address is stale and this entry point must not be used.
 //
 // The entry point calls no cudaMalloc, cudaFree or allocating library routine
 // and allocates no host memory either.  It uses cudaMemsetAsync, plain
@@ -163,6 +170,11 @@ extern "C" int pp_surfdist_noalloc(const float* xyz, uint64_t n, const float* tr
   const float grow = rp + slack;
   for (int k = 0; k < 3; ++k) { glo[k] -= grow + slack; ghi[k] += grow + slack; }
   unsigned long long* total_dev = reinterpret_cast<unsigned long long*>(base + 64);
+  // The cell edge is searched for scratch fit, not by the allocating path's
+  // cell-count rule, so the two grids may differ.  The result does not depend
+  // on the grid: every triangle whose box grown by R' + slack reaches a cell
+  // is listed there, so each ion meets every triangle within R' of it and
+  // takes the same minimum over the same float distances.
   double h = std::fmax((double)rp, 0.25);
   pp::Grid tg{};
   Layout L(ntri, 0);

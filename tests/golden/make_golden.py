@@ -127,11 +127,66 @@ def make(c, outdir):
         return stats
 
 
+# Statistics after clustering (clustertask::flag2exclude_guard and
+# generic_spatstat): the harness builds the clustering task's global KD-tree
+# with the reference's own kd_tree and runs the guard loop as written.  The
+# fixtures go to tests/golden/apost/ with the tree order, so that a test can
+# hand the cloud over in that order.
+APOST_CASES = [
+    dict(name="apost_rdf", n=20000, seed=201, what="rdf", r=("0.0", "0.01", "1.0"), frac=0.5),
+    dict(name="apost_1nn", n=20000, seed=202, what="1nn", r=("0.0", "0.005", "0.8"), frac=0.7),
+    dict(name="apost_ripk", n=25000, seed=203, what="ripk", r=("0.1", "0.02", "1.2"), frac=0.3),
+]
+APOST_DIR = os.path.join(HERE, "apost")
+
+
+def make_apost(c, outdir):
+    spec = synth.cone_specimen(n=c["n"], r_apex=7.0, half_angle_deg=10.0, length=16.0, n_clusters=15,
+                               members=40, nspecies=3, seed=c["seed"], nseg=64, stack=4.0)
+    # clustered ions: a seeded share of the cluster-forming species
+    rng = np.random.default_rng(c["seed"])
+    clustered = ((spec.labels == 2) & (rng.random(spec.labels.size) < c["frac"])).astype(np.uint8)
+    what_digit = {"rdf": "1", "1nn": "2", "ripk": "3"}[c["what"]]
+    with tempfile.TemporaryDirectory() as tmp:
+        pos, rrng, vtk = synth.write_inputs(spec, tmp, c["name"])
+        xml = os.path.join(tmp, "settings.xml")
+        synth.write_settings_xml(xml, pos, rrng, vtk, what_digit, synth.all_pairs_tasks(spec.nspecies), *c["r"],
+                                 mknn="")
+        cf = os.path.join(tmp, "clustered.u8")
+        clustered.tofile(cf)
+        out = os.path.join(tmp, "out")
+        cmd = [REF, "7", xml, "1", out, "--dump-surf", "--aposteriori", cf, c["what"]]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"{c['name']}: reference harness failed\n{r.stderr[-2000:]}")
+        stats = {}
+        for line in open(os.path.join(out, "apost_stats.txt")):
+            k, v = line.split()
+            stats[k] = int(v)
+        np.savez_compressed(
+            os.path.join(outdir, c["name"] + ".npz"),
+            xyz=spec.xyz, labels=spec.labels, clustered=clustered, hull=spec.hull,
+            surf=np.fromfile(os.path.join(out, "ion2surf.f32"), dtype=np.float32),
+            bins=np.fromfile(os.path.join(out, "raw_apost.u64"), dtype=np.uint64),
+            tree_order=np.fromfile(os.path.join(out, "tree_order.u64"), dtype=np.uint64),
+            meta=np.array(json.dumps(dict(case=c, stats=stats))))
+        return stats
+
+
 def main():
     if not os.path.exists(REF):
         raise SystemExit(f"{REF} missing: build it with make -C oracle/ref")
+    only = set(sys.argv[1:])
     for c in CASES:
+        if only and c["name"] not in only:
+            continue
         st = make(c, HERE)
+        print(c["name"], st)
+    os.makedirs(APOST_DIR, exist_ok=True)
+    for c in APOST_CASES:
+        if only and c["name"] not in only:
+            continue
+        st = make_apost(c, APOST_DIR)
         print(c["name"], st)
 
 

@@ -3,8 +3,14 @@ generic_spatstat, src/PARAPROBE_SolverHdl.cpp:4790-4945).
 
 CPU: the oracle against a brute-force numpy restatement on a small cloud and,
 with no ion clustered, against the plain statistics that the golden fixtures
-pin.  GPU: pp_run_aposteriori against the oracle, bit-exact.
+pin; its restatement of the reference's guard loop as written against
+fixtures the reference's own KD-tree code produced (tests/golden/apost/).
+GPU: pp_run_aposteriori against the oracle and, with option
+aposteriori_guard = 1, against those fixtures, bit-exact.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -126,3 +132,60 @@ def test_gpu_aposteriori_keeps_tasks(ctx):
     after = np.asarray(ctx.fetch())
     ctx.free(cid)
     assert np.array_equal(before, after)
+
+
+# ---- the reference's guard loop as written, pinned on reference-generated fixtures
+APOST_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "apost")
+APOST_FLAG = {"rdf": 1, "1nn": 2, "ripk": 4}
+
+
+def _apost_names():
+    return sorted(f[:-4] for f in os.listdir(APOST_DIR) if f.endswith(".npz")) if os.path.isdir(APOST_DIR) else []
+
+
+def _apost(name):
+    z = np.load(os.path.join(APOST_DIR, name + ".npz"))
+    meta = json.loads(str(z["meta"]))
+    c = meta["case"]
+    order = z["tree_order"].astype(np.int64)
+    r = tuple(np.float32(float(v)) for v in c["r"])
+    return dict(z=z, c=c, stats=meta["stats"], order=order, r=r, flags=APOST_FLAG[c["what"]])
+
+
+@pytest.mark.parametrize("name", _apost_names())
+def test_oracle_reference_guard_matches_reference(oracle, name):
+    """guard_mode 1 of the oracle against the reference's own KD-tree run of
+    flag2exclude_guard + generic_spatstat, the cloud in the tree's order."""
+    a = _apost(name)
+    z, o = a["z"], a["order"]
+    got, st = oracle.aposteriori(z["xyz"][o], z["clustered"][o], z["surf"][o], *a["r"], a["flags"], guard_mode=1)
+    assert (st[0], st[1], st[2]) == (a["stats"]["centres"], a["stats"]["guarded"], a["stats"]["lost"])
+    assert np.array_equal(got[a["c"]["what"]], z["bins"])
+
+
+def test_apost_fixtures_present():
+    assert len(_apost_names()) == 3
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", _apost_names())
+def test_gpu_reference_guard_matches_reference(ctx, name):
+    """pp_run_aposteriori with option aposteriori_guard = 1, the cloud
+    uploaded in the reference's KD-tree order, against the reference."""
+    a = _apost(name)
+    z, o = a["z"], a["order"]
+    cid = ctx.upload(z["xyz"][o], z["labels"][o])
+    ctx.hull(cid, z["hull"], 2.0)
+    ctx.hist(*a["r"])
+    ctx.set_option("aposteriori_guard", 1)
+    try:
+        ctx.run_aposteriori(cid, z["clustered"][o], a["flags"])
+    finally:
+        ctx.set_option("aposteriori_guard", 0)
+    got = np.asarray(ctx.fetch()).reshape(-1)
+    st = ctx.stats()
+    surf = ctx.surfdist_fetch(cid, o.size)
+    ctx.free(cid)
+    assert np.array_equal(surf.view(np.uint32), z["surf"][o].view(np.uint32))
+    assert st["centres"] == a["stats"]["centres"]
+    assert np.array_equal(got, z["bins"])

@@ -4,10 +4,20 @@ on two clouds, called twice in a row so the second call starts from the
 scratch contents the first one left.  Results are bit-identical: both paths
 take the minimum of the same per-triangle float distances.
 
+The entry point's promise -- it allocates nothing -- is checked through the
+device's free memory: unchanged across a call once the first call has set
+the scratch up.  With the runtime's lazy module loading, the 64 MiB scratch
+is taken at the first call on a device (a set-up call with n = 0), which a
+fresh process shows.
+
 Kept in a file of its own that pytest collects last; it passes alone in a
 fresh process as well as after the other tests.
 """
 import ctypes as C
+import json
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -55,6 +65,109 @@ def test_noalloc_matches_allocating_path_twice(ctx):
         assert got.dtype == np.float32 and got.shape == ref.shape
         assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
         assert (got < np.float32(max(rmax, carve)) ** 2).any()
+
+
+def test_noalloc_allocates_nothing(ctx):
+    """Free device memory is the same before and after a call on a new cloud
+    of the same size, once a first call has run (inputs allocated before)."""
+    torch = pytest.importorskip("torch")
+    lib = N.load()
+    specs = [synth.cone_specimen(n=50000, r_apex=8.0, half_angle_deg=10.0, length=18.0, n_clusters=20, members=40,
+                                 nspecies=3, seed=s, nseg=96, stack=3.0) for s in (51, 52)]
+    dev = []
+    for sp in specs:
+        dev.append((torch.from_numpy(sp.xyz.reshape(-1).copy()).to("cuda"),
+                    torch.from_numpy(sp.hull.reshape(-1).copy()).to("cuda"),
+                    torch.empty(sp.xyz.shape[0], dtype=torch.float32, device="cuda")))
+    err = C.create_string_buffer(256)
+
+    def call(k):
+        x, t, o = dev[k]
+        rc = lib.pp_surfdist_noalloc(C.c_void_p(x.data_ptr()), specs[k].xyz.shape[0], C.c_void_p(t.data_ptr()),
+                                     specs[k].hull.shape[0], 2.0, C.c_void_p(o.data_ptr()), None, err, 256)
+        assert rc == N.PP_OK, err.value.decode()
+        torch.cuda.synchronize()
+
+    call(0)
+    free0 = torch.cuda.mem_get_info()[0]
+    call(1)
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes across a call"
+
+
+_LAZY_CHILD = r"""
+import ctypes as C, json, sys
+sys.path.insert(0, sys.argv[1])
+import numpy as np, torch
+from paraprobe_gb300 import native as N
+from paraprobe_gb300 import synth
+lib = N.load()
+sp = synth.cylinder_specimen(n=20000, radius=5.0, height=10.0, nseg=48, stack=2.0, seed=61)
+x = torch.from_numpy(sp.xyz.reshape(-1).copy()).to("cuda")
+t = torch.from_numpy(sp.hull.reshape(-1).copy()).to("cuda")
+o = torch.empty(sp.xyz.shape[0], dtype=torch.float32, device="cuda")
+torch.cuda.synchronize()
+err = C.create_string_buffer(256)
+free = [torch.cuda.mem_get_info()[0]]
+rc = [lib.pp_surfdist_noalloc(None, 0, None, 0, 1.0, None, None, err, 256)]
+free.append(torch.cuda.mem_get_info()[0])
+for _ in range(2):
+    rc.append(lib.pp_surfdist_noalloc(C.c_void_p(x.data_ptr()), sp.xyz.shape[0], C.c_void_p(t.data_ptr()),
+                                      sp.hull.shape[0], 2.0, C.c_void_p(o.data_ptr()), None, err, 256))
+    torch.cuda.synchronize()
+    free.append(torch.cuda.mem_get_info()[0])
+print(json.dumps({"rc": rc, "free": free, "err": err.value.decode()}))
+"""
+
+
+def test_noalloc_setup_call_takes_the_scratch():
+    """In a fresh process with lazy module loading, the set-up call (n = 0)
+    is where the 64 MiB scratch is taken; later calls take nothing more than
+    the first launch of each kernel loads, and the second call nothing."""
+    pytest.importorskip("torch")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, CUDA_MODULE_LOADING="LAZY")
+    r = subprocess.run([sys.executable, "-c", _LAZY_CHILD, root], capture_output=True, text=True, env=env,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["rc"] == [0, 0, 0], out["err"]
+    f = out["free"]
+    mib = 1 << 20
+    assert 60 * mib <= f[0] - f[1] <= 96 * mib, f"set-up call took {(f[0] - f[1]) / mib:.1f} MiB"
+    assert f[1] - f[2] < 16 * mib, f"first call took {(f[1] - f[2]) / mib:.1f} MiB"
+    assert f[3] == f[2], f"second call took {f[2] - f[3]} bytes"
+
+
+def _raw_call(lib, torch, tri_np, n=16):
+    x = torch.zeros(3 * n, dtype=torch.float32, device="cuda")
+    t = torch.from_numpy(np.ascontiguousarray(tri_np, dtype=np.float32).reshape(-1)).to("cuda")
+    o = torch.full((n,), -1.0, dtype=torch.float32, device="cuda")
+    err = C.create_string_buffer(256)
+    rc = lib.pp_surfdist_noalloc(C.c_void_p(x.data_ptr()), n, C.c_void_p(t.data_ptr()), tri_np.shape[0], 2.0,
+                                 C.c_void_p(o.data_ptr()), None, err, 256)
+    torch.cuda.synchronize()
+    return rc, err.value.decode(), o.cpu().numpy()
+
+
+def test_noalloc_rejects_non_finite_hull(ctx):
+    torch = pytest.importorskip("torch")
+    tri = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0], [0, 0, 1, np.nan, 0, 1, 0, 1, 1]], dtype=np.float32)
+    rc, msg, out = _raw_call(N.load(), torch, tri)
+    assert rc == N.PP_ERR_INVALID and "non-finite" in msg
+    assert (out == -1.0).all()
+
+
+def test_noalloc_reports_a_grid_that_cannot_fit(ctx):
+    """Two triangles 2e30 apart: no cell edge the search tries gives a grid of
+    at most 2e9 cells, so the call fails with PP_ERR_OVERFLOW before any list
+    is built, leaving the output untouched."""
+    torch = pytest.importorskip("torch")
+    tri = np.array([[-1e30, 0, 0, -1e30, 1, 0, -1e30, 0, 1], [1e30, 0, 0, 1e30, 1, 0, 1e30, 0, 1]],
+                   dtype=np.float32)
+    rc, msg, out = _raw_call(N.load(), torch, tri)
+    assert rc == N.PP_ERR_OVERFLOW and "do not fit" in msg
+    assert (out == -1.0).all()
 
 
 def test_noalloc_rejects_oversized_hull(ctx):
