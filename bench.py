@@ -603,8 +603,9 @@ def served_leg(ctx, nq=240, rate=200.0):
     tip20m); queries arrive as a Poisson stream at `rate`/s, each with
     a random cloud, R ~ U[0.5, 3.0] nm, k ~ U[1, 20] and a random species pair
     (RDF + kNN, 0.01 nm bins).  Continuous batching on 4 worker streams,
-    admission by HBM footprint; compared with the same queries run one at a
-    time through pp_run."""
+    admission by HBM footprint; queries waiting on the same cloud run as one
+    merged pass; compared with the same queries run one at a time through
+    pp_run."""
     from paraprobe_gb300 import native as N
     sizes = (100_000, 1_000_000, 5_000_000, 10_000_000, 20_000_000, 50_000_000)
     clouds = []
@@ -650,6 +651,7 @@ def served_leg(ctx, nq=240, rate=200.0):
         pairs += srv.wait(t)[1]
     served_s = time.perf_counter() - t0
     st = srv.stats()
+    passes, taken = srv.passes()
     srv.close()
     # the same queries one at a time through the plain path
     t0 = time.perf_counter()
@@ -668,6 +670,8 @@ def served_leg(ctx, nq=240, rate=200.0):
             "queries": len(tickets), "value": pairs / served_s, "unit": UNIT,
             "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "admitted": int(st["admitted"]) - 4,
             "rejected": int(st["rejected"]), "slots": 4, "budget_bytes": budget,
+            "arrival_rate_per_s": rate, "served_queries_per_s": len(tickets) / served_s,
+            "merged_passes": int(passes) - 4, "queries_per_pass": (taken - 4) / max(passes - 4, 1),
             "plain_single_query": plain_pairs / plain_s, "ratio_vs_plain": (pairs / served_s) / (plain_pairs / plain_s)}
 
 

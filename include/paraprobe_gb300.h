@@ -247,6 +247,8 @@ int pp_fetch_npcorr(pp_ctx* ctx, uint32_t* counts, uint64_t cap, uint64_t* edge)
  *                       scan (default 1); 0 = the per-centre or brick scan.
  *                       Results are identical either way.
  *   "npcorr_order"      SpatStatKNNOrder - 1 for PP_NPCORR (0..31, default 0).
+ *   "server_batch"      most queries per merged serving pass (1..32, default
+ *                       32; 1 = every query alone), read by pp_server_create.
  *   "aposteriori_guard" pp_run_aposteriori's guard zone: 0 = every
  *                       unclustered ion within R of a clustered ion (default),
  *                       1 = the reference's guard loop as written (see there).
@@ -331,7 +333,15 @@ int pp_cloud_prepare(pp_ctx* ctx, int cloud, float r_lo, float r_hi);
 /* ---- serving loop (no counterpart in the reference, which runs one task per
  * process): clouds stay resident in the context; queries are admitted by
  * estimated HBM footprint as worker slots and memory free up, and run
- * concurrently on the workers' own streams. */
+ * concurrently on the workers' own streams.  Continuous batching: a free
+ * worker takes the oldest waiting query together with every other waiting
+ * query on the same cloud (up to option "server_batch", default 32, and 64
+ * tasks) and runs them as ONE merged pass -- one candidate walk per centre at
+ * the largest radius among the queries the centre belongs to, each query with
+ * its own radius, hull-distance test, histogram bins, tasks and kNN orders --
+ * so queries that arrive while others run join the next pass on their cloud.
+ * Each query's bins, pairs and centres are those pp_run gives it alone.
+ * Queries with PP_CNTNB, PP_NPCORR or k > 32 run alone on the plain path. */
 typedef struct pp_server pp_server;
 /* `slots` worker threads, each with its own stream and run buffers;
  * `budget_bytes` caps the estimated device memory of admitted queries. */
@@ -349,6 +359,8 @@ int pp_server_wait(pp_server* srv, uint64_t ticket, uint64_t* bins, size_t cap, 
 /* stats[0..7]: submitted, admitted, rejected, completed, in flight,
  * p50 ms, p99 ms, total pairs of completed queries (as doubles). */
 int pp_server_stats(pp_server* srv, double* stats);
+/* Merged passes run so far and the queries they took. */
+int pp_server_passes(pp_server* srv, uint64_t* passes, uint64_t* queries);
 void pp_server_destroy(pp_server* srv);
 
 /* Device the context runs on and its SM count. */

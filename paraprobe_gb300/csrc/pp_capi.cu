@@ -169,6 +169,8 @@ struct pp_ctx {
   // reference's guard loop as written (see pp_run_aposteriori)
   bool apost_ref = false;
   DevBuf apost_cnt;               // neighbours within R per ion (input order)
+  DevBuf multi_cmask, multi_cores;  // merged serving pass: hull-distance bits, cores + counters
+  int server_batch = pp::kMultiMaxQueries;  // option "server_batch": most queries per merged pass
   uint64_t apost_relabelled = 0;  // ions the last such run relabelled
   // batched geometry cache
   DevBuf pair_count, pair_off, pair_slot, pair_cat, geo_centres, centre_ok, real_labels, rois_dev;
@@ -1812,6 +1814,12 @@ int pp_set_option(pp_ctx* ctx, const char* name, int value) {
     ctx->npc_order = (uint32_t)value;
     return PP_OK;
   }
+  if (std::strcmp(name, "server_batch") == 0) {
+    if (value < 1 || value > pp::kMultiMaxQueries)
+      return fail(ctx, PP_ERR_INVALID, "server_batch must be in [1, %d]", pp::kMultiMaxQueries);
+    ctx->server_batch = value;
+    return PP_OK;
+  }
   if (std::strcmp(name, "aposteriori_guard") == 0) {
     if (value < 0 || value > 1) return fail(ctx, PP_ERR_INVALID, "aposteriori_guard must be 0 or 1");
     ctx->apost_ref = value == 1;
@@ -2466,6 +2474,7 @@ double now_ms() {
 struct ServerRequest {
   uint64_t ticket = 0;
   int cloud = -1;
+  bool mergeable = false;  // may share a merged pass with other queries of its cloud
   uint32_t flags = 0;
   float rmin = 0, rincr = 0, rmax = 0;
   std::vector<uint32_t> trg, env, ks;
@@ -2474,7 +2483,7 @@ struct ServerRequest {
   int rc = PP_OK;
   std::string err;
   std::vector<uint64_t> bins;
-  uint64_t pairs = 0;
+  uint64_t pairs = 0, centres = 0;
   double t_submit = 0, t_end = 0;
   bool done = false;
 };
@@ -2493,7 +2502,8 @@ struct pp_server {
   uint64_t next_ticket = 1;
   uint64_t budget = 0, inflight = 0;
   bool stop = false;
-  uint64_t submitted = 0, admitted = 0, rejected = 0, completed = 0;
+  uint64_t submitted = 0, admitted = 0, rejected = 0, completed = 0, batches = 0;
+  int max_batch = pp::kMultiMaxQueries;  // queries per merged pass (option "server_batch")
   double pairs_done = 0;
   std::vector<double> latencies;
 };
@@ -2517,31 +2527,325 @@ void serve_one(pp_ctx* w, cudaStream_t st, ServerRequest& q) {
   if (rc) q.err = w->err;
 }
 
+// Several queries on one cloud in one merged pass (k_multi): each keeps its
+// own radius, histogram geometry, hull-distance test, tasks and kNN orders,
+// and gets the bins, pairs and centres it would get alone through pp_run.
+// Sets rc, bins and pairs of every request.
+void run_multi(pp_ctx* w, const std::vector<ServerRequest*>& qs, cudaStream_t s) {
+  auto fail_all = [&](int rc) {
+    for (ServerRequest* r : qs) {
+      r->rc = rc;
+      r->err = w->err;
+    }
+  };
+  Cloud* cl = get_cloud(w, qs[0]->cloud);
+  const int nq = (int)qs.size();
+  if (!cl || nq < 1 || nq > pp::kMultiMaxQueries) return fail_all(fail(w, PP_ERR_INVALID, "bad merged batch"));
+  const uint64_t n = cl->n;
+  struct Prep {
+    Tables t;
+    std::vector<float> T;
+    std::vector<uint16_t> lut;
+    int shift = 0;
+    uint32_t base = 0;
+    std::vector<uint32_t> kvals;
+    float rp = 0.f;
+  };
+  std::vector<Prep> P(nq);
+  std::vector<pp::MultiQuery> MQ(nq);
+  std::vector<pp::MultiTask> MT;
+  std::vector<uint32_t> q_of_type(256, 0u);
+  std::vector<unsigned long long> t_of_type(256, 0ull), env_of_type(256, 0ull), t_of_q(nq, 0ull);
+  unsigned long long rdf_tasks = 0, knn_tasks = 0;
+  std::vector<float> Tall;
+  std::vector<uint16_t> Lall;
+  std::vector<int> Kall;
+  uint64_t rdf_words = 0, knn_words = 0;
+  float Rmax = 0.f;
+  for (int q = 0; q < nq; ++q) {
+    const ServerRequest& r = *qs[q];
+    Prep& p = P[q];
+    set_tables(p.t, r.rmin, r.rincr, r.rmax);
+    if (p.t.nbins == 0 || p.t.nbins + 2 > 16384) return fail_all(fail(w, PP_ERR_INVALID, "query histogram"));
+    p.T = threshold_table(p.t);
+    build_lut(p.T, p.t.rmax * p.t.rmax, 4096, p.lut, p.shift, p.base);
+    std::vector<uint32_t> ks;
+    if (r.flags & PP_MKNN) ks = r.ks;
+    if (r.flags & PP_1NN) ks.push_back(1);
+    std::sort(ks.begin(), ks.end());
+    ks.erase(std::unique(ks.begin(), ks.end()), ks.end());
+    p.kvals = ks;
+    const float R = p.t.rmax;
+    Rmax = std::max(Rmax, R);
+    pp::MultiQuery& Q = MQ[q];
+    Q.R = R;
+    Q.R2 = R * R;
+    const float Rm = R + cl->g.margin;
+    Q.Rm2 = Rm * Rm;
+    Q.H = (int)p.t.nbins + 2;
+    Q.cat_miss = category_of_distance(p.t, (float)((double)R + kEpsilon));
+    Q.lut_n = (int)p.lut.size();
+    Q.lut_shift = p.shift;
+    Q.lut_base = p.base;
+    Q.T_off = (uint32_t)Tall.size();
+    Q.lut_off = (uint32_t)Lall.size();
+    Q.kv_off = (uint32_t)Kall.size();
+    Q.nkI = (int)ks.size();
+    Q.kmax = ks.empty() ? 0 : (int)ks.back();
+    Tall.insert(Tall.end(), p.T.begin(), p.T.end());
+    Lall.insert(Lall.end(), p.lut.begin(), p.lut.end());
+    for (uint32_t k : ks) Kall.push_back((int)k);
+    for (int k = 0; k < r.ntasks; ++k) {
+      const int t = (int)MT.size();
+      if (t >= pp::kMultiMaxTasks) return fail_all(fail(w, PP_ERR_INVALID, "too many tasks in a merged batch"));
+      pp::MultiTask T{};
+      T.q = q;
+      T.rdf = 0xffffffffu;
+      T.knn = 0xffffffffu;
+      if (r.flags & (PP_RDF | PP_RIPK)) {
+        T.rdf = (uint32_t)rdf_words;
+        rdf_words += (uint64_t)Q.H;
+        rdf_tasks |= 1ull << t;
+      }
+      if (!ks.empty()) {
+        T.knn = (uint32_t)knn_words;
+        knn_words += (uint64_t)Q.H * ks.size();
+        knn_tasks |= 1ull << t;
+      }
+      for (int ty = 0; ty < 256; ++ty) {
+        if (has_type(&r.trg[8 * k], ty)) {
+          t_of_type[ty] |= 1ull << t;
+          q_of_type[ty] |= 1u << q;
+        }
+        if (has_type(&r.env[8 * k], ty)) env_of_type[ty] |= 1ull << t;
+      }
+      t_of_q[q] |= 1ull << t;
+      MT.push_back(T);
+    }
+  }
+  int lists = 0;
+  for (int ty = 0; ty < 256; ++ty) lists = std::max(lists, __builtin_popcountll(t_of_type[ty] & knn_tasks));
+  // the cloud's grid serves radii up to 6 cell edges (its stencil tables)
+  if (!cl->grid_ok || Rmax > cl->g.h * 6.f)
+    return fail_all(fail(w, PP_ERR_STATE, "cloud was not prepared for R = %g (pp_cloud_prepare)", (double)Rmax));
+  // hull-distance groups: queries sharing R' = max(R, carve) share one ion2surf
+  std::vector<float> grp_rp;
+  std::vector<int> grp_of(nq, 0);
+  for (int q = 0; q < nq; ++q) {
+    const float rp = cl->has_user_surf ? -1.f : std::max(P[q].t.rmax, cl->hull.carve);
+    int g = 0;
+    while (g < (int)grp_rp.size() && grp_rp[g] != rp) ++g;
+    if (g == (int)grp_rp.size()) grp_rp.push_back(rp);
+    grp_of[q] = g;
+  }
+  std::vector<float> grpR2;
+  std::vector<uint32_t> grpBits;
+  std::vector<int> grp_off(grp_rp.size() + 1, 0);
+  for (size_t g = 0; g < grp_rp.size(); ++g) {
+    grp_off[g] = (int)grpR2.size();
+    for (int q = 0; q < nq; ++q)
+      if (grp_of[q] == (int)g) {
+        grpR2.push_back(MQ[q].R2);
+        grpBits.push_back(1u << q);
+      }
+  }
+  grp_off[grp_rp.size()] = (int)grpR2.size();
+  // tables in one device block
+  std::vector<unsigned char> blob;
+  auto put = [&](const void* src, size_t bytes) {
+    size_t off = (blob.size() + 15) & ~size_t(15);
+    blob.resize(off + bytes);
+    if (bytes) std::memcpy(blob.data() + off, src, bytes);
+    return off;
+  };
+  int nrow = 0;
+  const int8_t* rows = pp::row_table_host(&nrow);
+  const size_t oQ = put(MQ.data(), MQ.size() * sizeof(pp::MultiQuery));
+  const size_t oT = put(MT.data(), MT.size() * sizeof(pp::MultiTask));
+  const size_t oqt = put(q_of_type.data(), 256 * 4);
+  const size_t ott = put(t_of_type.data(), 256 * 8);
+  const size_t oet = put(env_of_type.data(), 256 * 8);
+  const size_t otq = put(t_of_q.data(), t_of_q.size() * 8);
+  const size_t oTa = put(Tall.data(), Tall.size() * 4);
+  const size_t oL = put(Lall.data(), Lall.size() * 2);
+  const size_t oK = put(Kall.data(), std::max<size_t>(Kall.size(), 1) * 4);
+  const size_t oR = put(grpR2.data(), grpR2.size() * 4);
+  const size_t oB = put(grpBits.data(), grpBits.size() * 4);
+  const size_t orow = put(rows, (size_t)nrow * 2);
+  const uint64_t core_words = std::max<uint64_t>(rdf_words + knn_words, 1);
+  if (w->tables_dev.ensure(blob.size()) != cudaSuccess || w->multi_cmask.ensure(std::max<uint64_t>(n, 1) * 4) != cudaSuccess ||
+      w->multi_cores.ensure(core_words * 8 + 16 * pp::kMultiMaxQueries + 16) != cudaSuccess ||
+      w->centres.ensure(std::max<uint64_t>(n, 1) * 4) != cudaSuccess || w->centre_count.ensure(8) != cudaSuccess ||
+      w->sel_flags.ensure((n + 1) * 4) != cudaSuccess)
+    return fail_all(fail(w, PP_ERR_NOMEM, "device allocation for a merged pass failed"));
+  const uint64_t tmp_elems = (n + 1) / 2048 + 64;
+  if (w->sel_tmp.ensure(tmp_elems * 4 * 2) != cudaSuccess || w->work.ensure(32) != cudaSuccess)
+    return fail_all(fail(w, PP_ERR_NOMEM, "device allocation for a merged pass failed"));
+  unsigned char* b = w->tables_dev.as<unsigned char>();
+  unsigned long long* cores = w->multi_cores.as<unsigned long long>();
+  unsigned long long* counters = cores + core_words;
+  int* status = reinterpret_cast<int*>(counters + 2 * pp::kMultiMaxQueries);
+  uint32_t* cmask = w->multi_cmask.as<uint32_t>();
+  auto ck = [&](cudaError_t e) { return e == cudaSuccess; };
+  if (!ck(cudaMemcpyAsync(b, blob.data(), blob.size(), cudaMemcpyHostToDevice, s)) ||
+      !ck(cudaMemsetAsync(cores, 0, core_words * 8 + 16 * pp::kMultiMaxQueries + 16, s)) ||
+      !ck(cudaMemsetAsync(cmask, 0, std::max<uint64_t>(n, 1) * 4, s)) || !ck(cudaMemsetAsync(w->work.p, 0, 32, s)))
+    return fail_all(fail(w, PP_ERR_CUDA, "merged pass set-up failed"));
+  // hull-distance bits: each group's ion2surf as a lone query computes it
+  for (size_t g = 0; g < grp_rp.size(); ++g) {
+    const float* surf = nullptr;
+    int gq = 0;
+    while (grp_of[gq] != (int)g) ++gq;
+    int rc = ensure_surface(w, *cl, P[gq].t.rmax, s, &surf);
+    if (rc) return fail_all(rc);
+    pp::launch_cmask_or(surf, n, reinterpret_cast<const float*>(b + oR) + grp_off[g],
+                        reinterpret_cast<const uint32_t*>(b + oB) + grp_off[g], grp_off[g + 1] - grp_off[g], cmask, s);
+  }
+  pp::launch_multi_select(cl->label_sorted.as<uint8_t>(), cmask, reinterpret_cast<const uint32_t*>(b + oqt), n,
+                          w->sel_flags.as<uint32_t>(), w->sel_tmp.as<uint32_t>(), tmp_elems * 2,
+                          w->centres.as<uint32_t>(), w->centre_count.as<uint32_t>(), s);
+  uint32_t ncent = 0;
+  if (!ck(cudaGetLastError()) || !ck(cudaMemcpyAsync(&ncent, w->centre_count.p, 4, cudaMemcpyDeviceToHost, s)) ||
+      !ck(cudaStreamSynchronize(s)))
+    return fail_all(fail(w, PP_ERR_CUDA, "merged pass centre selection failed"));
+  if (ncent > 0) {
+    pp::MultiArgs m{};
+    pp::ScanArgs& a = m.s;
+    a.ions = cl->ions.as<float4>();
+    a.cell_start = cl->cell_start.as<uint32_t>();
+    a.g = cl->g;
+    a.labels = cl->label_sorted.as<uint8_t>();
+    a.rowtab = reinterpret_cast<const int8_t*>(b + orow);
+    a.status = status;
+    a.sym = 0;
+    m.cmask = cmask;
+    m.centres = w->centres.as<uint32_t>();
+    m.ncentres = ncent;
+    m.nq = nq;
+    m.nt = (int)MT.size();
+    m.qs = reinterpret_cast<const pp::MultiQuery*>(b + oQ);
+    m.ts = reinterpret_cast<const pp::MultiTask*>(b + oT);
+    m.q_of_type = reinterpret_cast<const uint32_t*>(b + oqt);
+    m.t_of_type = reinterpret_cast<const unsigned long long*>(b + ott);
+    m.env_of_type = reinterpret_cast<const unsigned long long*>(b + oet);
+    m.t_of_q = reinterpret_cast<const unsigned long long*>(b + otq);
+    m.rdf_tasks = rdf_tasks;
+    m.knn_tasks = knn_tasks;
+    m.T = reinterpret_cast<const float*>(b + oTa);
+    m.lut = reinterpret_cast<const uint16_t*>(b + oL);
+    m.kvals = reinterpret_cast<const int*>(b + oK);
+    m.rdf_core = cores;
+    m.knn_core = cores + rdf_words;
+    m.counters = counters;
+    m.rdf_words = (uint32_t)rdf_words;
+    m.lists = lists;
+    m.tile = 32;
+    m.work = w->work.as<uint32_t>();
+    size_t smem = 0;
+    const int rc = pp::launch_multi(m, w->sm_count, &smem, s);
+    if (rc) return fail_all(fail(w, PP_ERR_CUDA, "merged pass launch failed (%d, %zu B shared)", rc, smem));
+  }
+  std::vector<unsigned long long> hc(core_words + 2 * pp::kMultiMaxQueries + 2);
+  if (!ck(cudaMemcpyAsync(hc.data(), cores, hc.size() * 8, cudaMemcpyDeviceToHost, s)) ||
+      !ck(cudaStreamSynchronize(s)))
+    return fail_all(fail(w, PP_ERR_CUDA, "merged pass failed"));
+  int st = 0;
+  std::memcpy(&st, &hc[core_words + 2 * pp::kMultiMaxQueries], 4);
+  if (st) return fail_all(fail(w, PP_ERR_DEVICE, "merged pass: device status word 0x%x", st));
+  // each query's pp_fetch layout: RDF[tasks], 1NN[tasks], RIPK[tasks], MKNN[tasks][k]
+  int t0 = 0;
+  for (int q = 0; q < nq; ++q) {
+    ServerRequest& r = *qs[q];
+    const int H = MQ[q].H;
+    const std::vector<uint32_t>& kv = P[q].kvals;
+    auto kidx = [&](uint32_t k) { return (size_t)(std::lower_bound(kv.begin(), kv.end(), k) - kv.begin()); };
+    r.bins.clear();
+    auto rdf = [&](int t) {
+      const unsigned long long* c = hc.data() + MT[t].rdf;
+      r.bins.insert(r.bins.end(), c, c + H);
+    };
+    auto knn = [&](int t, uint32_t k) {
+      const unsigned long long* c = hc.data() + rdf_words + MT[t].knn + kidx(k) * H;
+      r.bins.insert(r.bins.end(), c, c + H);
+    };
+    if (r.flags & PP_RDF) for (int k = 0; k < r.ntasks; ++k) rdf(t0 + k);
+    if (r.flags & PP_1NN) for (int k = 0; k < r.ntasks; ++k) knn(t0 + k, 1);
+    if (r.flags & PP_RIPK) for (int k = 0; k < r.ntasks; ++k) rdf(t0 + k);
+    if (r.flags & PP_MKNN)
+      for (int k = 0; k < r.ntasks; ++k)
+        for (uint32_t kk : r.ks) knn(t0 + k, kk);
+    r.pairs = hc[core_words + 2 * q];
+    r.centres = hc[core_words + 2 * q + 1];
+    r.rc = PP_OK;
+    t0 += r.ntasks;
+  }
+}
+
+// Footprint of a merged pass on a cloud of n ions: hull-distance bits, a
+// private ion2surf, selection flags, scan partials and centre list (17 B per
+// ion), plus every query's result cores.
+uint64_t multi_base_bytes(uint64_t n) { return 17 * n + (1u << 20); }
+
 void worker_loop(pp_server* S, int k) {
   pp_ctx* w = S->workers[k];
   cudaSetDevice(w->device);
   for (;;) {
-    std::shared_ptr<ServerRequest> q;
+    std::vector<std::shared_ptr<ServerRequest>> batch;
+    uint64_t fp = 0;
     {
       std::unique_lock<std::mutex> lk(S->mu);
-      S->cv_queue.wait(lk, [&] {
-        return S->stop || (!S->queue.empty() && S->inflight + S->queue.front()->footprint <= S->budget);
-      });
+      // the head of the queue, and with it every queued query of its cloud
+      // that can share its pass, as far as the budget and the pass's limits
+      // allow; queries that arrived while earlier passes ran join here
+      auto head_fp = [&] {
+        const auto& h = S->queue.front();
+        return h->mergeable ? multi_base_bytes(S->ctx->clouds[h->cloud]->n) + h->footprint : h->footprint;
+      };
+      S->cv_queue.wait(lk, [&] { return S->stop || (!S->queue.empty() && S->inflight + head_fp() <= S->budget); });
       if (S->queue.empty()) return;  // stop requested and nothing left
-      q = S->queue.front();
+      std::shared_ptr<ServerRequest> h = S->queue.front();
       S->queue.pop_front();
-      S->inflight += q->footprint;
-      S->admitted++;
+      batch.push_back(h);
+      if (h->mergeable) {
+        fp = multi_base_bytes(S->ctx->clouds[h->cloud]->n) + h->footprint;
+        int tasks = h->ntasks;
+        for (auto it = S->queue.begin(); it != S->queue.end() && (int)batch.size() < S->max_batch;) {
+          const auto& q = *it;
+          if (q->mergeable && q->cloud == h->cloud && tasks + q->ntasks <= pp::kMultiMaxTasks &&
+              S->inflight + fp + q->footprint <= S->budget) {
+            fp += q->footprint;
+            tasks += q->ntasks;
+            batch.push_back(q);
+            it = S->queue.erase(it);
+          } else {
+            ++it;
+          }
+        }
+      } else {
+        fp = h->footprint;
+      }
+      S->inflight += fp;
+      S->admitted += batch.size();
+      S->batches++;
     }
-    serve_one(w, S->streams[k], *q);
+    if (batch[0]->mergeable) {
+      std::vector<ServerRequest*> raw;
+      for (auto& q : batch) raw.push_back(q.get());
+      run_multi(w, raw, S->streams[k]);
+    } else {
+      serve_one(w, S->streams[k], *batch[0]);
+    }
     {
       std::lock_guard<std::mutex> lk(S->mu);
-      S->inflight -= q->footprint;
-      q->t_end = now_ms();
-      q->done = true;
-      S->completed++;
-      S->pairs_done += (double)q->pairs;
-      S->latencies.push_back(q->t_end - q->t_submit);
+      S->inflight -= fp;
+      const double t = now_ms();
+      for (auto& q : batch) {
+        q->t_end = t;
+        q->done = true;
+        S->completed++;
+        S->pairs_done += (double)q->pairs;
+        S->latencies.push_back(q->t_end - q->t_submit);
+      }
     }
     S->cv_done.notify_all();
     S->cv_queue.notify_all();
@@ -2578,6 +2882,7 @@ int pp_server_create(pp_ctx* ctx, int slots, uint64_t budget_bytes, pp_server** 
   if (!S) return PP_ERR_NOMEM;
   S->ctx = ctx;
   S->budget = budget_bytes;
+  S->max_batch = ctx->server_batch;
   for (int k = 0; k < slots; ++k) {
     pp_ctx* w = new (std::nothrow) pp_ctx();
     cudaStream_t st = nullptr;
@@ -2615,15 +2920,28 @@ int pp_server_submit(pp_server* S, int cloud, uint32_t flags, float rmin, float 
   q->env.assign(env_mask, env_mask + 8 * (size_t)ntasks);
   q->ntasks = ntasks;
   if (nk) q->ks.assign(k_list, k_list + nk);
-  // device footprint of one query: centre list, flags, scan scratch, centre
-  // flags, private ion2surf, per-cell prefix, result cores
+  uint32_t kmax = (flags & PP_1NN) ? 1u : 0u;
+  if (flags & PP_MKNN)
+    for (int i = 0; i < nk; ++i) kmax = std::max(kmax, k_list[i]);
+  for (int i = 0; i < nk; ++i)
+    if (k_list[i] < 1) return PP_ERR_INVALID;
+  // queries of plain RDF / 1NN / RIPK / MKNN with k <= 32 and at most 64
+  // tasks share merged passes; the others run alone on the plain path
+  q->mergeable = !(flags & ~(uint32_t)(PP_RDF | PP_1NN | PP_RIPK | PP_MKNN)) && kmax <= (uint32_t)pp::kMultiMaxK &&
+                 ntasks <= pp::kMultiMaxTasks && S->max_batch > 1;
+  // device footprint: a merged query adds its result cores to its pass (whose
+  // own buffers the scheduler counts once per pass); a lone query its centre
+  // list, flags, scan scratch, centre flags, private ion2surf, per-cell
+  // prefix and result cores
   const double nb = (rincr > 0.f) ? std::floor(((double)rmax - (double)rmin) / (double)rincr) + 2.0 : 1.0;
   const double cores = 8.0 * nb * (double)ntasks * (3.0 + (double)nk);
-  q->footprint = (uint64_t)(13.0 * (double)cl->n + 4.0 * (double)cl->g.ncells + cores);
+  q->footprint = q->mergeable ? (uint64_t)cores + 4096
+                              : (uint64_t)(13.0 * (double)cl->n + 4.0 * (double)cl->g.ncells + cores);
   q->t_submit = now_ms();
+  const uint64_t need = q->footprint + (q->mergeable ? multi_base_bytes(cl->n) : 0);
   std::lock_guard<std::mutex> lk(S->mu);
   S->submitted++;
-  if (q->footprint > S->budget) {
+  if (need > S->budget) {
     S->rejected++;
     return PP_ERR_NOMEM;
   }
@@ -2676,6 +2994,14 @@ int pp_server_stats(pp_server* S, double* st) {
   st[5] = pct(0.50);
   st[6] = pct(0.99);
   st[7] = S->pairs_done;
+  return PP_OK;
+}
+
+int pp_server_passes(pp_server* S, uint64_t* passes, uint64_t* queries) {
+  if (!S) return PP_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (passes) *passes = S->batches;
+  if (queries) *queries = S->admitted;
   return PP_OK;
 }
 

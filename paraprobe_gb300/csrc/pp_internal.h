@@ -140,6 +140,56 @@ struct ApplyArgs {
   int* status;
 };
 
+// ---- merged pass of several queries on one cloud (the serving loop's
+// continuous batching).  Each query has its own radius, histogram geometry,
+// hull-distance test, kNN orders and tasks; one walk per centre at the
+// largest radius among the queries the centre belongs to serves them all.
+constexpr int kMultiMaxQueries = 32;  // queries per merged pass (bits of a uint32)
+constexpr int kMultiMaxTasks = 64;    // tasks per merged pass (bits of a uint64)
+constexpr int kMultiMaxK = 32;        // largest kNN order (one list row per warp lane)
+
+struct MultiQuery {
+  float R, R2, Rm2;          // SpatStatRadiusMax, float(R * R), (R + grid margin)^2
+  int H;                     // nbins + 2
+  int cat_miss;              // category of float(R + EPSILON)
+  int lut_n, lut_shift;
+  uint32_t lut_base;
+  uint32_t T_off, lut_off;   // offsets of its threshold table and category lookup
+  uint32_t kv_off;           // offset of its kNN orders (sorted, unique, 1-based)
+  int nkI, kmax;
+};
+
+struct MultiTask {
+  int q;                     // its query
+  uint32_t rdf;              // offset of its RDF core [H] (0xffffffff: none)
+  uint32_t knn;              // offset of its kNN core [nkI][H] (0xffffffff: none)
+};
+
+struct MultiArgs {
+  ScanArgs s;                          // cloud, grid, labels, row table, status
+  const uint32_t* cmask;               // [n] by slot: bit q = passes query q's hull-distance test
+  const uint32_t* centres;             // slots of the centres (cell order)
+  uint32_t ncentres;
+  int nq, nt;
+  const MultiQuery* qs;                // [nq]
+  const MultiTask* ts;                 // [nt]
+  const uint32_t* q_of_type;           // [256] queries with a task whose targets hold the type
+  const unsigned long long* t_of_type;   // [256] tasks whose targets hold the type
+  const unsigned long long* env_of_type; // [256] tasks whose environment holds the type
+  const unsigned long long* t_of_q;      // [nq] tasks of each query
+  unsigned long long rdf_tasks, knn_tasks;  // tasks with an RDF / a kNN core
+  const float* T;                      // threshold tables, all queries
+  const uint16_t* lut;                 // category lookups, all queries
+  const int* kvals;                    // kNN orders, all queries
+  unsigned long long* rdf_core;        // flat, offsets MultiTask::rdf
+  unsigned long long* knn_core;        // flat, offsets MultiTask::knn
+  unsigned long long* counters;        // [nq][2] pairs, centres
+  uint32_t rdf_words;                  // RDF counters of all tasks (binned in shared memory when > 0)
+  int lists;                           // most kNN tasks of one centre type: list rows per warp
+  uint32_t tile;                       // centres per block work item
+  uint32_t* work;
+};
+
 // kernel launchers (pp_kernels.cu)
 void launch_bbox(const float* xyz, uint64_t n, float* d_minmax, cudaStream_t s);
 void launch_bbox_pos(const uint32_t* be, uint64_t n, float* d_minmax, cudaStream_t s);
@@ -255,6 +305,14 @@ int launch_npcorr(const ScanArgs& a, const NpcArgs& p, int sm_count, cudaStream_
 // labels of the statistics after clustering: 1 free, 2 guard, 3 clustered
 void launch_guard(const ScanArgs& a, const uint8_t* clus, uint8_t* guard_then_labels, uint64_t n, int sm_count,
                   cudaStream_t s);
+
+// merged multi-query pass: hull-distance bits, centre selection, the scan
+void launch_cmask_or(const float* surf, uint64_t n, const float* R2, const uint32_t* bits, int nb, uint32_t* cmask,
+                     cudaStream_t s);
+void launch_multi_select(const uint8_t* labels, const uint32_t* cmask, const uint32_t* q_of_type, uint64_t n,
+                         uint32_t* flags, uint32_t* scan_tmp, uint64_t scan_tmp_elems, uint32_t* out, uint32_t* count,
+                         cudaStream_t s);
+int launch_multi(const MultiArgs& m, int sm_count, size_t* smem_used, cudaStream_t s);
 
 // neighbours within R of every slot (j != i), written by input index
 void launch_ball_count(const ScanArgs& a, const uint32_t* id_of_slot, uint64_t n, uint32_t* count_by_id, int sm_count,

@@ -610,10 +610,10 @@ struct ScanShared {
 // a time across the warp; f(valid, slot, d2, inball, type) is called
 // warp-uniformly once per 32 candidates.
 template <class F>
-__device__ __forceinline__ void for_each_candidate(const ScanArgs& a, const int8_t* __restrict__ rowtab, float4 cp,
-                                                   uint32_t self, int lane, F&& f) {
+__device__ __forceinline__ void for_each_candidate_r(const ScanArgs& a, const int8_t* __restrict__ rowtab, float4 cp,
+                                                     uint32_t self, int lane, float R, float Rm2, float R2, F&& f) {
   const Grid& g = a.g;
-  const float ext = a.R + g.margin;
+  const float ext = R + g.margin;
   auto clampc = [](int c, int n) { return c < 0 ? 0 : (c >= n ? n - 1 : c); };
   const int y0 = clampc((int)floorf((cp.y - ext - g.loy) * g.inv_h), g.ny);
   const int y1 = clampc((int)floorf((cp.y + ext - g.loy) * g.inv_h), g.ny);
@@ -642,7 +642,7 @@ __device__ __forceinline__ void for_each_candidate(const ScanArgs& a, const int8
       const float zlo = g.loz + (float)zz * g.h - g.margin, zhi = g.loz + (float)(zz + 1) * g.h + g.margin;
       const float dy = fmaxf(0.f, fmaxf(ylo - cp.y, cp.y - yhi));
       const float dz = fmaxf(0.f, fmaxf(zlo - cp.z, cp.z - zhi));
-      const float rem = a.Rm2 - dy * dy - dz * dz;
+      const float rem = Rm2 - dy * dy - dz * dz;
       if (rem >= 0.f) {
         const float half = sqrtf(rem) + g.margin;
         const int x0 = clampc((int)floorf((cp.x - half - g.lox) * g.inv_h), g.nx);
@@ -699,12 +699,19 @@ __device__ __forceinline__ void for_each_candidate(const ScanArgs& a, const int8
         d2 = dist2(cp.x, cp.y, cp.z, q.x, q.y, q.z);
         // symmetric mode: a pair of two centres is taken once, by the lower slot
         if (a.sym) jcentre = a.cflag[slot] != 0;
-        inball = (d2 <= a.R2) && (slot != self) && !(jcentre && slot < self);
+        inball = (d2 <= R2) && (slot != self) && !(jcentre && slot < self);
         m = a.labels ? (uint32_t)a.labels[slot] : __float_as_uint(q.w);
       }
       f(valid, slot, d2, inball, m, jcentre && slot > self);
     }
   }
+}
+
+// The same walk at the pass's radius (ScanArgs::R, Rm2, R2).
+template <class F>
+__device__ __forceinline__ void for_each_candidate(const ScanArgs& a, const int8_t* __restrict__ rowtab, float4 cp,
+                                                   uint32_t self, int lane, F&& f) {
+  for_each_candidate_r(a, rowtab, cp, self, lane, a.R, a.Rm2, a.R2, f);
 }
 
 template <int KR, int EMAX>
@@ -993,6 +1000,216 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
       if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
     }
   }
+}
+
+// ------------------------------------------------ merged multi-query pass
+// Hull-distance bits of a merged pass: for the queries whose R' = max(R,
+// SurfaceCellsCarvingRadius) gave `surf`, bit bits[j] of cmask is set where
+// surf >= R2[j] -- the centre test of each query alone
+// (src/PARAPROBE_SolverHdl.cpp:3847-3859), from the same ion2surf values.
+__global__ void k_cmask_or(const float* __restrict__ surf, uint64_t n, const float* __restrict__ R2,
+                           const uint32_t* __restrict__ bits, int nb, uint32_t* __restrict__ cmask) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const float v = surf[i];
+    uint32_t m = 0;
+    for (int j = 0; j < nb; ++j) m |= (v >= R2[j]) ? bits[j] : 0u;
+    cmask[i] |= m;
+  }
+}
+
+__global__ void k_multi_flags(const uint8_t* __restrict__ labels, const uint32_t* __restrict__ cmask,
+                              const uint32_t* __restrict__ q_of_type, uint64_t n, uint32_t* __restrict__ flags) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= n; i += (uint64_t)gridDim.x * blockDim.x)
+    flags[i] = (i < n && (cmask[i] & q_of_type[labels[i]]) != 0u) ? 1u : 0u;
+}
+
+__global__ void k_multi_write(const uint8_t* __restrict__ labels, const uint32_t* __restrict__ cmask,
+                              const uint32_t* __restrict__ q_of_type, uint64_t n, const uint32_t* __restrict__ pos,
+                              uint32_t* __restrict__ out, uint32_t* __restrict__ count) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    if ((cmask[i] & q_of_type[labels[i]]) != 0u) out[pos[i]] = (uint32_t)i;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *count = pos[n];
+}
+
+// One warp per centre.  The centre's queries are those with a task targeting
+// its type whose hull-distance test it passes; its tasks, the tasks of those
+// queries that target its type.  The warp walks the candidates within the
+// largest radius among its queries once (for_each_candidate_r, nearest rows
+// first); a candidate within a query's radius counts as one of that query's
+// in-ball pairs whatever its type, and adds to a task's RDF bins (category
+// from the query's own threshold table) and kNN list when its type is in the
+// task's environment -- exactly the per-centre loop of
+// compute_generic_spatstat3 (src/PARAPROBE_SolverHdl.cpp:3975-4101) run for
+// each query alone.  RDF bins of all tasks are uint32 counters in shared
+// memory, moved to the global uint64 cores whenever the block's adds cross a
+// multiple of 2^30; kNN lists are one 32-float row per task in the warp's
+// shared memory (rank r in lane r), filled by one ballot per 32 candidates.
+constexpr int kMultiWarps = 8;
+
+__global__ void __launch_bounds__(kMultiWarps * 32) k_multi(MultiArgs m) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const ScanArgs& a = m.s;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  unsigned char* sp = smem;
+  unsigned long long* since_flush = (unsigned long long*)sp; sp += 16;
+  unsigned long long* scnt = (unsigned long long*)sp; sp += kMultiMaxQueries * 2 * 8;
+  MultiQuery* sq = (MultiQuery*)sp; sp += ((sizeof(MultiQuery) * kMultiMaxQueries + 15) & ~size_t(15));
+  MultiTask* st = (MultiTask*)sp; sp += ((sizeof(MultiTask) * kMultiMaxTasks + 15) & ~size_t(15));
+  unsigned long long* stt = (unsigned long long*)sp; sp += 256 * 8;
+  unsigned long long* senv = (unsigned long long*)sp; sp += 256 * 8;
+  unsigned long long* stq = (unsigned long long*)sp; sp += kMultiMaxQueries * 8;
+  uint32_t* sqt = (uint32_t*)sp; sp += 256 * 4;
+  uint32_t* wpairs = (uint32_t*)sp; sp += nwarps * kMultiMaxQueries * 4;
+  int8_t* rowtab = (int8_t*)sp; sp += ((ROW_TABLE_ENTRIES * 2 + 15) & ~15);
+  float* lists = (float*)sp; sp += (size_t)nwarps * m.lists * 32 * 4;
+  uint32_t* srdf = (uint32_t*)sp;  // [rdf_words] when binned in shared memory
+  const bool rdf_smem = m.rdf_words > 0;
+  for (int i = threadIdx.x; i < m.nq; i += blockDim.x) { sq[i] = m.qs[i]; stq[i] = m.t_of_q[i]; }
+  for (int i = threadIdx.x; i < m.nt; i += blockDim.x) st[i] = m.ts[i];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    stt[i] = m.t_of_type[i];
+    senv[i] = m.env_of_type[i];
+    sqt[i] = m.q_of_type[i];
+  }
+  for (int i = threadIdx.x; i < kMultiMaxQueries * 2; i += blockDim.x) scnt[i] = 0ull;
+  for (int i = threadIdx.x; i < nwarps * kMultiMaxQueries; i += blockDim.x) wpairs[i] = 0u;
+  for (int i = threadIdx.x; i < ROW_TABLE_ENTRIES * 2; i += blockDim.x) rowtab[i] = a.rowtab[i];
+  for (uint32_t i = threadIdx.x; i < m.rdf_words; i += blockDim.x) srdf[i] = 0u;
+  if (threadIdx.x == 0) *since_flush = 0ull;
+  __syncthreads();
+
+  uint32_t* wp = wpairs + warp * kMultiMaxQueries;
+  float* L = lists + (size_t)warp * m.lists * 32;
+  constexpr unsigned long long FLUSH = 1ull << 30;
+  __shared__ uint32_t s_tile, s_next;
+  const uint32_t T = max(m.tile, 1u);
+  const uint32_t ntiles = (m.ncentres + T - 1) / T;
+  for (;;) {
+    if (threadIdx.x == 0) { s_tile = atomicAdd(m.work, 1u); s_next = 0; }
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= ntiles) break;
+    const uint32_t c0 = tile * T, clen = min(T, m.ncentres - c0);
+    for (;;) {
+      uint32_t kk = 0;
+      if (lane == 0) kk = atomicAdd(&s_next, 1u);
+      kk = __shfl_sync(FULL, kk, 0);
+      if (kk >= clen) break;
+      const uint32_t self = m.centres[c0 + kk];
+      const float4 cp = a.ions[self];
+      const uint32_t ct = (a.labels ? (uint32_t)a.labels[self] : __float_as_uint(cp.w)) & 255u;
+      const uint32_t aq = m.cmask[self] & sqt[ct];
+      if (!aq) {  // selection guarantees a query; record and skip otherwise
+        if (lane == 0) atomicOr(a.status, ST_TYPE_RANGE);
+        continue;
+      }
+      unsigned long long at = 0;
+      float R = 0.f, R2 = 0.f, Rm2 = 0.f;
+      for (uint32_t b = aq; b; b &= b - 1u) {
+        const int q = __ffs(b) - 1;
+        at |= stq[q];
+        if (sq[q].R > R) { R = sq[q].R; R2 = sq[q].R2; Rm2 = sq[q].Rm2; }
+      }
+      at &= stt[ct];
+      const unsigned long long atk = at & m.knn_tasks;
+      const int nl = __popcll(atk);
+      if (nl > m.lists) {  // the host sizes the rows; record and skip otherwise
+        if (lane == 0) atomicOr(a.status, ST_BAD_SLOT);
+        continue;
+      }
+      for (int e = lane; e < nl * 32; e += 32) L[e] = kInf();
+      __syncwarp();
+      uint32_t inb = 0;
+      for_each_candidate_r(a, rowtab, cp, self, lane, R, Rm2, R2,
+                           [&](bool, uint32_t, float d2, bool inball, uint32_t mt, bool) {
+        // in-ball pairs of every query of the centre, whatever the type
+        for (uint32_t b = aq; b; b &= b - 1u) {
+          const int q = __ffs(b) - 1;
+          const uint32_t c = __popc(__ballot_sync(FULL, inball && d2 <= sq[q].R2));
+          if (lane == 0) wp[q] += c;
+        }
+        const unsigned long long et = inball ? (senv[mt & 255u] & at) : 0ull;
+        // RDF / RIPK: this candidate's tasks, lane by lane
+        for (unsigned long long er = et & m.rdf_tasks; er; er &= er - 1ull) {
+          const int t = __ffsll((long long)er) - 1;
+          const MultiQuery& Q = sq[st[t].q];
+          if (d2 <= Q.R2) {
+            const int cat = category_lut(d2, m.lut + Q.lut_off, Q.lut_n, Q.lut_base, Q.lut_shift, m.T + Q.T_off, Q.H);
+            ++inb;
+            if (rdf_smem) atomicAdd(&srdf[st[t].rdf + cat], 1u);
+            else atomicAdd(&m.rdf_core[st[t].rdf + cat], 1ull);
+          }
+        }
+        // kNN: one list row per task of the centre, warp-uniform
+        int row = 0;
+        for (unsigned long long tb = atk; tb; tb &= tb - 1ull, ++row) {
+          const int t = __ffsll((long long)tb) - 1;
+          const MultiQuery& Q = sq[st[t].q];
+          float* lp = L + row * 32;
+          const bool want = ((et >> t) & 1ull) && d2 <= Q.R2;
+          uint32_t mask = __ballot_sync(FULL, want && d2 < lp[Q.kmax - 1]);
+          while (mask) {
+            const int srcl = __ffs(mask) - 1;
+            const float x = __shfl_sync(FULL, d2, srcl);
+            float v[1] = {lp[lane]};
+            list_insert<1>(v, x, lane);
+            __syncwarp();
+            lp[lane] = v[0];
+            __syncwarp();
+            mask &= ~(1u << srcl);
+            mask &= __ballot_sync(FULL, want && d2 < lp[Q.kmax - 1]);
+          }
+        }
+      });
+      // the k-th smallest d^2 of each kNN task -> its bin (or the miss bin)
+      int row = 0;
+      for (unsigned long long tb = atk; tb; tb &= tb - 1ull, ++row) {
+        const int t = __ffsll((long long)tb) - 1;
+        const MultiQuery& Q = sq[st[t].q];
+        for (int k2 = lane; k2 < Q.nkI; k2 += 32) {
+          const int kv = m.kvals[Q.kv_off + k2];
+          const float v = L[row * 32 + kv - 1];
+          const int cat = (v == kInf()) ? Q.cat_miss
+                                        : category_lut(v, m.lut + Q.lut_off, Q.lut_n, Q.lut_base, Q.lut_shift,
+                                                       m.T + Q.T_off, Q.H);
+          if (cat >= 0) atomicAdd(&m.knn_core[st[t].knn + (uint64_t)k2 * Q.H + cat], 1ull);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) {
+        for (uint32_t b = aq; b; b &= b - 1u) {
+          const int q = __ffs(b) - 1;
+          atomicAdd(&scnt[2 * q], (unsigned long long)wp[q]);
+          atomicAdd(&scnt[2 * q + 1], 1ull);
+          wp[q] = 0u;
+        }
+      }
+      __syncwarp();
+      if (rdf_smem) {
+        // keep every shared counter below 2^32: when the block's adds cross a
+        // multiple of 2^30 the warp that crossed it moves all bins out
+        uint32_t tot = inb;
+        for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+        unsigned long long old = 0;
+        if (lane == 0) old = atomicAdd(since_flush, (unsigned long long)tot);
+        old = __shfl_sync(FULL, old, 0);
+        if (old / FLUSH != (old + tot) / FLUSH) {
+          for (uint32_t i = lane; i < m.rdf_words; i += 32) {
+            const uint32_t v = atomicExch(&srdf[i], 0u);
+            if (v) atomicAdd(&m.rdf_core[i], (unsigned long long)v);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < m.rdf_words; i += blockDim.x) {
+    const uint32_t v = srdf[i];
+    if (v) atomicAdd(&m.rdf_core[i], (unsigned long long)v);
+  }
+  for (int i = threadIdx.x; i < 2 * m.nq; i += blockDim.x)
+    if (scnt[i]) atomicAdd(&m.counters[i], scnt[i]);
 }
 
 // ------------------------------------------------- statistics after clustering
@@ -2758,6 +2975,53 @@ int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_
     if (emax <= 8) return launch_scan_t<4, 8>(a, sm_count, smem, s);
   }
   return -2;
+}
+
+void launch_cmask_or(const float* surf, uint64_t n, const float* R2, const uint32_t* bits, int nb, uint32_t* cmask,
+                     cudaStream_t s) {
+  counted();
+  k_cmask_or<<<grid_for(n, 256), 256, 0, s>>>(surf, n, R2, bits, nb, cmask);
+}
+
+void launch_multi_select(const uint8_t* labels, const uint32_t* cmask, const uint32_t* q_of_type, uint64_t n,
+                         uint32_t* flags, uint32_t* scan_tmp, uint64_t scan_tmp_elems, uint32_t* out, uint32_t* count,
+                         cudaStream_t s) {
+  counted();
+  k_multi_flags<<<grid_for(n + 1, 256), 256, 0, s>>>(labels, cmask, q_of_type, n, flags);
+  excl_scan<uint32_t>(flags, n + 1, scan_tmp, scan_tmp_elems, s);
+  counted();
+  k_multi_write<<<grid_for(n, 256), 256, 0, s>>>(labels, cmask, q_of_type, n, flags, out, count);
+}
+
+static size_t multi_smem(const MultiArgs& m, uint32_t rdf_words) {
+  return 16 + kMultiMaxQueries * 2 * 8 + ((sizeof(MultiQuery) * kMultiMaxQueries + 15) & ~size_t(15)) +
+         ((sizeof(MultiTask) * kMultiMaxTasks + 15) & ~size_t(15)) + 256 * 8 * 2 + kMultiMaxQueries * 8 + 256 * 4 +
+         (size_t)kMultiWarps * kMultiMaxQueries * 4 + ((ROW_TABLE_ENTRIES * 2 + 15) & ~15) +
+         (size_t)kMultiWarps * m.lists * 32 * 4 + (size_t)rdf_words * 4;
+}
+
+int launch_multi(const MultiArgs& m0, int sm_count, size_t* smem_used, cudaStream_t s) {
+  if (m0.nq < 1 || m0.nq > kMultiMaxQueries || m0.nt < 1 || m0.nt > kMultiMaxTasks || m0.lists < 0 ||
+      m0.lists > kMultiMaxTasks)
+    return -3;
+  MultiArgs m = m0;
+  // RDF counters in shared memory when they fit beside the lists, else
+  // straight to the global cores
+  size_t smem = multi_smem(m, m.rdf_words);
+  if (smem > 160 * 1024) {
+    m.rdf_words = 0;
+    smem = multi_smem(m, 0);
+  }
+  if (smem_used) *smem_used = smem;
+  if (smem > 220 * 1024) return -3;
+  if (!allow_dynamic_smem((const void*)k_multi, smem)) return -1;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_multi, kMultiWarps * 32, smem) != cudaSuccess ||
+      per_sm < 1)
+    return -1;
+  counted();
+  k_multi<<<sm_count * per_sm, kMultiWarps * 32, smem, s>>>(m);
+  return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 void launch_ball_count(const ScanArgs& a, const uint32_t* id_of_slot, uint64_t n, uint32_t* count_by_id, int sm_count,

@@ -29,7 +29,7 @@ EXPORTS = (
     "pp_last_kernel_ms", "pp_autotune", "pp_cloud_tuning", "pp_set_option", "pp_cloud_prepare",
     "pp_server_create", "pp_server_submit", "pp_server_wait", "pp_server_stats", "pp_server_destroy",
     "pp_fp64_audit", "pp_surfdist_noalloc", "pp_batched_graph", "pp_cloud_inside", "pp_fetch_npcorr",
-    "pp_run_aposteriori", "pp_last_kernel", "pp_run_tests", "pp_run_masked",
+    "pp_run_aposteriori", "pp_last_kernel", "pp_run_tests", "pp_run_masked", "pp_server_passes",
 )
 
 _lib = None
@@ -88,6 +88,7 @@ def load():
         "pp_server_wait": ([vp, u64, vp, C.c_size_t, C.POINTER(u64), C.POINTER(u64), C.POINTER(C.c_double)], i32),
         "pp_server_stats": ([vp, C.POINTER(C.c_double)], i32),
         "pp_server_destroy": ([vp], None),
+        "pp_server_passes": ([vp, C.POINTER(u64), C.POINTER(u64)], i32),
         "pp_fp64_audit": ([vp, i32, u32, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(u64),
                            C.POINTER(u64), C.POINTER(u64), vp, vp, u64, C.POINTER(u64)], i32),
         "pp_surfdist_noalloc": ([vp, u64, vp, u64, f32, vp, vp, C.c_char_p, C.c_size_t], i32),
@@ -410,6 +411,12 @@ class Server:
         self.L.pp_server_stats(self.h, st)
         keys = ("submitted", "admitted", "rejected", "completed", "in_flight", "p50_ms", "p99_ms", "pairs")
         return dict(zip(keys, list(st)))
+
+    def passes(self):
+        """(merged passes run, queries they took)."""
+        p, q = C.c_uint64(), C.c_uint64()
+        self.L.pp_server_passes(self.h, C.byref(p), C.byref(q))
+        return p.value, q.value
 
     def close(self):
         if self.h:
