@@ -184,7 +184,8 @@ int pp_run_masked(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list
  * they leave the statistics as centres and as neighbours. */
 int pp_run_aposteriori(pp_ctx* ctx, int cloud, const uint8_t* clustered, uint32_t flags, void* stream);
 /* Project-written autotuner: times the pass on about `sample` centres
- * (0 = 200000) for cell edges R/2 .. R/5 -- for passes the centre-per-lane
+ * (0 = 200000; at least 8192 per SM, so that every kernel form fills the GPU)
+ * for cell edges R/2 .. R/5 -- for passes the centre-per-lane
  * scan takes, at the default cell block of that edge (about a warp of
  * centres) and two fixed shapes; for other passes with the per-centre scan at
  * block tiles of 32, 128 and 512 centres and with the brick scan at bricks of

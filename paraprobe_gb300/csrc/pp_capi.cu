@@ -1641,6 +1641,12 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
   if (!cl) return fail(ctx, PP_ERR_INVALID, "bad cloud");
   CK(cudaSetDevice(ctx->device));
   if (sample == 0) sample = 200000;
+  // The sample must fill the GPU several times over, or kernels whose work
+  // items hold many centres (the centre-per-lane scans: a warp takes four cell
+  // blocks of about a warp of centres at once) run partly idle and rank below
+  // the per-centre scan although they win on the whole cloud: at least 8192
+  // centres per SM (four work items for each of 64 warps).
+  sample = std::max<uint32_t>(sample, (uint32_t)ctx->sm_count * 8192u);
   const float R = ctx->tab.rmax;
   const float ratios[] = {2.0f, 3.0f, 4.0f, 5.0f};
   auto lanes_code = [](uint32_t bx, uint32_t by, uint32_t bz) {

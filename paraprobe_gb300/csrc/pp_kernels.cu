@@ -3119,10 +3119,13 @@ int launch_lanes_knn(const ScanArgs& a, bool disjoint_sets, int sm_count, size_t
     return -3;
   const size_t smem = lanes_knn_smem(a);
   if (smem_used) *smem_used = smem;
-  if (smem > 110 * 1024) return -3;  // at least two blocks of 8 warps per SM, or the per-centre scan
+  // lists of many sets or large k (e.g. 8 sets of k = 20: 20.6 KB a warp)
+  // leave room for one block of 8 warps per SM
+  if (smem > 200 * 1024) return -3;
   auto kern = a.kmax <= 8    ? k_lanes_knn<8>
               : a.kmax <= 10 ? k_lanes_knn<10>
               : a.kmax <= 16 ? k_lanes_knn<16>
+              : a.kmax <= 20 ? k_lanes_knn<20>
                              : k_lanes_knn<0>;
   if (!allow_dynamic_smem((const void*)kern, smem))
     return -1;
