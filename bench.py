@@ -482,6 +482,9 @@ def run_gpu(args):
             line["batched"] = batched_leg(ctx, torch, stream)
     if not args.no_served:
         line["served"] = served_leg(ctx)
+    if not args.no_large and args.workload != "tip150m" and world == 1:
+        del spec
+        line["large"] = large_leg(ctx, torch, stream, args)
     ctx.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -595,6 +598,61 @@ def batched_leg_large(ctx, cid, spec, trg, env, run, torch, stream, plain_pairs,
             "plain_single_query": plain, "ratio_vs_plain": (pairs / el) / plain,
             "includes": "pair-list geometry (count pass, per-chunk emit), label gathers and layouts, all "
                         "realisation passes, result fetch"}
+
+
+# ------------------------------------------------------------- the largest tip
+def large_leg(ctx, torch, stream, args):
+    """The largest single-GPU workload (tip150m: 150M ions, 8 species, 64
+    tasks, RDF + kNN k = 1..20 at R = 2.5 / 0.01 nm in one pass) on its own:
+    autotuned plain pass, timed on the resident cloud; its bins against the
+    oracle on the tip150m centre sample; then the measured labels with 32
+    label shuffles batched alongside."""
+    from paraprobe_gb300 import native as N
+    spec, trg, env, runs, cfg = workload("tip150m")
+    r = runs[0]
+    n = spec.xyz.shape[0]
+    sh = stream.cuda_stream
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks(trg, env)
+    ctx.hist(*r["hist"])
+    ratio, tile = ctx.autotune(cid, r["flags"], r["k"], sample=200000)
+    for _ in range(2):
+        ctx.run(cid, r["flags"], r["k"], stream=sh)
+        ctx.fetch()
+    steps = 3
+    ms, kms = [], []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.run(cid, r["flags"], r["k"], stream=sh)
+        e1.record(stream)
+        ctx.fetch()
+        ms.append(e0.elapsed_time(e1))
+        kms.append(ctx.last_kernel_ms())
+    pairs = ctx.stats()["pairs"]
+    kernel = ctx.last_kernel()
+    peak, kind = peaks()
+    t = statistics.mean(ms) / 1e3
+    out = {"workload": cfg["workload"], "ions": n, "value": pairs / t, "unit": UNIT, "ms_per_pass": round(t * 1e3, 2),
+           "pairs": int(pairs), "kernel": kernel, "kernel_ms": round(statistics.mean(kms), 2),
+           "roofline": {"achieved": round(BYTES_PER_PAIR * pairs / t / 1e9, 1), "peak": peak, "peak_kind": kind,
+                        "frac": round(BYTES_PER_PAIR * pairs / t / 1e9 / peak, 4)},
+           "tuning": {"cell_edge_nm": round(cfg["R_nm"] / ratio, 4), "tile": tile}}
+    if not args.no_cpu_baseline:
+        cpu_rec, cpu_bins = cpu_leg_subprocess("tip150m", steps=1, warmup=0)
+        ctx.run(cid, r["flags"], r["k"], stream=sh, centre_mask=sample_mask(n, CPU_SAMPLE["tip150m"]))
+        g = ctx.fetch()
+        st = ctx.stats()
+        out["parity"] = {"against": "oracle port on the tip150m CPU sample (same centre mask, same cloud)",
+                         "sample_fraction": CPU_SAMPLE["tip150m"], "centres": st["centres"], "pairs": st["pairs"],
+                         "bins": int(g.size), "kernel": ctx.last_kernel(),
+                         "bins_identical": bool(g.shape == cpu_bins[0].shape and np.array_equal(g, cpu_bins[0]))}
+        out["cpu_baseline"] = cpu_rec
+    if not args.no_batched:
+        out["batched"] = batched_leg_large(ctx, cid, spec, trg, env, r, torch, stream, pairs, ms)
+    ctx.free(cid)
+    return out
 
 
 # ------------------------------------------------------------- served queries
@@ -714,6 +772,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched realisation leg")
     ap.add_argument("--no-served", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-large", action="store_true", help="skip the 150M-ion tip leg")
     args = ap.parse_args()
     if args.cpu_leg:
         cpu_leg_main(args)

@@ -327,8 +327,10 @@ int pp_run_tests(pp_ctx* ctx, uint64_t* tests);
 
 /* Prepare a cloud for queries with r_lo <= rmax <= r_hi (r_hi <= 6 r_lo):
  * builds its cell grid with edge r_lo, the hull lists for R' up to
- * max(r_hi, carve radius) and the cached ion2surf for R' = max(r_lo, carve).
- * Required before a cloud is served. */
+ * max(r_hi, carve radius) and the cached ion2surf for R' = max(r_lo, carve);
+ * unless the cloud was tuned, passes of dense centres then take the
+ * centre-per-lane scans at a 4 x 2 x 2 cell block.  Required before a cloud
+ * is served. */
 int pp_cloud_prepare(pp_ctx* ctx, int cloud, float r_lo, float r_hi);
 
 /* ---- serving loop (no counterpart in the reference, which runs one task per
@@ -342,7 +344,10 @@ int pp_cloud_prepare(pp_ctx* ctx, int cloud, float r_lo, float r_hi);
  * its own radius, hull-distance test, histogram bins, tasks and kNN orders --
  * so queries that arrive while others run join the next pass on their cloud.
  * Each query's bins, pairs and centres are those pp_run gives it alone.
- * Queries with PP_CNTNB, PP_NPCORR or k > 32 run alone on the plain path. */
+ * Queries whose centre types are dense (at least 0.35 target ions per
+ * non-empty cell) run alone on the plain path, whose centre-per-lane scans
+ * (pp_cloud_prepare sets their cell block) are faster than a shared walk for
+ * them; so do queries with PP_CNTNB, PP_NPCORR or k > 32. */
 typedef struct pp_server pp_server;
 /* `slots` worker threads, each with its own stream and run buffers;
  * `budget_bytes` caps the estimated device memory of admitted queries. */

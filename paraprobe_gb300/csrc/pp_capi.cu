@@ -83,6 +83,10 @@ struct Cloud {
   // (0 = the defaults below)
   uint32_t lanes_bx = 0, lanes_by = 0, lanes_bz = 0;
   uint64_t occupied = 0;  // non-empty cells of the grid
+  // the cell block was set by pp_cloud_prepare rather than by tuning: passes
+  // take it only where centres are dense enough to fill a warp (default_block)
+  bool lanes_auto = false;
+  std::vector<uint64_t> type_count;  // ions of each type (pp_cloud_prepare)
   Hull hull;
   DevBuf user_surf;             // input order, when given
   bool has_user_surf = false;
@@ -1329,9 +1333,15 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   a.mode = 0;
   a.sample_stride = stride;
   a.rdf_in_smem = ((a.flags & PP_RDF) && (size_t)P.nC * P.nE * P.H * 4 <= 96 * 1024) ? 1 : 0;
+  // a cell block set by tuning applies to every pass; one set by
+  // pp_cloud_prepare only to passes of dense centres
+  int dbx = 0, dby = 0, dbz = 0;
+  const bool block_ok = cl->lanes_bx != 0 &&
+                        (!cl->lanes_auto || default_block(*cl, (uint64_t)ncent * std::max<uint32_t>(stride, 1),
+                                                          &dbx, &dby, &dbz));
   // RDF / RIPK and kNN in one pass on a cloud tuned to a centre-per-lane cell
   // block: two centre-per-lane passes, RDF / RIPK then kNN
-  const bool split = P.kr > 0 && (a.flags & PP_RDF) && cl->lanes_bx && !ctx->no_lanes &&
+  const bool split = P.kr > 0 && (a.flags & PP_RDF) && block_ok && !ctx->no_lanes &&
                      !(flags & (PP_CNTNB | PP_NPCORR));
   // RDF / RIPK alone: each pair of two centres is computed once and credited
   // to both (the counts are the same as the per-centre ball scan's)
@@ -1353,7 +1363,7 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
     // centre-per-lane scans: cell block and its stencil rows
     bool lanes = rows_fit && !ctx->no_lanes && !(flags & (PP_CNTNB | PP_NPCORR)) &&
                  (split || !(P.kr > 0 && (a.flags & PP_RDF)));
-    if (lanes && cl->lanes_bx) {
+    if (lanes && block_ok) {
       a.bx = (int)cl->lanes_bx;
       a.by = (int)std::max<uint32_t>(cl->lanes_by, 1);
       a.bz = (int)std::max<uint32_t>(cl->lanes_bz, 1);
@@ -1663,6 +1673,8 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
                                  (16u << 16) | 32u};
   const float keep_ratio = cl->cell_ratio;
   const uint32_t keep[5] = {cl->tile, cl->brick, cl->lanes_bx, cl->lanes_by, cl->lanes_bz};
+  const bool keep_auto = cl->lanes_auto;
+  cl->lanes_auto = false;  // the trials' cell blocks apply as tuned
   auto apply = [&](uint32_t t) {
     if (t >= 65536u && (t & 0xffffu) == PP_TILE_LANES) {
       cl->lanes_bx = (t >> 16) & 0xffu;
@@ -1725,11 +1737,13 @@ int pp_autotune(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_list, 
   }
   if (rc != PP_OK) {
     cl->cell_ratio = keep_ratio;
+    cl->lanes_auto = keep_auto;
     build_grid(ctx, *cl, R, 0);
     return rc;
   }
   cl->cell_ratio = bestr;
   if (bestt) apply(bestt);
+  else cl->lanes_auto = keep_auto;
   if ((rc = build_grid(ctx, *cl, R, 0))) return rc;
   ctx->res.valid = false;
   if (best_ratio) *best_ratio = bestr;
@@ -1850,6 +1864,7 @@ int pp_cloud_tuning(pp_ctx* ctx, int cloud, float cell_ratio, uint32_t tile) {
     cl->lanes_bx = bx;
     cl->lanes_by = by ? by : 1;
     cl->lanes_bz = bz ? bz : 1;
+    cl->lanes_auto = false;
   } else if (tile >= 65536u) {
     const uint32_t bx = tile >> 16, cap = tile & 0xffffu;
     if (bx < 1 || bx > 64 || cap < 1 || cap > 32)
@@ -2489,6 +2504,7 @@ struct ServerRequest {
   int rc = PP_OK;
   std::string err;
   std::vector<uint64_t> bins;
+  bool dense = false;       // centres dense enough for the centre-per-lane scans (runs alone)
   uint64_t pairs = 0, centres = 0;
   double t_submit = 0, t_end = 0;
   bool done = false;
@@ -2877,6 +2893,19 @@ int pp_cloud_prepare(pp_ctx* ctx, int cloud, float r_lo, float r_hi) {
   }
   const float* surf = nullptr;
   if ((rc = ensure_surface(ctx, *cl, r_lo, 0, &surf))) return rc;
+  // passes of dense centres take the centre-per-lane scans at a 4 x 2 x 2 cell
+  // block (cells of r_lo), unless the cloud was tuned already
+  if (!cl->lanes_bx) {
+    cl->lanes_bx = 4;
+    cl->lanes_by = 2;
+    cl->lanes_bz = 2;
+    cl->lanes_auto = true;
+  }
+  // ions per type: the serving scheduler's dense / sparse split
+  std::vector<uint8_t> lab(cl->n);
+  CK(cudaMemcpy(lab.data(), cl->label.p, cl->n, cudaMemcpyDeviceToHost));
+  cl->type_count.assign(256, 0);
+  for (uint8_t t : lab) cl->type_count[t]++;
   CK(cudaDeviceSynchronize());
   return PP_OK;
 }
@@ -2939,8 +2968,22 @@ int pp_server_submit(pp_server* S, int cloud, uint32_t flags, float rmin, float 
   // own buffers the scheduler counts once per pass); a lone query its centre
   // list, flags, scan scratch, centre flags, private ion2surf, per-cell
   // prefix and result cores
+  // dense centres (at least 0.35 ions of a target type per non-empty cell,
+  // the rule of default_block): the plain path's centre-per-lane scans beat a
+  // merged pass for such a query, so it runs alone
+  {
+    uint64_t cand = 0;
+    if (!cl->type_count.empty())
+      for (int ty = 0; ty < 256; ++ty) {
+        bool t = false;
+        for (int k = 0; k < ntasks; ++k) t |= has_type(&trg_mask[8 * k], ty);
+        if (t) cand += cl->type_count[ty];
+      }
+    q->dense = cl->occupied && (double)cand >= 0.35 * (double)cl->occupied;
+  }
   const double nb = (rincr > 0.f) ? std::floor(((double)rmax - (double)rmin) / (double)rincr) + 2.0 : 1.0;
   const double cores = 8.0 * nb * (double)ntasks * (3.0 + (double)nk);
+  q->mergeable = q->mergeable && !q->dense;
   q->footprint = q->mergeable ? (uint64_t)cores + 4096
                               : (uint64_t)(13.0 * (double)cl->n + 4.0 * (double)cl->g.ncells + cores);
   q->t_submit = now_ms();
