@@ -247,6 +247,10 @@ int pp_fetch_npcorr(pp_ctx* ctx, uint32_t* counts, uint64_t cap, uint64_t* edge)
  *   "lanes"             RDF/RIPK-only passes take the centre-per-lane brick
  *                       scan (default 1); 0 = the per-centre or brick scan.
  *                       Results are identical either way.
+ *   "uniform_sets"      the kNN centre-per-lane scan stages one set row per ion
+ *                       when every centre type maps types to sets alike
+ *                       (default 1); 0 decodes the set per centre slot.
+ *                       Results are identical either way.
  *   "npcorr_order"      SpatStatKNNOrder - 1 for PP_NPCORR (0..31, default 0).
  *   "server_batch"      most queries per merged serving pass (1..32, default
  *                       32; 1 = every query alone), read by pp_server_create.

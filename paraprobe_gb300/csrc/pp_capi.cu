@@ -197,6 +197,7 @@ struct pp_ctx {
   uint64_t grid_counter = 1;
   bool no_sym = false;  // testing hook: force the one-sided scan
   bool no_lanes = false;  // option "lanes" = 0: RDF passes take the per-centre or brick scan
+  bool no_uniform = false;  // option "uniform_sets" = 0: the kNN lane scan decodes sets per centre slot
   DevBuf brows;           // stencil rows of a cell block, nearest first (centre-per-lane scan)
   int brows_key[3] = {-1, -1, -1};
   pp_ctx* parent = nullptr;     // serving workers share the parent's clouds
@@ -739,6 +740,9 @@ void fill_scan_common(pp::ScanArgs& a, const Cloud& cl, const RunPlan& P, const 
   a.disjoint = (P.disjoint && (size_t)8 * std::max(P.emax, 1) * (P.kr * 32 + 1) * 4 <= 64 * 1024) ? 1 : 0;
   a.emax = std::max(P.emax, 1);
   a.setidx = D.setidx;
+  a.uniform_sets = 1;
+  for (int c = 1; c < P.nC && a.uniform_sets; ++c)
+    if (std::memcmp(&P.setidx[(size_t)c * 256], &P.setidx[0], 256) != 0) a.uniform_sets = 0;
   a.tile = std::max<uint32_t>(cl.tile, 1);
   a.rowtab = D.rowtab;
   a.sym = 0;
@@ -1314,6 +1318,7 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   CK(cudaMemsetAsync(ctx->work.p, 0, 32, s));
   pp::ScanArgs a{};
   fill_scan_common(a, *cl, P, D, ctx->tab);
+  if (ctx->no_uniform) a.uniform_sets = 0;
   a.labels = labels;
   a.centres = ctx->centres.as<uint32_t>();
   a.ncentres = ncent;
@@ -1829,6 +1834,7 @@ int pp_set_option(pp_ctx* ctx, const char* name, int value) {
   if (!ctx || !name) return PP_ERR_INVALID;
   if (std::strcmp(name, "symmetric") == 0) { ctx->no_sym = (value == 0); return PP_OK; }
   if (std::strcmp(name, "lanes") == 0) { ctx->no_lanes = (value == 0); return PP_OK; }
+  if (std::strcmp(name, "uniform_sets") == 0) { ctx->no_uniform = (value == 0); return PP_OK; }
   if (std::strcmp(name, "npcorr_order") == 0) {
     if (value < 0 || value > 31) return fail(ctx, PP_ERR_INVALID, "npcorr_order must be in [0, 31]");
     ctx->npc_order = (uint32_t)value;

@@ -85,6 +85,7 @@ struct ScanArgs {
   int disjoint;                  // every type is in at most one env set per centre slot
   int emax;                      // most env sets of one centre slot (shared kNN lists)
   const int8_t* setidx;          // [nC][256] that set's local index or -1 (disjoint only)
+  int uniform_sets;              // every centre slot's setidx row is the same
   uint32_t tile;                 // centres per block work item
   const int8_t* rowtab;          // stencil row offsets in distance order (row_table_offset)
   int sym;                       // symmetric pass: pairs of two centres are taken once

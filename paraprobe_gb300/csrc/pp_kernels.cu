@@ -2040,7 +2040,10 @@ constexpr int kLanesKnnWarps = 8;
 
 // KB > 0: K <= KB, and an insertion loads the whole list at once (KB
 // independent shared loads) instead of walking it; KB = 0: any K.
-template <int KB>
+// UNI: every centre slot maps a type to the same local environment set (the
+// usual all-pairs task lists); a staged ion then carries that set's list row
+// as a ready float offset instead of one 4-bit set index per centre slot.
+template <int KB, bool UNI>
 __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a) {
   constexpr int NW = kLanesKnnWarps;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -2059,9 +2062,14 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
   for (int i = threadIdx.x; i < 256; i += blockDim.x) {
     scs[i] = a.cslot_of[i];
     uint32_t key = 0;
-    for (int c = 0; c < a.nC; ++c) {
-      const int si = a.setidx[c * 256 + i];
-      key |= (uint32_t)(si < 0 ? EM : si) << (4 * c);
+    if (UNI) {
+      const int si = a.nC > 0 ? a.setidx[i] : -1;
+      key = (uint32_t)((si < 0 ? EM : si) * K * 32);
+    } else {
+      for (int c = 0; c < a.nC; ++c) {
+        const int si = a.setidx[c * 256 + i];
+        key |= (uint32_t)(si < 0 ? EM : si) << (4 * c);
+      }
     }
     skey[i] = key;
   }
@@ -2103,12 +2111,14 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     inb = 0;
     return cp;
   };
+  // list row (float offset) of a staged key's environment set for this lane's centre type
+  auto row_of = [&](uint32_t w) -> uint32_t { return UNI ? w : ((w >> sh) & 15u) * K * 32; };
   auto accept = [&](int, float d2, uint32_t w) {
-    // set of the staged ion for this lane's centre type (EM = none), then its K-th value
-    return d2 < L[((w >> sh) & 15u) * K * 32];
+    // the set's K-th value (the -inf row for ions in no set)
+    return d2 < L[row_of(w)];
   };
-  auto insert = [&](int p, float d2) {
-    float* Lp = L + p * K * 32;  // row s holds rank K - 1 - s
+  auto insert = [&](uint32_t row, float d2) {
+    float* Lp = L + row;  // row s holds rank K - 1 - s
     if (!(d2 < Lp[0])) return;
     if constexpr (KB > 0) {
       // the sorted list with d2 in and its largest value out, as a min/max
@@ -2143,7 +2153,7 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
       if (ccode[j] == me) continue;  // the centre itself
       const float4 q = staged_ion(cand, j);
       const float d2 = dist2(cx, cy, cz, q.x, q.y, q.z);
-      insert((int)((__float_as_uint(q.w) >> sh) & 15u), d2);
+      insert(row_of(__float_as_uint(q.w)), d2);
     }
   };
   auto finish = [&](uint32_t live) {
@@ -3122,11 +3132,12 @@ int launch_lanes_knn(const ScanArgs& a, bool disjoint_sets, int sm_count, size_t
   // lists of many sets or large k (e.g. 8 sets of k = 20: 20.6 KB a warp)
   // leave room for one block of 8 warps per SM
   if (smem > 200 * 1024) return -3;
-  auto kern = a.kmax <= 8    ? k_lanes_knn<8>
-              : a.kmax <= 10 ? k_lanes_knn<10>
-              : a.kmax <= 16 ? k_lanes_knn<16>
-              : a.kmax <= 20 ? k_lanes_knn<20>
-                             : k_lanes_knn<0>;
+  const bool uni = a.uniform_sets != 0;
+  auto kern = a.kmax <= 8    ? (uni ? k_lanes_knn<8, true> : k_lanes_knn<8, false>)
+              : a.kmax <= 10 ? (uni ? k_lanes_knn<10, true> : k_lanes_knn<10, false>)
+              : a.kmax <= 16 ? (uni ? k_lanes_knn<16, true> : k_lanes_knn<16, false>)
+              : a.kmax <= 20 ? (uni ? k_lanes_knn<20, true> : k_lanes_knn<20, false>)
+                             : (uni ? k_lanes_knn<0, true> : k_lanes_knn<0, false>);
   if (!allow_dynamic_smem((const void*)kern, smem))
     return -1;
   int per_sm = 0;
