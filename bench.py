@@ -80,6 +80,22 @@ def workload(name):
                            "5000 clusters, 64 pair tasks; one pass RDF + kNN k=1..20, R=2.5/0.01, hull-distance "
                            "exclusion",
                "ions": n, "tasks": 64, "R_nm": 2.5}
+    elif name == "tip8sp10m":
+        # a 10M-ion cut of the 150M-ion tip's kind (same apex, angle, density,
+        # cluster density, species and analyses), for profiling its kernels
+        n = 10_000_000
+        rho = 150_000_000 / synth.cone_volume(50.0, 12.0, 400.0)
+        length = synth.cone_length_for(n, rho, 50.0, 12.0)
+        spec = synth.cone_specimen(n=n, r_apex=50.0, half_angle_deg=12.0, length=length, n_clusters=333,
+                                   sigma=1.5, members=50, cluster_p=(0.7, 0.3),
+                                   iid=(0.02, 0.01, 0.005, 0.005, 0.002), nspecies=8, seed=20261208)
+        types = list(range(1, 9))
+        trg = [[a] for a in types for b in types]
+        env = [[b] for a in types for b in types]
+        runs = [dict(flags=1 | 8, hist=(0.0, 0.01, 2.5), k=list(range(20, 0, -1)))]
+        cfg = {"workload": f"tip8sp10m: 10M-ion cut (L {length:.1f} nm) of the 150M-ion tip's kind (r_apex 50 nm, "
+                           "12 deg), 8 species, 64 pair tasks; one pass RDF + kNN k=1..20, R=2.5/0.01",
+               "ions": n, "tasks": 64, "R_nm": 2.5}
     elif name == "cyl1m":
         spec = synth.cylinder_specimen(n=1_000_000, radius=10.0, height=63.66, fractions=(0.90, 0.08, 0.02),
                                        seed=20261204)
@@ -211,7 +227,7 @@ def reduce_max(pg, x):
 # reference arm): the ions whose key (uniform on [0, 1), numpy seed 7) is
 # below the workload's fraction may be centres; the whole cloud stays the
 # environment.  The same mask drives the GPU parity check of the GPU arm.
-CPU_SAMPLE = {"tip20m": 0.02, "tip10m": 0.04, "cyl1m": 1.0, "tip150m": 0.002}
+CPU_SAMPLE = {"tip20m": 0.02, "tip10m": 0.04, "cyl1m": 1.0, "tip150m": 0.002, "tip8sp10m": 0.02}
 
 
 def sample_mask(n, frac):
@@ -321,7 +337,13 @@ def run_gpu(args):
     heavy = runs[-1]
     ctx.tasks(trg, env)
     ctx.hist(*heavy["hist"])
-    ratio, tile = ctx.autotune(cid, heavy["flags"], heavy["k"], sample=200000)
+    if args.tuning:
+        # fixed tuning (ratio:tile code), e.g. for a profiler run with a
+        # predictable launch sequence
+        ratio, tile = float(args.tuning.split(":")[0]), int(args.tuning.split(":")[1], 0)
+        ctx.tuning(cid, ratio, tile)
+    else:
+        ratio, tile = ctx.autotune(cid, heavy["flags"], heavy["k"], sample=200000)
 
     pass_kernel = ["" for _ in runs]
     pass_tests = [0 for _ in runs]
@@ -766,7 +788,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="tip20m", choices=["tip20m", "tip10m", "cyl1m", "tip150m"])
+    ap.add_argument("--workload", default="tip20m", choices=["tip20m", "tip10m", "cyl1m", "tip150m", "tip8sp10m"])
+    ap.add_argument("--tuning", default=None, help="RATIO:TILE -- skip the autotuner, use this cell ratio and tile code")
     ap.add_argument("--cpu-leg", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--cpu-out", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--no-cpu-baseline", action="store_true")

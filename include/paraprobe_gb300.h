@@ -251,6 +251,10 @@ int pp_fetch_npcorr(pp_ctx* ctx, uint32_t* counts, uint64_t cap, uint64_t* edge)
  *                       when every centre type maps types to sets alike
  *                       (default 1); 0 decodes the set per centre slot.
  *                       Results are identical either way.
+ *   "knn_lists"         lists of the kNN centre-per-lane scan: 0 = distances
+ *                       while they fit two blocks per SM, bin categories
+ *                       beyond (default); 1 = distances; 2 = categories.
+ *                       Results are identical either way.
  *   "npcorr_order"      SpatStatKNNOrder - 1 for PP_NPCORR (0..31, default 0).
  *   "server_batch"      most queries per merged serving pass (1..32, default
  *                       32; 1 = every query alone), read by pp_server_create.

@@ -198,6 +198,7 @@ struct pp_ctx {
   bool no_sym = false;  // testing hook: force the one-sided scan
   bool no_lanes = false;  // option "lanes" = 0: RDF passes take the per-centre or brick scan
   bool no_uniform = false;  // option "uniform_sets" = 0: the kNN lane scan decodes sets per centre slot
+  int knn_lists = 0;        // option "knn_lists": 0 automatic, 1 d^2 lists, 2 category lists
   DevBuf brows;           // stencil rows of a cell block, nearest first (centre-per-lane scan)
   int brows_key[3] = {-1, -1, -1};
   pp_ctx* parent = nullptr;     // serving workers share the parent's clouds
@@ -1319,6 +1320,7 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   pp::ScanArgs a{};
   fill_scan_common(a, *cl, P, D, ctx->tab);
   if (ctx->no_uniform) a.uniform_sets = 0;
+  a.lists_mode = ctx->knn_lists;
   a.labels = labels;
   a.centres = ctx->centres.as<uint32_t>();
   a.ncentres = ncent;
@@ -1835,6 +1837,11 @@ int pp_set_option(pp_ctx* ctx, const char* name, int value) {
   if (std::strcmp(name, "symmetric") == 0) { ctx->no_sym = (value == 0); return PP_OK; }
   if (std::strcmp(name, "lanes") == 0) { ctx->no_lanes = (value == 0); return PP_OK; }
   if (std::strcmp(name, "uniform_sets") == 0) { ctx->no_uniform = (value == 0); return PP_OK; }
+  if (std::strcmp(name, "knn_lists") == 0) {
+    if (value < 0 || value > 2) return fail(ctx, PP_ERR_INVALID, "knn_lists must be 0, 1 or 2");
+    ctx->knn_lists = value;
+    return PP_OK;
+  }
   if (std::strcmp(name, "npcorr_order") == 0) {
     if (value < 0 || value > 31) return fail(ctx, PP_ERR_INVALID, "npcorr_order must be in [0, 31]");
     ctx->npc_order = (uint32_t)value;

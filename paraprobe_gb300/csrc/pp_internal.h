@@ -86,6 +86,7 @@ struct ScanArgs {
   int emax;                      // most env sets of one centre slot (shared kNN lists)
   const int8_t* setidx;          // [nC][256] that set's local index or -1 (disjoint only)
   int uniform_sets;              // every centre slot's setidx row is the same
+  int lists_mode;                // kNN lane scan lists: 0 = d^2, categories when large; 1 = d^2; 2 = categories
   uint32_t tile;                 // centres per block work item
   const int8_t* rowtab;          // stencil row offsets in distance order (row_table_offset)
   int sym;                       // symmetric pass: pairs of two centres are taken once

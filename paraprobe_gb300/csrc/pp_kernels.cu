@@ -2042,21 +2042,36 @@ constexpr int kLanesKnnWarps = 8;
 // independent shared loads) instead of walking it; KB = 0: any K.
 // UNI: every centre slot maps a type to the same local environment set (the
 // usual all-pairs task lists); a staged ion then carries that set's list row
-// as a ready float offset instead of one 4-bit set index per centre slot.
-template <int KB, bool UNI>
+// as a ready offset instead of one 4-bit set index per centre slot.
+// CAT: the lists hold bin categories (uint16), not d^2 -- half the shared
+// memory, for many sets of large k (8 sets of k = 20 fit two blocks of 8
+// warps per SM instead of one).  The k-th smallest category is the category
+// of the k-th smallest d^2 (categories rise with d^2), which is all the
+// histogram needs.  Each set keeps, beside its categories, the float test
+// threshold: the smallest d^2 of its K-th category (just above R^2 while the
+// list is not full); an ion beats it exactly when its category is below the
+// K-th one, so the test stays one float compare; a taken ion's category is
+// looked up once, at insertion, and the binning at the end needs none.
+template <int KB, bool UNI, bool CAT>
 __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a) {
   constexpr int NW = kLanesKnnWarps;
+  constexpr uint32_t CNONE = 0xffffu;  // CAT: an empty list place (above every category)
   extern __shared__ __align__(16) unsigned char smem[];
   const int H = a.H, K = a.kmax, EM = a.emax;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // per warp: float rows -- the lists (EM * K rows) or, with CAT, one threshold
+  // row per set -- then the row of "no set"; with CAT the category rows after
+  const int frows = CAT ? EM + 1 : EM * K + 1;
   unsigned char* sp = smem;
   float4* candA = (float4*)sp; sp += NW * 32 * 16;
   uint32_t* ccodeA = (uint32_t*)sp; sp += NW * 32 * 4;
-  float* listA = (float*)sp; sp += (size_t)NW * (EM * K + 1) * 32 * 4;
+  float* listA = (float*)sp; sp += (size_t)NW * frows * 32 * 4;
+  uint16_t* catA = (uint16_t*)sp; sp += CAT ? (((size_t)NW * EM * K * 32 * 2 + 15) & ~size_t(15)) : 0;
   float* sT = (float*)sp; sp += ((H + 3) & ~3) * 4;
   uint16_t* slut = (uint16_t*)sp; sp += ((a.lut_n + 7) & ~7) * 2;
   int8_t* scs = (int8_t*)sp; sp += 256;
   uint32_t* skey = (uint32_t*)sp;  // [256] per type: its environment set (EM: none) for every centre slot, 4 bits each
+  const uint32_t RSTRIDE = CAT ? 32u : (uint32_t)K * 32u;  // float rows between sets
   for (int i = threadIdx.x; i < H; i += blockDim.x) sT[i] = a.cat_T[i];
   for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) slut[i] = a.cat_lut[i];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) {
@@ -2064,7 +2079,7 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     uint32_t key = 0;
     if (UNI) {
       const int si = a.nC > 0 ? a.setidx[i] : -1;
-      key = (uint32_t)((si < 0 ? EM : si) * K * 32);
+      key = (uint32_t)(si < 0 ? EM : si) * RSTRIDE;
     } else {
       for (int c = 0; c < a.nC; ++c) {
         const int si = a.setidx[c * 256 + i];
@@ -2077,8 +2092,11 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
 
   float4* cand = candA + warp * 32;
   uint32_t* ccode = ccodeA + warp * 32;
-  float* L = listA + (size_t)warp * (EM * K + 1) * 32 + lane;  // set p, rank r at L[(p * K + K - 1 - r) * 32]
-  L[EM * K * 32] = -kInf();                                     // the row of "no set": nothing beats it
+  // set p, rank r at L[(p * K + K - 1 - r) * 32]; with CAT, set p's threshold
+  // at L[p * 32] and its rank r at C[(p * K + K - 1 - r) * 32]
+  float* L = listA + (size_t)warp * frows * 32 + lane;
+  uint16_t* C = catA + (size_t)warp * EM * K * 32 + lane;
+  L[(uint32_t)EM * RSTRIDE] = -kInf();  // the row of "no set": nothing beats it
   const float RUP = (a.R2 >= 0.f && a.R2 < kInf()) ? __uint_as_float(__float_as_uint(a.R2) + 1u) : kInf();
   unsigned long long pairs_lane = 0, centres = 0;
   uint32_t inb = 0;
@@ -2106,21 +2124,52 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     }
     nset = cs >= 0 ? a.nsets[cs] : 0;
     sh = 4 * (cs < 0 ? 0 : cs);
-    for (int e = 0; e < nset * K; ++e) L[e * 32] = RUP;
+    if constexpr (CAT) {
+      for (int p = 0; p < nset; ++p) L[p * 32] = RUP;
+      for (int e = 0; e < nset * K; ++e) C[e * 32] = (uint16_t)CNONE;
+    } else {
+      for (int e = 0; e < nset * K; ++e) L[e * 32] = RUP;
+    }
     me = cp.x != kInf() ? self : 0xffffffffu;
     inb = 0;
     return cp;
   };
-  // list row (float offset) of a staged key's environment set for this lane's centre type
-  auto row_of = [&](uint32_t w) -> uint32_t { return UNI ? w : ((w >> sh) & 15u) * K * 32; };
+  // float row (offset) of a staged key's environment set for this lane's centre type
+  auto row_of = [&](uint32_t w) -> uint32_t { return UNI ? w : ((w >> sh) & 15u) * RSTRIDE; };
   auto accept = [&](int, float d2, uint32_t w) {
-    // the set's K-th value (the -inf row for ions in no set)
+    // the set's K-th value or threshold (the -inf row for ions in no set)
     return d2 < L[row_of(w)];
   };
   auto insert = [&](uint32_t row, float d2) {
     float* Lp = L + row;  // row s holds rank K - 1 - s
     if (!(d2 < Lp[0])) return;
-    if constexpr (KB > 0) {
+    if constexpr (CAT) {
+      const int c = category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+      uint16_t* Cp = C + (row / 32u) * (uint32_t)K * 32u;
+      if constexpr (KB > 0) {
+        int v[KB];
+#pragma unroll
+        for (int s = 0; s < KB; ++s) v[s] = (s < K) ? (int)Cp[s * 32] : -1;
+#pragma unroll
+        for (int s = 0; s < KB; ++s)
+          if (s < K) v[s] = min(v[s], max(s + 1 < KB ? v[s + 1 < KB ? s + 1 : s] : -1, c));
+#pragma unroll
+        for (int s = 0; s < KB; ++s)
+          if (s < K) Cp[s * 32] = (uint16_t)v[s];
+        Lp[0] = (v[0] == (int)CNONE) ? RUP : sT[v[0]];
+      } else {
+        int r = K - 1;
+        while (r > 0) {
+          const int v = Cp[(K - r) * 32];  // rank r - 1
+          if (!(v > c)) break;
+          Cp[(K - 1 - r) * 32] = (uint16_t)v;
+          --r;
+        }
+        Cp[(K - 1 - r) * 32] = (uint16_t)c;
+        const int kth = Cp[0];
+        Lp[0] = (kth == (int)CNONE) ? RUP : sT[kth];
+      }
+    } else if constexpr (KB > 0) {
       // the sorted list with d2 in and its largest value out, as a min/max
       // network over ranks: new[r] = min(v[r], max(v[r - 1], d2)), new[0] =
       // min(v[0], d2); rank r - 1 is the next row
@@ -2160,12 +2209,18 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     if (lane == 0) centres += (unsigned long long)__popc(live);
     // every live centre met itself once in the in-ball count (d^2 = 0)
     pairs_lane += inb - (me != 0xffffffffu ? 1u : 0u);
-    // the k-th smallest d^2 of each set -> its bin (or the miss bin)
+    // the k-th smallest d^2 (category) of each set -> its bin (or the miss bin)
     for (int p = 0; p < nset; ++p) {
       const int Sg = a.set_list[cs * 32 + p];
       for (int kk = 0; kk < a.nkI; ++kk) {
-        const float v = L[(p * K + K - a.kvals[kk]) * 32];
-        const int cat = (v == RUP) ? a.cat_miss : category_lut(v, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+        int cat;
+        if constexpr (CAT) {
+          const int v = C[(p * K + K - a.kvals[kk]) * 32];
+          cat = (v == (int)CNONE) ? a.cat_miss : v;
+        } else {
+          const float v = L[(p * K + K - a.kvals[kk]) * 32];
+          cat = (v == RUP) ? a.cat_miss : category_lut(v, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+        }
         if (cat >= 0) atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
       }
     }
@@ -3117,27 +3172,40 @@ int launch_lanes(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cud
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-size_t lanes_knn_smem(const ScanArgs& a) {
+size_t lanes_knn_smem(const ScanArgs& a, bool cat) {
   constexpr int NW = kLanesKnnWarps;
-  return NW * 32 * 16 + NW * 32 * 4 + (size_t)NW * ((a.emax > 1 ? a.emax : 1) * a.kmax + 1) * 32 * 4 +
-         (size_t)((a.H + 3) & ~3) * 4 + (size_t)((a.lut_n + 7) & ~7) * 2 + 256 + 256 * 4;
+  const size_t em = a.emax > 1 ? a.emax : 1;
+  const size_t frows = cat ? em + 1 : em * a.kmax + 1;
+  const size_t crows = cat ? (((size_t)NW * em * a.kmax * 32 * 2 + 15) & ~size_t(15)) : 0;
+  return NW * 32 * 16 + NW * 32 * 4 + (size_t)NW * frows * 32 * 4 + crows + (size_t)((a.H + 3) & ~3) * 4 +
+         (size_t)((a.lut_n + 7) & ~7) * 2 + 256 + 256 * 4;
 }
 
 int launch_lanes_knn(const ScanArgs& a, bool disjoint_sets, int sm_count, size_t* smem_used, cudaStream_t s) {
   if (a.mode != 0 || (a.flags & (PP_CNTNB | PP_RDF)) || !disjoint_sets || a.kmax < 1 || a.kmax > 64 || a.bx < 1 ||
       a.by < 1 || a.bz < 1 || !a.brows || a.nC > 8 || a.emax > 15)  // sets packed 4 bits per centre slot
     return -3;
-  const size_t smem = lanes_knn_smem(a);
+  // d^2 lists while they leave room for two blocks of 8 warps per SM;
+  // category lists beyond that (e.g. 8 sets of k = 20: 20.6 KB a warp as d^2,
+  // 11.4 KB as categories); one block per SM for the largest
+  bool cat = a.lists_mode == 2;
+  size_t smem = lanes_knn_smem(a, cat);
+  if (!cat && a.lists_mode == 0 && smem > 110 * 1024 && lanes_knn_smem(a, true) < smem) {
+    cat = true;
+    smem = lanes_knn_smem(a, true);
+  }
   if (smem_used) *smem_used = smem;
-  // lists of many sets or large k (e.g. 8 sets of k = 20: 20.6 KB a warp)
-  // leave room for one block of 8 warps per SM
-  if (smem > 200 * 1024) return -3;
+  if (smem > 200 * 1024 || (cat && a.H > 65535)) return -3;
   const bool uni = a.uniform_sets != 0;
-  auto kern = a.kmax <= 8    ? (uni ? k_lanes_knn<8, true> : k_lanes_knn<8, false>)
-              : a.kmax <= 10 ? (uni ? k_lanes_knn<10, true> : k_lanes_knn<10, false>)
-              : a.kmax <= 16 ? (uni ? k_lanes_knn<16, true> : k_lanes_knn<16, false>)
-              : a.kmax <= 20 ? (uni ? k_lanes_knn<20, true> : k_lanes_knn<20, false>)
-                             : (uni ? k_lanes_knn<0, true> : k_lanes_knn<0, false>);
+#define PP_KNN_KERN(KBV) \
+  (cat ? (uni ? k_lanes_knn<KBV, true, true> : k_lanes_knn<KBV, false, true>) \
+       : (uni ? k_lanes_knn<KBV, true, false> : k_lanes_knn<KBV, false, false>))
+  auto kern = a.kmax <= 8    ? PP_KNN_KERN(8)
+              : a.kmax <= 10 ? PP_KNN_KERN(10)
+              : a.kmax <= 16 ? PP_KNN_KERN(16)
+              : a.kmax <= 20 ? PP_KNN_KERN(20)
+                             : PP_KNN_KERN(0);
+#undef PP_KNN_KERN
   if (!allow_dynamic_smem((const void*)kern, smem))
     return -1;
   int per_sm = 0;

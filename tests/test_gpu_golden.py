@@ -56,24 +56,35 @@ def _groups(flags, ntasks, nk, H):
     return out
 
 
+@pytest.mark.parametrize("lists", [0, 2])
 @pytest.mark.parametrize("name", G.names())
-def test_gpu_lanes_match_reference(ctx, name):
+def test_gpu_lanes_match_reference(ctx, name, lists):
     """The centre-per-lane scans on the reference fixtures, forced by a cell
     block shape: the fixture's RDF/RIPK analyses as one pass and its 1NN/kNN
     analyses as another, each against the matching groups of the reference's
     bins (passes the centre-per-lane kernels cannot take run the per-centre
-    scan and must match all the same)."""
+    scan and must match all the same).  lists = 2 keeps the kNN lists as bin
+    categories instead of distances."""
     c = G.load(name)
     flags = c["flags"] & (1 | 2 | 4 | 8)
-    ntasks, nk = len(c["trg"]), len(c["k"]) if c["flags"] & 8 else 0
-    H = c["stats"]["nbins"] + 2
-    ref = {f: c["bins"][o:o + n] for f, o, n in _groups(c["flags"], ntasks, nk, H)}
     cid = ctx.upload(c["xyz"], c["labels"])
     if c["hull"].shape[0]:
         ctx.hull(cid, c["hull"], 2.0)
     ctx.tuning(cid, 4.0, ((4 | 2 << 8 | 2 << 12) << 16) | 0x100)
     ctx.tasks(c["trg"], c["env"])
     ctx.hist(c["rmin"], c["rincr"], c["rmax"])
+    ctx.set_option("knn_lists", lists)
+    try:
+        _lanes_parts(ctx, c, cid, name, flags)
+    finally:
+        ctx.set_option("knn_lists", 0)
+        ctx.free(cid)
+
+
+def _lanes_parts(ctx, c, cid, name, flags):
+    ntasks, nk = len(c["trg"]), len(c["k"]) if c["flags"] & 8 else 0
+    H = c["stats"]["nbins"] + 2
+    ref = {f: c["bins"][o:o + n] for f, o, n in _groups(c["flags"], ntasks, nk, H)}
     kernels = []
     for part in (flags & (1 | 4), flags & (2 | 8)):
         if not part:
@@ -96,6 +107,5 @@ def test_gpu_lanes_match_reference(ctx, name):
         assert st["pairs"] == c["stats"]["pairs"] and st["centres"] == c["stats"]["centres"]
         want = np.concatenate([ref[f] for f, _, _ in _groups(flags, ntasks, len(ks), H)])
         assert np.array_equal(out, want), (name, flags, kernels[-1])
-    ctx.free(cid)
     assert kernels
     print(f"{name}: {kernels}")

@@ -103,14 +103,22 @@ def test_tip20m_cut_2m_both_passes(ctx, oracle):
     for flags, hist, ks in passes:
         ctx.hist(*hist)
         ref = oracle.spatstat(spec.xyz, spec.labels, surf, *hist, flags, trg, env, ks)
-        for tuning in (None, (4.0, lanes_code(4, 2, 2)), (4.0, lanes_code(3, 2, 2))):
+        for tuning, lists, uni in ((None, 0, 1), ((4.0, lanes_code(4, 2, 2)), 0, 1), ((4.0, lanes_code(3, 2, 2)), 0, 1),
+                                   ((4.0, lanes_code(4, 2, 2)), 2, 1), ((4.0, lanes_code(4, 2, 2)), 0, 0)):
             if tuning:
                 ctx.tuning(cid, *tuning)
-            ctx.run(cid, flags, ks)
-            gpu = ctx.fetch()
+            ctx.set_option("knn_lists", lists)
+            ctx.set_option("uniform_sets", uni)
+            try:
+                ctx.run(cid, flags, ks)
+                gpu = ctx.fetch()
+            finally:
+                ctx.set_option("knn_lists", 0)
+                ctx.set_option("uniform_sets", 1)
             kernels.add(ctx.last_kernel())
             assert ctx.stats()["pairs"] == ref["pairs"], (flags, tuning)
-            assert np.array_equal(gpu, ref["bins"]), f"{flags} {tuning} {ctx.last_kernel()}: " + _diff(gpu, ref["bins"])
+            assert np.array_equal(gpu, ref["bins"]), (f"{flags} {tuning} lists {lists} uniform {uni} "
+                                                      f"{ctx.last_kernel()}: " + _diff(gpu, ref["bins"]))
     assert {"k_lanes", "k_lanes_knn"} <= kernels
     ctx.free(cid)
 
@@ -156,14 +164,21 @@ def test_tip150m_cut_k20_8_species(ctx, oracle):
     surf = oracle.surface_distance(spec.xyz, spec.hull, 2.5)
     ref = oracle.spatstat(spec.xyz, spec.labels, surf, *hist, flags, trg, env, ks)
     assert ref["centres"] > 0.5 * spec.xyz.shape[0]
-    for tuning in (None, (5.0, lanes_code(4, 2, 2)), (4.0, lanes_code(3, 2, 2))):
+    # the kNN lane scan's lists: automatic (categories for 8 sets of k = 20),
+    # distances (one block per SM) and categories
+    for tuning, lists in ((None, 0), ((5.0, lanes_code(4, 2, 2)), 0), ((4.0, lanes_code(3, 2, 2)), 0),
+                          ((5.0, lanes_code(4, 2, 2)), 1), ((5.0, lanes_code(4, 2, 2)), 2)):
         if tuning:
             ctx.tuning(cid, *tuning)
-        ctx.run(cid, flags, ks)
-        gpu = ctx.fetch()
+        ctx.set_option("knn_lists", lists)
+        try:
+            ctx.run(cid, flags, ks)
+            gpu = ctx.fetch()
+        finally:
+            ctx.set_option("knn_lists", 0)
         kern = ctx.last_kernel()
         assert ctx.stats()["pairs"] == ref["pairs"], (tuning, kern)
-        assert np.array_equal(gpu, ref["bins"]), f"{tuning} {kern}: " + _diff(gpu, ref["bins"])
+        assert np.array_equal(gpu, ref["bins"]), f"{tuning} lists {lists} {kern}: " + _diff(gpu, ref["bins"])
     ctx.free(cid)
 
 
