@@ -251,10 +251,6 @@ int pp_fetch_npcorr(pp_ctx* ctx, uint32_t* counts, uint64_t cap, uint64_t* edge)
  *                       when every centre type maps types to sets alike
  *                       (default 1); 0 decodes the set per centre slot.
  *                       Results are identical either way.
- *   "knn_walk"          batched kNN walk: 0 = lanes over list entries, looping
- *                       over 32 realisations (disjoint sets of at most 8 per
- *                       centre type; default), 1 = one lane per realisation.
- *                       Results are identical either way.
  *   "knn_lists"         lists of the kNN centre-per-lane scan: 0 = distances
  *                       while they fit two blocks per SM, bin categories
  *                       beyond (default); 1 = distances; 2 = categories.

@@ -199,7 +199,6 @@ struct pp_ctx {
   bool no_lanes = false;  // option "lanes" = 0: RDF passes take the per-centre or brick scan
   bool no_uniform = false;  // option "uniform_sets" = 0: the kNN lane scan decodes sets per centre slot
   int knn_lists = 0;        // option "knn_lists": 0 automatic, 1 d^2 lists, 2 category lists
-  int knn_walk = 0;         // option "knn_walk": 0 transposed batched walk where it applies, 1 lane per realisation
   DevBuf brows;           // stencil rows of a cell block, nearest first (centre-per-lane scan)
   int brows_key[3] = {-1, -1, -1};
   pp_ctx* parent = nullptr;     // serving workers share the parent's clouds
@@ -1838,11 +1837,6 @@ int pp_set_option(pp_ctx* ctx, const char* name, int value) {
   if (std::strcmp(name, "symmetric") == 0) { ctx->no_sym = (value == 0); return PP_OK; }
   if (std::strcmp(name, "lanes") == 0) { ctx->no_lanes = (value == 0); return PP_OK; }
   if (std::strcmp(name, "uniform_sets") == 0) { ctx->no_uniform = (value == 0); return PP_OK; }
-  if (std::strcmp(name, "knn_walk") == 0) {
-    if (value < 0 || value > 1) return fail(ctx, PP_ERR_INVALID, "knn_walk must be 0 or 1");
-    ctx->knn_walk = value;
-    return PP_OK;
-  }
   if (std::strcmp(name, "knn_lists") == 0) {
     if (value < 0 || value > 2) return fail(ctx, PP_ERR_INVALID, "knn_lists must be 0, 1 or 2");
     ctx->knn_lists = value;
@@ -2251,7 +2245,6 @@ int pp_run_batched(pp_ctx* ctx, int cloud, uint32_t flags, const uint32_t* k_lis
       kq.cslot_of = D.cslot;
       kq.envbits = D.envbits;
       kq.disjoint = P.disjoint;
-      kq.walk_mode = ctx->knn_walk;
       kq.setidx = D.setidx;
       kq.nsets = D.nsets;
       kq.set_list = D.set_list;

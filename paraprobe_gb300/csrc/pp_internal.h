@@ -281,7 +281,6 @@ struct KnnArgs {
   uint32_t* work;
   uint32_t tile;                    // centres per walk work item / per bin work item
   int cblk;                         // centre types per bin histogram (set by knn32_check)
-  int walk_mode;                    // 0 = transposed walk where it applies, 1 = lane per realisation
   unsigned long long* knn_core;     // [nreal][nC][nS][nkI][H]
 };
 // -2 when a warp's records or the bin histogram do not fit shared memory

@@ -2628,127 +2628,6 @@ __global__ void __launch_bounds__(512, 2) k_knn_walk(KnnArgs a) {
   }
 }
 
-// Transposed walk, for disjoint environment sets of at most 8 per centre
-// type: lanes are list entries, 32 at a time, and the warp loops over the 32
-// realisations of its group.  Lane e fetches its entry's 32 labels (one per
-// realisation, 32 consecutive bytes) with two 16-byte loads.  For realisation
-// r every lane looks up its entry's set; one ballot per bit of the set index
-// gives each lane the earlier entries of its own set in this batch and each
-// lane q < nset the entries of set q, so an entry's rank among its set's
-// members is the count carried from earlier batches plus a population count.
-// Lane q keeps set q's counts of all 32 realisations as bytes of 8 registers
-// (saturating at 255; only min(count, k_max) matters).  A realisation leaves
-// the loop when each of its sets has k_max members.  Records as k_knn_walk's.
-__global__ void __launch_bounds__(512, 2) k_knn_walk_t(KnnArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31;
-  const int NT = a.nsmax * a.nkI;
-  const int nrow = (a.nC + 1) * 256;
-  int8_t* sTab = (int8_t*)smem;                             // [nC + 1][256] set of a type, -1 = none
-  int* sNs = (int*)(smem + ((nrow + 15) & ~15));            // [nC]
-  int8_t* sC = (int8_t*)(sNs + a.nC);                       // 256
-  int8_t* sK = sC + 256;                                    // 256
-  for (int i = threadIdx.x; i < nrow; i += blockDim.x) sTab[i] = i >= a.nC * 256 ? (int8_t)-1 : a.setidx[i];
-  for (int i = threadIdx.x; i < a.nC; i += blockDim.x) sNs[i] = a.nsets[i];
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) { sC[i] = a.cslot_of[i]; sK[i] = -1; }
-  __syncthreads();
-  for (int i = threadIdx.x; i < a.nkI; i += blockDim.x)
-    if (a.kvals[i] >= 1 && a.kvals[i] <= 255) sK[a.kvals[i]] = (int8_t)i;
-  __syncthreads();
-  const uint32_t lt = (1u << lane) - 1u;
-  const uint8_t* labg = a.labels + (uint64_t)a.grp * a.n * 32;
-  const uint8_t* okg = a.centre_ok + (uint64_t)a.grp * a.ncentres * 32;
-  const bool real = a.grp * 32 + lane < a.nreal;
-  const uint32_t kmax = (uint32_t)a.kmax;
-  const int nkI = a.nkI;
-  const uint32_t ntiles = (a.cn + a.tile - 1) / a.tile;
-  for (;;) {
-    uint32_t item = 0;
-    if (lane == 0) item = atomicAdd(a.work, 1u);
-    item = __shfl_sync(FULL, item, 0);
-    if (item >= ntiles) break;
-    const uint32_t l0 = item * a.tile, l1 = min(l0 + a.tile, a.cn);
-    for (uint32_t li = l0; li < l1; ++li) {
-      const uint32_t ci = a.c0 + li;
-      const uint32_t self = a.centres[ci];
-      // lane r: the centre's type slot and set count in realisation r
-      const bool ok = real && okg[(uint64_t)ci * 32 + lane] != 0;
-      const int c_l = ok ? (int)sC[labg[(uint64_t)self * 32 + lane]] : -1;
-      const int ns_l = c_l >= 0 ? sNs[c_l] : 0;
-      uint32_t open = __ballot_sync(FULL, ns_l > 0);
-      uint32_t cnt[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) cnt[j] = 0u;
-      uint16_t* out = a.rec + (uint64_t)li * NT * 32;
-      const unsigned long long o0 = a.pair_off[ci], o1 = a.pair_off[ci + 1];
-      uint32_t nx_slot = 0, nx_cat = 0;
-      if (o0 + lane < o1) {
-        nx_slot = a.pair_slot[o0 + lane - a.pair_base];
-        nx_cat = a.pair_cat[o0 + lane - a.pair_base];
-      }
-      for (unsigned long long e0 = o0; e0 < o1 && open; e0 += 32) {
-        const bool valid = e0 + lane < o1;
-        const uint32_t my_slot = nx_slot, my_cat = nx_cat;
-        if (e0 + 32 + lane < o1) {
-          nx_slot = a.pair_slot[e0 + 32 + lane - a.pair_base];
-          nx_cat = a.pair_cat[e0 + 32 + lane - a.pair_base];
-        }
-        uint4 w0 = make_uint4(0, 0, 0, 0), w1 = w0;
-        if (valid) {
-          const uint4* lp = (const uint4*)(labg + (uint64_t)my_slot * 32);
-          w0 = lp[0];
-          w1 = lp[1];
-        }
-        const uint32_t words[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
-#pragma unroll
-        for (int r = 0; r < 32; ++r) {
-          if (!((open >> r) & 1u)) continue;
-          const int c = __shfl_sync(FULL, c_l, r);
-          const int ns = __shfl_sync(FULL, ns_l, r);
-          const uint32_t t = (words[r >> 2] >> (8 * (r & 3))) & 255u;
-          const int q = valid ? (int)sTab[c * 256 + (int)t] : -1;
-          const uint32_t m0 = __ballot_sync(FULL, q >= 0);
-          if (!m0) continue;
-          uint32_t mine = m0, own = m0;
-          const int nb = ns > 1 ? 32 - __clz(ns - 1) : 0;
-          for (int b = 0; b < nb; ++b) {
-            const uint32_t bb = __ballot_sync(FULL, (q >> b) & 1);
-            mine &= ((q >> b) & 1) ? bb : ~bb;
-            own &= ((lane >> b) & 1) ? bb : ~bb;
-          }
-          const uint32_t mycnt = (cnt[r >> 2] >> (8 * (r & 3))) & 255u;  // lane q: set q's count
-          const uint32_t before = __shfl_sync(FULL, mycnt, q & 31);
-          if (q >= 0) {
-            const uint32_t rank = before + __popc(mine & lt);
-            if (rank < kmax) {
-              const int kk = sK[rank + 1];
-              if (kk >= 0) out[((uint32_t)q * nkI + kk) * 32 + r] = (uint16_t)my_cat;
-            }
-          }
-          const uint32_t nc = min(mycnt + (lane < ns ? (uint32_t)__popc(own) : 0u), 255u);
-          cnt[r >> 2] = (cnt[r >> 2] & ~(255u << (8 * (r & 3)))) | (nc << (8 * (r & 3)));
-          if (__all_sync(FULL, lane >= ns || nc >= kmax)) open &= ~(1u << r);
-        }
-      }
-      // the slots not met: misses of the sets, no slot beyond them (lane r:
-      // realisation r; its counts are byte r of lane q's registers)
-      for (int q = 0; q < a.nsmax; ++q) {
-        uint32_t got = 0;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const uint32_t v = __shfl_sync(FULL, cnt[j], q);
-          if ((lane >> 2) == j) got = (v >> (8 * (lane & 3))) & 255u;
-        }
-        for (int kk = 0; kk < nkI; ++kk) {
-          if (q < ns_l && got >= (uint32_t)a.kvals[kk]) continue;
-          out[((uint32_t)q * nkI + kk) * 32 + lane] = q < ns_l ? (uint16_t)a.cat_miss : (uint16_t)0xffff;
-        }
-      }
-      a.rec_c[(uint64_t)li * 32 + lane] = c_l >= 0 ? (uint8_t)c_l : (uint8_t)0xff;
-    }
-  }
-}
-
 // Bin: one work item = (slot t = set q * nkI + order kk, range of centres).
 // The block histograms that slot for all 32 realisations at once in shared
 // memory laid out [nC][H][32], so lane r always hits bank r; the bins go to
@@ -3423,17 +3302,6 @@ int knn32_check(KnnArgs& k) {
 }
 
 int launch_knn_walk(const KnnArgs& k, int sm_count, cudaStream_t s) {
-  // the transposed walk for disjoint sets of at most 8 per centre type
-  if (k.walk_mode != 1 && k.disjoint && k.nsmax <= 8 && k.kmax <= 254) {
-    const size_t smem = (((size_t)(k.nC + 1) * 256 + 15) & ~size_t(15)) + (size_t)k.nC * 4 + 512;
-    if (!allow_dynamic_smem((const void*)k_knn_walk_t, smem)) return -1;
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_knn_walk_t, 512, smem) != cudaSuccess || per_sm < 1)
-      return -1;
-    counted();
-    k_knn_walk_t<<<sm_count * per_sm, 512, smem, s>>>(k);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
-  }
   const int w = knn_walk_warps(k);
   if (!w) return -2;
   const size_t smem = knn_walk_bytes(k, w);

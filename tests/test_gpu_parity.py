@@ -333,13 +333,11 @@ def test_batched_chunked_geometry(ctx, oracle, rincr):
     ctx.free(cid)
 
 
-@pytest.mark.parametrize("walk", [0, 1])
 @pytest.mark.parametrize("nsets", [33, 40])
-def test_batched_32_lane_groups_and_rest(ctx, oracle, nsets, walk):
+def test_batched_32_lane_groups_and_rest(ctx, oracle, nsets):
     """More than 32 realisations: full 32-lane kNN groups, plus either a short
     rest taken by the rank walk (1 + 33 = 34: rest 2) or a partly filled group
-    (1 + 40 = 41: rest 9); realisations on both sides of the split checked,
-    with the transposed walk (0) and the lane-per-realisation walk (1)."""
+    (1 + 40 = 41: rest 9); realisations on both sides of the split checked."""
     spec = synth.cone_specimen(n=20000, r_apex=8.0, half_angle_deg=10.0, length=10.0, n_clusters=10,
                                members=40, nspecies=3, seed=71, nseg=48, stack=4.0)
     types = [1, 2, 3]
@@ -352,11 +350,7 @@ def test_batched_32_lane_groups_and_rest(ctx, oracle, nsets, walk):
     ctx.hull(cid, spec.hull, 2.0)
     ctx.tasks(trg, env)
     ctx.hist(0.0, 0.02, 1.1)
-    ctx.set_option("knn_walk", walk)
-    try:
-        ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets)
-    finally:
-        ctx.set_option("knn_walk", 0)
+    ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets)
     assert ctx.batched_count() == 1 + nsets
     surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
     for r in (0, 5, 31, 32, 33, nsets):
@@ -366,13 +360,11 @@ def test_batched_32_lane_groups_and_rest(ctx, oracle, nsets, walk):
     ctx.free(cid)
 
 
-@pytest.mark.parametrize("walk", [0, 1])
 @pytest.mark.parametrize("nspecies,ks", [(10, [12, 3, 1]), (6, [20, 9, 2, 1]), (8, [5, 4, 3, 2, 1])])
-def test_batched_walk_set_counts(ctx, oracle, nspecies, ks, walk):
+def test_batched_walk_set_counts(ctx, oracle, nspecies, ks):
     """The 32-realisation kNN walk with one environment set per species for
-    every centre type (six, eight or ten sets: the transposed walk takes up to
-    eight), k up to 20, realisations of the first 32-lane group and of the
-    second, with both walks."""
+    every centre type (six, eight or ten sets), k up to 20, realisations of the
+    first 32-lane group and of the second."""
     spec = synth.cone_specimen(n=20000, r_apex=8.0, half_angle_deg=10.0, length=10.0, n_clusters=10,
                                members=40, nspecies=nspecies, seed=83 + nspecies, nseg=48, stack=4.0,
                                iid=(0.04, 0.03, 0.02))
@@ -385,11 +377,7 @@ def test_batched_walk_set_counts(ctx, oracle, nspecies, ks, walk):
     ctx.hull(cid, spec.hull, 2.0)
     ctx.tasks(trg, env)
     ctx.hist(0.0, 0.01, 1.2)
-    ctx.set_option("knn_walk", walk)
-    try:
-        ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets)
-    finally:
-        ctx.set_option("knn_walk", 0)
+    ctx.run_batched(cid, flags, ks, include_original=True, label_sets=sets)
     assert ctx.batched_count() == 34
     surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
     for r in (0, 1, 31, 32, 33):
