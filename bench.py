@@ -704,7 +704,6 @@ def served_leg(ctx, nq=240, rate=200.0):
         k = int(rng.integers(1, 21))
         a, b = (int(x) for x in rng.integers(1, 7, size=2))
         qs.append((c, N.PP_RDF | N.PP_MKNN, (0.0, 0.01, R), [[a]], [[b]], [k]))
-    gaps = rng.exponential(1.0 / rate, size=nq)
     free = 0
     try:
         import torch
@@ -712,27 +711,38 @@ def served_leg(ctx, nq=240, rate=200.0):
     except Exception:
         pass
     budget = int(max(2 << 30, free * 0.6))
-    srv = N.Server(ctx, slots=4, budget_bytes=budget)
-    for q in qs[:4]:  # warm the workers
-        srv.wait(srv.submit(*q))
-    t0 = time.perf_counter()
-    tickets, t_next = [], t0
-    for q, g in zip(qs, gaps):
-        t_next += g
-        dt = t_next - time.perf_counter()
-        if dt > 0:
-            time.sleep(dt)
-        try:
-            tickets.append(srv.submit(*q))
-        except N.PPError:
-            pass
-    pairs = 0
-    for t in tickets:
-        pairs += srv.wait(t)[1]
-    served_s = time.perf_counter() - t0
-    st = srv.stats()
-    passes, taken = srv.passes()
-    srv.close()
+
+    def stream(arrival, seed):
+        """The queries as a Poisson stream at `arrival`/s through a fresh server."""
+        gaps = np.random.default_rng(seed).exponential(1.0 / arrival, size=nq)
+        srv = N.Server(ctx, slots=4, budget_bytes=budget)
+        for q in qs[:4]:  # warm the workers
+            srv.wait(srv.submit(*q))
+        t0 = time.perf_counter()
+        tickets, t_next = [], t0
+        for q, g in zip(qs, gaps):
+            t_next += g
+            dt = t_next - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            try:
+                tickets.append(srv.submit(*q))
+            except N.PPError:
+                pass
+        got = 0
+        for t in tickets:
+            got += srv.wait(t)[1]
+        el = time.perf_counter() - t0
+        st = srv.stats()
+        npass, taken = srv.passes()
+        srv.close()
+        return tickets, got, el, st, npass, taken
+
+    tickets, pairs, served_s, st, passes, taken = stream(rate, 20261209)
+    # the same stream at a rate the server sustains (70% of the queries per
+    # second it completed above): latency without a growing queue
+    rate_ok = round(0.7 * len(tickets) / served_s, 1)
+    t2, pairs2, s2, st2, passes2, taken2 = stream(rate_ok, 20261210)
     # the same queries one at a time through the plain path
     t0 = time.perf_counter()
     plain_pairs = 0
@@ -752,7 +762,10 @@ def served_leg(ctx, nq=240, rate=200.0):
             "rejected": int(st["rejected"]), "slots": 4, "budget_bytes": budget,
             "arrival_rate_per_s": rate, "served_queries_per_s": len(tickets) / served_s,
             "merged_passes": int(passes) - 4, "queries_per_pass": (taken - 4) / max(passes - 4, 1),
-            "plain_single_query": plain_pairs / plain_s, "ratio_vs_plain": (pairs / served_s) / (plain_pairs / plain_s)}
+            "plain_single_query": plain_pairs / plain_s, "ratio_vs_plain": (pairs / served_s) / (plain_pairs / plain_s),
+            "sustained": {"arrival_rate_per_s": rate_ok, "value": pairs2 / s2, "p50_ms": st2["p50_ms"],
+                          "p99_ms": st2["p99_ms"], "served_queries_per_s": len(t2) / s2,
+                          "merged_passes": int(passes2) - 4, "rejected": int(st2["rejected"])}}
 
 
 # ------------------------------------------------------------ reference arm
