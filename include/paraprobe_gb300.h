@@ -93,6 +93,9 @@ int pp_cloud_upload_device(pp_ctx* ctx, const float* d_xyz, const uint8_t* d_lab
 int pp_cloud_upload_pos(pp_ctx* ctx, const void* pos_bytes, uint64_t n,
                         const float* range_lo, const float* range_hi,
                         const uint8_t* range_type, int nranges, int* cloud);
+/* Release a cloud.  The context keeps the device buffers of up to two freed
+ * clouds and gives them to later uploads (no cudaMalloc / cudaFree in an
+ * upload-run-free loop); pp_destroy releases them. */
 int pp_cloud_free(pp_ctx* ctx, int cloud);
 /* Type ids of a cloud in input order (n bytes), e.g. after pp_cloud_upload_pos. */
 int pp_cloud_labels(pp_ctx* ctx, int cloud, uint8_t* label_out, uint64_t n);

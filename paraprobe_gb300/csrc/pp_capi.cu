@@ -32,6 +32,7 @@ using pp::Grid;
 namespace {
 
 constexpr double kEpsilon = 1.0e-6;  // src/PARAPROBE_Numerics.h:44
+constexpr size_t kSpareClouds = 2;    // freed clouds whose device buffers a context keeps
 
 struct DevBuf {
   void* p = nullptr;
@@ -158,6 +159,7 @@ struct pp_ctx {
   int sm_count = 0;
   std::string err;
   std::vector<std::unique_ptr<Cloud>> clouds;
+  std::vector<std::unique_ptr<Cloud>> spare;  // freed clouds whose device buffers later uploads reuse
   bool tasks_ok = false;
   int ntasks = 0;
   std::vector<uint32_t> trg, env;
@@ -921,9 +923,32 @@ int pp_device_info(pp_ctx* ctx, int* device, int* sm_count) {
   return PP_OK;
 }
 
+// A new cloud takes the device buffers of a freed one when one is kept
+// (pp_cloud_free), so that upload-run-free loops do not pay cudaMalloc /
+// cudaFree (which synchronises the device) on every cloud.
+static void adopt_buffers(Cloud& to, Cloud& from) {
+  DevBuf* a[] = {&to.xyz, &to.label, &to.ions, &to.cell_start, &to.slot_of_id, &to.id_of_slot, &to.label_sorted,
+                 &to.user_surf, &to.surf, &to.tri_dev, &to.tri_box, &to.tcell_start, &to.tcell_list};
+  DevBuf* b[] = {&from.xyz, &from.label, &from.ions, &from.cell_start, &from.slot_of_id, &from.id_of_slot,
+                 &from.label_sorted, &from.user_surf, &from.surf, &from.tri_dev, &from.tri_box, &from.tcell_start,
+                 &from.tcell_list};
+  for (size_t i = 0; i < sizeof a / sizeof a[0]; ++i) {
+    std::swap(a[i]->p, b[i]->p);
+    std::swap(a[i]->bytes, b[i]->bytes);
+  }
+}
+
 static int new_cloud(pp_ctx* ctx, uint64_t n, int* cloud, Cloud** out) {
   if (n > 0xfffffff0ull) return fail(ctx, PP_ERR_UNSUPPORTED, "clouds are limited to 2^32-16 ions");
   auto c = std::make_unique<Cloud>();
+  if (!ctx->spare.empty()) {
+    // the kept buffers that fit this cloud best: the largest position buffer
+    size_t best = 0;
+    for (size_t i = 1; i < ctx->spare.size(); ++i)
+      if (ctx->spare[i]->xyz.bytes > ctx->spare[best]->xyz.bytes) best = i;
+    adopt_buffers(*c, *ctx->spare[best]);
+    ctx->spare.erase(ctx->spare.begin() + (long)best);
+  }
   c->n = n;
   CK(c->xyz.ensure(std::max<uint64_t>(n, 1) * 12));
   CK(c->label.ensure(std::max<uint64_t>(n, 1)));
@@ -991,6 +1016,8 @@ int pp_cloud_free(pp_ctx* ctx, int cloud) {
   if (!ctx || !get_cloud(ctx, cloud)) return fail(ctx, PP_ERR_INVALID, "bad cloud");
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
+  // keep the buffers of up to kSpareClouds freed clouds for later uploads
+  if (ctx->spare.size() < kSpareClouds) ctx->spare.push_back(std::move(ctx->clouds[cloud]));
   ctx->clouds[cloud].reset();
   if (ctx->geo_cloud == cloud) ctx->geo_cloud = -1;
   return PP_OK;
