@@ -585,3 +585,25 @@ def test_lanes_small_and_sparse_clouds(ctx, oracle, block):
     finally:
         ctx.set_option("symmetric", 1)
         ctx.free(cid)
+
+
+def test_freed_cloud_buffers_reused(ctx, oracle):
+    """Uploads after pp_cloud_free take the freed clouds' device buffers
+    (smaller and larger clouds, with and without a hull); every result still
+    equals the oracle's."""
+    flags, ks = N.PP_RDF | N.PP_MKNN, [4, 1]
+    for i, n in enumerate((40000, 15000, 60000, 25000)):
+        spec = synth.cylinder_specimen(n=n, radius=5.0, height=n / 2000.0, seed=300 + i, nseg=64, stack=4.0)
+        cid = ctx.upload(spec.xyz, spec.labels)
+        hull = i != 3
+        if hull:
+            ctx.hull(cid, spec.hull, 2.0)
+        ctx.tasks([[2], [1]], [[1, 2, 3], [1]])
+        ctx.hist(0.0, 0.01, 1.0)
+        ctx.run(cid, flags, ks)
+        gpu = ctx.fetch()
+        surf = (oracle.surface_distance(spec.xyz, spec.hull, 2.0) if hull
+                else np.full(n, np.float32(2.0) * np.float32(2.0), dtype=np.float32))
+        ref = oracle.spatstat(spec.xyz, spec.labels, surf, 0.0, 0.01, 1.0, flags, [[2], [1]], [[1, 2, 3], [1]], ks)
+        assert np.array_equal(gpu, ref["bins"]), n
+        ctx.free(cid)
