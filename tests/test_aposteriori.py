@@ -189,3 +189,34 @@ def test_gpu_reference_guard_matches_reference(ctx, name):
     assert np.array_equal(surf.view(np.uint32), z["surf"][o].view(np.uint32))
     assert st["centres"] == a["stats"]["centres"]
     assert np.array_equal(got, z["bins"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("which", ["rdf_1nn", "ripk"])
+def test_gpu_reference_guard_matches_oracle_at_size(ctx, oracle, which):
+    """Option aposteriori_guard = 1 on a 200k-ion clustered cone against the
+    oracle's restatement of the reference loop (pinned on the fixtures above),
+    with the cloud's input order as the positions; and with no clustered ion,
+    where both guard rules give the plain statistics over every ion."""
+    from paraprobe_gb300 import native as N
+    flags = {"rdf_1nn": N.PP_RDF | N.PP_1NN, "ripk": N.PP_RIPK}[which]
+    spec, clus = _case()
+    rmin, rincr, rmax = 0.0, 0.01, 1.5
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.hist(rmin, rincr, rmax)
+    for c in (clus, np.zeros_like(clus)):
+        ctx.set_option("aposteriori_guard", 1)
+        try:
+            ctx.run_aposteriori(cid, c, flags)
+        finally:
+            ctx.set_option("aposteriori_guard", 0)
+        got = np.asarray(ctx.fetch()).reshape(-1)
+        surf = ctx.surfdist_fetch(cid, spec.xyz.shape[0])
+        ref, st = oracle.aposteriori(spec.xyz, c, surf, rmin, rincr, rmax, flags, guard_mode=1)
+        want = np.concatenate([ref[k] for k in ("rdf", "1nn", "ripk") if k in ref])
+        assert np.array_equal(got, want)
+        if not c.any():
+            ctx.run_aposteriori(cid, c, flags)
+            assert np.array_equal(np.asarray(ctx.fetch()).reshape(-1), want)
+    ctx.free(cid)

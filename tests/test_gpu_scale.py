@@ -225,3 +225,31 @@ def test_batched_5m_shuffles_and_rois(ctx, oracle):
         refq = oracle.spatstat(spec.xyz, spec.labels, surf, *hist, flags, trg, env, ks, centre_mask=mask)
         assert np.array_equal(outs[4 + q], refq["bins"]), f"roi {q}: " + _diff(outs[4 + q], refq["bins"])
     ctx.free(cid)
+
+
+def test_masked_edge_cases(ctx, oracle):
+    """A mask that selects no centre gives empty bins (every histogram zero,
+    no kNN miss either), one that selects a single ion that ion's ball, and a
+    mask of ones the unmasked pass."""
+    spec, _ = tip20m_cut(200_000, seed=20261214)
+    trg, env = all_pairs(6)
+    n = spec.xyz.shape[0]
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks(trg, env)
+    flags, hist, ks = N.PP_RDF | N.PP_MKNN, (0.0, 0.01, 2.0), [5, 1]
+    ctx.hist(*hist)
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    one = np.zeros(n, np.uint8)
+    one[int(np.argmax(surf))] = 1  # the ion deepest inside: a centre for sure
+    for mask in (np.zeros(n, np.uint8), one, np.ones(n, np.uint8)):
+        ctx.run(cid, flags, ks, centre_mask=mask)
+        gpu = ctx.fetch()
+        ref = oracle.spatstat(spec.xyz, spec.labels, surf, *hist, flags, trg, env, ks, centre_mask=mask)
+        assert ctx.stats()["centres"] == ref["centres"]
+        assert np.array_equal(gpu, ref["bins"])
+        if not mask.any():
+            assert ref["centres"] == 0 and not gpu.any()
+    ctx.run(cid, flags, ks)
+    assert np.array_equal(ctx.fetch(), gpu)
+    ctx.free(cid)
