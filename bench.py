@@ -475,43 +475,59 @@ def run_gpu(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # the oracle on the workload's centre sample (a fresh process), then
         # the GPU pass on the same sample: the bins must be identical
-        rec, cpu_bins = cpu_leg_subprocess(args.workload, steps=2, warmup=1)
-        line["cpu_baseline"] = rec
-        mask = sample_mask(n, CPU_SAMPLE[args.workload])
-        checks = []
-        for i, r in enumerate(runs):
-            ctx.tasks(trg, env)
-            ctx.hist(*r["hist"])
-            ctx.run(cid, r["flags"], r["k"], stream=sh, centre_mask=mask)
-            g = ctx.fetch()
-            st = ctx.stats()
-            same = g.shape == cpu_bins[i].shape and bool(np.array_equal(g, cpu_bins[i]))
-            checks.append({"pass": i + 1, "kernel": ctx.last_kernel(), "centres": st["centres"],
-                           "pairs": st["pairs"], "bins": int(g.size), "bins_identical": same,
-                           "bins_differing": int(np.count_nonzero(g != cpu_bins[i])) if g.shape == cpu_bins[i].shape
-                           else int(g.size)})
-        line["parity"] = {"against": "oracle port on the cpu_baseline sample (same centre mask, same cloud)",
-                          "sample_fraction": CPU_SAMPLE[args.workload],
-                          "centres": sum(c["centres"] for c in checks), "pairs": sum(c["pairs"] for c in checks),
-                          "bins_identical": all(c["bins_identical"] for c in checks), "passes": checks}
-    if not args.no_batched:
-        if args.workload == "tip150m":
-            line["batched"] = batched_leg_large(ctx, cid, spec, trg, env, runs[0], torch, stream,
-                                                per_pass_pairs[0], per_pass_ms[0])
-            ctx.free(cid)
-        else:
-            ctx.free(cid)
-            line["batched"] = batched_leg(ctx, torch, stream)
+        line.update(guarded("cpu_baseline", lambda: parity_leg(ctx, cid, sh, spec, trg, env, runs, args)))
+    if not args.no_batched and args.workload == "tip150m":
+        line.update(guarded("batched", lambda: batched_leg_large(ctx, cid, spec, trg, env, runs[0], torch, stream,
+                                                                 per_pass_pairs[0], per_pass_ms[0])))
+    ctx.free(cid)
+    if not args.no_batched and args.workload != "tip150m":
+        line.update(guarded("batched", lambda: batched_leg(ctx, torch, stream)))
     if not args.no_served:
-        line["served"] = served_leg(ctx)
+        line.update(guarded("served", lambda: served_leg(ctx)))
     if not args.no_large and args.workload != "tip150m" and world == 1:
         del spec
-        line["large"] = large_leg(ctx, torch, stream, args)
+        line.update(guarded("large", lambda: large_leg(ctx, torch, stream, args)))
     ctx.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
+
+
+def guarded(key, fn):
+    """An optional leg of the bench: {key: its result} (or the keys it returns
+    itself, when it returns several), or {key: {"error": ...}} when it fails,
+    so that a failing leg never costs the bench line."""
+    try:
+        out = fn()
+        return out if key in out and isinstance(out[key], dict) and len(out) > 1 else {key: out}
+    except Exception as e:  # noqa: BLE001 -- reported in the line
+        return {key: {"error": f"{type(e).__name__}: {e}"[:300]}}
+
+
+def parity_leg(ctx, cid, sh, spec, trg, env, runs, args):
+    """The oracle on the workload's centre sample (cpu_baseline) and the GPU
+    passes on the same sample (parity): {"cpu_baseline": ..., "parity": ...}."""
+    n = spec.xyz.shape[0]
+    rec, cpu_bins = cpu_leg_subprocess(args.workload, steps=2, warmup=1)
+    mask = sample_mask(n, CPU_SAMPLE[args.workload])
+    checks = []
+    for i, r in enumerate(runs):
+        ctx.tasks(trg, env)
+        ctx.hist(*r["hist"])
+        ctx.run(cid, r["flags"], r["k"], stream=sh, centre_mask=mask)
+        g = ctx.fetch()
+        st = ctx.stats()
+        same = g.shape == cpu_bins[i].shape and bool(np.array_equal(g, cpu_bins[i]))
+        checks.append({"pass": i + 1, "kernel": ctx.last_kernel(), "centres": st["centres"],
+                       "pairs": st["pairs"], "bins": int(g.size), "bins_identical": same,
+                       "bins_differing": int(np.count_nonzero(g != cpu_bins[i])) if g.shape == cpu_bins[i].shape
+                       else int(g.size)})
+    parity = {"against": "oracle port on the cpu_baseline sample (same centre mask, same cloud)",
+              "sample_fraction": CPU_SAMPLE[args.workload],
+              "centres": sum(c["centres"] for c in checks), "pairs": sum(c["pairs"] for c in checks),
+              "bins_identical": all(c["bins_identical"] for c in checks), "passes": checks}
+    return {"cpu_baseline": rec, "parity": parity}
 
 
 # ---------------------------------------------------- batched (null model + ROIs)
@@ -662,17 +678,20 @@ def large_leg(ctx, torch, stream, args):
                         "frac": round(BYTES_PER_PAIR * pairs / t / 1e9 / peak, 4)},
            "tuning": {"cell_edge_nm": round(cfg["R_nm"] / ratio, 4), "tile": tile}}
     if not args.no_cpu_baseline:
-        cpu_rec, cpu_bins = cpu_leg_subprocess("tip150m", steps=1, warmup=0)
-        ctx.run(cid, r["flags"], r["k"], stream=sh, centre_mask=sample_mask(n, CPU_SAMPLE["tip150m"]))
-        g = ctx.fetch()
-        st = ctx.stats()
-        out["parity"] = {"against": "oracle port on the tip150m CPU sample (same centre mask, same cloud)",
-                         "sample_fraction": CPU_SAMPLE["tip150m"], "centres": st["centres"], "pairs": st["pairs"],
-                         "bins": int(g.size), "kernel": ctx.last_kernel(),
-                         "bins_identical": bool(g.shape == cpu_bins[0].shape and np.array_equal(g, cpu_bins[0]))}
-        out["cpu_baseline"] = cpu_rec
+        def parity():
+            cpu_rec, cpu_bins = cpu_leg_subprocess("tip150m", steps=1, warmup=0)
+            ctx.run(cid, r["flags"], r["k"], stream=sh, centre_mask=sample_mask(n, CPU_SAMPLE["tip150m"]))
+            g = ctx.fetch()
+            st = ctx.stats()
+            return {"parity": {"against": "oracle port on the tip150m CPU sample (same centre mask, same cloud)",
+                               "sample_fraction": CPU_SAMPLE["tip150m"], "centres": st["centres"],
+                               "pairs": st["pairs"], "bins": int(g.size), "kernel": ctx.last_kernel(),
+                               "bins_identical": bool(g.shape == cpu_bins[0].shape and
+                                                      np.array_equal(g, cpu_bins[0]))},
+                    "cpu_baseline": cpu_rec}
+        out.update(guarded("parity", parity))
     if not args.no_batched:
-        out["batched"] = batched_leg_large(ctx, cid, spec, trg, env, r, torch, stream, pairs, ms)
+        out.update(guarded("batched", lambda: batched_leg_large(ctx, cid, spec, trg, env, r, torch, stream, pairs, ms)))
     ctx.free(cid)
     return out
 
