@@ -258,6 +258,10 @@ int pp_fetch_npcorr(pp_ctx* ctx, uint32_t* counts, uint64_t cap, uint64_t* edge)
  *                       while they fit two blocks per SM, bin categories
  *                       beyond (default); 1 = distances; 2 = categories.
  *                       Results are identical either way.
+ *   "box_filter"        the centre-per-lane scans test only ions within R of
+ *                       the bounding box of a batch's centres (default 1);
+ *                       0 tests every ion of the block's stencil rows.
+ *                       Results are identical either way.
  *   "npcorr_order"      SpatStatKNNOrder - 1 for PP_NPCORR (0..31, default 0).
  *   "server_batch"      most queries per merged serving pass (1..32, default
  *                       32; 1 = every query alone), read by pp_server_create.

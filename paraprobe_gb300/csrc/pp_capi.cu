@@ -200,6 +200,7 @@ struct pp_ctx {
   bool no_sym = false;  // testing hook: force the one-sided scan
   bool no_lanes = false;  // option "lanes" = 0: RDF passes take the per-centre or brick scan
   bool no_uniform = false;  // option "uniform_sets" = 0: the kNN lane scan decodes sets per centre slot
+  bool no_box = false;      // option "box_filter" = 0: the lane scans stage every candidate of the cell rows
   int knn_lists = 0;        // option "knn_lists": 0 automatic, 1 d^2 lists, 2 category lists
   DevBuf brows;           // stencil rows of a cell block, nearest first (centre-per-lane scan)
   int brows_key[3] = {-1, -1, -1};
@@ -717,6 +718,8 @@ void fill_scan_common(pp::ScanArgs& a, const Cloud& cl, const RunPlan& P, const 
   a.g = cl.g;
   a.R = t.rmax;
   a.R2 = t.rmax * t.rmax;
+  a.box_R2 = std::nextafter(a.R2 * (1.f + 1.f / 4096.f) + 1e-30f, std::numeric_limits<float>::infinity());
+  a.no_box_filter = 0;
   const float Rm = t.rmax + cl.g.margin;
   a.Rm2 = Rm * Rm;
   a.H = P.H;
@@ -1347,6 +1350,7 @@ int run_plain(pp_ctx* ctx, Cloud* cl, uint32_t flags, const uint32_t* k_list, in
   pp::ScanArgs a{};
   fill_scan_common(a, *cl, P, D, ctx->tab);
   if (ctx->no_uniform) a.uniform_sets = 0;
+  if (ctx->no_box) a.no_box_filter = 1;
   a.lists_mode = ctx->knn_lists;
   a.labels = labels;
   a.centres = ctx->centres.as<uint32_t>();
@@ -1864,6 +1868,7 @@ int pp_set_option(pp_ctx* ctx, const char* name, int value) {
   if (std::strcmp(name, "symmetric") == 0) { ctx->no_sym = (value == 0); return PP_OK; }
   if (std::strcmp(name, "lanes") == 0) { ctx->no_lanes = (value == 0); return PP_OK; }
   if (std::strcmp(name, "uniform_sets") == 0) { ctx->no_uniform = (value == 0); return PP_OK; }
+  if (std::strcmp(name, "box_filter") == 0) { ctx->no_box = (value == 0); return PP_OK; }
   if (std::strcmp(name, "knn_lists") == 0) {
     if (value < 0 || value > 2) return fail(ctx, PP_ERR_INVALID, "knn_lists must be 0, 1 or 2");
     ctx->knn_lists = value;

@@ -39,6 +39,8 @@ struct ScanArgs {
   // geometry of the query
   float R, R2;                 // SpatStatRadiusMax and float(R*R)
   float Rm2;                   // (R + margin)^2 for conservative row trimming
+  float box_R2;                // R2 (1 + 2^-12): centre-per-lane box filter bound
+  int no_box_filter;           // centre-per-lane scans stage every candidate
   // bins: categories 0 = lowest, 1..nb = bins, nb+1 = highest
   int H;                       // nb + 2
   const float* cat_T;          // [H] smallest d^2 of each category (index 0 unused)

@@ -83,8 +83,10 @@ __device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsig
 // ...) against two ions whose x, y and z come as pairs: differences and
 // squares packed, the two sums scalar, in dist2's order.  Bit-identical to
 // dist2 on the GPU (checked on 2M random pairs); with the sums packed as well
-// (add.rn.f32x2) 40% of the results differed from dist2 by an ulp or two, so
-// they are not.
+// (add.rn.f32x2) the results differ from dist2 by an ulp or two for about one
+// pair in five (measured on 134M pairs, with or without --fmad=false passed to
+// ptxas: a product feeding only a packed add comes out unrounded, as from a
+// fused multiply-add), so they are not.
 __device__ __forceinline__ void dist2_x2(unsigned long long cxx, unsigned long long cyy, unsigned long long czz,
                                          unsigned long long xx, unsigned long long yy, unsigned long long zz,
                                          float& d0, float& d1) {
@@ -101,6 +103,9 @@ __device__ __forceinline__ void dist2_x2(unsigned long long cxx, unsigned long l
 __device__ __forceinline__ uint32_t f2o(float f) {
   const uint32_t u = __float_as_uint(f);
   return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float o2f(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
 // d_minmax holds 6 order-preserving keys (min x,y,z as min keys, max x,y,z)
@@ -1642,13 +1647,16 @@ __global__ void __launch_bounds__(256) k_brick(ScanArgs a) {
 // [xb, xe) x [yb, ye) x [zb, ze): rows are (yy, zz) with yy in [yb - sr,
 // ye - 1 + sr] and zz in [zb - sr, ze - 1 + sr], row r at (yb - sr + ry,
 // zb - sr + rz) for (ry, rz) = a.brows[r] (nearest to the block first), each
-// trimmed in x to the block's reach; len = 0 when the row cannot hold a
+// trimmed in x to the block's reach and to the reach of the batch's centre
+// box [box[0], box[1]] (world coordinates; rows and cells beyond R of the box
+// hold no neighbour of these centres); len = 0 when the row cannot hold a
 // neighbour of a point of the block.  In symmetric mode the
 // leading cells that precede the block's first cell in slot order and hold
 // only centres are dropped: their pairs with the block are taken from their
 // side (every ion of such a cell has a lower slot than every block centre).
 __device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nrows, int sr, int xb, int xe, int yb,
-                                                int ye, int zb, int ze, bool sym, uint32_t& st, uint32_t& len) {
+                                                int ye, int zb, int ze, bool sym, const float4* box,
+                                                uint32_t& st, uint32_t& len) {
   const Grid& g = a.g;
   st = 0;
   len = 0;
@@ -1665,8 +1673,22 @@ __device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nr
   const float rem = Rp2 - gy * gy - gz * gz;
   if (rem < 0.f) return;
   const float half = sqrtf(rem);
-  const int x0 = max(0, (int)floorf(((float)xb * g.h - m2 - half) * g.inv_h));
-  const int x1 = min(g.nx - 1, (int)floorf(((float)xe * g.h + m2 + half) * g.inv_h));
+  int x0 = max(0, (int)floorf(((float)xb * g.h - m2 - half) * g.inv_h));
+  int x1 = min(g.nx - 1, (int)floorf(((float)xe * g.h + m2 + half) * g.inv_h));
+  {
+    // the same against the centre box: the row's ions lie within margin of
+    // its cells [lo + c h, lo + (c + 1) h]
+    const float4 lo = box[0], hi = box[1];
+    const float ry0 = g.loy + (float)yy * g.h, rz0 = g.loz + (float)zz * g.h;
+    const float by = fmaxf(0.f, fmaxf(lo.y - (ry0 + g.h), ry0 - hi.y) - m2);
+    const float bz = fmaxf(0.f, fmaxf(lo.z - (rz0 + g.h), rz0 - hi.z) - m2);
+    const float brem = Rp2 - by * by - bz * bz;
+    if (brem < 0.f) return;
+    const float bhalf = sqrtf(brem);
+    x0 = max(x0, (int)floorf((lo.x - g.lox - m2 - bhalf) * g.inv_h));
+    x1 = min(x1, (int)floorf((hi.x - g.lox + m2 + bhalf) * g.inv_h));
+    if (x1 < x0) return;
+  }
   const uint64_t cb = ((uint64_t)zz * g.ny + yy) * g.nx;
   int xs = x0;
   if (sym) {
@@ -1701,6 +1723,24 @@ __device__ __forceinline__ void block_row_range(const ScanArgs& a, int r, int nr
 // k_lanes_knn: kNN lists).  Warps fetch blocks `tile` at a time
 // from the global work counter, without block barriers.
 //
+// Box filter: the cell rows hold, beside the centres' neighbours, every ion
+// within reach of any point of the cell block.  Each batch of centres takes
+// the bounding box of its live centres (kept in shared memory, sbox); the
+// rows and their x-ranges are trimmed to the cells within R of that box, and
+// before staging each lane measures its candidate's distance to the box and
+// drops it when that exceeds R.  The bound is R^2 (1 + 2^-12): the float d^2
+// of a centre and the float box distance each lie within a few ulp of their
+// exact values (every operation is correctly rounded and the box distance
+// never exceeds a centre's distance), so no ion an exact test would take is
+// dropped.  Survivors are packed into the staging buffer in stencil order; a
+// batch of tests runs each time 32 have gathered, and once more for the rest
+// after the last row.  A survivor that finds the buffer full keeps only its
+// slot and is reloaded and staged after the tests, so nothing else stays live
+// across them.  On the 20M-ion tip (cells of R/4, 4 x 2 x 2 blocks) this took
+// the distance tests per pair from 2.66 to 1.78 (RDF) and from 4.43 to 2.92
+// (kNN).  Option ScanArgs::no_box_filter stages every candidate, as an A/B
+// switch.
+//
 // lanes_walk calls, warp-uniformly,
 //   stage(slot, q, key, code)  per staged ion (its lane): key and code to stage
 //   start(self)                a new batch; self = this lane's centre slot or
@@ -1725,8 +1765,9 @@ __device__ __forceinline__ float4 staged_ion(const float4* cand, int j) {
 
 template <bool SYM, bool COUNT, bool KEYED, bool GATED, class Stage, class Start, class Accept, class Taken,
           class Finish>
-__device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, float4* cand, uint32_t* ccode, Stage stage,
-                                           Start start, Accept accept, Taken taken, Finish finish) {
+__device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, float4* cand, uint32_t* ccode, float4* sbox,
+                                                         Stage stage, Start start, Accept accept, Taken taken,
+                                                         Finish finish) {
   const Grid& g = a.g;
   const int lane = threadIdx.x & 31;
   const uint32_t lemask = (2u << lane) - 1u;
@@ -1792,13 +1833,58 @@ __device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, floa
         }
         if (mc == 0) break;
         const float4 cp = start(self);
-        const uint32_t live = __ballot_sync(FULL, cp.x != kInf());
-        if (live) self = (cp.x != kInf()) ? self : 0xffffffffu;
+        const bool lv = cp.x != kInf();
+        const uint32_t live = __ballot_sync(FULL, lv);
+        if (live) self = lv ? self : 0xffffffffu;
         const unsigned long long cxx = f2_pack(cp.x, cp.x), cyy = f2_pack(cp.y, cp.y), czz = f2_pack(cp.z, cp.z);
-        // ---- stencil rows of the block
+        {
+          // the live centres' bounding box (order-preserving keys: min and max
+          // are exact), kept in shared memory: sbox[0] low, sbox[1] high corner
+          const float blx = o2f(__reduce_min_sync(FULL, f2o(lv ? cp.x : kInf())));
+          const float bly = o2f(__reduce_min_sync(FULL, f2o(lv ? cp.y : kInf())));
+          const float blz = o2f(__reduce_min_sync(FULL, f2o(lv ? cp.z : kInf())));
+          const float bhx = o2f(__reduce_max_sync(FULL, f2o(lv ? cp.x : -kInf())));
+          const float bhy = o2f(__reduce_max_sync(FULL, f2o(lv ? cp.y : -kInf())));
+          const float bhz = o2f(__reduce_max_sync(FULL, f2o(lv ? cp.z : -kInf())));
+          if (lane == 0) {
+            sbox[0] = make_float4(blx, bly, blz, 0.f);
+            sbox[1] = make_float4(bhx, bhy, bhz, 0.f);
+          }
+          __syncwarp();
+        }
+        auto put = [&](uint32_t p, const float4& q, uint32_t key, uint32_t code) {
+          float* f = (float*)cand + (p >> 1) * 8 + (p & 1);
+          f[0] = q.x;
+          f[2] = q.y;
+          f[4] = q.z;
+          f[6] = __uint_as_float(key);
+          ccode[p] = code;
+        };
+        uint32_t fill = 0;  // staged ions waiting for a batch of tests (warp-uniform)
+        // the tests of the first nb staged ions (the rest of the buffer holds ions at infinity)
+        auto run_batch = [&](uint32_t nb) {
+          if (lane >= nb) put(lane, make_float4(kInf(), kInf(), kInf(), 0.f), 0u, 0u);  // no lane takes these
+          __syncwarp();
+          tests += (unsigned long long)__popc(live) * nb;
+          uint32_t tm = 0, nin = 0;
+#pragma unroll
+          for (int j = 0; j < 32; j += 2) {
+            const float4 c0 = cand[j], c1 = cand[j + 1];
+            float d0, d1;
+            dist2_x2(cxx, cyy, czz, f2_pack(c0.x, c0.y), f2_pack(c0.z, c0.w), f2_pack(c1.x, c1.y), d0, d1);
+            const uint32_t k0 = __float_as_uint(c1.z), k1 = __float_as_uint(c1.w);
+            const bool in0 = (d0 <= R2) && (!KEYED || (SYM ? (k0 > self) : (k0 != self)));
+            const bool in1 = (d1 <= R2) && (!KEYED || (SYM ? (k1 > self) : (k1 != self)));
+            if (COUNT) nin += (in0 ? 1u : 0u) + (in1 ? 1u : 0u);
+            tm |= ((GATED || in0) && accept(j, d0, k0)) ? (1u << j) : 0u;
+            tm |= ((GATED || in1) && accept(j + 1, d1, k1)) ? (2u << j) : 0u;
+          }
+          taken(tm, nin, cxx, cyy, czz);
+          __syncwarp();
+        };
         for (int r0 = 0; r0 < nrows && live; r0 += 32) {
           uint32_t st, len;
-          block_row_range(a, r0 + lane, nrows, sr, xb, xe, yb, ye, zb, ze, SYM, st, len);
+          block_row_range(a, r0 + lane, nrows, sr, xb, xe, yb, ye, zb, ze, SYM, sbox, st, len);
           const uint32_t ne = __ballot_sync(FULL, len > 0);
           const int cnt_rows = __popc(ne);
           if (cnt_rows == 0) continue;
@@ -1816,8 +1902,6 @@ __device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, floa
           const uint32_t total = __shfl_sync(FULL, inc, 31);
           int before = 0;
           for (uint32_t bb = 0; bb < total; bb += 32) {
-            tests += (unsigned long long)__popc(live) * min(32u, total - bb);
-            // stage 32 ions; past the end an ion at infinity, which no lane takes
             const uint32_t bitv = (lane < cnt_rows && rlen > 0 && exc >= bb && exc < bb + 32) ? (1u << (exc - bb)) : 0u;
             const uint32_t smask = __reduce_or_sync(FULL, bitv);
             const int row = before + __popc(smask & lemask) - 1;
@@ -1826,40 +1910,47 @@ __device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, floa
             const uint32_t rs = __shfl_sync(FULL, rst, rowc);
             const uint32_t rp = __shfl_sync(FULL, exc, rowc);
             const uint32_t t = bb + lane;
-            float4 q = make_float4(kInf(), kInf(), kInf(), 0.f);
-            uint32_t key = 0u, code = 0u;
+            bool keep = false;
+            uint32_t slot = 0;
+            float4 q;
             if (t < total) {
-              const uint32_t slot = rs + (t - rp);
+              slot = rs + (t - rp);
               q = __ldg(a.ions + slot);
-              stage(slot, q, key, code);
+              const float4 lo = sbox[0], hi = sbox[1];
+              const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, q.x), __fsub_rn(q.x, hi.x)), 0.f);
+              const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, q.y), __fsub_rn(q.y, hi.y)), 0.f);
+              const float gz = fmaxf(fmaxf(__fsub_rn(lo.z, q.z), __fsub_rn(q.z, hi.z)), 0.f);
+              const float bd = __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
+              keep = a.no_box_filter || bd <= a.box_R2;
             }
-            {
-              float* f = (float*)cand + (lane >> 1) * 8 + (lane & 1);
-              f[0] = q.x;
-              f[2] = q.y;
-              f[4] = q.z;
-              f[6] = __uint_as_float(key);
+            const uint32_t km = __ballot_sync(FULL, keep);
+            const uint32_t at = fill + (uint32_t)__popc(km & (lemask >> 1));
+            uint32_t over = 0xffffffffu;
+            if (keep) {
+              if (at < 32u) {
+                uint32_t key, code;
+                stage(slot, q, key, code);
+                put(at, q, key, code);
+              } else {
+                over = slot;
+              }
             }
-            ccode[lane] = code;
-            __syncwarp();
-            // ---- every lane tests the 32 staged ions against its centre, two at a time
-            uint32_t tm = 0, nin = 0;
-#pragma unroll
-            for (int j = 0; j < 32; j += 2) {
-              const float4 c0 = cand[j], c1 = cand[j + 1];
-              float d0, d1;
-              dist2_x2(cxx, cyy, czz, f2_pack(c0.x, c0.y), f2_pack(c0.z, c0.w), f2_pack(c1.x, c1.y), d0, d1);
-              const uint32_t k0 = __float_as_uint(c1.z), k1 = __float_as_uint(c1.w);
-              const bool in0 = (d0 <= R2) && (!KEYED || (SYM ? (k0 > self) : (k0 != self)));
-              const bool in1 = (d1 <= R2) && (!KEYED || (SYM ? (k1 > self) : (k1 != self)));
-              if (COUNT) nin += (in0 ? 1u : 0u) + (in1 ? 1u : 0u);
-              tm |= ((GATED || in0) && accept(j, d0, k0)) ? (1u << j) : 0u;
-              tm |= ((GATED || in1) && accept(j + 1, d1, k1)) ? (2u << j) : 0u;
+            fill += (uint32_t)__popc(km);
+            if (fill >= 32u) {
+              run_batch(32u);
+              fill -= 32u;
+              const uint32_t om = __ballot_sync(FULL, over != 0xffffffffu);
+              if (over != 0xffffffffu) {
+                const float4 qo = __ldg(a.ions + over);
+                uint32_t key, code;
+                stage(over, qo, key, code);
+                put((uint32_t)__popc(om & (lemask >> 1)), qo, key, code);
+              }
+              __syncwarp();
             }
-            taken(tm, nin, cxx, cyy, czz);
-            __syncwarp();
           }
         }
+        if (fill > 0u) run_batch(fill);
         finish(live);
         __syncwarp();
       }
@@ -1874,10 +1965,15 @@ __device__ __forceinline__ unsigned long long lanes_walk(const ScanArgs& a, floa
 // bin lookup and the histogram atomics run for in-ball pairs only.  In
 // symmetric mode a staged ion carries key = its slot when it is a centre and
 // 0xffffffff otherwise, and a pair of two centres is taken by the lower slot
-// and credited to both.
+// and credited to both.  SMEM (bins in shared memory, fewer than 2^16 of
+// them): the staged ion's code and the lane's centre info hold ready bin
+// offsets, 16 bits each -- code: env offset (its env slot * H) | its centre
+// base (centre slot * nE * H) << 16; info: centre base | env offset << 16;
+// 0xffff for none, 0xfffe for a centre without a slot -- so a pair's bin is
+// two additions away from its category.
 constexpr int kLanesWarps = 16;  // warps per block of k_lanes
 
-template <bool SYM>
+template <bool SYM, bool SMEM>
 __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
   constexpr int NW = kLanesWarps;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1887,36 +1983,45 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
   unsigned long long* since_flush = (unsigned long long*)sp; sp += 16;
   float4* candA = (float4*)sp; sp += NW * 32 * 16;
   float4* cposA = (float4*)sp; sp += NW * 32 * 16;
+  float4* boxA = (float4*)sp; sp += NW * 2 * 16;
   uint32_t* ccodeA = (uint32_t*)sp; sp += NW * 32 * 4;
   uint32_t* cinfoA = (uint32_t*)sp; sp += NW * 32 * 4;
   uint16_t* plistA = (uint16_t*)sp; sp += NW * 1024 * 2;
   float* sT = (float*)sp; sp += ((H + 3) & ~3) * 4;
-  uint32_t* srdf = (uint32_t*)sp; sp += (a.rdf_in_smem ? (size_t)a.nC * a.nE * H * 4 : 0);
+  uint32_t* srdf = (uint32_t*)sp; sp += (SMEM ? (size_t)a.nC * a.nE * H * 4 : 0);
   uint16_t* slut = (uint16_t*)sp; sp += ((a.lut_n + 7) & ~7) * 2;
   int8_t* scs = (int8_t*)sp; sp += 256;
   int8_t* ses = (int8_t*)sp;
   for (int i = threadIdx.x; i < H; i += blockDim.x) sT[i] = a.cat_T[i];
   for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) slut[i] = a.cat_lut[i];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) { scs[i] = a.cslot_of[i]; ses[i] = a.eslot_of[i]; }
-  if (a.rdf_in_smem) for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) srdf[i] = 0;
+  if (SMEM) for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) srdf[i] = 0;
   if (threadIdx.x == 0) *since_flush = 0ull;
   __syncthreads();
 
   float4* cand = candA + warp * 32;
   float4* cpos = cposA + warp * 32;        // centre of lane c
   uint32_t* ccode = ccodeA + warp * 32;
-  uint32_t* cinfo = cinfoA + warp * 32;    // lane c: centre slot * nE | (env slot + 1) << 16
+  uint32_t* cinfo = cinfoA + warp * 32;    // lane c: centre slot * nE | (env slot + 1) << 16, or SMEM's offsets
   uint16_t* plist = plistA + warp * 1024;  // the staged batch's pairs, (lane << 5) | staged index
   unsigned long long pairs_lane = 0, centres = 0;
   constexpr unsigned long long FLUSH = 1ull << 30;
   uint32_t inb = 0;
 
+  const uint32_t cH = (uint32_t)a.nE * (uint32_t)H;  // bins of one centre slot
   auto stage = [&](uint32_t slot, const float4& q, uint32_t& key, uint32_t& code) {
-    // (env slot + 1) | (centre slot + 1) << 8 | is-centre << 16
     const uint32_t m = a.labels ? (uint32_t)a.labels[slot] : __float_as_uint(q.w);
     const bool jc = SYM && a.cflag[slot] != 0;
     key = SYM ? (jc ? slot : 0xffffffffu) : slot;
-    code = (uint32_t)(ses[m & 255] + 1) | (jc ? ((uint32_t)(scs[m & 255] + 1) << 8) | 0x10000u : 0u);
+    const int es = ses[m & 255];
+    if constexpr (SMEM) {
+      const int cs = scs[m & 255];
+      const uint32_t cb = !jc ? 0xffffu : (cs < 0 ? 0xfffeu : (uint32_t)cs * cH);
+      code = (es < 0 ? 0xffffu : (uint32_t)es * (uint32_t)H) | (cb << 16);
+    } else {
+      // (env slot + 1) | (centre slot + 1) << 8 | is-centre << 16
+      code = (uint32_t)(es + 1) | (jc ? ((uint32_t)(scs[m & 255] + 1) << 8) | 0x10000u : 0u);
+    }
   };
   auto start = [&](uint32_t self) {
     float4 cp = make_float4(kInf(), kInf(), kInf(), 0.f);
@@ -1932,7 +2037,10 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
       }
     }
     cpos[lane] = cp;
-    cinfo[lane] = (uint32_t)(cs < 0 ? 0 : cs) * (uint32_t)a.nE | ((uint32_t)(es + 1) << 16);
+    if constexpr (SMEM)
+      cinfo[lane] = (uint32_t)(cs < 0 ? 0 : cs) * cH | ((es < 0 ? 0xffffu : (uint32_t)es * (uint32_t)H) << 16);
+    else
+      cinfo[lane] = (uint32_t)(cs < 0 ? 0 : cs) * (uint32_t)a.nE | ((uint32_t)(es + 1) << 16);
     inb = 0;
     return cp;
   };
@@ -1942,22 +2050,23 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
     const float4 q = staged_ion(cand, j);
     const float d2 = dist2(p.x, p.y, p.z, q.x, q.y, q.z);
     const uint32_t cj = ccode[j], ci = cinfo[c];
-    const int cat = category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
-    const int esj = (int)(cj & 255u) - 1;
-    if (esj >= 0) {
-      const uint32_t idx = ((ci & 0xffffu) + (uint32_t)esj) * (uint32_t)H + (uint32_t)cat;
-      if (a.rdf_in_smem) atomicAdd(&srdf[idx], 1u);
-      else atomicAdd(&a.rdf_core[idx], 1ull);
-    }
-    if (SYM && (cj & 0x10000u)) {
-      // the same pair seen from the staged ion, a centre too
-      ++inb;
-      const int csj = (int)((cj >> 8) & 255u) - 1;
-      const int esc = (int)(ci >> 16) - 1;
-      if (esc >= 0 && csj >= 0) {
-        const uint32_t idx = ((uint32_t)csj * a.nE + (uint32_t)esc) * (uint32_t)H + (uint32_t)cat;
-        if (a.rdf_in_smem) atomicAdd(&srdf[idx], 1u);
-        else atomicAdd(&a.rdf_core[idx], 1ull);
+    const uint32_t cat = (uint32_t)category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+    if constexpr (SMEM) {
+      if ((cj & 0xffffu) != 0xffffu) atomicAdd(&srdf[(ci & 0xffffu) + (cj & 0xffffu) + cat], 1u);
+      if (SYM && (cj >> 16) != 0xffffu) {
+        // the same pair seen from the staged ion, a centre too
+        ++inb;
+        if ((cj >> 16) != 0xfffeu && (ci >> 16) != 0xffffu) atomicAdd(&srdf[(cj >> 16) + (ci >> 16) + cat], 1u);
+      }
+    } else {
+      const int esj = (int)(cj & 255u) - 1;
+      if (esj >= 0) atomicAdd(&a.rdf_core[((ci & 0xffffu) + (uint32_t)esj) * (uint32_t)H + cat], 1ull);
+      if (SYM && (cj & 0x10000u)) {
+        ++inb;
+        const int csj = (int)((cj >> 8) & 255u) - 1;
+        const int esc = (int)(ci >> 16) - 1;
+        if (esc >= 0 && csj >= 0)
+          atomicAdd(&a.rdf_core[((uint32_t)csj * a.nE + (uint32_t)esc) * (uint32_t)H + cat], 1ull);
       }
     }
   };
@@ -1988,7 +2097,7 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
   auto finish = [&](uint32_t live) {
     pairs_lane += inb;
     if (lane == 0) centres += (unsigned long long)__popc(live);
-    if (a.rdf_in_smem) {
+    if (SMEM) {
       // keep every shared bin below 2^32 (see k_scan)
       uint32_t tot = inb;
       for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
@@ -2004,7 +2113,7 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
     }
   };
   auto accept = [](int, float, uint32_t) { return true; };
-  const unsigned long long tests = lanes_walk<SYM, false, true, false>(a, cand, ccode, stage, start, accept, taken, finish);
+  const unsigned long long tests = lanes_walk<SYM, false, true, false>(a, cand, ccode, boxA + warp * 2, stage, start, accept, taken, finish);
   if (lane == 0 && a.tests) atomicAdd(a.tests, tests);
 
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
@@ -2013,7 +2122,7 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
     atomicAdd(&a.counters[1], centres);
   }
   __syncthreads();
-  if (a.rdf_in_smem) {
+  if (SMEM) {
     for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) {
       const uint32_t v = srdf[i];
       if (v) atomicAdd(&a.rdf_core[i], (unsigned long long)v);
@@ -2064,6 +2173,7 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
   const int frows = CAT ? EM + 1 : EM * K + 1;
   unsigned char* sp = smem;
   float4* candA = (float4*)sp; sp += NW * 32 * 16;
+  float4* boxA = (float4*)sp; sp += NW * 2 * 16;
   uint32_t* ccodeA = (uint32_t*)sp; sp += NW * 32 * 4;
   float* listA = (float*)sp; sp += (size_t)NW * frows * 32 * 4;
   uint16_t* catA = (uint16_t*)sp; sp += CAT ? (((size_t)NW * EM * K * 32 * 2 + 15) & ~size_t(15)) : 0;
@@ -2225,7 +2335,7 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
       }
     }
   };
-  const unsigned long long tests = lanes_walk<false, true, false, true>(a, cand, ccode, stage, start, accept, taken, finish);
+  const unsigned long long tests = lanes_walk<false, true, false, true>(a, cand, ccode, boxA + warp * 2, stage, start, accept, taken, finish);
   if (lane == 0 && a.tests) atomicAdd(a.tests, tests);
 
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
@@ -3147,7 +3257,7 @@ int launch_brick(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cud
 
 size_t lanes_smem(const ScanArgs& a) {
   constexpr int NW = kLanesWarps;
-  size_t b = 16 + 2 * NW * 32 * 16 + 2 * NW * 32 * 4 + NW * 1024 * 2 + (size_t)((a.H + 3) & ~3) * 4;
+  size_t b = 16 + 2 * NW * 32 * 16 + NW * 2 * 16 + 2 * NW * 32 * 4 + NW * 1024 * 2 + (size_t)((a.H + 3) & ~3) * 4;
   if (a.rdf_in_smem) b += (size_t)a.nC * a.nE * a.H * 4;
   b += (size_t)((a.lut_n + 7) & ~7) * 2 + 512;
   return b;
@@ -3160,7 +3270,8 @@ int launch_lanes(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cud
   const size_t smem = lanes_smem(a);
   if (smem_used) *smem_used = smem;
   if (smem > 200 * 1024) return -3;
-  auto kern = a.sym ? k_lanes<true> : k_lanes<false>;
+  auto kern = a.sym ? (a.rdf_in_smem ? k_lanes<true, true> : k_lanes<true, false>)
+                    : (a.rdf_in_smem ? k_lanes<false, true> : k_lanes<false, false>);
   if (!allow_dynamic_smem((const void*)kern, smem))
     return -1;
   int per_sm = 0;
@@ -3177,7 +3288,7 @@ size_t lanes_knn_smem(const ScanArgs& a, bool cat) {
   const size_t em = a.emax > 1 ? a.emax : 1;
   const size_t frows = cat ? em + 1 : em * a.kmax + 1;
   const size_t crows = cat ? (((size_t)NW * em * a.kmax * 32 * 2 + 15) & ~size_t(15)) : 0;
-  return NW * 32 * 16 + NW * 32 * 4 + (size_t)NW * frows * 32 * 4 + crows + (size_t)((a.H + 3) & ~3) * 4 +
+  return NW * 32 * 16 + NW * 2 * 16 + NW * 32 * 4 + (size_t)NW * frows * 32 * 4 + crows + (size_t)((a.H + 3) & ~3) * 4 +
          (size_t)((a.lut_n + 7) & ~7) * 2 + 256 + 256 * 4;
 }
 

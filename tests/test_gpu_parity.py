@@ -506,6 +506,50 @@ def test_lanes_knn_scan(ctx, oracle, block, ratio, with_rdf):
     assert kernel == ("k_lanes+k_lanes_knn" if with_rdf else "k_lanes_knn")
 
 
+@pytest.mark.parametrize("shift", [0.0, 4096.0])
+@pytest.mark.parametrize("block", [(1, 1, 1), (4, 2, 2), (4, 4, 4)])
+def test_lanes_box_filter(ctx, oracle, shift, block):
+    """The centre-per-lane scans drop candidates beyond R of the bounding box of
+    a batch's centres and trim stencil rows to that box: RDF (symmetric and
+    one-sided) and kNN bins and pair counts are the same with the filter off,
+    and equal the oracle's, on a cloud far from the origin too (coarser float
+    spacing); the filter leaves fewer distance tests."""
+    spec = synth.cone_specimen(n=40000, r_apex=8.0, half_angle_deg=10.0, length=14.0, n_clusters=20,
+                               members=40, nspecies=3, seed=83, nseg=64, stack=4.0)
+    off = np.array([shift, -0.5 * shift, 0.25 * shift], dtype=np.float32)
+    xyz = (spec.xyz + off).astype(np.float32)
+    hull = (spec.hull.reshape(-1, 3) + off).astype(np.float32).reshape(spec.hull.shape)
+    cid = ctx.upload(xyz, spec.labels)
+    ctx.hull(cid, hull, 2.0)
+    ctx.tuning(cid, 4.0, LANES(*block))
+    surf = oracle.surface_distance(xyz, hull, 2.0)
+    types = [1, 2, 3]
+    trg = [[a] for a in types for b in types]
+    env = [[b] for a in types for b in types]
+    ctx.tasks(trg, env)
+    cases = [(N.PP_RDF | N.PP_RIPK, [], (0.0, 0.01, 1.2), 1), (N.PP_RDF, [], (0.05, 0.02, 1.1), 0),
+             (N.PP_1NN | N.PP_MKNN, [9, 4, 1], (0.0, 0.005, 1.2), 1)]
+    try:
+        for flags, ks, hist, sym in cases:
+            ctx.hist(*hist)
+            ctx.set_option("symmetric", sym)
+            out = {}
+            for box in (1, 0):
+                ctx.set_option("box_filter", box)
+                ctx.run(cid, flags, ks)
+                out[box] = (ctx.fetch(), ctx.stats(), ctx.run_tests(), ctx.last_kernel())
+            ref = oracle.spatstat(xyz, spec.labels, surf, *hist, flags, trg, env, ks)
+            (b1, s1, t1, k1), (b0, s0, t0, k0) = out[1], out[0]
+            assert k1 == k0 and k1.startswith("k_lanes")
+            assert s1["pairs"] == s0["pairs"] == ref["pairs"] and s1["centres"] == ref["centres"]
+            assert np.array_equal(b1, ref["bins"]) and np.array_equal(b0, ref["bins"])
+            assert t1 < t0
+    finally:
+        ctx.set_option("box_filter", 1)
+        ctx.set_option("symmetric", 1)
+    ctx.free(cid)
+
+
 @pytest.mark.parametrize("symmetric", [1, 0])
 def test_combined_pass_split_with_overlapping_sets(ctx, oracle, symmetric):
     """RDF/RIPK with kNN on a cloud tuned to a cell block, overlapping
