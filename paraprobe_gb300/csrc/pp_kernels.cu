@@ -2319,19 +2319,33 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     if (lane == 0) centres += (unsigned long long)__popc(live);
     // every live centre met itself once in the in-ball count (d^2 = 0)
     pairs_lane += inb - (me != 0xffffffffu ? 1u : 0u);
-    // the k-th smallest d^2 (category) of each set -> its bin (or the miss bin)
+    // the k-th smallest d^2 (category) of each set -> its bin (or the miss
+    // bin); with KB, a set's categories are found first (independent loads)
+    // and added after
     for (int p = 0; p < nset; ++p) {
       const int Sg = a.set_list[cs * 32 + p];
-      for (int kk = 0; kk < a.nkI; ++kk) {
-        int cat;
+      unsigned long long* core = a.knn_core + ((uint64_t)cs * a.nS + Sg) * a.nkI * H;
+      auto cat_of = [&](int kk) {
         if constexpr (CAT) {
           const int v = C[(p * K + K - a.kvals[kk]) * 32];
-          cat = (v == (int)CNONE) ? a.cat_miss : v;
+          return (v == (int)CNONE) ? a.cat_miss : v;
         } else {
           const float v = L[(p * K + K - a.kvals[kk]) * 32];
-          cat = (v == RUP) ? a.cat_miss : category_lut(v, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+          return (v == RUP) ? a.cat_miss : category_lut(v, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
         }
-        if (cat >= 0) atomicAdd(&a.knn_core[(((uint64_t)cs * a.nS + Sg) * a.nkI + kk) * H + cat], 1ull);
+      };
+      if constexpr (KB > 0) {
+        int cats[KB];
+#pragma unroll
+        for (int kk = 0; kk < KB; ++kk) cats[kk] = kk < a.nkI ? cat_of(kk) : -1;
+#pragma unroll
+        for (int kk = 0; kk < KB; ++kk)
+          if (cats[kk] >= 0) atomicAdd(&core[(uint64_t)kk * H + cats[kk]], 1ull);
+      } else {
+        for (int kk = 0; kk < a.nkI; ++kk) {
+          const int cat = cat_of(kk);
+          if (cat >= 0) atomicAdd(&core[(uint64_t)kk * H + cat], 1ull);
+        }
       }
     }
   };
