@@ -131,6 +131,7 @@ struct RunPlan {
   uint32_t npc_edge = 0;
   int lut_shift = 0;
   uint32_t lut_base = 0;
+  bool lut_one = false;            // one threshold step after the table is exact for every d^2 <= R^2
   int disjoint = 0;
   std::vector<int8_t> setidx;      // [nC][256]
 };
@@ -299,7 +300,7 @@ std::vector<float> threshold_table(const Tables& t) {
 // finest that keeps the table within max_cells, so a cell rarely spans more
 // than one threshold.
 void build_lut(const std::vector<float>& T, float r2, int max_cells, std::vector<uint16_t>& lut, int& shift,
-               uint32_t& base) {
+               uint32_t& base, bool* one_step = nullptr) {
   const int H = (int)T.size();
   auto bits = [](float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; };
   auto cat = [&](float d2) {
@@ -324,6 +325,14 @@ void build_lut(const std::vector<float>& T, float r2, int max_cells, std::vector
     float f;
     std::memcpy(&f, &u, 4);
     lut[c] = (uint16_t)cat(f);
+  }
+  if (one_step) {
+    // categories rise with d^2, so within cell c they run from lut[c] to at
+    // most lut[c + 1] (cell 0 also takes every d^2 below it: no positive
+    // threshold lies there); the last cell holds r2, and only d^2 <= r2 count
+    bool one = true;
+    for (int c = 0; c + 1 < n && one; ++c) one = lut[c + 1] <= lut[c] + 1;
+    *one_step = one && cat(std::max(r2, 0.f)) <= lut[n - 1] + 1;
   }
 }
 
@@ -652,7 +661,7 @@ int make_plan(pp_ctx* ctx, uint32_t flags, const uint32_t* k_list, int nk, RunPl
       }
   }
   P.catT = threshold_table(t);
-  build_lut(P.catT, t.rmax * t.rmax, 4096, P.lut, P.lut_shift, P.lut_base);
+  build_lut(P.catT, t.rmax * t.rmax, 4096, P.lut, P.lut_shift, P.lut_base, &P.lut_one);
   P.cat_miss = category_of_distance(t, (float)((double)t.rmax + kEpsilon));
   return PP_OK;
 }
@@ -730,6 +739,7 @@ void fill_scan_common(pp::ScanArgs& a, const Cloud& cl, const RunPlan& P, const 
   a.lut_n = (int)P.lut.size();
   a.lut_shift = P.lut_shift;
   a.lut_base = P.lut_base;
+  a.lut_one = P.lut_one ? 1 : 0;
   a.cat_miss = P.cat_miss;
   a.cslot_of = D.cslot;
   a.eslot_of = D.eslot;

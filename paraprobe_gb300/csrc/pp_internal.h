@@ -50,6 +50,7 @@ struct ScanArgs {
   const uint16_t* cat_lut;
   int lut_n, lut_shift;
   uint32_t lut_base;
+  int lut_one;                 // the cell's category plus at most one step is exact for d^2 <= R^2
   // brick scan: cells per brick, centres per warp batch, bricks to process;
   // the centre-per-lane scan takes blocks of bx x by x bz cells
   int bx, bcap;

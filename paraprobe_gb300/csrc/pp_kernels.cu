@@ -1987,12 +1987,12 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
   uint32_t* ccodeA = (uint32_t*)sp; sp += NW * 32 * 4;
   uint32_t* cinfoA = (uint32_t*)sp; sp += NW * 32 * 4;
   uint16_t* plistA = (uint16_t*)sp; sp += NW * 1024 * 2;
-  float* sT = (float*)sp; sp += ((H + 3) & ~3) * 4;
+  float* sT = (float*)sp; sp += ((H + 4) & ~3) * 4;  // H thresholds, then +inf
   uint32_t* srdf = (uint32_t*)sp; sp += (SMEM ? (size_t)a.nC * a.nE * H * 4 : 0);
   uint16_t* slut = (uint16_t*)sp; sp += ((a.lut_n + 7) & ~7) * 2;
   int8_t* scs = (int8_t*)sp; sp += 256;
   int8_t* ses = (int8_t*)sp;
-  for (int i = threadIdx.x; i < H; i += blockDim.x) sT[i] = a.cat_T[i];
+  for (int i = threadIdx.x; i <= H; i += blockDim.x) sT[i] = i < H ? a.cat_T[i] : kInf();
   for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) slut[i] = a.cat_lut[i];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) { scs[i] = a.cslot_of[i]; ses[i] = a.eslot_of[i]; }
   if (SMEM) for (int i = threadIdx.x; i < a.nC * a.nE * H; i += blockDim.x) srdf[i] = 0;
@@ -2050,7 +2050,16 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
     const float4 q = staged_ion(cand, j);
     const float d2 = dist2(p.x, p.y, p.z, q.x, q.y, q.z);
     const uint32_t cj = ccode[j], ci = cinfo[c];
-    const uint32_t cat = (uint32_t)category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+    uint32_t cat;
+    if (a.lut_one) {
+      // the table's cells hold at most one threshold below R^2: one step, no loop
+      int t = (int)(__float_as_uint(d2) >> a.lut_shift) - (int)a.lut_base;
+      t = t < 0 ? 0 : (t >= a.lut_n ? a.lut_n - 1 : t);
+      const uint32_t g = slut[t];
+      cat = g + (sT[g + 1] <= d2 ? 1u : 0u);
+    } else {
+      cat = (uint32_t)category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+    }
     if constexpr (SMEM) {
       if ((cj & 0xffffu) != 0xffffu) atomicAdd(&srdf[(ci & 0xffffu) + (cj & 0xffffu) + cat], 1u);
       if (SYM && (cj >> 16) != 0xffffu) {
@@ -3271,7 +3280,7 @@ int launch_brick(const ScanArgs& a, int kr, int sm_count, size_t* smem_used, cud
 
 size_t lanes_smem(const ScanArgs& a) {
   constexpr int NW = kLanesWarps;
-  size_t b = 16 + 2 * NW * 32 * 16 + NW * 2 * 16 + 2 * NW * 32 * 4 + NW * 1024 * 2 + (size_t)((a.H + 3) & ~3) * 4;
+  size_t b = 16 + 2 * NW * 32 * 16 + NW * 2 * 16 + 2 * NW * 32 * 4 + NW * 1024 * 2 + (size_t)((a.H + 4) & ~3) * 4;
   if (a.rdf_in_smem) b += (size_t)a.nC * a.nE * a.H * 4;
   b += (size_t)((a.lut_n + 7) & ~7) * 2 + 512;
   return b;

@@ -527,8 +527,11 @@ def test_lanes_box_filter(ctx, oracle, shift, block):
     trg = [[a] for a in types for b in types]
     env = [[b] for a in types for b in types]
     ctx.tasks(trg, env)
+    # 0.01 nm bins: every category-table cell holds at most one threshold and
+    # the RDF binning takes one step from the table; 0.001 nm bins: the
+    # general threshold walk
     cases = [(N.PP_RDF | N.PP_RIPK, [], (0.0, 0.01, 1.2), 1), (N.PP_RDF, [], (0.05, 0.02, 1.1), 0),
-             (N.PP_1NN | N.PP_MKNN, [9, 4, 1], (0.0, 0.005, 1.2), 1)]
+             (N.PP_RDF, [], (0.0, 0.001, 1.2), 1), (N.PP_1NN | N.PP_MKNN, [9, 4, 1], (0.0, 0.005, 1.2), 1)]
     try:
         for flags, ks, hist, sym in cases:
             ctx.hist(*hist)
