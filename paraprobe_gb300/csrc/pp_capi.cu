@@ -58,8 +58,32 @@ struct DevBuf {
   template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
+// Page-locked host staging (result downloads), grown on demand.
+struct PinBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  PinBuf() = default;
+  PinBuf(const PinBuf&) = delete;
+  PinBuf& operator=(const PinBuf&) = delete;
+  ~PinBuf() { release(); }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t b) {
+    if (b <= bytes && p) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMallocHost(&p, b);
+    if (e == cudaSuccess) bytes = b;
+    else p = nullptr;
+    return e;
+  }
+};
+
 struct Hull {
   std::vector<float> tri;  // ntri * 9
+  float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f};  // bounds of the vertices
   float carve = 2.0f;
   bool present = false;
 };
@@ -151,6 +175,7 @@ struct Result {
   cudaStream_t stream = nullptr;
   bool fetched = false;
   std::vector<unsigned long long> rdf_h, knn_h, cnt_h;
+  PinBuf stage;  // one download of status, cores and counters
 };
 
 }  // namespace
@@ -451,17 +476,8 @@ int ensure_tri_bins(pp_ctx* ctx, Cloud& cl, float rp, cudaStream_t s) {
   if (cl.tri_ok && cl.tri_grow >= rp + cl.tri_slack) return PP_OK;
   const std::vector<float>& tri = cl.hull.tri;
   const uint64_t nt = tri.size() / 9;
-  std::vector<float> box(6 * nt);
-  float glo[3] = {INFINITY, INFINITY, INFINITY}, ghi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (uint64_t t = 0; t < nt; ++t) {
-    const float* v = &tri[9 * t];
-    for (int k = 0; k < 3; ++k) {
-      const float l = std::fmin(std::fmin(v[k], v[3 + k]), v[6 + k]);
-      const float h = std::fmax(std::fmax(v[k], v[3 + k]), v[6 + k]);
-      box[6 * t + k] = l; box[6 * t + 3 + k] = h;
-      glo[k] = std::min(glo[k], l); ghi[k] = std::max(ghi[k], h);
-    }
-  }
+  // the hull's bounds were taken at upload; the boxes are built on the device
+  float glo[3] = {cl.hull.lo[0], cl.hull.lo[1], cl.hull.lo[2]}, ghi[3] = {cl.hull.hi[0], cl.hull.hi[1], cl.hull.hi[2]};
   const float slack = 1e-3f + 1e-5f * std::max({std::fabs(glo[0]), std::fabs(ghi[0]), std::fabs(glo[1]),
                                                  std::fabs(ghi[1]), std::fabs(glo[2]), std::fabs(ghi[2])});
   const float grow = rp + slack;
@@ -485,8 +501,8 @@ int ensure_tri_bins(pp_ctx* ctx, Cloud& cl, float rp, cudaStream_t s) {
   tg.ncells = (uint64_t)tg.nx * tg.ny * tg.nz;
   CK(cl.tri_dev.ensure(std::max<size_t>(tri.size(), 1) * 4));
   CK(cudaMemcpyAsync(cl.tri_dev.p, tri.data(), tri.size() * 4, cudaMemcpyHostToDevice, s));
-  CK(cl.tri_box.ensure(std::max<size_t>(box.size(), 1) * 4));
-  CK(cudaMemcpyAsync(cl.tri_box.p, box.data(), box.size() * 4, cudaMemcpyHostToDevice, s));
+  CK(cl.tri_box.ensure(std::max<size_t>(6 * nt, 1) * 4));
+  if (nt) pp::launch_tri_box(cl.tri_dev.as<float>(), nt, cl.tri_box.as<float>(), s);
   CK(cl.tcell_start.ensure((tg.ncells + 1) * 4));
   CK(ctx->tri_fill.ensure((tg.ncells + 1) * 4));
   const uint64_t tmp_elems = (tg.ncells + 1) / 2048 + 64;
@@ -504,7 +520,7 @@ int ensure_tri_bins(pp_ctx* ctx, Cloud& cl, float rp, cudaStream_t s) {
                               ctx->scan_tmp.as<uint32_t>(), tmp_elems * 4, &total, s);
   }
   if (brc) return fail(ctx, PP_ERR_CUDA, "triangle binning failed");
-  CK(cudaStreamSynchronize(s));  // host box vector dies here
+  CK(cudaStreamSynchronize(s));  // the triangles were copied from the cloud's host vector
   cl.tg = tg;
   cl.tri_grow = grow;
   cl.tri_slack = slack;
@@ -774,25 +790,31 @@ void finalize(const Result& R, int r, uint64_t* out) {
   const unsigned long long* knn = R.knn_h.empty() ? nullptr : R.knn_h.data() + (size_t)r * knn_sz;
   uint64_t o = 0;
   auto kidx = [&](uint32_t k) { return (int)(std::lower_bound(P.kvals.begin(), P.kvals.end(), k) - P.kvals.begin()); };
+  // a task's histogram is the sum of the per-type cores it covers: the cores
+  // are listed once per task, then added bin row by bin row
+  std::vector<const unsigned long long*> rows;
+  auto add_rows = [&]() {
+    uint64_t* dst = out + o;
+    std::fill(dst, dst + H, 0ull);
+    for (const unsigned long long* src : rows)
+      for (int b = 0; b < H; ++b) dst[b] += src[b];
+    o += (uint64_t)H;
+  };
   auto rdf_task = [&](int t) {
-    for (int b = 0; b < H; ++b) {
-      unsigned long long s = 0;
-      for (int c = 0; c < P.nC; ++c) {
-        if (!has_type(&R.trg[8 * t], P.ctype[c])) continue;
-        for (int e = 0; e < P.nE; ++e)
-          if (has_type(&R.env[8 * t], P.etype[e])) s += rdf[((size_t)c * P.nE + e) * H + b];
-      }
-      out[o++] = s;
+    rows.clear();
+    for (int c = 0; c < P.nC; ++c) {
+      if (!has_type(&R.trg[8 * t], P.ctype[c])) continue;
+      for (int e = 0; e < P.nE; ++e)
+        if (has_type(&R.env[8 * t], P.etype[e])) rows.push_back(rdf + ((size_t)c * P.nE + e) * H);
     }
+    add_rows();
   };
   auto knn_task = [&](int t, int ki) {
     const int Sg = P.task_set[t];
-    for (int b = 0; b < H; ++b) {
-      unsigned long long s = 0;
-      for (int c = 0; c < P.nC; ++c)
-        if (has_type(&R.trg[8 * t], P.ctype[c])) s += knn[(((size_t)c * P.nS + Sg) * P.kvals.size() + ki) * H + b];
-      out[o++] = s;
-    }
+    rows.clear();
+    for (int c = 0; c < P.nC; ++c)
+      if (has_type(&R.trg[8 * t], P.ctype[c])) rows.push_back(knn + (((size_t)c * P.nS + Sg) * P.kvals.size() + ki) * H);
+    add_rows();
   };
   if (P.flags & PP_RDF) for (int t = 0; t < nt; ++t) rdf_task(t);
   if (P.flags & PP_1NN) for (int t = 0; t < nt; ++t) knn_task(t, kidx(1));
@@ -816,23 +838,29 @@ int fetch_cores(pp_ctx* ctx) {
   Result& R = ctx->res;
   if (!R.valid) return fail(ctx, PP_ERR_STATE, "no run to fetch");
   if (R.fetched) return PP_OK;
+  const RunPlan& P = R.plan;
+  const size_t rdf_sz = (P.flags & (PP_RDF | PP_RIPK)) ? (size_t)P.nC * P.nE * P.H * R.nreal : 0;
+  const size_t knn_sz = P.kr ? (size_t)P.nC * P.nS * P.kvals.size() * P.H * R.nreal : 0;
+  const size_t cnt_sz = ((P.flags & PP_CNTNB) && !R.batched) ? (size_t)P.nC * P.nE * (P.cmax + 1) : 0;
+  const size_t ctr_sz = 2 * (size_t)R.nreal;
+  // everything through one page-locked buffer: [status pad] [counters] [rdf] [knn] [cnt]
+  CK(R.stage.ensure(8 * (1 + ctr_sz + rdf_sz + knn_sz + cnt_sz)));
+  unsigned long long* h = static_cast<unsigned long long*>(R.stage.p);
+  CK(cudaMemcpyAsync(h, R.status.p, 4, cudaMemcpyDeviceToHost, R.stream));
+  CK(cudaMemcpyAsync(h + 1, R.counters.p, 8 * ctr_sz, cudaMemcpyDeviceToHost, R.stream));
+  if (rdf_sz) CK(cudaMemcpyAsync(h + 1 + ctr_sz, R.rdf.p, 8 * rdf_sz, cudaMemcpyDeviceToHost, R.stream));
+  if (knn_sz) CK(cudaMemcpyAsync(h + 1 + ctr_sz + rdf_sz, R.knn.p, 8 * knn_sz, cudaMemcpyDeviceToHost, R.stream));
+  if (cnt_sz)
+    CK(cudaMemcpyAsync(h + 1 + ctr_sz + rdf_sz + knn_sz, R.cnt.p, 8 * cnt_sz, cudaMemcpyDeviceToHost, R.stream));
   CK(cudaStreamSynchronize(R.stream));
   int status = 0;
-  CK(cudaMemcpy(&status, R.status.p, 4, cudaMemcpyDeviceToHost));
-  const RunPlan& P = R.plan;
-  const size_t rdf_sz = (size_t)P.nC * P.nE * P.H * R.nreal;
-  const size_t knn_sz = (size_t)P.nC * P.nS * P.kvals.size() * P.H * R.nreal;
-  R.rdf_h.assign(rdf_sz, 0);
-  R.knn_h.assign(P.kr ? knn_sz : 0, 0);
-  if ((P.flags & (PP_RDF | PP_RIPK)) && rdf_sz) CK(cudaMemcpy(R.rdf_h.data(), R.rdf.p, rdf_sz * 8, cudaMemcpyDeviceToHost));
-  if (P.kr && knn_sz) CK(cudaMemcpy(R.knn_h.data(), R.knn.p, knn_sz * 8, cudaMemcpyDeviceToHost));
-  if ((P.flags & PP_CNTNB) && !R.batched) {
-    const size_t cs = (size_t)P.nC * P.nE * (P.cmax + 1);
-    R.cnt_h.assign(cs, 0);
-    CK(cudaMemcpy(R.cnt_h.data(), R.cnt.p, cs * 8, cudaMemcpyDeviceToHost));
-  }
-  R.counters_h.assign(2 * R.nreal, 0);
-  CK(cudaMemcpy(R.counters_h.data(), R.counters.p, 16 * R.nreal, cudaMemcpyDeviceToHost));
+  std::memcpy(&status, h, 4);
+  R.counters_h.assign(h + 1, h + 1 + ctr_sz);
+  // finalize indexes the RDF cores whenever the plan has RDF bins
+  R.rdf_h.assign((size_t)P.nC * P.nE * P.H * R.nreal, 0);
+  if (rdf_sz) std::memcpy(R.rdf_h.data(), h + 1 + ctr_sz, 8 * rdf_sz);
+  R.knn_h.assign(h + 1 + ctr_sz + rdf_sz, h + 1 + ctr_sz + rdf_sz + knn_sz);
+  if (cnt_sz) R.cnt_h.assign(h + 1 + ctr_sz + rdf_sz + knn_sz, h + 1 + ctr_sz + rdf_sz + knn_sz + cnt_sz);
   R.fetched = true;
   if (status & pp::ST_CNT_OVERFLOW) return fail(ctx, PP_ERR_OVERFLOW, "a neighbour count exceeded the CNTNB capacity");
   if (status & pp::ST_LIST_OVERFLOW) return fail(ctx, PP_ERR_OVERFLOW, "a pair list exceeded its allocation");
@@ -1049,6 +1077,15 @@ int pp_hull_upload(pp_ctx* ctx, int cloud, const float* tri, uint64_t ntri, floa
   c->hull.tri.assign(tri, tri + 9 * ntri);
   for (float v : c->hull.tri)
     if (!std::isfinite(v)) return fail(ctx, PP_ERR_INVALID, "hull has non-finite vertices");
+  float lo0 = INFINITY, lo1 = INFINITY, lo2 = INFINITY, hi0 = -INFINITY, hi1 = -INFINITY, hi2 = -INFINITY;
+  const float* v = c->hull.tri.data();
+  for (uint64_t i = 0; i < 3 * ntri; ++i) {
+    lo0 = std::fmin(lo0, v[3 * i]); hi0 = std::fmax(hi0, v[3 * i]);
+    lo1 = std::fmin(lo1, v[3 * i + 1]); hi1 = std::fmax(hi1, v[3 * i + 1]);
+    lo2 = std::fmin(lo2, v[3 * i + 2]); hi2 = std::fmax(hi2, v[3 * i + 2]);
+  }
+  c->hull.lo[0] = lo0; c->hull.lo[1] = lo1; c->hull.lo[2] = lo2;
+  c->hull.hi[0] = hi0; c->hull.hi[1] = hi1; c->hull.hi[2] = hi2;
   c->hull.carve = carve_radius;
   c->hull.present = ntri > 0;
   c->tri_ok = false;

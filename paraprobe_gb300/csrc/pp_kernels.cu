@@ -256,16 +256,21 @@ __global__ void k_u32_to_u64(const uint32_t* in, uint64_t n, unsigned long long*
 __global__ void k_scatter(const float* __restrict__ xyz, const uint8_t* __restrict__ label, uint64_t n,
                           const uint32_t* __restrict__ cell_of, const uint32_t* __restrict__ rank,
                           const uint32_t* __restrict__ cell_start, float4* __restrict__ ions,
-                          uint32_t* __restrict__ slot_of_id, uint32_t* __restrict__ id_of_slot,
-                          uint8_t* __restrict__ label_sorted) {
+                          uint32_t* __restrict__ slot_of_id, uint32_t* __restrict__ id_of_slot) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t slot = cell_start[cell_of[i]] + rank[i];
     const uint32_t lab = label[i];
     ions[slot] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], __uint_as_float(lab));
     slot_of_id[i] = slot;
     id_of_slot[slot] = (uint32_t)i;
-    label_sorted[slot] = (uint8_t)lab;
   }
+}
+
+// The labels in slot order from the records' fourth word: a coalesced pass
+// after the scatter, which thereby avoids a scattered one-byte store per ion.
+__global__ void k_labels_of_ions(const float4* __restrict__ ions, uint64_t n, uint8_t* __restrict__ label_sorted) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    label_sorted[i] = (uint8_t)__float_as_uint(ions[i].w);
 }
 
 // label sets given in input order -> sorted-slot order, nsets arrays at once
@@ -3018,8 +3023,9 @@ void launch_scatter(const float* xyz, const uint8_t* label, uint64_t n, const ui
                     const uint32_t* cell_start, float4* ions, uint32_t* slot_of_id, uint32_t* id_of_slot,
                     uint8_t* label_sorted, cudaStream_t s) {
   counted();
-  k_scatter<<<grid_for(n, 256), 256, 0, s>>>(xyz, label, n, cell_of, rank, cell_start, ions, slot_of_id, id_of_slot,
-                                             label_sorted);
+  k_scatter<<<grid_for(n, 256), 256, 0, s>>>(xyz, label, n, cell_of, rank, cell_start, ions, slot_of_id, id_of_slot);
+  counted();
+  k_labels_of_ions<<<grid_for(n, 256), 256, 0, s>>>(ions, n, label_sorted);
 }
 
 void launch_gather_labels(const uint8_t* src, const uint32_t* id_of_slot, uint64_t n, uint8_t* dst, int nsets,
