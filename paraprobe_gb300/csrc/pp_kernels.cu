@@ -489,30 +489,41 @@ __device__ __forceinline__ void tri_cell_range(const float* b, Grid tg, float gr
   }
 }
 
+// A warp per triangle, its lanes over the cells of the triangle's range (a
+// triangle reaches tens of cells; one thread walking them all left the list
+// fill latency-bound on its chain of returning atomics).
+__device__ __forceinline__ uint64_t tri_range_cell(const Grid& tg, const int* c0, const int* c1, uint32_t i) {
+  const uint32_t nx = (uint32_t)(c1[0] - c0[0] + 1), ny = (uint32_t)(c1[1] - c0[1] + 1);
+  const int x = c0[0] + (int)(i % nx), y = c0[1] + (int)((i / nx) % ny), z = c0[2] + (int)(i / (nx * ny));
+  return ((uint64_t)z * tg.ny + y) * tg.nx + x;
+}
+
 __global__ void k_tri_count(const float* __restrict__ tbox, uint64_t ntri, Grid tg, float grow,
                             uint32_t* __restrict__ cnt) {
-  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ntri; t += (uint64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t t = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; t < ntri; t += nw) {
     int c0[3], c1[3];
     tri_cell_range(tbox + 6 * t, tg, grow, c0, c1);
-    for (int z = c0[2]; z <= c1[2]; ++z)
-      for (int y = c0[1]; y <= c1[1]; ++y)
-        for (int x = c0[0]; x <= c1[0]; ++x) atomicAdd(&cnt[((uint64_t)z * tg.ny + y) * tg.nx + x], 1u);
+    const uint32_t m = (uint32_t)(c1[0] - c0[0] + 1) * (uint32_t)(c1[1] - c0[1] + 1) * (uint32_t)(c1[2] - c0[2] + 1);
+    for (uint32_t i = lane; i < m; i += 32) atomicAdd(&cnt[tri_range_cell(tg, c0, c1, i)], 1u);
   }
 }
 
 __global__ void k_tri_fill(const float* __restrict__ tbox, uint64_t ntri, Grid tg, float grow,
                            uint32_t* __restrict__ fill, uint32_t* __restrict__ list, uint64_t cap,
                            int* __restrict__ status) {
-  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ntri; t += (uint64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t t = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; t < ntri; t += nw) {
     int c0[3], c1[3];
     tri_cell_range(tbox + 6 * t, tg, grow, c0, c1);
-    for (int z = c0[2]; z <= c1[2]; ++z)
-      for (int y = c0[1]; y <= c1[1]; ++y)
-        for (int x = c0[0]; x <= c1[0]; ++x) {
-          const uint32_t at = atomicAdd(&fill[((uint64_t)z * tg.ny + y) * tg.nx + x], 1u);
-          if (at < cap) list[at] = (uint32_t)t;
-          else if (status) atomicOr(status, ST_LIST_OVERFLOW);
-        }
+    const uint32_t m = (uint32_t)(c1[0] - c0[0] + 1) * (uint32_t)(c1[1] - c0[1] + 1) * (uint32_t)(c1[2] - c0[2] + 1);
+    for (uint32_t i = lane; i < m; i += 32) {
+      const uint32_t at = atomicAdd(&fill[tri_range_cell(tg, c0, c1, i)], 1u);
+      if (at < cap) list[at] = (uint32_t)t;
+      else if (status) atomicOr(status, ST_LIST_OVERFLOW);
+    }
   }
 }
 
@@ -3094,7 +3105,7 @@ int launch_tri_bins(const float* tbox, uint64_t ntri, Grid tg, float grow, uint3
                     uint64_t* total_out, cudaStream_t s) {
   if (cudaMemsetAsync(tstart, 0, (tg.ncells + 1) * 4, s) != cudaSuccess) return -1;
   counted();
-  k_tri_count<<<grid_for(ntri, 128), 128, 0, s>>>(tbox, ntri, tg, grow, tstart);
+  k_tri_count<<<grid_for(ntri * 32, 256), 256, 0, s>>>(tbox, ntri, tg, grow, tstart);
   excl_scan<uint32_t>(tstart, tg.ncells + 1, scan_tmp, scan_tmp_elems, s);
   uint32_t total = 0;
   if (cudaMemcpyAsync(&total, tstart + tg.ncells, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) return -1;
@@ -3103,7 +3114,7 @@ int launch_tri_bins(const float* tbox, uint64_t ntri, Grid tg, float grow, uint3
   if (total > list_cap) return 1;  // caller grows the list and calls again
   if (cudaMemcpyAsync(tfill, tstart, (tg.ncells + 1) * 4, cudaMemcpyDeviceToDevice, s) != cudaSuccess) return -1;
   counted();
-  k_tri_fill<<<grid_for(ntri, 128), 128, 0, s>>>(tbox, ntri, tg, grow, tfill, tlist, list_cap, nullptr);
+  k_tri_fill<<<grid_for(ntri * 32, 256), 256, 0, s>>>(tbox, ntri, tg, grow, tfill, tlist, list_cap, nullptr);
   return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
