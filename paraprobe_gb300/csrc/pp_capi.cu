@@ -119,7 +119,9 @@ struct Cloud {
   float surf_rp = -1.f;
   uint64_t surf_version = ~0ull;
   DevBuf tri_dev, tri_box, tcell_start, tcell_list;
-  Grid tg{};
+  Grid tg{};                    // hull grid: the ion grid coarsened tri_f times per axis
+  int tri_f = 1;
+  uint64_t tri_grid_version = ~0ull;
   float tri_grow = -1.f, tri_slack = 0.f;
   bool tri_ok = false;
 };
@@ -471,34 +473,39 @@ int ensure_grid(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s) {
 // Triangle boxes (fmin/fmax of the vertices, src/PARAPROBE_SolverHdl.cpp:
 // 2712-2717) and per-cell triangle lists of a hull grid.  A triangle is listed
 // in every cell its box grown by `grow` reaches, so the lists serve every
-// query radius R' with R' + slack <= grow.
+// query radius R' with R' + slack <= grow.  The hull grid is the cloud's ion
+// grid coarsened f times per axis (f ~ R' / h), so it is rebuilt with the ion
+// grid and the hull distance walks each hull cell's ions as whole rows.
 int ensure_tri_bins(pp_ctx* ctx, Cloud& cl, float rp, cudaStream_t s) {
-  if (cl.tri_ok && cl.tri_grow >= rp + cl.tri_slack) return PP_OK;
+  if (cl.tri_ok && cl.tri_grow >= rp + cl.tri_slack && cl.tri_grid_version == cl.grid_version) return PP_OK;
   const std::vector<float>& tri = cl.hull.tri;
   const uint64_t nt = tri.size() / 9;
   // the hull's bounds were taken at upload; the boxes are built on the device
   float glo[3] = {cl.hull.lo[0], cl.hull.lo[1], cl.hull.lo[2]}, ghi[3] = {cl.hull.hi[0], cl.hull.hi[1], cl.hull.hi[2]};
-  const float slack = 1e-3f + 1e-5f * std::max({std::fabs(glo[0]), std::fabs(ghi[0]), std::fabs(glo[1]),
-                                                 std::fabs(ghi[1]), std::fabs(glo[2]), std::fabs(ghi[2])});
+  // slack: float rounding of cell indices, of the hull's and of the ions'
+  // coordinates (the ion grid's margin)
+  const float slack = std::max(1e-3f + 1e-5f * std::max({std::fabs(glo[0]), std::fabs(ghi[0]), std::fabs(glo[1]),
+                                                         std::fabs(ghi[1]), std::fabs(glo[2]), std::fabs(ghi[2])}),
+                               cl.grid_ok ? 2.f * cl.g.margin : 0.f);
   const float grow = rp + slack;
-  if (cl.tri_ok && cl.tri_grow >= grow) return PP_OK;
+  if (cl.tri_ok && cl.tri_grow >= grow && cl.tri_grid_version == cl.grid_version) return PP_OK;
   if (ctx->readonly_clouds)
     return fail(ctx, PP_ERR_STATE, "hull lists were not prepared for R' = %g (pp_cloud_prepare)", (double)rp);
+  if (!cl.grid_ok) return fail(ctx, PP_ERR_STATE, "hull lists need the cloud's grid");
+  const Grid& g = cl.g;
+  int f = std::max(1, (int)std::lround((double)rp / (double)g.h));
+  auto hull_cells = [&](int ff) {
+    return (uint64_t)((g.nx + ff - 1) / ff) * (uint64_t)((g.ny + ff - 1) / ff) * (uint64_t)((g.nz + ff - 1) / ff);
+  };
+  while (hull_cells(f) >= 60000000ull) ++f;
   Grid tg{};
-  double h = std::max((double)rp, 0.25);
-  for (int k = 0; k < 3; ++k) { glo[k] -= grow + slack; ghi[k] += grow + slack; }
-  for (;;) {
-    double c = 1;
-    for (int k = 0; k < 3; ++k) c *= std::floor((ghi[k] - glo[k]) / h) + 1;
-    if (c < 6.0e7) break;
-    h *= 1.25;
-  }
-  tg.h = (float)h; tg.inv_h = (float)(1.0 / h);
-  tg.lox = glo[0]; tg.loy = glo[1]; tg.loz = glo[2];
-  tg.nx = (int)std::floor((ghi[0] - glo[0]) / h) + 1;
-  tg.ny = (int)std::floor((ghi[1] - glo[1]) / h) + 1;
-  tg.nz = (int)std::floor((ghi[2] - glo[2]) / h) + 1;
-  tg.ncells = (uint64_t)tg.nx * tg.ny * tg.nz;
+  tg.h = g.h * (float)f;
+  tg.inv_h = (float)(1.0 / ((double)g.h * f));
+  tg.lox = g.lox; tg.loy = g.loy; tg.loz = g.loz;
+  tg.nx = (g.nx + f - 1) / f;
+  tg.ny = (g.ny + f - 1) / f;
+  tg.nz = (g.nz + f - 1) / f;
+  tg.ncells = hull_cells(f);
   CK(cl.tri_dev.ensure(std::max<size_t>(tri.size(), 1) * 4));
   CK(cudaMemcpyAsync(cl.tri_dev.p, tri.data(), tri.size() * 4, cudaMemcpyHostToDevice, s));
   CK(cl.tri_box.ensure(std::max<size_t>(6 * nt, 1) * 4));
@@ -522,6 +529,8 @@ int ensure_tri_bins(pp_ctx* ctx, Cloud& cl, float rp, cudaStream_t s) {
   if (brc) return fail(ctx, PP_ERR_CUDA, "triangle binning failed");
   CK(cudaStreamSynchronize(s));  // the triangles were copied from the cloud's host vector
   cl.tg = tg;
+  cl.tri_f = f;
+  cl.tri_grid_version = cl.grid_version;
   cl.tri_grow = grow;
   cl.tri_slack = slack;
   cl.tri_ok = true;
@@ -558,8 +567,9 @@ int ensure_surface(pp_ctx* ctx, Cloud& cl, float R, cudaStream_t s, const float*
   } else {
     int rc = ensure_tri_bins(ctx, cl, rp, s);
     if (rc) return rc;
-    pp::launch_surface(cl.ions.as<float4>(), n, cl.tri_box.as<float>(), cl.tri_dev.as<float>(),
-                       cl.tcell_start.as<uint32_t>(), cl.tcell_list.as<uint32_t>(), cl.tg, rp, dst->as<float>(), s);
+    pp::launch_surface_cells(cl.ions.as<float4>(), cl.cell_start.as<uint32_t>(), cl.g, cl.tri_f,
+                             cl.tri_box.as<float>(), cl.tri_dev.as<float>(), cl.tcell_start.as<uint32_t>(),
+                             cl.tcell_list.as<uint32_t>(), cl.tg, rp, dst->as<float>(), s);
     CK(cudaGetLastError());
   }
   if (!ctx->readonly_clouds) {

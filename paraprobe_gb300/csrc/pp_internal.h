@@ -212,6 +212,9 @@ void launch_gather_labels(const uint8_t* src_by_id, const uint32_t* id_of_slot, 
                           uint8_t* dst_by_slot, int nsets, cudaStream_t s);
 void launch_permute_labels(const uint8_t* label_by_id, const uint32_t* perm, const uint32_t* id_of_slot,
                            uint64_t n, uint8_t* dst_by_slot, cudaStream_t s);
+void launch_surface_cells(const float4* ions, const uint32_t* cell_start, Grid g, int f, const float* tri_box,
+                          const float* tri, const uint32_t* tcs, const uint32_t* tct, Grid tg, float rprime,
+                          float* surf, cudaStream_t s);
 void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const float* tri,
                     const uint32_t* tcell_start, const uint32_t* tcell_tri, Grid tg, float rprime,
                     float* surf_d2, cudaStream_t s);

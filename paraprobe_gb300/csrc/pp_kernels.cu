@@ -378,6 +378,107 @@ __global__ void k_surface(const float4* __restrict__ ions, uint64_t n, const flo
   }
 }
 
+// ion2surf per sorted slot, one warp per hull cell: the hull grid `tg` is the
+// ion grid `g` coarsened f times per axis (same origin), so a hull cell's ions
+// are f x f row segments of consecutive slots.  The warp takes them 32 at a
+// time (rows concatenated); the cell's triangles are staged in shared memory
+// 32 at a time (box and vertices, loaded by the lanes together) and every
+// lane tests them against its own ion in list order -- the test, distance and
+// minimum of k_surface, without its chain of dependent global loads per
+// triangle and without lanes walking different lists.  The ion's hull cell
+// (its ion cell divided by f) lists every triangle whose box grown by
+// R' + slack reaches it: the two cell computations can only disagree within
+// float rounding of a boundary, which the slack covers.
+constexpr int kSurfWarps = 8;
+__global__ void __launch_bounds__(kSurfWarps * 32) k_surface_cells(const float4* __restrict__ ions,
+                                                              const uint32_t* __restrict__ cell_start, Grid g, int f,
+                                                              const float* __restrict__ tbox,
+                                                              const float* __restrict__ tri,
+                                                              const uint32_t* __restrict__ tstart,
+                                                              const uint32_t* __restrict__ tlist, Grid tg, float rp,
+                                                              float* __restrict__ out) {
+  // per staged triangle: box lo x,y,z, hi x,y,z, the 9 vertex coordinates, a pad (17 words: conflict-free stores)
+  __shared__ float stri[kSurfWarps][32][17];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float (*st)[17] = stri[warp];
+  const uint32_t lemask = (2u << lane) - 1u;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const float rp2 = __fmul_rn(rp, rp);
+  for (uint64_t tc = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; tc < tg.ncells; tc += nwarps) {
+    const int tx = (int)(tc % (uint64_t)tg.nx);
+    const uint64_t tr = tc / (uint64_t)tg.nx;
+    const int ty = (int)(tr % (uint64_t)tg.ny), tz = (int)(tr / (uint64_t)tg.ny);
+    const uint32_t k0 = tstart[tc], k1 = tstart[tc + 1];
+    const int x0 = tx * f, x1 = min(x0 + f, g.nx);
+    const int ny = min(f, g.ny - ty * f), nz = min(f, g.nz - tz * f);
+    const int nrows = ny * nz;
+    for (int r0 = 0; r0 < nrows; r0 += 32) {
+      // row r0 + lane: its slots; then the rows with ions, concatenated
+      uint32_t st0 = 0, len = 0;
+      if (r0 + lane < nrows) {
+        const int yy = ty * f + (r0 + lane) % ny, zz = tz * f + (r0 + lane) / ny;
+        const uint64_t rowb = ((uint64_t)zz * g.ny + yy) * g.nx;
+        st0 = cell_start[rowb + x0];
+        len = cell_start[rowb + x1] - st0;
+      }
+      const uint32_t ne = __ballot_sync(FULL, len > 0);
+      const int cnt_rows = __popc(ne);
+      if (cnt_rows == 0) continue;
+      const int src = lane < cnt_rows ? (int)__fns(ne, 0, lane + 1) : 0;
+      const uint32_t rst = __shfl_sync(FULL, st0, src);
+      uint32_t rlen = __shfl_sync(FULL, len, src);
+      if (lane >= cnt_rows) rlen = 0;
+      uint32_t inc = rlen;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc += t;
+      }
+      const uint32_t exc = inc - rlen;
+      const uint32_t total = __shfl_sync(FULL, inc, 31);
+      int before = 0;
+      for (uint32_t bb = 0; bb < total; bb += 32) {
+        const uint32_t bitv = (lane < cnt_rows && rlen > 0 && exc >= bb && exc < bb + 32) ? (1u << (exc - bb)) : 0u;
+        const uint32_t smask = __reduce_or_sync(FULL, bitv);
+        const int row = before + __popc(smask & lemask) - 1;
+        before += __popc(smask);
+        const int rowc = row < 0 ? 0 : (row > 31 ? 31 : row);
+        const uint32_t rs = __shfl_sync(FULL, rst, rowc);
+        const uint32_t rpos = __shfl_sync(FULL, exc, rowc);
+        const uint32_t t = bb + lane;
+        const bool have = t < total;
+        const uint32_t slot = rs + (t - rpos);
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (have) p = ions[slot];
+        float best = rp2;
+        const float lx = __fsub_rn(p.x, rp), ly = __fsub_rn(p.y, rp), lz = __fsub_rn(p.z, rp);
+        const float hx = __fadd_rn(p.x, rp), hy = __fadd_rn(p.y, rp), hz = __fadd_rn(p.z, rp);
+        for (uint32_t kb = k0; kb < k1; kb += 32) {
+          if (kb + lane < k1) {
+            const uint32_t tt = tlist[kb + lane];
+            const float* b = tbox + 6 * (uint64_t)tt;
+            const float* v = tri + 9 * (uint64_t)tt;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) st[lane][q] = b[q];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) st[lane][6 + q] = v[q];
+          }
+          __syncwarp();
+          const int m = (int)min(32u, k1 - kb);
+          for (int j = 0; j < m; ++j) {
+            const float* b = st[j];
+            if (!have || b[3] < lx || b[0] > hx || b[4] < ly || b[1] > hy || b[5] < lz || b[2] > hz) continue;
+            const float v = tri_dist2(b + 6, p.x, p.y, p.z);
+            if (!(v > best)) best = v;
+          }
+          __syncwarp();
+        }
+        if (have) out[slot] = best;
+      }
+    }
+  }
+}
+
 // Occupancy grid behind the RDF header: voxel of every ion as
 // threadmemory::rectangular_transfer computes it (src/PARAPROBE_SolverHdl.cpp:
 // 1471-1508): t = (p - lo) / w in float, voxel 1 + (size_t)t unless that
@@ -486,6 +587,8 @@ __device__ __forceinline__ void tri_cell_range(const float* b, Grid tg, float gr
     int hi = (int)floorf((b[3 + k] + grow - org[k]) * tg.inv_h);
     c0[k] = lo < 0 ? 0 : (lo >= nmax[k] ? nmax[k] - 1 : lo);
     c1[k] = hi < 0 ? 0 : (hi >= nmax[k] ? nmax[k] - 1 : hi);
+    // a grown box wholly beyond the grid (which covers every ion) reaches no ion
+    if (hi < 0 || lo >= nmax[k]) { c0[k] = 1; c1[k] = 0; }
   }
 }
 
@@ -3055,6 +3158,14 @@ void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const 
                     const uint32_t* tct, Grid tg, float rprime, float* surf, cudaStream_t s) {
   counted();
   k_surface<<<grid_for(n, 256), 256, 0, s>>>(ions, n, tri_box, tri, tcs, tct, tg, rprime, surf);
+}
+
+void launch_surface_cells(const float4* ions, const uint32_t* cell_start, Grid g, int f, const float* tri_box,
+                          const float* tri, const uint32_t* tcs, const uint32_t* tct, Grid tg, float rprime,
+                          float* surf, cudaStream_t s) {
+  counted();
+  k_surface_cells<<<grid_for(tg.ncells * 32, kSurfWarps * 32), kSurfWarps * 32, 0, s>>>(ions, cell_start, g, f, tri_box,
+                                                                                     tri, tcs, tct, tg, rprime, surf);
 }
 
 // number of cells holding at least one ion
