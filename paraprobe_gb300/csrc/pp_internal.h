@@ -215,9 +215,6 @@ void launch_permute_labels(const uint8_t* label_by_id, const uint32_t* perm, con
 void launch_surface_cells(const float4* ions, const uint32_t* cell_start, Grid g, int f, const float* tri_box,
                           const float* tri, const uint32_t* tcs, const uint32_t* tct, Grid tg, float rprime,
                           float* surf, cudaStream_t s);
-void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const float* tri,
-                    const uint32_t* tcell_start, const uint32_t* tcell_tri, Grid tg, float rprime,
-                    float* surf_d2, cudaStream_t s);
 // packed caller-order xyz in, ion2surf out in the same order (no cell sort)
 void launch_surface_xyz(const float* xyz, uint64_t n, const float* tbox, const float* tri, const uint32_t* tstart,
                         const uint32_t* tlist, Grid tg, float rp, float* out, cudaStream_t s);

@@ -4,7 +4,7 @@
 //  K1 k_cell_count / k_scan_* / k_scatter
 //                      uniform-grid counting sort: ions -> cell-sorted float4
 //                      records (x-fastest cells, so stencil rows are contiguous)
-//  K2 k_surface        squared ion-to-hull distance, same candidate test and
+//  K2 k_surface_cells  squared ion-to-hull distance, same candidate test and
 //                      float evaluation order as the reference
 //  K3 k_scan<KR,EMAX>  warp-per-centre scan of the trimmed cell stencil: RDF
 //                      bins in shared memory, kNN as register-resident sorted
@@ -351,41 +351,16 @@ __device__ float tri_dist2(const float* __restrict__ t, float px, float py, floa
 
 // ion2surf per sorted slot: R'^2, lowered to the smallest tri_dist2 over the
 // triangles whose float AABB overlaps [p - R', p + R'] (touching counts,
-// src/PARAPROBE_AABBTree.cpp:112-124).  Triangles are pre-binned (host) into
-// every cell of `tg` that their AABB grown by R' reaches.
-__global__ void k_surface(const float4* __restrict__ ions, uint64_t n, const float* __restrict__ tbox,
-                          const float* __restrict__ tri, const uint32_t* __restrict__ tstart,
-                          const uint32_t* __restrict__ tlist, Grid tg, float rp, float* __restrict__ out) {
-  const float rp2 = __fmul_rn(rp, rp);
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const float4 p = ions[i];
-    float best = rp2;
-    const int cx = (int)floorf((p.x - tg.lox) * tg.inv_h), cy = (int)floorf((p.y - tg.loy) * tg.inv_h),
-              cz = (int)floorf((p.z - tg.loz) * tg.inv_h);
-    if (cx >= 0 && cy >= 0 && cz >= 0 && cx < tg.nx && cy < tg.ny && cz < tg.nz) {
-      const uint64_t c = ((uint64_t)cz * tg.ny + cy) * tg.nx + cx;
-      const float lx = __fsub_rn(p.x, rp), ly = __fsub_rn(p.y, rp), lz = __fsub_rn(p.z, rp);
-      const float hx = __fadd_rn(p.x, rp), hy = __fadd_rn(p.y, rp), hz = __fadd_rn(p.z, rp);
-      for (uint32_t k = tstart[c]; k < tstart[c + 1]; ++k) {
-        const uint32_t t = tlist[k];
-        const float* b = tbox + 6 * (uint64_t)t;
-        if (b[3] < lx || b[0] > hx || b[4] < ly || b[1] > hy || b[5] < lz || b[2] > hz) continue;
-        const float v = tri_dist2(tri + 9 * (uint64_t)t, p.x, p.y, p.z);
-        if (!(v > best)) best = v;
-      }
-    }
-    out[i] = best;
-  }
-}
-
-// ion2surf per sorted slot, one warp per hull cell: the hull grid `tg` is the
+// src/PARAPROBE_AABBTree.cpp:112-124), in the order of the cell's list; every
+// triangle is listed in each hull cell its AABB grown by R' + slack reaches.
+// One warp per hull cell: the hull grid `tg` is the
 // ion grid `g` coarsened f times per axis (same origin), so a hull cell's ions
 // are f x f row segments of consecutive slots.  The warp takes them 32 at a
 // time (rows concatenated); the cell's triangles are staged in shared memory
 // 32 at a time (box and vertices, loaded by the lanes together) and every
-// lane tests them against its own ion in list order -- the test, distance and
-// minimum of k_surface, without its chain of dependent global loads per
-// triangle and without lanes walking different lists.  The ion's hull cell
+// lane tests them against its own ion in list order (an ion per thread
+// walking its own list took 25% longer: lanes of a warp span several hull
+// cells, and each triangle was a chain of dependent global loads).  The ion's hull cell
 // (its ion cell divided by f) lists every triangle whose box grown by
 // R' + slack reaches it: the two cell computations can only disagree within
 // float rounding of a boundary, which the slack covers.
@@ -505,7 +480,7 @@ __global__ void k_voxel_count(const float* __restrict__ xyz, uint64_t n, float l
 
 // Caller-order variant for the entry point without allocations: positions as
 // packed xyz triples and ion2surf written in the same order.  The candidate
-// test and the minimum are those of k_surface, so both give the same bits.
+// test and the minimum are those of k_surface_cells, so both give the same bits.
 __global__ void k_surface_xyz(const float* __restrict__ xyz, uint64_t n, const float* __restrict__ tbox,
                               const float* __restrict__ tri, const uint32_t* __restrict__ tstart,
                               const uint32_t* __restrict__ tlist, Grid tg, float rp, float* __restrict__ out) {
@@ -533,7 +508,7 @@ __global__ void k_surface_xyz(const float* __restrict__ xyz, uint64_t n, const f
 }
 
 // Triangle boxes on the device: per axis the smallest and largest vertex
-// coordinate (lo x,y,z then hi x,y,z), as the host builds them for k_surface.
+// coordinate (lo x,y,z then hi x,y,z), for the hull cell lists and distances.
 __global__ void k_tri_box(const float* __restrict__ tri, uint64_t ntri, float* __restrict__ box) {
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ntri; t += (uint64_t)gridDim.x * blockDim.x) {
     const float* v = tri + 9 * t;
@@ -3152,12 +3127,6 @@ void launch_permute_labels(const uint8_t* label_by_id, const uint32_t* perm, con
                            uint8_t* dst, cudaStream_t s) {
   counted();
   k_permute_labels<<<grid_for(n, 256), 256, 0, s>>>(label_by_id, perm, id_of_slot, n, dst);
-}
-
-void launch_surface(const float4* ions, uint64_t n, const float* tri_box, const float* tri, const uint32_t* tcs,
-                    const uint32_t* tct, Grid tg, float rprime, float* surf, cudaStream_t s) {
-  counted();
-  k_surface<<<grid_for(n, 256), 256, 0, s>>>(ions, n, tri_box, tri, tcs, tct, tg, rprime, surf);
 }
 
 void launch_surface_cells(const float4* ions, const uint32_t* cell_start, Grid g, int f, const float* tri_box,
