@@ -2412,9 +2412,9 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     while (tm) {
       const int j = __ffs(tm) - 1;
       tm &= tm - 1u;
-      if (ccode[j] == me) continue;  // the centre itself
       const float4 q = staged_ion(cand, j);
       const float d2 = dist2(cx, cy, cz, q.x, q.y, q.z);
+      if (d2 == 0.f && ccode[j] == me) continue;  // the centre itself
       insert(row_of(__float_as_uint(q.w)), d2);
     }
   };
