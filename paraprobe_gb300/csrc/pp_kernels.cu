@@ -360,10 +360,10 @@ __device__ float tri_dist2(const float* __restrict__ t, float px, float py, floa
 // 32 at a time (box and vertices, loaded by the lanes together) and every
 // lane tests them against its own ion in list order (an ion per thread
 // walking its own list took 25% longer: lanes of a warp span several hull
-// cells, and each triangle was a chain of dependent global loads).  The ion's hull cell
-// (its ion cell divided by f) lists every triangle whose box grown by
-// R' + slack reaches it: the two cell computations can only disagree within
-// float rounding of a boundary, which the slack covers.
+// cells, and each triangle was a chain of dependent global loads).  The ion's
+// hull cell (its ion cell divided by f) lists every triangle whose box grown
+// by R' + slack reaches it: the two cell computations can only disagree
+// within float rounding of a boundary, which the slack covers.
 constexpr int kSurfWarps = 8;
 __global__ void __launch_bounds__(kSurfWarps * 32) k_surface_cells(const float4* __restrict__ ions,
                                                               const uint32_t* __restrict__ cell_start, Grid g, int f,
@@ -372,7 +372,8 @@ __global__ void __launch_bounds__(kSurfWarps * 32) k_surface_cells(const float4*
                                                               const uint32_t* __restrict__ tstart,
                                                               const uint32_t* __restrict__ tlist, Grid tg, float rp,
                                                               float* __restrict__ out) {
-  // per staged triangle: box lo x,y,z, hi x,y,z, the 9 vertex coordinates, a pad (17 words: conflict-free stores)
+  // per staged triangle: box lo x,y,z, hi x,y,z, the 9 vertex coordinates and
+  // a pad (17 words: conflict-free stores)
   __shared__ float stri[kSurfWarps][32][17];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float (*st)[17] = stri[warp];
