@@ -2217,7 +2217,8 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
     }
   };
   auto accept = [](int, float, uint32_t) { return true; };
-  const unsigned long long tests = lanes_walk<SYM, false, true, false>(a, cand, ccode, boxA + warp * 2, stage, start, accept, taken, finish);
+  const unsigned long long tests =
+      lanes_walk<SYM, false, true, false>(a, cand, ccode, boxA + warp * 2, stage, start, accept, taken, finish);
   if (lane == 0 && a.tests) atomicAdd(a.tests, tests);
 
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
@@ -2453,7 +2454,8 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
       }
     }
   };
-  const unsigned long long tests = lanes_walk<false, true, false, true>(a, cand, ccode, boxA + warp * 2, stage, start, accept, taken, finish);
+  const unsigned long long tests =
+      lanes_walk<false, true, false, true>(a, cand, ccode, boxA + warp * 2, stage, start, accept, taken, finish);
   if (lane == 0 && a.tests) atomicAdd(a.tests, tests);
 
   for (int o = 16; o; o >>= 1) pairs_lane += __shfl_xor_sync(FULL, pairs_lane, o);
