@@ -1084,16 +1084,19 @@ int pp_cloud_labels(pp_ctx* ctx, int cloud, uint8_t* out, uint64_t n) {
 int pp_hull_upload(pp_ctx* ctx, int cloud, const float* tri, uint64_t ntri, float carve_radius) {
   Cloud* c = ctx ? get_cloud(ctx, cloud) : nullptr;
   if (!c || (ntri && !tri) || !(carve_radius >= 0.f)) return fail(ctx, PP_ERR_INVALID, "bad argument");
-  c->hull.tri.assign(tri, tri + 9 * ntri);
-  for (float v : c->hull.tri)
-    if (!std::isfinite(v)) return fail(ctx, PP_ERR_INVALID, "hull has non-finite vertices");
+  // one pass over the caller's vertices: all finite (else the cloud's hull is
+  // left as it was), and their bounds
   float lo0 = INFINITY, lo1 = INFINITY, lo2 = INFINITY, hi0 = -INFINITY, hi1 = -INFINITY, hi2 = -INFINITY;
-  const float* v = c->hull.tri.data();
+  bool finite = true;
   for (uint64_t i = 0; i < 3 * ntri; ++i) {
-    lo0 = std::fmin(lo0, v[3 * i]); hi0 = std::fmax(hi0, v[3 * i]);
-    lo1 = std::fmin(lo1, v[3 * i + 1]); hi1 = std::fmax(hi1, v[3 * i + 1]);
-    lo2 = std::fmin(lo2, v[3 * i + 2]); hi2 = std::fmax(hi2, v[3 * i + 2]);
+    const float x = tri[3 * i], y = tri[3 * i + 1], z = tri[3 * i + 2];
+    finite &= std::isfinite(x) & std::isfinite(y) & std::isfinite(z);
+    lo0 = std::fmin(lo0, x); hi0 = std::fmax(hi0, x);
+    lo1 = std::fmin(lo1, y); hi1 = std::fmax(hi1, y);
+    lo2 = std::fmin(lo2, z); hi2 = std::fmax(hi2, z);
   }
+  if (!finite) return fail(ctx, PP_ERR_INVALID, "hull has non-finite vertices");
+  c->hull.tri.assign(tri, tri + 9 * ntri);
   c->hull.lo[0] = lo0; c->hull.lo[1] = lo1; c->hull.lo[2] = lo2;
   c->hull.hi[0] = hi0; c->hull.hi[1] = hi1; c->hull.hi[2] = hi2;
   c->hull.carve = carve_radius;

@@ -654,3 +654,26 @@ def test_freed_cloud_buffers_reused(ctx, oracle):
         ref = oracle.spatstat(spec.xyz, spec.labels, surf, 0.0, 0.01, 1.0, flags, [[2], [1]], [[1, 2, 3], [1]], ks)
         assert np.array_equal(gpu, ref["bins"]), n
         ctx.free(cid)
+
+
+def test_hull_with_non_finite_vertex_is_refused(ctx, oracle):
+    """A hull with a NaN vertex is refused with PP_ERR_INVALID and leaves the
+    cloud's previous hull (and its ion2surf) in place."""
+    spec = synth.cylinder_specimen(n=20000, radius=5.0, height=16.0, seed=21, nseg=64, stack=4.0)
+    cid = ctx.upload(spec.xyz, spec.labels)
+    ctx.hull(cid, spec.hull, 2.0)
+    ctx.tasks([[1]], [[1, 2, 3]])
+    ctx.hist(0.0, 0.01, 1.0)
+    ctx.run(cid, N.PP_RDF, [])
+    before = ctx.fetch()
+    bad = spec.hull.copy()
+    bad[7, 4] = np.nan
+    with pytest.raises(N.PPError) as err:
+        ctx.hull(cid, bad, 2.0)
+    assert err.value.code == N.PP_ERR_INVALID
+    ctx.run(cid, N.PP_RDF, [])
+    assert np.array_equal(ctx.fetch(), before)
+    surf = oracle.surface_distance(spec.xyz, spec.hull, 2.0)
+    ref = oracle.spatstat(spec.xyz, spec.labels, surf, 0.0, 0.01, 1.0, N.PP_RDF, [[1]], [[1, 2, 3]], [])
+    assert np.array_equal(before, ref["bins"])
+    ctx.free(cid)
