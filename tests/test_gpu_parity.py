@@ -677,3 +677,27 @@ def test_hull_with_non_finite_vertex_is_refused(ctx, oracle):
     ref = oracle.spatstat(spec.xyz, spec.labels, surf, 0.0, 0.01, 1.0, N.PP_RDF, [[1]], [[1, 2, 3]], [])
     assert np.array_equal(before, ref["bins"])
     ctx.free(cid)
+
+
+@pytest.mark.parametrize("R", [0.5, 1.0, 2.5])
+def test_hull_distance_hull_beyond_the_cloud(ctx, oracle, R):
+    """The hull grid covers the ions only: a hull reaching far beyond them (a
+    third of the cylinder's ions kept) and one shifted wholly away still give
+    ion2surf bit-identical to the oracle, for hull cells of 1 to 10 ion cells."""
+    spec = synth.cylinder_specimen(n=30000, radius=5.0, height=24.0, seed=23, nseg=64, stack=4.0)
+    keep = spec.xyz[:, 2] < 8.0
+    xyz, labels = spec.xyz[keep], spec.labels[keep]
+    away = spec.hull.copy()
+    away[:, 2::3] += 40.0
+    for hull in (spec.hull, away):
+        cid = ctx.upload(xyz, labels)
+        ctx.hull(cid, hull, 2.0)
+        ctx.tasks([[1]], [[1, 2, 3]])
+        ctx.hist(0.0, 0.01, R)
+        ctx.run(cid, N.PP_RDF, [])
+        ctx.fetch()
+        gs = ctx.surfdist_fetch(cid, xyz.shape[0])
+        rp = max(np.float32(R), np.float32(2.0))
+        cs = oracle.surface_distance(xyz, hull, rp)
+        assert np.array_equal(gs.view(np.uint32), cs.view(np.uint32))
+        ctx.free(cid)
