@@ -2282,12 +2282,12 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
   uint32_t* ccodeA = (uint32_t*)sp; sp += NW * 32 * 4;
   float* listA = (float*)sp; sp += (size_t)NW * frows * 32 * 4;
   uint16_t* catA = (uint16_t*)sp; sp += CAT ? (((size_t)NW * EM * K * 32 * 2 + 15) & ~size_t(15)) : 0;
-  float* sT = (float*)sp; sp += ((H + 3) & ~3) * 4;
+  float* sT = (float*)sp; sp += ((H + 4) & ~3) * 4;  // H thresholds, then +inf
   uint16_t* slut = (uint16_t*)sp; sp += ((a.lut_n + 7) & ~7) * 2;
   int8_t* scs = (int8_t*)sp; sp += 256;
   uint32_t* skey = (uint32_t*)sp;  // [256] per type: its environment set (EM: none) for every centre slot, 4 bits each
   const uint32_t RSTRIDE = CAT ? 32u : (uint32_t)K * 32u;  // float rows between sets
-  for (int i = threadIdx.x; i < H; i += blockDim.x) sT[i] = a.cat_T[i];
+  for (int i = threadIdx.x; i <= H; i += blockDim.x) sT[i] = i < H ? a.cat_T[i] : kInf();
   for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) slut[i] = a.cat_lut[i];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) {
     scs[i] = a.cslot_of[i];
@@ -2359,7 +2359,16 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     float* Lp = L + row;  // row s holds rank K - 1 - s
     if (!(d2 < Lp[0])) return;
     if constexpr (CAT) {
-      const int c = category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+      int c;
+      if (a.lut_one) {
+        // at most one threshold per table cell below R^2: one step, no loop
+        int t = (int)(__float_as_uint(d2) >> a.lut_shift) - (int)a.lut_base;
+        t = t < 0 ? 0 : (t >= a.lut_n ? a.lut_n - 1 : t);
+        c = slut[t];
+        c += sT[c + 1] <= d2 ? 1 : 0;
+      } else {
+        c = category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
+      }
       uint16_t* Cp = C + (row / 32u) * (uint32_t)K * 32u;
       if constexpr (KB > 0) {
         int v[KB];
@@ -3411,7 +3420,7 @@ size_t lanes_knn_smem(const ScanArgs& a, bool cat) {
   const size_t em = a.emax > 1 ? a.emax : 1;
   const size_t frows = cat ? em + 1 : em * a.kmax + 1;
   const size_t crows = cat ? (((size_t)NW * em * a.kmax * 32 * 2 + 15) & ~size_t(15)) : 0;
-  return NW * 32 * 16 + NW * 2 * 16 + NW * 32 * 4 + (size_t)NW * frows * 32 * 4 + crows + (size_t)((a.H + 3) & ~3) * 4 +
+  return NW * 32 * 16 + NW * 2 * 16 + NW * 32 * 4 + (size_t)NW * frows * 32 * 4 + crows + (size_t)((a.H + 4) & ~3) * 4 +
          (size_t)((a.lut_n + 7) & ~7) * 2 + 256 + 256 * 4;
 }
 
