@@ -657,6 +657,17 @@ __device__ __forceinline__ int category_lut(float d2, const uint16_t* __restrict
   return g;
 }
 
+// The same category for an in-ball d^2 (d^2 <= R^2) when every table cell
+// below R^2 holds at most one threshold (ScanArgs::lut_one, checked by the
+// host): the cell's category plus one branch-free step.  T holds +inf at H.
+__device__ __forceinline__ int category_one(float d2, const uint16_t* __restrict__ lut, int lut_n, uint32_t lut_base,
+                                            int lut_shift, const float* __restrict__ T) {
+  int t = (int)(__float_as_uint(d2) >> lut_shift) - (int)lut_base;
+  t = t < 0 ? 0 : (t >= lut_n ? lut_n - 1 : t);
+  const int g = lut[t];
+  return g + (T[g + 1] <= d2 ? 1 : 0);
+}
+
 template <int KR>
 __device__ __forceinline__ void list_insert(float (&l)[KR], float x, int lane) {
   int pos = 0;
@@ -827,7 +838,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
     unsigned char* p = smem;
     S.since_flush = (unsigned long long*)p; p += 16;
     S.rowtab = (int8_t*)p; p += ROW_TABLE_ENTRIES * 2;
-    S.T = (float*)p; p += ((H + 3) & ~3) * 4;
+    S.T = (float*)p; p += ((H + 4) & ~3) * 4;  // H thresholds, then +inf
     S.lut = (uint16_t*)p; p += ((a.lut_n + 7) & ~7) * 2;
     S.cs = (int8_t*)p; p += 256;
     S.es = (int8_t*)p; p += 256;
@@ -838,7 +849,7 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
     S.hist = (int*)p; p += (a.mode == 2 ? nwarps * H * 4 : 0);
     S.sidx = (int8_t*)p;
   }
-  for (int i = threadIdx.x; i < H; i += blockDim.x) S.T[i] = a.cat_T[i];
+  for (int i = threadIdx.x; i <= H; i += blockDim.x) S.T[i] = i < H ? a.cat_T[i] : kInf();
   for (int i = threadIdx.x; i < a.lut_n; i += blockDim.x) S.lut[i] = a.cat_lut[i];
   for (int i = threadIdx.x; i < ROW_TABLE_ENTRIES * 2; i += blockDim.x) S.rowtab[i] = a.rowtab[i];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) { S.cs[i] = a.cslot_of[i]; S.es[i] = a.eslot_of[i]; }
@@ -917,7 +928,8 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
             const int es = S.es[m & 255];
             int cat = -1;
             if (doR && es >= 0) {
-              cat = category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H);
+              cat = a.lut_one ? category_one(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T)
+                              : category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H);
               const uint32_t idx = ((uint32_t)cs * a.nE + es) * H + cat;
               if (a.rdf_in_smem) atomicAdd(&S.rdf[idx], 1u);
               else atomicAdd(&a.rdf_core[idx], 1ull);
@@ -927,7 +939,9 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
               ++inb;
               const int csj = S.cs[m & 255], esi = S.es[ct & 255];
               if (doR && esi >= 0 && csj >= 0) {
-                if (cat < 0) cat = category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H);
+                if (cat < 0)
+                  cat = a.lut_one ? category_one(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T)
+                                  : category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H);
                 const uint32_t idx = ((uint32_t)csj * a.nE + esi) * H + cat;
                 if (a.rdf_in_smem) atomicAdd(&S.rdf[idx], 1u);
                 else atomicAdd(&a.rdf_core[idx], 1ull);
@@ -1029,7 +1043,9 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
         // mode 2: counting sort of the ball by category into the pair list
         int* hist = S.hist + warp * H;
         for_each_candidate(a, S.rowtab, cp, self, lane, [&](bool, uint32_t, float d2, bool inball, uint32_t, bool) {
-          if (inball) atomicAdd(&hist[category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H)], 1);
+          if (inball)
+            atomicAdd(&hist[a.lut_one ? category_one(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T)
+                                      : category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H)], 1);
         });
         __syncwarp();
         int run = 0;
@@ -1050,7 +1066,8 @@ __global__ void __launch_bounds__(256) k_scan(ScanArgs a) {
         const unsigned long long lim = a.pair_off[ci + 1];
         for_each_candidate(a, S.rowtab, cp, self, lane, [&](bool, uint32_t slot, float d2, bool inball, uint32_t, bool) {
           if (inball) {
-            const int cat = category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H);
+            const int cat = a.lut_one ? category_one(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T)
+                                      : category_lut(d2, S.lut, a.lut_n, a.lut_base, a.lut_shift, S.T, H);
             const unsigned long long at = off + (unsigned long long)atomicAdd(&hist[cat], 1);
             if (at < lim && at - a.pair_base < a.pair_cap) {
               a.pair_slot[at - a.pair_base] = slot;
@@ -2147,11 +2164,7 @@ __global__ void __launch_bounds__(kLanesWarps * 32, 2) k_lanes(ScanArgs a) {
     const uint32_t cj = ccode[j], ci = cinfo[c];
     uint32_t cat;
     if (a.lut_one) {
-      // the table's cells hold at most one threshold below R^2: one step, no loop
-      int t = (int)(__float_as_uint(d2) >> a.lut_shift) - (int)a.lut_base;
-      t = t < 0 ? 0 : (t >= a.lut_n ? a.lut_n - 1 : t);
-      const uint32_t g = slut[t];
-      cat = g + (sT[g + 1] <= d2 ? 1u : 0u);
+      cat = (uint32_t)category_one(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT);
     } else {
       cat = (uint32_t)category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
     }
@@ -2361,11 +2374,7 @@ __global__ void __launch_bounds__(kLanesKnnWarps * 32, 3) k_lanes_knn(ScanArgs a
     if constexpr (CAT) {
       int c;
       if (a.lut_one) {
-        // at most one threshold per table cell below R^2: one step, no loop
-        int t = (int)(__float_as_uint(d2) >> a.lut_shift) - (int)a.lut_base;
-        t = t < 0 ? 0 : (t >= a.lut_n ? a.lut_n - 1 : t);
-        c = slut[t];
-        c += sT[c + 1] <= d2 ? 1 : 0;
+        c = category_one(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT);
       } else {
         c = category_lut(d2, slut, a.lut_n, a.lut_base, a.lut_shift, sT, H);
       }
@@ -3259,7 +3268,7 @@ static int launch_scan_t(const ScanArgs& a, int sm_count, size_t smem, cudaStrea
 
 int launch_scan(const ScanArgs& a, int kr, int emax, int sm_count, size_t* smem_used, cudaStream_t s) {
   const int nwarps = 8;
-  size_t smem = 16 + ROW_TABLE_ENTRIES * 2 + (size_t)((a.H + 3) & ~3) * 4 + (size_t)((a.lut_n + 7) & ~7) * 2 + 512;
+  size_t smem = 16 + ROW_TABLE_ENTRIES * 2 + (size_t)((a.H + 4) & ~3) * 4 + (size_t)((a.lut_n + 7) & ~7) * 2 + 512;
   if (kr > 0) smem += (size_t)a.nC * 256 * 4;
   if (kr > 0 && a.disjoint) smem += (size_t)nwarps * a.emax * (kr * 32 + 1) * 4;
   if (a.rdf_in_smem) smem += (size_t)a.nC * a.nE * a.H * 4;
